@@ -1,0 +1,198 @@
+// apic_device.cuh — device helpers that restate the reference's scalar rules.
+//
+// Compiled with -fmad=false: no multiply-add is contracted unless written as
+// __fmaf_rn, which is used exactly where src/apic.rs calls mul_add.  Division
+// and sqrt are IEEE (-prec-div=true -prec-sqrt=true, the nvcc defaults).
+#pragma once
+
+#include <climits>
+#include <cstdint>
+
+#include "apic_internal.h"
+
+namespace apic {
+
+// wide::f32x8::fast_max / fast_min (x86 maxps/minps operand rule).
+__device__ __forceinline__ float fmax_x86(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ float fmin_x86(float a, float b) { return a < b ? a : b; }
+// wide::f32x8::fast_trunc_int (cvttps2dq: out of range or NaN -> INT_MIN).
+__device__ __forceinline__ int trunc_x86(float x) {
+    return (x >= -2147483648.0f && x < 2147483648.0f) ? __float2int_rz(x) : INT_MIN;
+}
+// Rust f32::clamp.
+__device__ __forceinline__ float rclamp(float x, float lo, float hi) {
+    if (x < lo) x = lo;
+    if (x > hi) x = hi;
+    return x;
+}
+
+// temporal_kernel_w_t, src/apic.rs:31-46.
+__device__ __forceinline__ float temporal_w(float tau) {
+    float ts = tau - 0.5f;
+    float tsq = ts * ts;
+    float inner = fmax_x86(1.0f - tsq, 0.0f);
+    float w = inner * inner * inner;
+    float wt = w * 2.1875f;
+    return fmax_x86(wt, 1e-5f);
+}
+
+// Apic::random_simd for one lane, src/apic.rs:946-975.
+__device__ __forceinline__ float random_lane(uint32_t slot, uint32_t seed) {
+    uint32_t m = slot ^ seed;
+    m ^= m >> 16;
+    m *= 0x7feb352du;
+    m ^= m >> 15;
+    m *= 0x846ca68bu;
+    m ^= m >> 16;
+    return __uint_as_float((m & 0x007FFFFFu) | 0x3F800000u) - 1.5f;
+}
+
+// expand_bits / morton_code, src/apic.rs:185-203.
+__device__ __forceinline__ uint32_t expand_bits(uint32_t v) {
+    v &= 0x0000FFFFu;
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+__device__ __forceinline__ uint32_t morton(uint32_t x, uint32_t y) { return expand_bits(x) | (expand_bits(y) << 1); }
+
+// calculate_theta, src/apic.rs:1628-1638.
+__device__ __forceinline__ float theta(float rho, float rho_center, float target) {
+    float threshold = target * 0.5f;
+    float diff = rho_center - rho;
+    if (fabsf(diff) <= 1e-5f) return 1.0f;
+    return rclamp((rho_center - threshold) / diff, 0.1f, 1.0f);
+}
+
+// u_index_simd / v_index_simd, src/apic.rs:1029-1041.
+__device__ __forceinline__ uint32_t u_index(int i, int j, int W, int H) {
+    uint32_t ci = uint32_t(max(min(i, W), 0));
+    uint32_t cj = uint32_t(max(min(j, H - 1), 0));
+    return cj * uint32_t(W + 1) + ci;
+}
+__device__ __forceinline__ uint32_t v_index(int i, int j, int W, int H) {
+    uint32_t ci = uint32_t(max(min(i, W - 1), 0));
+    uint32_t cj = uint32_t(max(min(j, H), 0));
+    return cj * uint32_t(W) + ci;
+}
+
+// Staggered bilinear stencil (get_u_grid / get_v_grid / get_grid_distances,
+// src/apic.rs:1113-1216): node indices bl, br, tl, tr, weights, node offsets.
+struct Stencil {
+    uint32_t idx[4];
+    float w[4];
+    float ox[4], oy[4];
+    float tx, ty;
+};
+
+__device__ __forceinline__ void stencil_weights(Stencil& s) {
+    float itx = 1.0f - s.tx, ity = 1.0f - s.ty;
+    s.w[0] = itx * ity;
+    s.w[1] = s.tx * ity;
+    s.w[2] = itx * s.ty;
+    s.w[3] = s.tx * s.ty;
+}
+__device__ __forceinline__ void stencil_offsets(Stencil& s, float dx) {
+    float itx = 1.0f - s.tx, ity = 1.0f - s.ty;
+    s.ox[0] = -s.tx * dx; s.oy[0] = -s.ty * dx;
+    s.ox[1] = itx * dx;   s.oy[1] = -s.ty * dx;
+    s.ox[2] = -s.tx * dx; s.oy[2] = ity * dx;
+    s.ox[3] = itx * dx;   s.oy[3] = ity * dx;
+}
+__device__ __forceinline__ void u_stencil(float gx, float gy, int W, int H, float dx, Stencil& s) {
+    float ugx = gx, ugy = gy - 0.5f;
+    float bx = floorf(ugx), by = floorf(ugy);
+    int ix = trunc_x86(bx), iy = trunc_x86(by);
+    s.idx[0] = u_index(ix, iy, W, H);
+    s.idx[1] = u_index(ix + 1, iy, W, H);
+    s.idx[2] = u_index(ix, iy + 1, W, H);
+    s.idx[3] = u_index(ix + 1, iy + 1, W, H);
+    s.tx = ugx - bx;
+    s.ty = ugy - by;
+    stencil_weights(s);
+    stencil_offsets(s, dx);
+}
+__device__ __forceinline__ void v_stencil(float gx, float gy, int W, int H, float dx, Stencil& s) {
+    float vgx = gx - 0.5f, vgy = gy;
+    float bx = floorf(vgx), by = floorf(vgy);
+    s.tx = vgx - bx;
+    s.ty = vgy - by;
+    stencil_weights(s);
+    int ix = trunc_x86(bx), iy = trunc_x86(by);
+    s.idx[0] = v_index(ix, iy, W, H);
+    s.idx[1] = v_index(ix + 1, iy, W, H);
+    s.idx[2] = v_index(ix, iy + 1, W, H);
+    s.idx[3] = v_index(ix + 1, iy + 1, W, H);
+    stencil_offsets(s, dx);
+}
+
+// ---- bit masks (u32 words) ----
+__device__ __forceinline__ uint32_t bit_at(const uint32_t* m, uint32_t i) { return (m[i >> 5] >> (i & 31)) & 1u; }
+// Raw-index fluid test with the reference's index arithmetic; indices outside
+// [0, cells) read as non-fluid (the padding rows of the padded layout are zero).
+__device__ __forceinline__ uint32_t fluid_raw(const uint32_t* m, long long i, uint32_t cells) {
+    if (i < 0 || i >= (long long)cells) return 0;
+    return bit_at(m, uint32_t(i));
+}
+__device__ __forceinline__ uint32_t obstacle_raw(const uint32_t* m, long long i, uint32_t cells) {
+    if (i < 0 || i >= (long long)cells) return 1;
+    return bit_at(m, uint32_t(i));
+}
+// Apic::is_obstacle (src/apic.rs:994-1003): outside the grid is solid.
+__device__ __forceinline__ uint32_t obstacle_xy(const uint32_t* m, int i, int j, int W, int H) {
+    if (i < 0 || i >= W || j < 0 || j >= H) return 1;
+    return bit_at(m, uint32_t(j * W + i));
+}
+// Apic::is_fluid (src/apic.rs:1015-1022).
+__device__ __forceinline__ uint32_t fluid_xy(const uint32_t* m, int i, int j, int W, int H) {
+    if (i < 0 || i >= W || j < 0 || j >= H) return 0;
+    return bit_at(m, uint32_t(j * W + i));
+}
+
+// ---- reductions ----
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_maxf(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Deterministic block sum into partials[blockIdx.x]; returns true in the last
+// block to finish, whose thread 0 receives the total of all partials summed in
+// block order (threadfence reduction; no block waits on another).
+template <int kThreads>
+__device__ __forceinline__ bool block_sum_last(double v, double* partials, uint32_t* counter, double* total) {
+    __shared__ double s_w[kThreads / 32];
+    __shared__ bool s_last;
+    v = warp_sum(v);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_w[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0;
+        for (int w = 0; w < kThreads / 32; ++w) b += s_w[w];
+        partials[blockIdx.x] = b;
+        __threadfence();
+        uint32_t prev = atomicAdd(counter, 1u);
+        s_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        volatile double* vp = partials;
+        for (uint32_t b = 0; b < gridDim.x; ++b) t += vp[b];
+        *total = t;
+        *counter = 0;
+    }
+    return true;
+}
+
+}  // namespace apic

@@ -1,0 +1,199 @@
+// apic_internal.h — device state of one scene and the launchers of each stage.
+//
+// Layout in HBM (one scene):
+//   particles   9 SoA float arrays of npad = 8*ceil(N/8) lanes (+ a second set
+//               for the Morton permutation), i.e. the reference's AoSoA-8
+//               `Vec2x8` chunks (src/apic.rs:757-767) unrolled to SoA so that a
+//               warp reads 128 contiguous bytes per field;
+//   MAC faces   u: (W+1)*H, v: W*(H+1) floats, valid flags as bytes;
+//   cells       density / smoothed / pressure: W*H floats;
+//   bit masks   u32 words (count rounded to even so a u64 view matches the
+//               reference's Vec<u64> masks bit for bit);
+//   levels      per multigrid level: fluid mask words, the ascending list of
+//               non-zero mask words ("segments": 32 consecutive cells each,
+//               one warp per segment), and the pressure system in the
+//               reference's padded layout (index = cell + width, size
+//               cells + 2*width) so +-1 / +-width stencil reads stay in bounds.
+// All per-substep scalars (dt, time, PCG coefficients, counts) live in a
+// device-resident `Ctl` block so kernels never need host round trips.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/apic_gpu.h"
+
+namespace apic {
+
+constexpr int kMaxLevels = 20;        // base + coarse levels
+constexpr int kSegBlock = 256;        // threads per block of segment kernels
+constexpr int kSegWarps = kSegBlock / 32;
+constexpr int kMaxRedBlocks = 1216;   // 152 SMs x 8: grid of reduction kernels
+constexpr int kSortTile = 2048;       // keys per block in the radix sort
+constexpr int kSortThreads = 256;
+
+// Device-resident control block of one scene.
+struct Ctl {
+    // substep loop (src/apic.rs:2429-2474)
+    float frame_dt;
+    float t;
+    float dt;
+    float prev_dt;
+    float cfl_cs;           // cfl * cell_size (src/apic.rs:2436)
+    uint32_t timestamp;
+    uint32_t substeps;
+    uint32_t go;            // 1 while another substep is due
+    uint32_t sort_now;      // sort on this substep
+    uint32_t flags;         // APIC_UPDATE_* of the running update
+    uint32_t vmax_bits;     // max |v| over all lanes, as float bits
+    uint32_t status;        // error bits (kStatus*)
+    uint32_t nonfinite;     // non-finite particle lanes after G2P
+    uint32_t has_ext;       // external force fields may be non-zero
+    uint32_t has_post;      // post force fields may be non-zero
+    // pressure solve
+    float gamma;            // r.z of the current iteration (FP32, as the reference)
+    float alpha;
+    float beta;
+    uint32_t max_r_bits;    // max |r| (float bits)
+    uint32_t pcg_done;
+    uint32_t pcg_iters;
+    uint32_t pcg_iters_total;
+    uint32_t not_converged;
+    uint32_t refinements;
+    uint32_t inner_cap;     // iteration cap of the running (inner) solve
+    double dgamma;          // FP64 copies for the relative-tolerance modes
+    double bnorm2;          // ||b||^2 of the running solve
+    double rnorm2;          // ||r||^2 of the recursive residual
+    double true_rel;        // ||b - A p|| / ||b|| (FP64)
+    double target_rel;      // tolerance of the running inner solve
+    // fluid bookkeeping, per level (0 = base)
+    uint32_t seg_count[kMaxLevels];
+    uint32_t fluid_cells;   // base fluid cells (src/apic.rs:1461-1485)
+    uint32_t last_fluid;    // padded index of the last base fluid cell
+    uint32_t pad_count;     // duplicates padding the base list to a multiple of 8
+    uint32_t red_counter;   // last-block-done counter of the reductions
+};
+
+enum : uint32_t {
+    kStatusNonfinite = 1u,
+    kStatusBadStep = 2u,
+    kStatusTimeout = 4u,
+};
+
+struct Level {
+    uint32_t w = 0, h = 0, cells = 0;
+    uint32_t words = 0;     // u32 mask words (even)
+    uint32_t padded = 0;    // cells + 2w rounded up to 8
+    uint32_t* fluid = nullptr;
+    uint32_t* seg = nullptr;
+    float* diag = nullptr;
+    float* inv_diag = nullptr;
+    float* px = nullptr;
+    float* py = nullptr;
+    float* res = nullptr;
+    float* err = nullptr;
+};
+
+// Particle field order, matching apic_field ids 0..8.
+enum { PX = 0, PY, VX, VY, CUX, CUY, CVX, CVY, TR, NPF };
+
+// Device-resident table of the particle arrays.  The Morton permutation
+// gathers `f` into `alt` and then swaps the two tables on the device, so a
+// captured CUDA graph never holds a stale particle pointer.
+struct PartPtrs {
+    float* f[NPF];
+    float* alt[NPF];
+};
+
+struct Scene {
+    uint32_t W = 0, H = 0, cells = 0;
+    float dx = 0;
+    apic_world_props props{};
+    uint32_t n = 0, nchunks = 0, npad = 0;
+    uint32_t part_cap = 0;                 // allocated lanes
+    float* part[NPF] = {};                 // allocation A of each field
+    float* part_alt[NPF] = {};             // allocation B of each field
+    PartPtrs* pp = nullptr;                // device table: which allocation is current
+    uint32_t* keys = nullptr;
+    uint32_t* vals = nullptr;
+    uint32_t* keys_alt = nullptr;
+    uint32_t* vals_alt = nullptr;
+    uint32_t* sort_hist = nullptr;         // 256 * sort blocks
+    uint32_t* sort_scan_tmp = nullptr;
+
+    uint32_t uf = 0, vf = 0;               // face counts
+    float *u = nullptr, *v = nullptr, *u_alt = nullptr, *v_alt = nullptr;
+    uint8_t *valid_u = nullptr, *valid_v = nullptr, *valid_u_alt = nullptr, *valid_v_alt = nullptr;
+    float *acc_u = nullptr, *acc_uw = nullptr, *acc_v = nullptr, *acc_vw = nullptr;
+    float *ext_u = nullptr, *ext_v = nullptr, *post_u = nullptr, *post_v = nullptr;
+    uint32_t *u_open = nullptr, *v_open = nullptr;
+    uint32_t u_open_words = 0, v_open_words = 0;
+
+    float *density = nullptr, *sm_a = nullptr, *sm_b = nullptr, *pressure = nullptr;
+    uint32_t* obstacle = nullptr;
+    float *search = nullptr, *ap = nullptr;   // base, padded layout
+    float* corr = nullptr;                    // correction of an inner solve (padded)
+    double* p64 = nullptr;                    // FP64 pressure of the refinement loop (padded)
+    double* b64 = nullptr;                    // FP64 right-hand side (padded)
+
+    int nlevels = 0;                          // including the base (levels[0])
+    Level lv[kMaxLevels];
+    float *cg_s = nullptr, *cg_ap = nullptr, *cg_r = nullptr;  // coarsest level CG
+
+    Ctl* ctl = nullptr;                       // device
+    Ctl* ctl_host = nullptr;                  // pinned mirror
+    double* partials = nullptr;               // kMaxRedBlocks doubles
+    uint32_t* scan_tmp = nullptr;             // compaction block counts
+    uint32_t scan_tmp_len = 0;
+
+    cudaStream_t stream = nullptr;
+    int solver_mode = APIC_SOLVER_REFERENCE;
+    float rel_tol = 1e-6f;
+    uint32_t max_iter = 500;
+    bool vmax_valid = false;
+    bool world_ready = false;
+    bool has_ext = false, has_post = false;
+
+    // measurement
+    bool profiling = false;
+    double stage_ms[APIC_STAGE_COUNT] = {};
+    uint64_t stage_launches[APIC_STAGE_COUNT] = {};
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+
+    apic_step_stats stats{};
+};
+
+// ---- launchers (each enqueues on s.stream) --------------------------------
+// sort.cu
+cudaError_t launch_sort(Scene& s);
+// Exclusive scan of data[0..n) in place; tmp holds div_up(n, 1024) words.
+cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t n, uint32_t* tmp, cudaStream_t st);
+// particles.cu
+cudaError_t launch_p2g(Scene& s);
+cudaError_t launch_g2p(Scene& s);
+cudaError_t launch_vmax(Scene& s);
+cudaError_t launch_permute(Scene& s);
+// grid.cu
+cudaError_t launch_finalize_faces(Scene& s, bool forces, bool gravity);
+cudaError_t launch_base_lists(Scene& s);
+cudaError_t launch_external_forces(Scene& s);
+cudaError_t launch_build_pressure(Scene& s);
+cudaError_t launch_multilevel(Scene& s);
+cudaError_t launch_gradient(Scene& s, bool post);
+cudaError_t launch_post_forces(Scene& s);
+cudaError_t launch_extrapolate(Scene& s);
+cudaError_t launch_smoothed_view(Scene& s, float* out);
+cudaError_t launch_level_lists(Scene& s, int level);
+// solver.cu
+cudaError_t launch_solve(Scene& s);
+// runtime.cu
+cudaError_t launch_plan_first(Scene& s);
+cudaError_t launch_advance(Scene& s);
+
+// helpers shared by the launchers
+inline uint32_t div_up(uint64_t a, uint64_t b) { return uint32_t((a + b - 1) / b); }
+uint32_t seg_grid(uint32_t words);     // blocks for a segment kernel over `words` words
+
+}  // namespace apic

@@ -1,0 +1,532 @@
+// grid.cu — MAC-grid and cell stages of the substep.
+//
+//   k_faces          normalise the P2G sums (src/apic.rs:1428-1459), add the
+//                    external force (:1607-1612) and gravity on faces next to
+//                    fluid (:1614-1625); one thread per face, fused.
+//   k_compact_*      fluid mask clean-up (:1463-1464) and the ascending list of
+//                    non-zero mask words of a level (the GPU form of the
+//                    reference's fluid/red/black index lists, :1461-1494 and
+//                    :1526-1553), with the fluid-cell count and the last fluid
+//                    cell that the padded list duplicates (:1487-1494).
+//   k_smooth_density three Jacobi passes over fluid cells (:1653-1685).
+//   k_laplacian      divergence, ghost-fluid diagonal, +x/+y couplings and
+//                    the density-correction right-hand side (:1698-1784).
+//   k_coarsen        one multigrid level from its finer level (:1499-1602).
+//   k_gradient       pressure projection per face (:1958-2055), fused with the
+//                    post-force add (:2453-2458).
+//   k_extrapolate    one Jacobi sweep of velocity extrapolation for u and v
+//                    (:2266-2350).
+//
+// Cell stages run one warp per non-zero 32-bit mask word ("segment"): lane k
+// owns raw cell 32*word + k, so every field access of a warp is one 128-byte
+// line.  Neighbour reads are gated by the neighbour's fluid bit, which equals
+// the reference's reads of zero-filled or zero-coefficient entries.
+#include <cuda_runtime.h>
+
+#include "apic_device.cuh"
+#include "apic_internal.h"
+
+namespace apic {
+namespace {
+
+constexpr int kCompactWords = 1024;  // mask words per compaction block
+
+__global__ void __launch_bounds__(256) k_faces(uint32_t uf, uint32_t vf, int W, int H, const float* __restrict__ acc_u,
+                                               const float* __restrict__ acc_uw, const float* __restrict__ acc_v,
+                                               const float* __restrict__ acc_vw, float* __restrict__ u,
+                                               float* __restrict__ v, uint8_t* __restrict__ valid_u,
+                                               uint8_t* __restrict__ valid_v, const float* __restrict__ ext_u,
+                                               const float* __restrict__ ext_v, const uint32_t* __restrict__ fluid,
+                                               const uint32_t* __restrict__ obstacle, const Ctl* __restrict__ ctl,
+                                               float gravity, int normalize, int forces, int apply_gravity) {
+    uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= uf + vf) return;
+    const float dt = ctl->dt;
+    const bool ext = forces && ctl->has_ext;
+    if (f < uf) {
+        float val;
+        if (normalize) {
+            float w = acc_uw[f];
+            val = 0.0f;
+            uint8_t ok = 0;
+            if (w > 0.0f) { val = acc_u[f] / w; ok = 1; }
+            valid_u[f] = ok;
+        } else {
+            val = u[f];
+        }
+        if (ext) val += ext_u[f] * dt;
+        u[f] = val;
+    } else {
+        uint32_t g = f - uf;
+        float val;
+        if (normalize) {
+            float w = acc_vw[g];
+            val = 0.0f;
+            uint8_t ok = 0;
+            if (w > 0.0f) { val = acc_v[g] / w; ok = 1; }
+            valid_v[g] = ok;
+        } else {
+            val = v[g];
+        }
+        if (ext) val += ext_v[g] * dt;
+        if (apply_gravity) {
+            int x = int(g % uint32_t(W)), y = int(g / uint32_t(W));
+            // fluid bits net of obstacles, whether or not the mask has been cleaned yet
+            uint32_t fb = fluid_xy(fluid, x, y - 1, W, H) & (1u - obstacle_xy(obstacle, x, y - 1, W, H));
+            uint32_t ft = fluid_xy(fluid, x, y, W, H) & (1u - obstacle_xy(obstacle, x, y, W, H));
+            if (fb || ft) val += gravity * dt;
+        }
+        v[g] = val;
+    }
+}
+
+// Block b of the compaction owns mask words [b*1024, b*1024 + 1024).
+__device__ __forceinline__ uint32_t load_clean_word(uint32_t* fluid, const uint32_t* obstacle, uint32_t w, uint32_t words,
+                                                    bool write_back) {
+    if (w >= words) return 0u;
+    uint32_t m = fluid[w];
+    if (obstacle) {
+        uint32_t c = m & ~obstacle[w];
+        if (write_back && c != m) fluid[w] = c;
+        m = c;
+    }
+    return m;
+}
+
+__global__ void __launch_bounds__(256) k_compact_count(uint32_t* __restrict__ fluid, const uint32_t* __restrict__ obstacle,
+                                                       uint32_t words, uint32_t* __restrict__ cnt) {
+    uint32_t nz = 0, cells = 0, last = 0;
+    for (int k = 0; k < 4; ++k) {
+        uint32_t w = blockIdx.x * kCompactWords + threadIdx.x * 4 + k;
+        uint32_t m = load_clean_word(fluid, obstacle, w, words, true);
+        if (m) { nz++; cells += __popc(m); last = max(last, w + 1); }
+    }
+    __shared__ uint32_t s[3][256];
+    s[0][threadIdx.x] = nz; s[1][threadIdx.x] = cells; s[2][threadIdx.x] = last;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            s[0][threadIdx.x] += s[0][threadIdx.x + o];
+            s[1][threadIdx.x] += s[1][threadIdx.x + o];
+            s[2][threadIdx.x] = max(s[2][threadIdx.x], s[2][threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        cnt[3 * blockIdx.x + 0] = s[0][0];
+        cnt[3 * blockIdx.x + 1] = s[1][0];
+        cnt[3 * blockIdx.x + 2] = s[2][0];
+    }
+}
+
+__device__ __forceinline__ uint32_t scan_1024(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t sw[32];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sw[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t s = lane < int(blockDim.x / 32) ? sw[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        sw[lane] = s;
+    }
+    __syncthreads();
+    uint32_t pre = warp > 0 ? sw[warp - 1] : 0u;
+    *total = sw[blockDim.x / 32 - 1];
+    __syncthreads();
+    return pre + x - v;
+}
+
+// Single block: exclusive scan of the per-block word counts, totals into Ctl.
+__global__ void __launch_bounds__(1024) k_compact_scan(uint32_t* __restrict__ cnt, uint32_t nb,
+                                                       const uint32_t* __restrict__ fluid, uint32_t W, int level,
+                                                       Ctl* __restrict__ ctl) {
+    uint32_t carry = 0, cells = 0, last = 0;
+    for (uint32_t c = 0; c < nb; c += 1024) {
+        uint32_t i = c + threadIdx.x;
+        uint32_t v = i < nb ? cnt[3 * i] : 0u;
+        uint32_t tot;
+        uint32_t ex = scan_1024(v, &tot);
+        if (i < nb) {
+            cnt[3 * i] = carry + ex;
+            cells += cnt[3 * i + 1];
+            last = max(last, cnt[3 * i + 2]);
+        }
+        carry += tot;
+    }
+    // reduce cells and last over the block
+    __shared__ uint32_t sc[1024], sl[1024];
+    sc[threadIdx.x] = cells;
+    sl[threadIdx.x] = last;
+    __syncthreads();
+    for (int o = 512; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            sc[threadIdx.x] += sc[threadIdx.x + o];
+            sl[threadIdx.x] = max(sl[threadIdx.x], sl[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        ctl->seg_count[level] = carry;
+        if (level == 0) {
+            uint32_t f = sc[0];
+            ctl->fluid_cells = f;
+            uint32_t lw = sl[0];
+            if (f > 0 && lw > 0) {
+                uint32_t m = fluid[lw - 1];
+                uint32_t raw = (lw - 1) * 32u + (31u - uint32_t(__clz(m)));
+                ctl->last_fluid = raw + W;
+            } else {
+                ctl->last_fluid = 0;
+            }
+            ctl->pad_count = (8u - f % 8u) % 8u;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_compact_write(const uint32_t* __restrict__ fluid, uint32_t words,
+                                                       const uint32_t* __restrict__ cnt, uint32_t* __restrict__ seg) {
+    uint32_t m[4], nz = 0;
+    for (int k = 0; k < 4; ++k) {
+        uint32_t w = blockIdx.x * kCompactWords + threadIdx.x * 4 + k;
+        m[k] = w < words ? fluid[w] : 0u;
+        nz += m[k] ? 1u : 0u;
+    }
+    uint32_t tot;
+    uint32_t off = cnt[3 * blockIdx.x] + scan_1024(nz, &tot);
+    for (int k = 0; k < 4; ++k)
+        if (m[k]) seg[off++] = blockIdx.x * kCompactWords + threadIdx.x * 4 + k;
+}
+
+// Smoothed density as the consumers see it: the three-pass result at fluid
+// cells, the P2G density elsewhere (src/apic.rs:1649-1685 smooths fluid cells only).
+__device__ __forceinline__ float smoothed_at(const float* sm, const float* dens, const uint32_t* fluid, uint32_t c) {
+    return bit_at(fluid, c) ? sm[c] : dens[c];
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_smooth_density(const uint32_t* __restrict__ fluid,
+                                                               const uint32_t* __restrict__ seg,
+                                                               const Ctl* __restrict__ ctl, uint32_t W, uint32_t cells,
+                                                               const float* __restrict__ src, float* __restrict__ dst) {
+    const uint32_t nseg = ctl->seg_count[0];
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nseg; s += nw) {
+        uint32_t word = seg[s];
+        uint32_t bits = fluid[word];
+        if (!((bits >> lane) & 1u)) continue;
+        long long raw = (long long)word * 32 + lane;
+        float fl = float(fluid_raw(fluid, raw - 1, cells)), fr = float(fluid_raw(fluid, raw + 1, cells));
+        float fb = float(fluid_raw(fluid, raw - (long long)W, cells)), ft = float(fluid_raw(fluid, raw + (long long)W, cells));
+        float sum = src[raw] * 4.0f;
+        float weight = 4.0f;
+        if (fl != 0.0f) sum += src[raw - 1];
+        if (fr != 0.0f) sum += src[raw + 1];
+        if (fb != 0.0f) sum += src[raw - W];
+        if (ft != 0.0f) sum += src[raw + W];
+        weight += fl + fr + fb + ft;
+        dst[raw] = sum / weight;
+    }
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_laplacian(const uint32_t* __restrict__ fluid,
+                                                          const uint32_t* __restrict__ obstacle,
+                                                          const uint32_t* __restrict__ seg, const Ctl* __restrict__ ctl,
+                                                          uint32_t W, uint32_t cells, float dx,
+                                                          const float* __restrict__ u, const float* __restrict__ v,
+                                                          const float* __restrict__ sm, const float* __restrict__ dens,
+                                                          float* __restrict__ res, float* __restrict__ diag_o,
+                                                          float* __restrict__ inv_o, float* __restrict__ px_o,
+                                                          float* __restrict__ py_o) {
+    const uint32_t nseg = ctl->seg_count[0];
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const float target = 9.0f;
+    const float noise = target * 1.15f;
+    const float corr = 0.1f;
+    for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nseg; s += nw) {
+        uint32_t word = seg[s];
+        uint32_t bits = fluid[word];
+        if (!((bits >> lane) & 1u)) continue;
+        long long raw = (long long)word * 32 + lane;
+        uint32_t fi = uint32_t(raw) + W;
+        uint32_t gx = uint32_t(raw) % W, gy = uint32_t(raw) / W;
+        uint32_t ui = gy * (W + 1) + gx;
+        float ul = u[ui], ur = u[ui + 1], vb = v[raw], vt = v[raw + W];
+        uint32_t nol = 1u - obstacle_raw(obstacle, raw - 1, cells), nor = 1u - obstacle_raw(obstacle, raw + 1, cells);
+        uint32_t nob = 1u - obstacle_raw(obstacle, raw - (long long)W, cells);
+        uint32_t not_ = 1u - obstacle_raw(obstacle, raw + (long long)W, cells);
+        ul *= float(nol);
+        ur *= float(nor);
+        vb *= float(nob);
+        vt *= float(not_);
+        float div = (ur - ul) + (vt - vb);
+        float rc = sm[raw];
+        float excess = fminf(fmaxf(rc - noise, 0.0f), target);
+        uint32_t fl = fluid_raw(fluid, raw - 1, cells), fr = fluid_raw(fluid, raw + 1, cells);
+        uint32_t fb = fluid_raw(fluid, raw - (long long)W, cells), ft = fluid_raw(fluid, raw + (long long)W, cells);
+        float diag = 0.0f, px = 0.0f, py = 0.0f;
+        if (nol) {
+            if (fl) diag += 1.0f;
+            else diag += 1.0f / theta(smoothed_at(sm, dens, fluid, uint32_t(raw - 1)), rc, target);
+        }
+        if (nor) {
+            if (fr) { diag += 1.0f; px = -1.0f; }
+            else diag += 1.0f / theta(smoothed_at(sm, dens, fluid, uint32_t(raw + 1)), rc, target);
+        }
+        if (nob) {
+            if (fb) diag += 1.0f;
+            else diag += 1.0f / theta(smoothed_at(sm, dens, fluid, uint32_t(raw - W)), rc, target);
+        }
+        if (not_) {
+            if (ft) { diag += 1.0f; py = -1.0f; }
+            else diag += 1.0f / theta(smoothed_at(sm, dens, fluid, uint32_t(raw + W)), rc, target);
+        }
+        res[fi] = -div * dx + excess * corr * dx * dx;
+        px_o[fi] = px;
+        py_o[fi] = py;
+        diag_o[fi] = diag;
+        inv_o[fi] = diag > 1e-6f ? 1.0f / diag : 0.0f;
+    }
+}
+
+// One coarse level from its finer level: thread per coarse cell, one warp per
+// coarse mask word.
+__global__ void __launch_bounds__(256) k_coarsen(Level f, Level c) {
+    uint32_t raw = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t word = raw >> 5;
+    if (word >= c.words) return;  // whole warps exit together
+    bool on = false;
+    uint32_t cx = 0, cy = 0;
+    if (raw < c.cells) {
+        cx = raw % c.w;
+        cy = raw / c.w;
+        for (uint32_t dy = 0; dy < 2; ++dy)
+            for (uint32_t dx = 0; dx < 2; ++dx) {
+                uint32_t fx = cx * 2 + dx, fy = cy * 2 + dy;
+                if (fx < f.w && fy < f.h && bit_at(f.fluid, fy * f.w + fx)) on = true;
+            }
+    }
+    uint32_t ballot = __ballot_sync(0xffffffffu, on);
+    if ((threadIdx.x & 31) == 0) c.fluid[word] = ballot;
+    if (!on) return;
+    float diag = 0.0f, px = 0.0f, py = 0.0f;
+    for (uint32_t dy = 0; dy < 2; ++dy)
+        for (uint32_t dx = 0; dx < 2; ++dx) {
+            uint32_t fx = cx * 2 + dx, fy = cy * 2 + dy;
+            if (fx >= f.w || fy >= f.h) continue;
+            uint32_t fr = fy * f.w + fx, fp = fr + f.w;
+            if (bit_at(f.fluid, fr)) {
+                diag += f.diag[fp];
+                if (dx == 0) diag += 2.0f * f.px[fp];
+                if (dy == 0) diag += 2.0f * f.py[fp];
+                if (dx == 1) px += f.px[fp];
+                if (dy == 1) py += f.py[fp];
+            }
+        }
+    uint32_t cp = raw + c.w;
+    float fd = diag * 0.5f;
+    c.diag[cp] = fd;
+    c.inv_diag[cp] = fd > 1e-6f ? 1.0f / fd : 0.0f;
+    c.px[cp] = px * 0.5f;
+    c.py[cp] = py * 0.5f;
+}
+
+__global__ void __launch_bounds__(256) k_gradient(uint32_t uf, uint32_t vf, int W, int H, float inv_dx,
+                                                  float* __restrict__ u, float* __restrict__ v,
+                                                  uint8_t* __restrict__ valid_u, uint8_t* __restrict__ valid_v,
+                                                  const uint32_t* __restrict__ fluid,
+                                                  const uint32_t* __restrict__ obstacle,
+                                                  const float* __restrict__ p, const float* __restrict__ sm,
+                                                  const float* __restrict__ dens, const float* __restrict__ post_u,
+                                                  const float* __restrict__ post_v, const Ctl* __restrict__ ctl,
+                                                  int do_gradient, int do_post) {
+    uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= uf + vf) return;
+    const float target = 9.0f;
+    const bool post = do_post && ctl->has_post;
+    if (f < uf) {
+        int x = int(f % uint32_t(W + 1)), y = int(f / uint32_t(W + 1));
+        float val = u[f];
+        if (do_gradient) {
+            uint32_t lo = obstacle_xy(obstacle, x - 1, y, W, H), ro = obstacle_xy(obstacle, x, y, W, H);
+            if (lo != ro) {
+                val = 0.0f;
+                valid_u[f] = 1;
+            } else {
+                uint32_t lf = fluid_xy(fluid, x - 1, y, W, H), rf = fluid_xy(fluid, x, y, W, H);
+                float dp = 0.0f;
+                uint32_t li = uint32_t(y * W + x - 1), ri = uint32_t(y * W + x);
+                if (lf && rf) dp = p[ri] - p[li];
+                else if (lf) dp = -p[li] / theta(smoothed_at(sm, dens, fluid, ri), sm[li], target);
+                else if (rf) dp = p[ri] / theta(smoothed_at(sm, dens, fluid, li), sm[ri], target);
+                val -= dp * inv_dx;
+            }
+        }
+        if (post) val += post_u[f] * ctl->dt;
+        u[f] = val;
+    } else {
+        uint32_t g = f - uf;
+        int x = int(g % uint32_t(W)), y = int(g / uint32_t(W));
+        float val = v[g];
+        if (do_gradient) {
+            uint32_t bo = obstacle_xy(obstacle, x, y - 1, W, H), to = obstacle_xy(obstacle, x, y, W, H);
+            if (bo != to) {
+                val = 0.0f;
+                valid_v[g] = 1;
+            } else {
+                uint32_t bf = fluid_xy(fluid, x, y - 1, W, H), tf = fluid_xy(fluid, x, y, W, H);
+                float dp = 0.0f;
+                uint32_t bi = uint32_t((y - 1) * W + x), ti = uint32_t(y * W + x);
+                if (bf && tf) dp = p[ti] - p[bi];
+                else if (bf) dp = -p[bi] / theta(smoothed_at(sm, dens, fluid, ti), sm[bi], target);
+                else if (tf) dp = p[ti] / theta(smoothed_at(sm, dens, fluid, bi), sm[ti], target);
+                val -= dp * inv_dx;
+            }
+        }
+        if (post) val += post_v[g] * ctl->dt;
+        v[g] = val;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_extrapolate(uint32_t uf, uint32_t vf, int W, int H,
+                                                     const float* __restrict__ ou, const uint8_t* __restrict__ ovu,
+                                                     float* __restrict__ nu, uint8_t* __restrict__ nvu,
+                                                     const float* __restrict__ ov, const uint8_t* __restrict__ ovv,
+                                                     float* __restrict__ nv, uint8_t* __restrict__ nvv) {
+    uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= uf + vf) return;
+    if (f < uf) {
+        uint32_t x = f % uint32_t(W + 1), y = f / uint32_t(W + 1);
+        if (ovu[f]) { nu[f] = ou[f]; nvu[f] = 1; return; }
+        float sum = 0.0f;
+        uint32_t cnt = 0;
+        if (x > 0 && ovu[f - 1]) { sum += ou[f - 1]; cnt++; }
+        if (x < uint32_t(W) && ovu[f + 1]) { sum += ou[f + 1]; cnt++; }
+        if (y > 0 && ovu[f - (W + 1)]) { sum += ou[f - (W + 1)]; cnt++; }
+        if (y < uint32_t(H - 1) && ovu[f + W + 1]) { sum += ou[f + W + 1]; cnt++; }
+        if (cnt > 0) { nu[f] = sum / float(cnt); nvu[f] = 1; }
+        else { nu[f] = ou[f]; nvu[f] = 0; }
+    } else {
+        uint32_t g = f - uf;
+        uint32_t x = g % uint32_t(W), y = g / uint32_t(W);
+        if (ovv[g]) { nv[g] = ov[g]; nvv[g] = 1; return; }
+        float sum = 0.0f;
+        uint32_t cnt = 0;
+        if (x > 0 && ovv[g - 1]) { sum += ov[g - 1]; cnt++; }
+        if (x < uint32_t(W - 1) && ovv[g + 1]) { sum += ov[g + 1]; cnt++; }
+        if (y > 0 && ovv[g - W]) { sum += ov[g - W]; cnt++; }
+        if (y < uint32_t(H) && ovv[g + W]) { sum += ov[g + W]; cnt++; }
+        if (cnt > 0) { nv[g] = sum / float(cnt); nvv[g] = 1; }
+        else { nv[g] = ov[g]; nvv[g] = 0; }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_smoothed_view(uint32_t cells, const float* __restrict__ sm,
+                                                       const float* __restrict__ dens,
+                                                       const uint32_t* __restrict__ fluid, float* __restrict__ out) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < cells) out[c] = smoothed_at(sm, dens, fluid, c);
+}
+
+}  // namespace
+
+uint32_t seg_grid(uint32_t words) {
+    uint32_t b = div_up(words, kSegWarps);
+    if (b > uint32_t(kMaxRedBlocks)) b = kMaxRedBlocks;
+    return b ? b : 1;
+}
+
+cudaError_t launch_finalize_faces(Scene& s, bool forces, bool gravity) {
+    uint32_t nf = s.uf + s.vf;
+    k_faces<<<div_up(nf, 256), 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), s.acc_u, s.acc_uw, s.acc_v,
+                                                    s.acc_vw, s.u, s.v, s.valid_u, s.valid_v, s.ext_u, s.ext_v,
+                                                    s.lv[0].fluid, s.obstacle, s.ctl, s.props.gravity, 1,
+                                                    forces ? 1 : 0, gravity ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_external_forces(Scene& s) {
+    uint32_t nf = s.uf + s.vf;
+    k_faces<<<div_up(nf, 256), 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), s.acc_u, s.acc_uw, s.acc_v,
+                                                    s.acc_vw, s.u, s.v, s.valid_u, s.valid_v, s.ext_u, s.ext_v,
+                                                    s.lv[0].fluid, s.obstacle, s.ctl, s.props.gravity, 0, 1, 1);
+    return cudaGetLastError();
+}
+
+static cudaError_t compact_level(Scene& s, int level, const uint32_t* obstacle) {
+    Level& L = s.lv[level];
+    uint32_t nb = div_up(L.words, kCompactWords);
+    k_compact_count<<<nb, 256, 0, s.stream>>>(L.fluid, obstacle, L.words, s.scan_tmp);
+    k_compact_scan<<<1, 1024, 0, s.stream>>>(s.scan_tmp, nb, L.fluid, L.w, level, s.ctl);
+    k_compact_write<<<nb, 256, 0, s.stream>>>(L.fluid, L.words, s.scan_tmp, L.seg);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_base_lists(Scene& s) { return compact_level(s, 0, s.obstacle); }
+cudaError_t launch_level_lists(Scene& s, int level) { return compact_level(s, level, nullptr); }
+
+cudaError_t launch_build_pressure(Scene& s) {
+    const Level& B = s.lv[0];
+    uint32_t g = seg_grid(B.words);
+    k_smooth_density<<<g, kSegBlock, 0, s.stream>>>(B.fluid, B.seg, s.ctl, s.W, s.cells, s.density, s.sm_a);
+    k_smooth_density<<<g, kSegBlock, 0, s.stream>>>(B.fluid, B.seg, s.ctl, s.W, s.cells, s.sm_a, s.sm_b);
+    k_smooth_density<<<g, kSegBlock, 0, s.stream>>>(B.fluid, B.seg, s.ctl, s.W, s.cells, s.sm_b, s.sm_a);
+    k_laplacian<<<g, kSegBlock, 0, s.stream>>>(B.fluid, s.obstacle, B.seg, s.ctl, s.W, s.cells, s.dx, s.u, s.v,
+                                               s.sm_a, s.density, B.res, B.diag, B.inv_diag, B.px, B.py);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_multilevel(Scene& s) {
+    for (int l = 1; l < s.nlevels; ++l) {
+        Level& c = s.lv[l];
+        k_coarsen<<<div_up(uint64_t(c.words) * 32, 256), 256, 0, s.stream>>>(s.lv[l - 1], c);
+        cudaError_t e = compact_level(s, l, nullptr);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gradient(Scene& s, bool post) {
+    uint32_t nf = s.uf + s.vf;
+    k_gradient<<<div_up(nf, 256), 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), 1.0f / s.dx, s.u, s.v,
+                                                       s.valid_u, s.valid_v, s.lv[0].fluid, s.obstacle, s.pressure,
+                                                       s.sm_a, s.density, s.post_u, s.post_v, s.ctl, 1, post ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_post_forces(Scene& s) {
+    uint32_t nf = s.uf + s.vf;
+    k_gradient<<<div_up(nf, 256), 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), 1.0f / s.dx, s.u, s.v,
+                                                       s.valid_u, s.valid_v, s.lv[0].fluid, s.obstacle, s.pressure,
+                                                       s.sm_a, s.density, s.post_u, s.post_v, s.ctl, 0, 1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_extrapolate(Scene& s) {
+    uint32_t nf = s.uf + s.vf;
+    uint32_t g = div_up(nf, 256);
+    for (int k = 0; k < 2; ++k) {
+        k_extrapolate<<<g, 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), s.u, s.valid_u, s.u_alt,
+                                               s.valid_u_alt, s.v, s.valid_v, s.v_alt, s.valid_v_alt);
+        k_extrapolate<<<g, 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), s.u_alt, s.valid_u_alt, s.u,
+                                               s.valid_u, s.v_alt, s.valid_v_alt, s.v, s.valid_v);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_smoothed_view(Scene& s, float* out) {
+    k_smoothed_view<<<div_up(s.cells, 256), 256, 0, s.stream>>>(s.cells, s.sm_a, s.density, s.lv[0].fluid, out);
+    return cudaGetLastError();
+}
+
+}  // namespace apic

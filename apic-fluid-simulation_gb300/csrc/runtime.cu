@@ -1,0 +1,876 @@
+// runtime.cu — scene lifetime, the substep loop and the C-ABI (include/apic_gpu.h).
+//
+// Apic::new (src/apic.rs:779-916) becomes apic_create: all grids, the solid
+// border, the reference's default particle block, the multigrid hierarchy
+// (halve while both sides are even and > 4, :900-908) and the open-face masks
+// (update_world, :918-944) are set up on the device.  Apic::update
+// (:2429-2474) becomes apic_update: the CFL substep size is computed on the
+// device from the max speed that the previous G2P reduced, and every substep
+// runs the stage kernels in the reference's order on the handle's stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "apic_device.cuh"
+#include "apic_internal.h"
+
+using namespace apic;
+
+struct apic_handle {
+    Scene s;
+    std::vector<uint32_t> obstacle_host;  // u32 words
+};
+
+namespace {
+
+thread_local std::string g_last_error = "";
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return fail(APIC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// ---- device control kernels ---------------------------------------------
+
+__global__ void k_begin_update(Ctl* ctl, float frame_dt, uint32_t flags, uint32_t has_ext, uint32_t has_post) {
+    ctl->frame_dt = frame_dt;
+    ctl->t = 0.0f;
+    ctl->flags = flags;
+    ctl->substeps = 0;
+    ctl->pcg_iters_total = 0;
+    ctl->not_converged = 0;
+    ctl->has_ext = has_ext;
+    ctl->has_post = has_post;
+    ctl->status = 0;
+}
+
+// Substep size (src/apic.rs:2433-2441) and the loop condition (:2432).
+__device__ void plan(Ctl* ctl) {
+    float t = ctl->t, frame = ctl->frame_dt;
+    if (!(t < frame)) { ctl->go = 0; return; }
+    float vmax = __uint_as_float(ctl->vmax_bits);
+    float safe = vmax > 1e-5f ? ctl->cfl_cs / vmax : frame;
+    float step = fminf(safe, frame - t);
+    if (!(step > 0.0f) || ctl->substeps >= 100000u) {  // the reference would loop forever
+        ctl->status |= kStatusBadStep;
+        ctl->go = 0;
+        return;
+    }
+    ctl->dt = step;
+    ctl->go = 1;
+    ctl->sort_now = (!(ctl->flags & APIC_UPDATE_DISABLE_SORT) && t == 0.0f) ? 1u : 0u;
+    ctl->vmax_bits = 0;    // the coming G2P reduces the next maximum
+    ctl->nonfinite = 0;
+}
+
+__global__ void k_plan_first(Ctl* ctl) { plan(ctl); }
+
+// End of a substep (src/apic.rs:2463-2467), then plan the next one.
+__global__ void k_advance(Ctl* ctl) {
+    ctl->t = ctl->t + ctl->dt;
+    ctl->prev_dt = ctl->dt;
+    ctl->timestamp += 1;
+    ctl->substeps += 1;
+    plan(ctl);
+}
+
+__global__ void k_set_dt(Ctl* ctl, float dt, uint32_t has_ext, uint32_t has_post) {
+    ctl->dt = dt;
+    ctl->has_ext = has_ext;
+    ctl->has_post = has_post;
+}
+
+__global__ void k_stage_finish(Ctl* ctl, float dt) {
+    ctl->prev_dt = dt;
+    ctl->timestamp += 1;
+}
+
+// add_radial_force, src/apic.rs:2352-2410: one thread per (x, y) of the box.
+__device__ __forceinline__ int sat_i32(float v) {  // Rust `as i32`: saturating, NaN -> 0
+    if (!(v == v)) return 0;
+    if (v >= 2147483647.0f) return INT_MAX;
+    if (v <= -2147483648.0f) return INT_MIN;
+    return int(v);
+}
+__global__ void k_radial_force(int W, int H, float cs, float wx, float wy, float radius, float strength, uint32_t x0,
+                               uint32_t y0, uint32_t nx, uint32_t ny, float* __restrict__ ext_u,
+                               float* __restrict__ ext_v, float* __restrict__ post_u, float* __restrict__ post_v) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nx * ny) return;
+    uint32_t x = x0 + k % nx, y = y0 + k / nx;
+    float r2 = radius * radius;
+    bool repel = strength > 0.0f;
+    if (x <= uint32_t(W) && y < uint32_t(H)) {
+        float dx = float(x) * cs - wx, dy = (float(y) + 0.5f) * cs - wy;
+        float d2 = dx * dx + dy * dy;
+        if (d2 < r2 && d2 > 1e-5f) {
+            float d = sqrtf(d2);
+            float fall = 1.0f - (d / radius);
+            float force = (dx / d) * strength * fall;
+            uint32_t ui = u_index(int(x), int(y), W, H);
+            float* f = repel ? post_u : ext_u;
+            f[ui] = f[ui] + force;
+        }
+    }
+    if (x < uint32_t(W) && y <= uint32_t(H)) {
+        float dx = (float(x) + 0.5f) * cs - wx, dy = float(y) * cs - wy;
+        float d2 = dx * dx + dy * dy;
+        if (d2 < r2 && d2 > 1e-5f) {
+            float d = sqrtf(d2);
+            float fall = 1.0f - (d / radius);
+            float force = (dy / d) * strength * fall;
+            uint32_t vi = v_index(int(x), int(y), W, H);
+            float* f = repel ? post_v : ext_v;
+            f[vi] = f[vi] + force;
+        }
+    }
+}
+__global__ void k_force_box(float wx, float wy, float radius, float cs, int W, int H, uint32_t* box) {
+    int mnx = max(sat_i32(floorf((wx - radius) / cs)), 0);
+    int mxx = min(sat_i32(ceilf((wx + radius) / cs)), W);
+    int mny = max(sat_i32(floorf((wy - radius) / cs)), 0);
+    int mxy = min(sat_i32(ceilf((wy + radius) / cs)), H);
+    box[0] = uint32_t(mnx); box[1] = uint32_t(mxx); box[2] = uint32_t(mny); box[3] = uint32_t(mxy);
+}
+
+// ---- host helpers ---------------------------------------------------------
+
+template <class T> cudaError_t dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
+    if (e != cudaSuccess) return e;
+    return cudaMemset(*p, 0, sizeof(T) * count);
+}
+template <class T> void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+uint32_t even_words(uint64_t bits) { return uint32_t(((bits + 63) / 64) * 2); }
+
+void free_particles(Scene& s) {
+    for (int f = 0; f < NPF; ++f) { dfree(s.part[f]); dfree(s.part_alt[f]); }
+    dfree(s.keys); dfree(s.vals); dfree(s.keys_alt); dfree(s.vals_alt);
+    dfree(s.sort_hist); dfree(s.sort_scan_tmp);
+    s.part_cap = 0;
+}
+
+void free_scene(Scene& s) {
+    free_particles(s);
+    dfree(s.pp);
+    float** fl[] = {&s.u, &s.v, &s.u_alt, &s.v_alt, &s.acc_u, &s.acc_uw, &s.acc_v, &s.acc_vw, &s.ext_u,
+                    &s.ext_v, &s.post_u, &s.post_v, &s.density, &s.sm_a, &s.sm_b, &s.pressure, &s.search,
+                    &s.ap, &s.corr, &s.cg_s, &s.cg_ap, &s.cg_r};
+    for (float** p : fl) dfree(*p);
+    dfree(s.valid_u); dfree(s.valid_v); dfree(s.valid_u_alt); dfree(s.valid_v_alt);
+    dfree(s.u_open); dfree(s.v_open); dfree(s.obstacle);
+    dfree(s.p64); dfree(s.b64);
+    for (int l = 0; l < s.nlevels; ++l) {
+        Level& L = s.lv[l];
+        dfree(L.fluid); dfree(L.seg); dfree(L.diag); dfree(L.inv_diag); dfree(L.px); dfree(L.py);
+        dfree(L.res); dfree(L.err);
+    }
+    dfree(s.ctl);
+    if (s.ctl_host) cudaFreeHost(s.ctl_host);
+    s.ctl_host = nullptr;
+    dfree(s.partials); dfree(s.scan_tmp);
+    if (s.ev_a) cudaEventDestroy(s.ev_a);
+    if (s.ev_b) cudaEventDestroy(s.ev_b);
+    if (s.stream) cudaStreamDestroy(s.stream);
+    s.stream = nullptr;
+}
+
+// Open-face masks from the obstacle mask (update_world, src/apic.rs:918-944).
+void open_masks(const Scene& s, const std::vector<uint32_t>& obst, std::vector<uint32_t>& uo,
+                std::vector<uint32_t>& vo) {
+    auto is_obst = [&](int i, int j) -> uint32_t {
+        if (i < 0 || i >= int(s.W) || j < 0 || j >= int(s.H)) return 1;
+        uint32_t idx = uint32_t(j) * s.W + uint32_t(i);
+        return (obst[idx >> 5] >> (idx & 31)) & 1u;
+    };
+    uo.assign(s.u_open_words, 0);
+    vo.assign(s.v_open_words, 0);
+    for (uint64_t idx = 0; idx < s.uf; ++idx) {
+        int i = int(idx % (s.W + 1)), j = int(idx / (s.W + 1));
+        if ((is_obst(i - 1, j) | is_obst(i, j)) == 0) uo[idx >> 5] |= 1u << (idx & 31);
+    }
+    for (uint64_t idx = 0; idx < s.vf; ++idx) {
+        int i = int(idx % s.W), j = int(idx / s.W);
+        if ((is_obst(i, j - 1) | is_obst(i, j)) == 0) vo[idx >> 5] |= 1u << (idx & 31);
+    }
+}
+
+int upload_world(apic_handle* h) {
+    Scene& s = h->s;
+    std::vector<uint32_t> uo, vo;
+    open_masks(s, h->obstacle_host, uo, vo);
+    CK(cudaMemcpy(s.obstacle, h->obstacle_host.data(), sizeof(uint32_t) * h->obstacle_host.size(),
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.u_open, uo.data(), sizeof(uint32_t) * uo.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.v_open, vo.data(), sizeof(uint32_t) * vo.size(), cudaMemcpyHostToDevice));
+    s.world_ready = true;
+    return APIC_OK;
+}
+
+int alloc_particles(Scene& s, uint32_t npad, uint32_t n) {
+    if (npad <= s.part_cap && s.part_cap > 0) return APIC_OK;
+    free_particles(s);
+    for (int f = 0; f < NPF; ++f) {
+        CK(dalloc(&s.part[f], npad));
+        CK(dalloc(&s.part_alt[f], npad));
+    }
+    CK(dalloc(&s.keys, npad)); CK(dalloc(&s.vals, npad));
+    CK(dalloc(&s.keys_alt, npad)); CK(dalloc(&s.vals_alt, npad));
+    uint32_t nb = div_up(std::max<uint32_t>(n, 1), kSortTile);
+    CK(dalloc(&s.sort_hist, size_t(256) * nb));
+    CK(dalloc(&s.sort_scan_tmp, div_up(uint64_t(256) * nb, 1024) + 1));
+    s.part_cap = npad;
+    return APIC_OK;
+}
+
+// Upload particles (positions, velocities) with the reference's padding.
+int load_particles(apic_handle* h, uint32_t n, const float* px, const float* py, const float* vx, const float* vy) {
+    Scene& s = h->s;
+    uint32_t nchunks = (n + 7) / 8, npad = nchunks * 8;
+    int rc = alloc_particles(s, npad, n);
+    if (rc != APIC_OK) return rc;
+    // sort scratch may need to grow when n grows within the same capacity
+    {
+        uint32_t nb = div_up(std::max<uint32_t>(n, 1), kSortTile);
+        dfree(s.sort_hist); dfree(s.sort_scan_tmp);
+        CK(dalloc(&s.sort_hist, size_t(256) * nb));
+        CK(dalloc(&s.sort_scan_tmp, div_up(uint64_t(256) * nb, 1024) + 1));
+    }
+    std::vector<float> buf(std::max<uint32_t>(npad, 1), 0.0f);
+    auto put = [&](int f, const float* src, bool pad_last) -> int {
+        std::fill(buf.begin(), buf.end(), 0.0f);
+        if (src) std::memcpy(buf.data(), src, sizeof(float) * n);
+        if (pad_last && n > 0 && src)
+            for (uint32_t l = n; l < npad; ++l) buf[l] = src[n - 1];
+        CK(cudaMemcpy(s.part[f], buf.data(), sizeof(float) * npad, cudaMemcpyHostToDevice));
+        CK(cudaMemset(s.part_alt[f], 0, sizeof(float) * npad));
+        return APIC_OK;
+    };
+    if (npad) {
+        if ((rc = put(PX, px, true)) || (rc = put(PY, py, true))) return rc;
+        if ((rc = put(VX, vx, false)) || (rc = put(VY, vy, false))) return rc;
+        for (int f = CUX; f < NPF; ++f)
+            if ((rc = put(f, nullptr, false))) return rc;
+    }
+    PartPtrs t;
+    for (int f = 0; f < NPF; ++f) { t.f[f] = s.part[f]; t.alt[f] = s.part_alt[f]; }
+    CK(cudaMemcpy(s.pp, &t, sizeof(PartPtrs), cudaMemcpyHostToDevice));
+    s.n = n;
+    s.nchunks = nchunks;
+    s.npad = npad;
+    CK(launch_vmax(s));
+    s.vmax_valid = true;
+    return APIC_OK;
+}
+
+PartPtrs read_ptrs(Scene& s) {
+    PartPtrs t;
+    cudaMemcpy(&t, s.pp, sizeof(PartPtrs), cudaMemcpyDeviceToHost);
+    return t;
+}
+
+int sync_ctl(Scene& s) {
+    CK(cudaMemcpyAsync(s.ctl_host, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s.stream));
+    CK(cudaStreamSynchronize(s.stream));
+    return APIC_OK;
+}
+
+// ---- stage timing --------------------------------------------------------
+struct StageTimer {
+    Scene& s;
+    int stage;
+    StageTimer(Scene& sc, int st) : s(sc), stage(st) {
+        if (s.profiling) cudaEventRecord(s.ev_a, s.stream);
+    }
+    ~StageTimer() {
+        if (!s.profiling) return;
+        cudaEventRecord(s.ev_b, s.stream);
+        cudaEventSynchronize(s.ev_b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, s.ev_a, s.ev_b);
+        s.stage_ms[stage] += ms;
+        s.stage_launches[stage] += 1;
+    }
+};
+
+cudaError_t clear_p2g_targets(Scene& s) {
+    cudaStream_t st = s.stream;
+    cudaMemsetAsync(s.acc_u, 0, sizeof(float) * s.uf, st);
+    cudaMemsetAsync(s.acc_uw, 0, sizeof(float) * s.uf, st);
+    cudaMemsetAsync(s.acc_v, 0, sizeof(float) * s.vf, st);
+    cudaMemsetAsync(s.acc_vw, 0, sizeof(float) * s.vf, st);
+    cudaMemsetAsync(s.density, 0, sizeof(float) * s.cells, st);
+    cudaMemsetAsync(s.lv[0].fluid, 0, sizeof(uint32_t) * s.lv[0].words, st);
+    return cudaGetLastError();
+}
+
+// One substep after planning (src/apic.rs:2446-2461).
+int run_substep(Scene& s, bool sort_now) {
+    if (sort_now) { StageTimer t(s, APIC_STAGE_SORT); CK(launch_sort(s)); }
+    { StageTimer t(s, APIC_STAGE_P2G); CK(clear_p2g_targets(s)); CK(launch_p2g(s)); }
+    { StageTimer t(s, APIC_STAGE_FORCES); CK(launch_finalize_faces(s, true, true)); CK(launch_base_lists(s)); }
+    { StageTimer t(s, APIC_STAGE_BUILD); CK(launch_build_pressure(s)); }
+    { StageTimer t(s, APIC_STAGE_MG); CK(launch_multilevel(s)); }
+    { StageTimer t(s, APIC_STAGE_PCG); CK(launch_solve(s)); }
+    { StageTimer t(s, APIC_STAGE_GRAD); CK(launch_gradient(s, true)); }
+    { StageTimer t(s, APIC_STAGE_EXTRAP); CK(launch_extrapolate(s)); }
+    { StageTimer t(s, APIC_STAGE_G2P); CK(launch_g2p(s)); }
+    k_advance<<<1, 1, 0, s.stream>>>(s.ctl);
+    CK(cudaGetLastError());
+    return APIC_OK;
+}
+
+float bits_to_float(uint32_t b) {
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+int valid_handle(apic_handle* h) {
+    if (!h) return fail(APIC_ERR_INVALID_ARG, "null handle");
+    return APIC_OK;
+}
+
+}  // namespace
+
+// ---- scene generators live in scene.cpp ----------------------------------
+
+extern "C" {
+
+const char* apic_last_error(void) { return g_last_error.c_str(); }
+
+int apic_device_count(int* n_out) {
+    if (!n_out) return fail(APIC_ERR_INVALID_ARG, "null output");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) n = 0;
+    *n_out = n;
+    return APIC_OK;
+}
+
+int apic_create(uint32_t width, uint32_t height, float cell_size, const apic_world_props* props, apic_handle** out) {
+    if (!out || !props) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (width == 0 || height == 0 || !(cell_size > 0.0f) || !std::isfinite(cell_size))
+        return fail(APIC_ERR_INVALID_ARG, "width, height and cell_size must be positive");
+    if (uint64_t(width) * height > (1ull << 31)) return fail(APIC_ERR_INVALID_ARG, "grid too large");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(APIC_ERR_NO_DEVICE, "no CUDA device");
+
+    // the reference's default particles (src/apic.rs:831-849)
+    std::vector<float> ix, iy;
+    for (uint32_t y = 0; y < height; ++y)
+        for (uint32_t x = 0; x < width; ++x) {
+            bool border = x == 0 || x == width - 1 || y == 0 || y == height - 1;
+            if (!border && x > 4 && x < width - 4 && y > 4 && y < height / 2)
+                for (int py = 0; py < 3; ++py)
+                    for (int px = 0; px < 3; ++px) {
+                        ix.push_back((float(x) + (float(px) + 0.5f) / 3.0f) * cell_size);
+                        iy.push_back((float(y) + (float(py) + 0.5f) / 3.0f) * cell_size);
+                    }
+        }
+
+    apic_handle* h = new (std::nothrow) apic_handle();
+    if (!h) return fail(APIC_ERR_OOM, "host allocation failed");
+    Scene& s = h->s;
+    s.W = width; s.H = height; s.cells = width * height; s.dx = cell_size; s.props = *props;
+    s.uf = (width + 1) * height;
+    s.vf = width * (height + 1);
+    s.u_open_words = even_words(s.uf);
+    s.v_open_words = even_words(s.vf);
+
+    // levels: base + halvings (src/apic.rs:900-908)
+    s.lv[0].w = width; s.lv[0].h = height;
+    s.nlevels = 1;
+    {
+        uint32_t cw = width, ch = height;
+        while (cw % 2 == 0 && ch % 2 == 0 && cw > 4 && ch > 4 && s.nlevels < kMaxLevels) {
+            cw /= 2; ch /= 2;
+            s.lv[s.nlevels].w = cw; s.lv[s.nlevels].h = ch;
+            s.nlevels++;
+        }
+    }
+    if (!ix.empty() && s.nlevels < 2) {
+        delete h;
+        return fail(APIC_ERR_INVALID_ARG, "grid sides must be even and > 4 (no multigrid level; the reference panics)");
+    }
+
+    auto bail = [&](int rc) { free_scene(s); delete h; return rc; };
+    cudaError_t e;
+#define AL(ptr, count) if ((e = dalloc(&(ptr), (count))) != cudaSuccess) return bail(fail(APIC_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e)))
+    if ((e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(fail(APIC_ERR_CUDA, cudaGetErrorString(e)));
+    cudaEventCreate(&s.ev_a);
+    cudaEventCreate(&s.ev_b);
+    AL(s.pp, 1);
+    AL(s.u, s.uf); AL(s.u_alt, s.uf); AL(s.acc_u, s.uf); AL(s.acc_uw, s.uf); AL(s.ext_u, s.uf); AL(s.post_u, s.uf);
+    AL(s.v, s.vf); AL(s.v_alt, s.vf); AL(s.acc_v, s.vf); AL(s.acc_vw, s.vf); AL(s.ext_v, s.vf); AL(s.post_v, s.vf);
+    AL(s.valid_u, s.uf); AL(s.valid_u_alt, s.uf); AL(s.valid_v, s.vf); AL(s.valid_v_alt, s.vf);
+    AL(s.u_open, s.u_open_words); AL(s.v_open, s.v_open_words);
+    AL(s.density, s.cells); AL(s.sm_a, s.cells); AL(s.sm_b, s.cells); AL(s.pressure, s.cells);
+    AL(s.obstacle, even_words(s.cells));
+    size_t padded0 = (size_t(s.cells) + 2 * size_t(width) + 7) / 8 * 8;
+    AL(s.search, padded0); AL(s.ap, padded0); AL(s.corr, padded0);
+    AL(s.p64, padded0); AL(s.b64, padded0);
+    uint32_t max_words = 0;
+    for (int l = 0; l < s.nlevels; ++l) {
+        Level& L = s.lv[l];
+        L.cells = L.w * L.h;
+        L.words = even_words(L.cells);
+        L.padded = uint32_t((size_t(L.cells) + 2 * size_t(L.w) + 7) / 8 * 8);
+        max_words = std::max(max_words, L.words);
+        AL(L.fluid, L.words); AL(L.seg, L.words);
+        AL(L.diag, L.padded); AL(L.inv_diag, L.padded); AL(L.px, L.padded); AL(L.py, L.padded);
+        AL(L.res, L.padded); AL(L.err, L.padded);
+    }
+    {
+        Level& C = s.lv[s.nlevels - 1];
+        AL(s.cg_s, C.padded); AL(s.cg_ap, C.padded); AL(s.cg_r, C.padded);
+    }
+    AL(s.ctl, 1);
+    AL(s.partials, 2 * kMaxRedBlocks);
+    s.scan_tmp_len = 3 * (div_up(max_words, 1024) + 1);
+    AL(s.scan_tmp, s.scan_tmp_len);
+#undef AL
+    if ((e = cudaMallocHost(&s.ctl_host, sizeof(Ctl))) != cudaSuccess) return bail(fail(APIC_ERR_OOM, "pinned alloc"));
+    std::memset(s.ctl_host, 0, sizeof(Ctl));
+    s.ctl_host->prev_dt = 1.0f / 60.0f;  // src/apic.rs:824
+    s.ctl_host->cfl_cs = props->cfl * cell_size;
+    if ((e = cudaMemcpy(s.ctl, s.ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(fail(APIC_ERR_CUDA, cudaGetErrorString(e)));
+
+    // solid one-cell border (src/apic.rs:834-836)
+    h->obstacle_host.assign(even_words(s.cells), 0);
+    for (uint32_t y = 0; y < height; ++y)
+        for (uint32_t x = 0; x < width; ++x)
+            if (x == 0 || x == width - 1 || y == 0 || y == height - 1) {
+                uint32_t i = y * width + x;
+                h->obstacle_host[i >> 5] |= 1u << (i & 31);
+            }
+    int rc = upload_world(h);
+    if (rc != APIC_OK) return bail(rc);
+    rc = load_particles(h, uint32_t(ix.size()), ix.data(), iy.data(), nullptr, nullptr);
+    if (rc != APIC_OK) return bail(rc);
+    if ((e = cudaStreamSynchronize(s.stream)) != cudaSuccess) return bail(fail(APIC_ERR_CUDA, cudaGetErrorString(e)));
+    *out = h;
+    return APIC_OK;
+}
+
+int apic_destroy(apic_handle* h) {
+    if (!h) return APIC_OK;
+    if (h->s.stream) cudaStreamSynchronize(h->s.stream);
+    free_scene(h->s);
+    delete h;
+    return APIC_OK;
+}
+
+int apic_set_particles(apic_handle* h, uint32_t n, const float* px, const float* py, const float* vx,
+                       const float* vy) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    if (n > 0 && (!px || !py)) return fail(APIC_ERR_INVALID_ARG, "positions required");
+    if (n > 0 && h->s.nlevels < 2)
+        return fail(APIC_ERR_INVALID_ARG, "grid sides must be even and > 4 (no multigrid level)");
+    if (uint64_t(n) + 8 > (1ull << 31)) return fail(APIC_ERR_INVALID_ARG, "too many particles");
+    CK(cudaStreamSynchronize(h->s.stream));
+    int rc = load_particles(h, n, px, py, vx, vy);
+    if (rc == APIC_OK) CK(cudaStreamSynchronize(h->s.stream));
+    return rc;
+}
+
+int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterations) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    if (mode < APIC_SOLVER_REFERENCE || mode > APIC_SOLVER_REL_MIXED || !(rel_tol > 0.0f) || max_iterations == 0)
+        return fail(APIC_ERR_INVALID_ARG, "bad solver configuration");
+    h->s.solver_mode = mode;
+    h->s.rel_tol = rel_tol;
+    h->s.max_iter = max_iterations;
+    return APIC_OK;
+}
+
+int apic_update(apic_handle* h, uint32_t flags, float frame_dt) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    Scene& s = h->s;
+    if (!std::isfinite(frame_dt)) return fail(APIC_ERR_INVALID_ARG, "frame_deltatime must be finite");
+    cudaStream_t st = s.stream;
+    s.stats = apic_step_stats{};
+    k_begin_update<<<1, 1, 0, st>>>(s.ctl, frame_dt, flags, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
+    if (!s.vmax_valid) { CK(launch_vmax(s)); s.vmax_valid = true; }
+    k_plan_first<<<1, 1, 0, st>>>(s.ctl);
+    CK(cudaGetLastError());
+    bool first = true;
+    uint32_t refinements = 0;
+    for (;;) {
+        int rc = sync_ctl(s);
+        if (rc != APIC_OK) return rc;
+        if (!s.ctl_host->go) break;
+        bool sort_now = first && !(flags & APIC_UPDATE_DISABLE_SORT);
+        rc = run_substep(s, sort_now);
+        if (rc != APIC_OK) return rc;
+        refinements += s.stats.refinement_steps;
+        first = false;
+    }
+    if (s.has_ext) { CK(cudaMemsetAsync(s.ext_u, 0, sizeof(float) * s.uf, st)); CK(cudaMemsetAsync(s.ext_v, 0, sizeof(float) * s.vf, st)); }
+    if (s.has_post) { CK(cudaMemsetAsync(s.post_u, 0, sizeof(float) * s.uf, st)); CK(cudaMemsetAsync(s.post_v, 0, sizeof(float) * s.vf, st)); }
+    s.has_ext = s.has_post = false;
+    int rc = sync_ctl(s);
+    if (rc != APIC_OK) return rc;
+    const Ctl& c = *s.ctl_host;
+    s.stats.substeps = c.substeps;
+    s.stats.pcg_iterations = c.pcg_iters;
+    s.stats.pcg_iterations_total = c.pcg_iters_total;
+    s.stats.refinement_steps = refinements;
+    s.stats.residual_max = bits_to_float(c.max_r_bits);
+    s.stats.residual_rel = c.bnorm2 > 0 ? float(std::sqrt(c.rnorm2 / c.bnorm2)) : 0.0f;
+    s.stats.true_residual_rel = c.true_rel;
+    s.stats.not_converged = c.not_converged;
+    s.stats.nonfinite_lanes = c.nonfinite;
+    if (c.status & kStatusBadStep) return fail(APIC_ERR_NONFINITE, "substep size is not positive (non-finite velocities)");
+    return APIC_OK;
+}
+
+int apic_add_radial_force(apic_handle* h, float wx, float wy, float radius, float strength) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    Scene& s = h->s;
+    uint32_t* box = nullptr;
+    CK(cudaMallocHost(&box, 4 * sizeof(uint32_t)));
+    uint32_t* dbox = reinterpret_cast<uint32_t*>(s.partials);  // scratch, idle between calls
+    k_force_box<<<1, 1, 0, s.stream>>>(wx, wy, radius, s.dx, int(s.W), int(s.H), dbox);
+    cudaMemcpyAsync(box, dbox, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream);
+    cudaError_t e = cudaStreamSynchronize(s.stream);
+    if (e != cudaSuccess) { cudaFreeHost(box); return fail(APIC_ERR_CUDA, cudaGetErrorString(e)); }
+    uint32_t x0 = box[0], x1 = box[1], y0 = box[2], y1 = box[3];
+    cudaFreeHost(box);
+    if (x1 >= x0 && y1 >= y0) {
+        uint32_t nx = x1 - x0 + 1, ny = y1 - y0 + 1;
+        k_radial_force<<<div_up(uint64_t(nx) * ny, 256), 256, 0, s.stream>>>(
+            int(s.W), int(s.H), s.dx, wx, wy, radius, strength, x0, y0, nx, ny, s.ext_u, s.ext_v, s.post_u, s.post_v);
+        CK(cudaGetLastError());
+        if (strength > 0.0f) s.has_post = true;
+        else s.has_ext = true;
+    }
+    return APIC_OK;
+}
+
+int apic_max_particle_velocity(apic_handle* h, float* out) {
+    if (valid_handle(h) || !out) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    Scene& s = h->s;
+    CK(launch_vmax(s));
+    int rc = sync_ctl(s);
+    if (rc) return rc;
+    *out = bits_to_float(s.ctl_host->vmax_bits);
+    s.vmax_valid = true;
+    return APIC_OK;
+}
+
+int apic_is_fluid(apic_handle* h, int32_t i, int32_t j, uint64_t* out) {
+    if (valid_handle(h) || !out) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    Scene& s = h->s;
+    *out = 0;
+    if (i < 0 || i >= int32_t(s.W) || j < 0 || j >= int32_t(s.H)) return APIC_OK;
+    uint32_t idx = uint32_t(j) * s.W + uint32_t(i), word = 0;
+    CK(cudaStreamSynchronize(s.stream));
+    CK(cudaMemcpy(&word, s.lv[0].fluid + (idx >> 5), sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    *out = (word >> (idx & 31)) & 1u;
+    return APIC_OK;
+}
+
+int apic_update_world(apic_handle* h) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    CK(cudaStreamSynchronize(h->s.stream));
+    return upload_world(h);
+}
+
+int apic_get_info(apic_handle* h, apic_info* out) {
+    if (valid_handle(h) || !out) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    Scene& s = h->s;
+    int rc = sync_ctl(s);
+    if (rc) return rc;
+    out->width = s.W; out->height = s.H; out->cells = s.cells; out->cell_size = s.dx;
+    out->num_chunks = s.nchunks; out->num_particles = s.n;
+    out->fluid_cells = s.ctl_host->fluid_cells;
+    out->timestamp = s.ctl_host->timestamp;
+    out->prev_deltatime = s.ctl_host->prev_dt;
+    out->mg_levels = uint32_t(s.nlevels > 0 ? s.nlevels - 1 : 0);
+    return APIC_OK;
+}
+
+int apic_get_stats(apic_handle* h, apic_step_stats* out) {
+    if (valid_handle(h) || !out) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    *out = h->s.stats;
+    return APIC_OK;
+}
+
+}  // extern "C"
+
+// ---- field access ---------------------------------------------------------
+namespace {
+
+enum Kind { kF32, kU8, kU32, kMask };
+struct FieldDesc {
+    void* dev = nullptr;
+    uint64_t count = 0;   // elements as exposed
+    uint32_t elem = 0;
+    Kind kind = kF32;
+    bool ok = false;
+};
+
+FieldDesc describe(apic_handle* h, int id, const PartPtrs* pp) {
+    Scene& s = h->s;
+    FieldDesc d;
+    uint64_t padded = uint64_t(s.cells) + 2ull * s.W;
+    auto F = [&](void* p, uint64_t n) { d.dev = p; d.count = n; d.elem = 4; d.kind = kF32; d.ok = true; };
+    auto M = [&](void* p, uint64_t u32words) { d.dev = p; d.count = u32words / 2; d.elem = 8; d.kind = kMask; d.ok = true; };
+    if (id >= APIC_F_POS_X && id <= APIC_F_TRES) { F(pp ? pp->f[id] : nullptr, s.npad); return d; }
+    switch (id) {
+        case APIC_F_U: F(s.u, s.uf); return d;
+        case APIC_F_V: F(s.v, s.vf); return d;
+        case APIC_F_VALID_U: d = {s.valid_u, s.uf, 1, kU8, true}; return d;
+        case APIC_F_VALID_V: d = {s.valid_v, s.vf, 1, kU8, true}; return d;
+        case APIC_F_DENSITY: F(s.density, s.cells); return d;
+        case APIC_F_SMOOTHED_DENSITY: F(s.sm_a, s.cells); return d;
+        case APIC_F_PRESSURE: F(s.pressure, s.cells); return d;
+        case APIC_F_FLUID_BITS: M(s.lv[0].fluid, s.lv[0].words); return d;
+        case APIC_F_OBSTACLE_BITS: M(s.obstacle, even_words(s.cells)); return d;
+        case APIC_F_U_OPEN_BITS: M(s.u_open, s.u_open_words); return d;
+        case APIC_F_V_OPEN_BITS: M(s.v_open, s.v_open_words); return d;
+        case APIC_F_RESIDUAL: F(s.lv[0].res, padded); return d;
+        case APIC_F_DIAG: F(s.lv[0].diag, padded); return d;
+        case APIC_F_INV_DIAG: F(s.lv[0].inv_diag, padded); return d;
+        case APIC_F_PLUS_X: F(s.lv[0].px, padded); return d;
+        case APIC_F_PLUS_Y: F(s.lv[0].py, padded); return d;
+        case APIC_F_SORT_KEYS: d = {s.keys, s.n, 4, kU32, true}; return d;
+        case APIC_F_SORT_VALS: d = {s.vals, s.n, 4, kU32, true}; return d;
+        case APIC_F_FLUID_LIST: d = {nullptr, 0, 4, kU32, true}; return d;  // derived on read
+        case APIC_F_EXT_FORCE_U: F(s.ext_u, s.uf); return d;
+        case APIC_F_EXT_FORCE_V: F(s.ext_v, s.vf); return d;
+        case APIC_F_POST_FORCE_U: F(s.post_u, s.uf); return d;
+        case APIC_F_POST_FORCE_V: F(s.post_v, s.vf); return d;
+        default: break;
+    }
+    if (id >= APIC_F_MG_FLUID_BITS) {
+        int l = id / APIC_F_MG_LEVEL_STRIDE + 1;
+        int f = id % APIC_F_MG_LEVEL_STRIDE;
+        if (l < 1 || l >= s.nlevels) return d;
+        Level& L = s.lv[l];
+        uint64_t lp = uint64_t(L.cells) + 2ull * L.w;
+        switch (f) {
+            case APIC_F_MG_FLUID_BITS: M(L.fluid, L.words); return d;
+            case APIC_F_MG_DIAG: F(L.diag, lp); return d;
+            case APIC_F_MG_INV_DIAG: F(L.inv_diag, lp); return d;
+            case APIC_F_MG_PLUS_X: F(L.px, lp); return d;
+            case APIC_F_MG_PLUS_Y: F(L.py, lp); return d;
+            default: break;
+        }
+    }
+    return d;
+}
+
+std::vector<uint32_t> fluid_list(apic_handle* h) {
+    Scene& s = h->s;
+    std::vector<uint32_t> words(s.lv[0].words), out;
+    cudaMemcpy(words.data(), s.lv[0].fluid, sizeof(uint32_t) * words.size(), cudaMemcpyDeviceToHost);
+    for (uint32_t w = 0; w < words.size(); ++w) {
+        uint32_t m = words[w];
+        while (m) {
+            uint32_t raw = w * 32 + uint32_t(__builtin_ctz(m));
+            if (raw < s.cells) out.push_back(raw + s.W);
+            m &= m - 1;
+        }
+    }
+    return out;
+}
+
+}  // namespace
+
+extern "C" {
+
+int apic_field_shape(apic_handle* h, int field, uint64_t* count, uint32_t* elem_bytes) {
+    if (valid_handle(h) || !count || !elem_bytes) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    CK(cudaStreamSynchronize(h->s.stream));
+    FieldDesc d = describe(h, field, nullptr);
+    if (!d.ok) return fail(APIC_ERR_INVALID_ARG, "unknown field " + std::to_string(field));
+    if (field == APIC_F_FLUID_LIST) d.count = fluid_list(h).size();
+    *count = d.count;
+    *elem_bytes = d.elem;
+    return APIC_OK;
+}
+
+int apic_read_field(apic_handle* h, int field, void* dst, uint64_t bytes) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    Scene& s = h->s;
+    CK(cudaStreamSynchronize(s.stream));
+    PartPtrs pp = read_ptrs(s);
+    FieldDesc d = describe(h, field, &pp);
+    if (!d.ok) return fail(APIC_ERR_INVALID_ARG, "unknown field " + std::to_string(field));
+    if (field == APIC_F_FLUID_LIST) {
+        std::vector<uint32_t> l = fluid_list(h);
+        if (bytes != l.size() * 4) return fail(APIC_ERR_INVALID_ARG, "size mismatch");
+        if (bytes) std::memcpy(dst, l.data(), bytes);
+        return APIC_OK;
+    }
+    if (bytes != d.count * d.elem) return fail(APIC_ERR_INVALID_ARG, "size mismatch");
+    if (bytes == 0) return APIC_OK;
+    if (!dst) return fail(APIC_ERR_INVALID_ARG, "null destination");
+    if (field == APIC_F_SMOOTHED_DENSITY) {
+        float* tmp = s.sm_b;  // free between substeps
+        CK(launch_smoothed_view(s, tmp));
+        CK(cudaMemcpyAsync(dst, tmp, bytes, cudaMemcpyDeviceToHost, s.stream));
+        CK(cudaStreamSynchronize(s.stream));
+        return APIC_OK;
+    }
+    CK(cudaMemcpy(dst, d.dev, bytes, cudaMemcpyDeviceToHost));
+    return APIC_OK;
+}
+
+int apic_write_field(apic_handle* h, int field, const void* src, uint64_t bytes) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    Scene& s = h->s;
+    CK(cudaStreamSynchronize(s.stream));
+    PartPtrs pp = read_ptrs(s);
+    FieldDesc d = describe(h, field, &pp);
+    if (!d.ok || field == APIC_F_FLUID_LIST || field == APIC_F_SORT_KEYS || field == APIC_F_SORT_VALS)
+        return fail(APIC_ERR_INVALID_ARG, "field not writable: " + std::to_string(field));
+    if (bytes != d.count * d.elem) return fail(APIC_ERR_INVALID_ARG, "size mismatch");
+    if (bytes == 0) return APIC_OK;
+    if (!src) return fail(APIC_ERR_INVALID_ARG, "null source");
+    CK(cudaMemcpy(d.dev, src, bytes, cudaMemcpyHostToDevice));
+    if (field == APIC_F_VEL_X || field == APIC_F_VEL_Y) s.vmax_valid = false;
+    if (field == APIC_F_OBSTACLE_BITS) {
+        std::memcpy(h->obstacle_host.data(), src, bytes);
+        int rc = upload_world(h);
+        if (rc) return rc;
+    }
+    if (field == APIC_F_FLUID_BITS) {
+        CK(launch_base_lists(s));
+        CK(cudaStreamSynchronize(s.stream));
+    }
+    if (field >= APIC_F_MG_FLUID_BITS && field % APIC_F_MG_LEVEL_STRIDE == APIC_F_MG_FLUID_BITS) {
+        CK(launch_level_lists(s, field / APIC_F_MG_LEVEL_STRIDE + 1));
+        CK(cudaStreamSynchronize(s.stream));
+    }
+    if (field == APIC_F_EXT_FORCE_U || field == APIC_F_EXT_FORCE_V) s.has_ext = true;
+    if (field == APIC_F_POST_FORCE_U || field == APIC_F_POST_FORCE_V) s.has_post = true;
+    return APIC_OK;
+}
+
+int apic_read_vec2x8(apic_handle* h, int which, float* dst, uint64_t floats) {
+    if (valid_handle(h) || which < 0 || which > 3) return fail(APIC_ERR_INVALID_ARG, "bad argument");
+    Scene& s = h->s;
+    if (floats != uint64_t(s.nchunks) * 16) return fail(APIC_ERR_INVALID_ARG, "size mismatch");
+    if (floats == 0) return APIC_OK;
+    if (!dst) return fail(APIC_ERR_INVALID_ARG, "null destination");
+    CK(cudaStreamSynchronize(s.stream));
+    PartPtrs pp = read_ptrs(s);
+    int fx = 2 * which, fy = 2 * which + 1;
+    // per chunk: 8 x lanes then 8 y lanes (ultraviolet::Vec2x8 {x: f32x8, y: f32x8})
+    CK(cudaMemcpy2D(dst, 16 * sizeof(float), pp.f[fx], 8 * sizeof(float), 8 * sizeof(float), s.nchunks,
+                    cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy2D(dst + 8, 16 * sizeof(float), pp.f[fy], 8 * sizeof(float), 8 * sizeof(float), s.nchunks,
+                    cudaMemcpyDeviceToHost));
+    return APIC_OK;
+}
+
+int apic_set_profiling(apic_handle* h, int enabled) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    h->s.profiling = enabled != 0;
+    return APIC_OK;
+}
+
+int apic_get_stage_times(apic_handle* h, double* ms, uint64_t* launches, int n) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    for (int i = 0; i < n && i < APIC_STAGE_COUNT; ++i) {
+        if (ms) ms[i] = h->s.stage_ms[i];
+        if (launches) launches[i] = h->s.stage_launches[i];
+    }
+    return APIC_OK;
+}
+
+int apic_reset_stage_times(apic_handle* h) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    for (int i = 0; i < APIC_STAGE_COUNT; ++i) { h->s.stage_ms[i] = 0; h->s.stage_launches[i] = 0; }
+    return APIC_OK;
+}
+
+int apic_synchronize(apic_handle* h) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    CK(cudaStreamSynchronize(h->s.stream));
+    return APIC_OK;
+}
+
+int apic_get_stream(apic_handle* h, void** stream_out) {
+    if (valid_handle(h) || !stream_out) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    *stream_out = reinterpret_cast<void*>(h->s.stream);
+    return APIC_OK;
+}
+
+int apic_debug_run_stage(apic_handle* h, int stage, float dt) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    Scene& s = h->s;
+    cudaStream_t st = s.stream;
+    k_set_dt<<<1, 1, 0, st>>>(s.ctl, dt, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
+    switch (stage) {
+        case APIC_STAGE_SORT: CK(launch_sort(s)); break;
+        case APIC_STAGE_P2G:
+            CK(clear_p2g_targets(s));
+            CK(launch_p2g(s));
+            CK(launch_finalize_faces(s, false, false));
+            CK(launch_base_lists(s));
+            break;
+        case APIC_STAGE_FORCES: CK(launch_external_forces(s)); break;
+        case APIC_STAGE_BUILD: CK(launch_base_lists(s)); CK(launch_build_pressure(s)); break;
+        case APIC_STAGE_MG: CK(launch_base_lists(s)); CK(launch_multilevel(s)); break;
+        case APIC_STAGE_PCG: {
+            k_begin_update<<<1, 1, 0, st>>>(s.ctl, 0.0f, 0u, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
+            k_set_dt<<<1, 1, 0, st>>>(s.ctl, dt, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
+            CK(launch_solve(s));
+            int rc = sync_ctl(s);
+            if (rc) return rc;
+            const Ctl& c = *s.ctl_host;
+            s.stats.pcg_iterations = c.pcg_iters;
+            s.stats.pcg_iterations_total = c.pcg_iters_total;
+            s.stats.residual_max = bits_to_float(c.max_r_bits);
+            s.stats.true_residual_rel = c.true_rel;
+            s.stats.not_converged = c.not_converged;
+            break;
+        }
+        case APIC_STAGE_GRAD: CK(launch_gradient(s, false)); break;
+        case APIC_STAGE_POST: CK(launch_post_forces(s)); break;
+        case APIC_STAGE_EXTRAP: CK(launch_extrapolate(s)); break;
+        case APIC_STAGE_G2P: {
+            CK(launch_g2p(s));
+            break;
+        }
+        case APIC_STAGE_VMAX: CK(launch_vmax(s)); s.vmax_valid = true; break;
+        default: return fail(APIC_ERR_INVALID_ARG, "unknown stage");
+    }
+    CK(cudaStreamSynchronize(st));
+    return APIC_OK;
+}
+
+// Test hook: end-of-substep bookkeeping (prev_deltatime, timestamp).
+int apic_debug_finish_substep(apic_handle* h, float dt) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    k_stage_finish<<<1, 1, 0, h->s.stream>>>(h->s.ctl, dt);
+    CK(cudaStreamSynchronize(h->s.stream));
+    return APIC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,588 @@
+// solver.cu — multigrid-preconditioned CG pressure solve.
+//
+// Restates Apic::solve_pcg (src/apic.rs:1865-1956) with its preconditioner
+// apply_preconditioner (:1788-1821): one V-cycle of red/black SOR (omega 1.2,
+// one pre- and one post-sweep, MultiGridLevel::smooth_level :471-535),
+// residual restriction over 2x2 children (:537-594), piecewise-constant
+// prolongation (:596-616; on the base level the last fluid cell receives the
+// correction once more per duplicate that pads the reference's list to a
+// multiple of 8, :1487-1494) and plain CG on the coarsest level
+// (solve_coarse_exact :618-704, one CTA here).
+//
+// Every kernel is a grid-stride loop over the level's segment list whose
+// length lives in device memory, and returns at once when the device-side
+// `pcg_done` flag is set, so an iteration costs no host round trip.  Dot
+// products accumulate FP32 products in FP64 and are reduced deterministically
+// (per-block partials summed in block order by the last block).  The
+// reference's alpha/beta/gamma are FP32 and so are they here: the FP64 sums
+// are rounded to float before the reference's FP32 divisions.
+//
+// Solver modes: APIC_SOLVER_REFERENCE keeps the reference's exits (max|r| <
+// solve_error, gamma/delta < 1e-5, 100 iterations).  APIC_SOLVER_REL_FP32
+// iterates to ||r||_2 <= tol*||b||_2.  APIC_SOLVER_REL_MIXED wraps FP32 inner
+// solves in FP64 iterative refinement on the true residual b - A p.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "apic_device.cuh"
+#include "apic_internal.h"
+
+namespace apic {
+namespace {
+
+constexpr float kOmega = 1.2f;
+constexpr float kSafety = 1e-5f;  // SAFTY, src/apic.rs:8
+
+#define SEG_LOOP(level_idx)                                                        \
+    const uint32_t nseg = ctl->seg_count[level_idx];                               \
+    const int lane = threadIdx.x & 31;                                             \
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;                         \
+    for (uint32_t s_ = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s_ < nseg; s_ += nwarps)
+
+__global__ void k_pcg_begin(Ctl* ctl) {
+    ctl->pcg_done = 0;
+    ctl->pcg_iters = 0;
+    ctl->gamma = 0.0f;
+    ctl->alpha = 0.0f;
+    ctl->beta = 0.0f;
+    ctl->rnorm2 = 0.0;
+}
+
+// src/apic.rs:471-535 for one colour.  init: first sweep after the level's
+// error was zero-filled (src/apic.rs:1792 and :540); own and not yet swept
+// neighbour values are zero then.
+__global__ void __launch_bounds__(kSegBlock) k_smooth(Level L, int li, const Ctl* __restrict__ ctl, int color, int init) {
+    if (ctl->pcg_done) return;
+    SEG_LOOP(li) {
+        uint32_t word = L.seg[s_];
+        uint32_t bits = L.fluid[word];
+        if (!((bits >> lane) & 1u)) continue;
+        long long raw = (long long)word * 32 + lane;
+        uint32_t x = uint32_t(raw) % L.w, y = uint32_t(raw) / L.w;
+        if (int((x + y) & 1u) != color) continue;
+        uint32_t c = uint32_t(raw) + L.w;
+        float inv = L.inv_diag[c];
+        if (inv != 0.0f) {
+            float old = init ? 0.0f : L.err[c];
+            float sum = L.res[c];
+            if (!(init && color == 0)) {
+                const long long W = L.w;
+                if (fluid_raw(L.fluid, raw + 1, L.cells)) sum = __fmaf_rn(-L.px[c], L.err[c + 1], sum);
+                if (fluid_raw(L.fluid, raw + W, L.cells)) sum = __fmaf_rn(-L.py[c], L.err[c + W], sum);
+                if (fluid_raw(L.fluid, raw - 1, L.cells)) sum = __fmaf_rn(-L.px[c - 1], L.err[c - 1], sum);
+                if (fluid_raw(L.fluid, raw - W, L.cells)) sum = __fmaf_rn(-L.py[c - W], L.err[c - W], sum);
+            }
+            float gs = sum * inv;
+            L.err[c] = old + (kOmega * (gs - old));
+        } else if (init) {
+            L.err[c] = 0.0f;
+        }
+    }
+}
+
+// restrict, src/apic.rs:537-594: coarse residual of each coarse fluid cell.
+__global__ void __launch_bounds__(kSegBlock) k_restrict(Level f, Level c, int lc, const Ctl* __restrict__ ctl) {
+    if (ctl->pcg_done) return;
+    SEG_LOOP(lc) {
+        uint32_t word = c.seg[s_];
+        uint32_t bits = c.fluid[word];
+        if (!((bits >> lane) & 1u)) continue;
+        uint32_t rc = word * 32 + lane;
+        uint32_t cx = rc % c.w, cy = rc / c.w;
+        float sum = 0.0f;
+        for (uint32_t dy = 0; dy < 2; ++dy)
+            for (uint32_t dx = 0; dx < 2; ++dx) {
+                uint32_t fx = cx * 2 + dx, fy = cy * 2 + dy;
+                long long rf = (long long)fy * f.w + fx;
+                if (!fluid_raw(f.fluid, rf, f.cells)) continue;
+                uint32_t pf = uint32_t(rf) + f.w;
+                const long long W = f.w;
+                float b = f.res[pf];
+                float ax = f.diag[pf] * f.err[pf];
+                if (fluid_raw(f.fluid, rf + 1, f.cells)) ax += f.px[pf] * f.err[pf + 1];
+                if (fluid_raw(f.fluid, rf + W, f.cells)) ax += f.py[pf] * f.err[pf + W];
+                if (fluid_raw(f.fluid, rf - 1, f.cells)) ax += f.px[pf - 1] * f.err[pf - 1];
+                if (fluid_raw(f.fluid, rf - W, f.cells)) ax += f.py[pf - W] * f.err[pf - W];
+                sum += b - ax;
+            }
+        c.res[rc + c.w] = sum;
+    }
+}
+
+// prolongate, src/apic.rs:596-616.
+__global__ void __launch_bounds__(kSegBlock) k_prolong(Level c, Level f, int lf, const Ctl* __restrict__ ctl, int base) {
+    if (ctl->pcg_done) return;
+    const uint32_t last = ctl->last_fluid, extra = ctl->pad_count;
+    SEG_LOOP(lf) {
+        uint32_t word = f.seg[s_];
+        uint32_t bits = f.fluid[word];
+        if (!((bits >> lane) & 1u)) continue;
+        uint32_t rf = word * 32 + lane;
+        uint32_t pf = rf + f.w;
+        uint32_t cx = (rf % f.w) / 2, cy = (rf / f.w) / 2;
+        float ec = c.err[cy * c.w + cx + c.w];
+        float e = f.err[pf] + ec;
+        if (base && pf == last)
+            for (uint32_t k = 0; k < extra; ++k) e += ec;
+        f.err[pf] = e;
+    }
+}
+
+// solve_coarse_exact, src/apic.rs:618-704, in one CTA.
+constexpr int kCoarseThreads = 1024;
+__device__ __forceinline__ double cta_sum(double v, double* sh) {
+    v = warp_sum(v);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double t = 0;
+    for (int w = 0; w < kCoarseThreads / 32; ++w) t += sh[w];
+    return t;
+}
+__device__ __forceinline__ float cta_max(float v, float* sh) {
+    v = warp_maxf(v);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    float t = 0.0f;
+    for (int w = 0; w < kCoarseThreads / 32; ++w) t = fmaxf(t, sh[w]);
+    return t;
+}
+
+__global__ void __launch_bounds__(kCoarseThreads) k_coarse_solve(Level L, float* __restrict__ cs,
+                                                                 float* __restrict__ cap, float* __restrict__ cr,
+                                                                 const Ctl* __restrict__ ctl) {
+    if (ctl->pcg_done) return;
+    __shared__ double shd[32];
+    __shared__ float shf[32];
+    const long long W = L.w;
+    uint32_t nf = 0;
+    double g = 0;
+    for (uint32_t r = threadIdx.x; r < L.cells; r += kCoarseThreads) {
+        uint32_t c = r + L.w;
+        if (bit_at(L.fluid, r)) {
+            float rv = L.res[c];
+            L.err[c] = 0.0f;
+            cr[c] = rv;
+            cs[c] = rv;
+            g += double(rv * rv);
+            nf++;
+        }
+    }
+    float gamma = float(cta_sum(g, shd));
+    uint32_t nfl = uint32_t(cta_sum(double(nf), shd));
+    if (gamma < 1e-12f) return;
+    uint32_t max_it = min(nfl, 100u);
+    for (uint32_t it = 0; it < max_it; ++it) {
+        __syncthreads();
+        double d = 0;
+        for (uint32_t r = threadIdx.x; r < L.cells; r += kCoarseThreads) {
+            if (!bit_at(L.fluid, r)) continue;
+            uint32_t c = r + L.w;
+            float v = L.diag[c] * cs[c];
+            if (fluid_raw(L.fluid, (long long)r + 1, L.cells)) v = __fmaf_rn(L.px[c], cs[c + 1], v);
+            if (fluid_raw(L.fluid, (long long)r - 1, L.cells)) v = __fmaf_rn(L.px[c - 1], cs[c - 1], v);
+            if (fluid_raw(L.fluid, (long long)r + W, L.cells)) v = __fmaf_rn(L.py[c], cs[c + W], v);
+            if (fluid_raw(L.fluid, (long long)r - W, L.cells)) v = __fmaf_rn(L.py[c - W], cs[c - W], v);
+            cap[c] = v;
+            d += double(cs[c] * v);
+        }
+        float delta = float(cta_sum(d, shd));
+        if (fabsf(delta) < kSafety) break;
+        float alpha = gamma / delta;
+        float me = 0.0f;
+        for (uint32_t r = threadIdx.x; r < L.cells; r += kCoarseThreads) {
+            if (!bit_at(L.fluid, r)) continue;
+            uint32_t c = r + L.w;
+            L.err[c] = L.err[c] + alpha * cs[c];
+            float nr = cr[c] - alpha * cap[c];
+            cr[c] = nr;
+            me = fmaxf(me, fabsf(nr));
+        }
+        float max_err = cta_max(me, shf);
+        if (max_err < 1e-6f) break;
+        double ng = 0;
+        for (uint32_t r = threadIdx.x; r < L.cells; r += kCoarseThreads) {
+            if (!bit_at(L.fluid, r)) continue;
+            uint32_t c = r + L.w;
+            ng += double(cr[c] * cr[c]);
+        }
+        float new_gamma = float(cta_sum(ng, shd));
+        float beta = new_gamma / gamma;
+        gamma = new_gamma;
+        for (uint32_t r = threadIdx.x; r < L.cells; r += kCoarseThreads) {
+            if (!bit_at(L.fluid, r)) continue;
+            uint32_t c = r + L.w;
+            cs[c] = cr[c] + (beta * cs[c]);
+        }
+    }
+}
+
+// ---- PCG kernels on the base level ---------------------------------------
+
+__global__ void __launch_bounds__(kSegBlock) k_clear_pressure(Level B, float* __restrict__ p, const Ctl* __restrict__ ctl) {
+    SEG_LOOP(0) {
+        uint32_t word = B.seg[s_];
+        if ((B.fluid[word] >> lane) & 1u) p[word * 32 + lane] = 0.0f;
+    }
+}
+
+// s = z and gamma = r.z (src/apic.rs:1887-1892).
+__global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* __restrict__ s, Ctl* __restrict__ ctl,
+                                                         double* __restrict__ partials, int mode) {
+    double acc = 0;
+    SEG_LOOP(0) {
+        uint32_t word = B.seg[s_];
+        if (!((B.fluid[word] >> lane) & 1u)) continue;
+        uint32_t c = word * 32 + lane + B.w;
+        float z = B.err[c], r = B.res[c];
+        s[c] = z;
+        acc += double(r * z);
+    }
+    double tot;
+    if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
+        float gamma = float(tot);
+        ctl->gamma = gamma;
+        ctl->dgamma = tot;
+        if (mode == APIC_SOLVER_REFERENCE ? (gamma < kSafety) : !(gamma != 0.0f)) ctl->pcg_done = 1;
+    }
+}
+
+// Ap = A s and delta = s.Ap (apply_matrix_and_dot, src/apic.rs:1823-1863).
+__global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* __restrict__ s, float* __restrict__ ap,
+                                                        Ctl* __restrict__ ctl, double* __restrict__ partials,
+                                                        int mode) {
+    if (ctl->pcg_done) return;
+    double acc = 0;
+    const long long W = B.w;
+    SEG_LOOP(0) {
+        uint32_t word = B.seg[s_];
+        if (!((B.fluid[word] >> lane) & 1u)) continue;
+        long long raw = (long long)word * 32 + lane;
+        uint32_t c = uint32_t(raw) + B.w;
+        float sc = s[c];
+        float v = B.diag[c] * sc;
+        if (fluid_raw(B.fluid, raw + 1, B.cells)) v = __fmaf_rn(B.px[c], s[c + 1], v);
+        if (fluid_raw(B.fluid, raw - 1, B.cells)) v = __fmaf_rn(B.px[c - 1], s[c - 1], v);
+        if (fluid_raw(B.fluid, raw + W, B.cells)) v = __fmaf_rn(B.py[c], s[c + W], v);
+        if (fluid_raw(B.fluid, raw - W, B.cells)) v = __fmaf_rn(B.py[c - W], s[c - W], v);
+        ap[c] = v;
+        acc += double(v * sc);
+    }
+    double tot;
+    if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
+        float delta = float(tot);
+        ctl->pcg_iters++;
+        if (mode == APIC_SOLVER_REFERENCE) {
+            if (fabsf(delta) < kSafety) { ctl->pcg_done = 1; return; }
+            ctl->alpha = ctl->gamma / delta;
+        } else {
+            if (!(delta != 0.0f) || !isfinite(delta)) { ctl->pcg_done = 1; return; }
+            ctl->alpha = ctl->gamma / delta;
+        }
+    }
+}
+
+// p += alpha s, r = fma(-alpha, Ap, r), max|r| (src/apic.rs:1907-1932);
+// relative modes reduce ||r||^2 instead.  Relative modes accumulate into x.
+__global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* __restrict__ p, int p_padded,
+                                                          const float* __restrict__ s, const float* __restrict__ ap,
+                                                          Ctl* __restrict__ ctl, double* __restrict__ partials,
+                                                          int mode, float solve_error) {
+    if (ctl->pcg_done) return;
+    const float alpha = ctl->alpha;
+    double acc = 0;
+    float mx = 0.0f;
+    SEG_LOOP(0) {
+        uint32_t word = B.seg[s_];
+        if (!((B.fluid[word] >> lane) & 1u)) continue;
+        uint32_t raw = word * 32 + lane;
+        uint32_t c = raw + B.w;
+        uint32_t pi = p_padded ? c : raw;
+        p[pi] = p[pi] + alpha * s[c];
+        float nr = __fmaf_rn(-alpha, ap[c], B.res[c]);
+        B.res[c] = nr;
+        mx = fmaxf(mx, fabsf(nr));
+        acc += double(nr) * double(nr);
+    }
+    double tot;
+    if (mode == APIC_SOLVER_REFERENCE) {
+        // max is exact in any order; reuse the sum machinery with a max
+        __shared__ float sm[kSegWarps];
+        __shared__ bool last;
+        float m = warp_maxf(mx);
+        if (lane == 0) sm[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float b = 0.0f;
+            for (int w = 0; w < kSegWarps; ++w) b = fmaxf(b, sm[w]);
+            partials[blockIdx.x] = double(b);
+            __threadfence();
+            last = atomicAdd(&ctl->red_counter, 1u) == gridDim.x - 1;
+        }
+        __syncthreads();
+        if (last && threadIdx.x == 0) {
+            __threadfence();
+            volatile double* vp = partials;
+            double t = 0;
+            for (uint32_t b = 0; b < gridDim.x; ++b) t = fmax(t, vp[b]);
+            ctl->red_counter = 0;
+            ctl->max_r_bits = __float_as_uint(float(t));
+            if (float(t) < solve_error) ctl->pcg_done = 1;
+        }
+    } else {
+        if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
+            ctl->rnorm2 = tot;
+            double rel = ctl->bnorm2 > 0.0 ? sqrt(tot / ctl->bnorm2) : 0.0;
+            if (rel <= ctl->target_rel) ctl->pcg_done = 1;
+        }
+    }
+}
+
+// gamma' = r.z, beta (src/apic.rs:1934-1943).
+__global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* __restrict__ ctl, double* __restrict__ partials,
+                                                      int mode) {
+    if (ctl->pcg_done) return;
+    double acc = 0;
+    SEG_LOOP(0) {
+        uint32_t word = B.seg[s_];
+        if (!((B.fluid[word] >> lane) & 1u)) continue;
+        uint32_t c = word * 32 + lane + B.w;
+        acc += double(B.res[c] * B.err[c]);
+    }
+    double tot;
+    if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
+        float ng = float(tot);
+        if (mode == APIC_SOLVER_REFERENCE ? (ng < kSafety) : !(ng != 0.0f)) { ctl->pcg_done = 1; return; }
+        ctl->beta = ng / ctl->gamma;
+        ctl->gamma = ng;
+    }
+}
+
+// s = z + beta s (src/apic.rs:1945-1954); counts the iteration cap.
+__global__ void __launch_bounds__(kSegBlock) k_search(Level B, float* __restrict__ s, const Ctl* __restrict__ ctl) {
+    if (ctl->pcg_done) return;
+    const float beta = ctl->beta;
+    SEG_LOOP(0) {
+        uint32_t word = B.seg[s_];
+        if (!((B.fluid[word] >> lane) & 1u)) continue;
+        uint32_t c = word * 32 + lane + B.w;
+        s[c] = B.err[c] + (beta * s[c]);
+    }
+}
+
+// ---- FP64 refinement helpers (APIC_SOLVER_REL_MIXED) ----------------------
+
+// b64 = res (FP64 copy of the right-hand side), p64 = 0.
+__global__ void __launch_bounds__(kSegBlock) k_mixed_init(Level B, double* __restrict__ b64, double* __restrict__ p64,
+                                                          const Ctl* __restrict__ ctl) {
+    SEG_LOOP(0) {
+        uint32_t word = B.seg[s_];
+        if (!((B.fluid[word] >> lane) & 1u)) continue;
+        uint32_t c = word * 32 + lane + B.w;
+        b64[c] = double(B.res[c]);
+        p64[c] = 0.0;
+    }
+}
+
+// r64 = b64 - A p64 in FP64 and the true relative residual; flags bit 0:
+// res = float(r64), bit 1: x = 0 (start of an inner correction solve).
+__global__ void __launch_bounds__(kSegBlock) k_true_residual(Level B, const double* __restrict__ b64,
+                                                             const double* __restrict__ p64, float* __restrict__ x,
+                                                             Ctl* __restrict__ ctl, double* __restrict__ partials,
+                                                             int flags) {
+    double rr = 0;
+    const long long W = B.w;
+    SEG_LOOP(0) {
+        uint32_t word = B.seg[s_];
+        if (!((B.fluid[word] >> lane) & 1u)) continue;
+        long long raw = (long long)word * 32 + lane;
+        uint32_t c = uint32_t(raw) + B.w;
+        double v = double(B.diag[c]) * p64[c];
+        if (fluid_raw(B.fluid, raw + 1, B.cells)) v += double(B.px[c]) * p64[c + 1];
+        if (fluid_raw(B.fluid, raw - 1, B.cells)) v += double(B.px[c - 1]) * p64[c - 1];
+        if (fluid_raw(B.fluid, raw + W, B.cells)) v += double(B.py[c]) * p64[c + W];
+        if (fluid_raw(B.fluid, raw - W, B.cells)) v += double(B.py[c - W]) * p64[c - W];
+        double r = b64[c] - v;
+        rr += r * r;
+        if (flags & 1) B.res[c] = float(r);
+        if (flags & 2) x[c] = 0.0f;
+    }
+    double tot;
+    if (block_sum_last<kSegBlock>(rr, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
+        ctl->true_rel = ctl->bnorm2 > 0.0 ? sqrt(tot / ctl->bnorm2) : 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_bnorm(Level B, const double* __restrict__ b64, Ctl* __restrict__ ctl,
+                                                     double* __restrict__ partials) {
+    double bb = 0;
+    SEG_LOOP(0) {
+        uint32_t word = B.seg[s_];
+        if (!((B.fluid[word] >> lane) & 1u)) continue;
+        uint32_t c = word * 32 + lane + B.w;
+        bb += b64[c] * b64[c];
+    }
+    double tot;
+    if (block_sum_last<kSegBlock>(bb, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) ctl->bnorm2 = tot;
+}
+
+// p64 += x; optionally pressure = float(p64) at the end.
+__global__ void __launch_bounds__(kSegBlock) k_mixed_accumulate(Level B, double* __restrict__ p64,
+                                                                const float* __restrict__ x,
+                                                                float* __restrict__ pressure,
+                                                                const Ctl* __restrict__ ctl, int finalize) {
+    SEG_LOOP(0) {
+        uint32_t word = B.seg[s_];
+        if (!((B.fluid[word] >> lane) & 1u)) continue;
+        uint32_t raw = word * 32 + lane;
+        uint32_t c = raw + B.w;
+        if (!finalize) p64[c] += double(x[c]);
+        else pressure[raw] = float(p64[c]);
+    }
+}
+
+// Pressure as FP64 field (for the true residual of modes 1 and 2).
+__global__ void __launch_bounds__(kSegBlock) k_pressure_to64(Level B, const float* __restrict__ pressure,
+                                                             double* __restrict__ p64, const Ctl* __restrict__ ctl) {
+    SEG_LOOP(0) {
+        uint32_t word = B.seg[s_];
+        if (!((B.fluid[word] >> lane) & 1u)) continue;
+        uint32_t raw = word * 32 + lane;
+        p64[raw + B.w] = double(pressure[raw]);
+    }
+}
+
+__global__ void k_set_target(Ctl* ctl, double tol, int from_true) {
+    ctl->pcg_done = 0;
+    if (from_true) {
+        double t = ctl->true_rel > 0.0 ? tol / ctl->true_rel : 1.0;
+        ctl->target_rel = t < 1.0 ? t : 1.0;
+    } else {
+        ctl->target_rel = tol;
+    }
+}
+
+__global__ void k_finish_solve(Ctl* ctl, int mode, uint32_t cap) {
+    ctl->pcg_iters_total += ctl->pcg_iters;
+    if (ctl->pcg_iters >= cap && !ctl->pcg_done) ctl->not_converged++;
+    (void)mode;
+}
+
+// Mixed mode: iterations summed over the inner solves.
+__global__ void k_set_iters(Ctl* ctl, uint32_t total, uint32_t failed) {
+    ctl->pcg_iters = total;
+    ctl->pcg_iters_total += total;
+    ctl->not_converged += failed;
+}
+
+#undef SEG_LOOP
+
+}  // namespace
+
+// One V-cycle: z = M^-1 r in lv[0].err (apply_preconditioner, src/apic.rs:1788-1821).
+static void vcycle(Scene& s) {
+    cudaStream_t st = s.stream;
+    auto grid = [&](int l) { return seg_grid(s.lv[l].words); };
+    Level* L = s.lv;
+    k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 0, 1);
+    k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 1, 1);
+    int last = s.nlevels - 1;
+    if (last >= 1) {
+        k_restrict<<<grid(1), kSegBlock, 0, st>>>(L[0], L[1], 1, s.ctl);
+        for (int l = 1; l < last; ++l) {
+            k_smooth<<<grid(l), kSegBlock, 0, st>>>(L[l], l, s.ctl, 0, 1);
+            k_smooth<<<grid(l), kSegBlock, 0, st>>>(L[l], l, s.ctl, 1, 1);
+            k_restrict<<<grid(l + 1), kSegBlock, 0, st>>>(L[l], L[l + 1], l + 1, s.ctl);
+        }
+        k_coarse_solve<<<1, kCoarseThreads, 0, st>>>(L[last], s.cg_s, s.cg_ap, s.cg_r, s.ctl);
+        for (int l = last - 1; l >= 1; --l) {
+            k_prolong<<<grid(l), kSegBlock, 0, st>>>(L[l + 1], L[l], l, s.ctl, 0);
+            k_smooth<<<grid(l), kSegBlock, 0, st>>>(L[l], l, s.ctl, 1, 0);
+            k_smooth<<<grid(l), kSegBlock, 0, st>>>(L[l], l, s.ctl, 0, 0);
+        }
+        k_prolong<<<grid(0), kSegBlock, 0, st>>>(L[1], L[0], 0, s.ctl, 1);
+    }
+    k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 1, 0);
+    k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 0, 0);
+}
+
+static bool read_done(Scene& s) {
+    cudaMemcpyAsync(&s.ctl_host->pcg_done, &s.ctl->pcg_done, sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream);
+    cudaStreamSynchronize(s.stream);
+    return s.ctl_host->pcg_done != 0;
+}
+
+// One PCG solve into `x` (pressure in the reference layout when p_padded == 0).
+// Iterations run in batches; the host reads the device flag between batches.
+static void pcg(Scene& s, int mode, float* x, int p_padded, uint32_t cap) {
+    cudaStream_t st = s.stream;
+    const Level& B = s.lv[0];
+    uint32_t g = seg_grid(B.words);
+    k_pcg_begin<<<1, 1, 0, st>>>(s.ctl);
+    if (mode == APIC_SOLVER_REFERENCE) k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
+    vcycle(s);
+    k_pcg_start<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl, s.partials, mode);
+    const uint32_t batch = mode == APIC_SOLVER_REFERENCE ? 2u : 8u;
+    for (uint32_t it = 0; it < cap; ++it) {
+        if (it % batch == 0 && read_done(s)) break;
+        k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, s.partials, mode);
+        k_pcg_update<<<g, kSegBlock, 0, st>>>(B, x, p_padded, s.search, s.ap, s.ctl, s.partials, mode,
+                                              s.props.solve_error);
+        vcycle(s);
+        k_dot_rz<<<g, kSegBlock, 0, st>>>(B, s.ctl, s.partials, mode);
+        k_search<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl);
+    }
+}
+
+cudaError_t launch_solve(Scene& s) {
+    cudaStream_t st = s.stream;
+    const Level& B = s.lv[0];
+    uint32_t g = seg_grid(B.words);
+    int mode = s.solver_mode;
+    s.stats.refinement_steps = 0;
+    if (mode == APIC_SOLVER_REFERENCE) {
+        pcg(s, mode, s.pressure, 0, 100);
+        k_finish_solve<<<1, 1, 0, st>>>(s.ctl, mode, 100);
+        return cudaGetLastError();
+    }
+    // relative-tolerance modes: keep b in FP64 for the true residual
+    k_mixed_init<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.ctl);
+    k_bnorm<<<g, kSegBlock, 0, st>>>(B, s.b64, s.ctl, s.partials);
+    k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
+    if (mode == APIC_SOLVER_REL_FP32) {
+        k_set_target<<<1, 1, 0, st>>>(s.ctl, double(s.rel_tol), 0);
+        pcg(s, mode, s.pressure, 0, s.max_iter);
+        k_finish_solve<<<1, 1, 0, st>>>(s.ctl, mode, s.max_iter);
+    } else {
+        // FP64 iterative refinement: r = b - A p (FP64), FP32 PCG on A d = r, p += d.
+        uint32_t used = 0, refinements = 0, total = 0;
+        for (int outer = 0; outer < 32 && used < s.max_iter; ++outer) {
+            k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 3);
+            cudaMemcpyAsync(s.ctl_host, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
+            cudaStreamSynchronize(st);
+            if (!(s.ctl_host->true_rel > double(s.rel_tol))) break;
+            refinements++;
+            k_set_target<<<1, 1, 0, st>>>(s.ctl, double(s.rel_tol), 1);
+            pcg(s, APIC_SOLVER_REL_FP32, s.corr, 1, s.max_iter - used);
+            k_mixed_accumulate<<<g, kSegBlock, 0, st>>>(B, s.p64, s.corr, s.pressure, s.ctl, 0);
+            cudaMemcpyAsync(s.ctl_host, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
+            cudaStreamSynchronize(st);
+            used += s.ctl_host->pcg_iters;
+            total += s.ctl_host->pcg_iters;
+        }
+        k_mixed_accumulate<<<g, kSegBlock, 0, st>>>(B, s.p64, s.corr, s.pressure, s.ctl, 1);
+        k_set_iters<<<1, 1, 0, st>>>(s.ctl, total, (s.ctl_host->true_rel > double(s.rel_tol)) ? 1u : 0u);
+        s.stats.refinement_steps = refinements;
+    }
+    // true residual of the FP32 pressure that the projection will use
+    k_pressure_to64<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.p64, s.ctl);
+    k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 1);
+    return cudaGetLastError();
+}
+
+}  // namespace apic

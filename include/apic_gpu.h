@@ -1,0 +1,232 @@
+/*
+ * apic_gpu.h — C-ABI of the GB300 (sm_103a) APIC/FLIP time step.
+ *
+ * This is the drop-in boundary for the reference crate's simulation API
+ * (fireblade2534/APIC-Fluid-Simulation, `src/apic.rs`).  Every entry point
+ * names the reference item it replaces.  A Rust caller binds these with an
+ * `extern "C"` block; Python binds them with ctypes.  Only plain pointers,
+ * sizes and PODs cross the boundary.
+ *
+ * Ownership: a handle owns all device memory of one scene.  Host buffers are
+ * caller-owned and only copied in or out.  Calls on one handle must be
+ * serialised by the caller (the reference's methods take `&mut self`);
+ * distinct handles may be driven from different threads.  Each handle runs on
+ * its own CUDA stream.
+ *
+ * Errors: every call returns an `int` status (APIC_OK == 0).  The reference
+ * has no error path (it panics; `Cargo.toml:18` sets panic = "abort"); a Rust
+ * shim turns a non-zero status into `panic!` to keep the reference signatures.
+ */
+#ifndef APIC_GPU_H
+#define APIC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define APIC_OK                 0
+#define APIC_ERR_INVALID_ARG    1  /* bad size or pointer; odd or <=4 side with particles (src/apic.rs:910 panics there) */
+#define APIC_ERR_OOM            2  /* device allocation failed */
+#define APIC_ERR_CUDA           3  /* a CUDA runtime call failed; see apic_last_error() */
+#define APIC_ERR_TIMEOUT        4  /* a bounded device wait gave up */
+#define APIC_ERR_NONFINITE      5  /* non-finite particle state detected */
+#define APIC_ERR_NOT_CONVERGED  6  /* warning: a pressure solve hit its iteration cap */
+#define APIC_ERR_NO_DEVICE      7  /* no CUDA device visible */
+#define APIC_ERR_UNSUPPORTED    8
+
+/* ---- update flags (DebugOptions, src/apic.rs:397-400) ------------------ */
+#define APIC_UPDATE_DISABLE_SORT  0x1u  /* DebugOptions::disable_particle_sort */
+
+/* ---- pressure-solver modes --------------------------------------------- */
+/* Reference semantics (src/apic.rs:1865-1956): absolute max-norm exit at
+ * solve_error, 100-iteration cap, 1e-5 early exits on gamma and delta. */
+#define APIC_SOLVER_REFERENCE   0
+/* FP32 PCG with the same V-cycle preconditioner, run to
+ * ||r||_2 <= rel_tol * ||b||_2 (recursively updated residual). */
+#define APIC_SOLVER_REL_FP32    1
+/* FP64 outer iterative refinement around an FP32 inner PCG; converged on the
+ * true residual ||b - A p||_2 <= rel_tol * ||b||_2 evaluated in FP64. */
+#define APIC_SOLVER_REL_MIXED   2
+
+/* WorldProperties (src/apic.rs:707-713). */
+typedef struct apic_world_props {
+    float gravity;
+    float border_damping;
+    float cfl;          /* the reference recommends 5.0 */
+    float solve_error;  /* the reference recommends 1e-5 */
+} apic_world_props;
+
+/* Scalars among the reference's public `Apic` fields (src/apic.rs:716-776). */
+typedef struct apic_info {
+    uint32_t width, height, cells;
+    float    cell_size;
+    uint32_t num_chunks;      /* ceil(num_particles / 8): AoSoA-8 chunks */
+    uint32_t num_particles;
+    uint32_t fluid_cells;     /* base-grid fluid cells of the last substep */
+    uint32_t timestamp;       /* substeps taken so far (src/apic.rs:2467) */
+    float    prev_deltatime;  /* last substep dt (src/apic.rs:2465) */
+    uint32_t mg_levels;       /* coarse multigrid levels (src/apic.rs:900-908) */
+} apic_info;
+
+/* Statistics of the last apic_update (the reference only shows HUD text,
+ * src/main.rs:514-583). */
+typedef struct apic_step_stats {
+    uint32_t substeps;             /* substeps taken by the last apic_update */
+    uint32_t pcg_iterations;       /* PCG iterations of the last substep */
+    uint32_t pcg_iterations_total; /* summed over the substeps of the last update */
+    uint32_t refinement_steps;     /* outer FP64 refinements of the last substep */
+    float    residual_max;         /* max |r| of the recursive residual, last substep */
+    float    residual_rel;         /* ||r||_2 / ||b||_2 of the recursive residual */
+    double   true_residual_rel;    /* ||b - A p||_2 / ||b||_2 in FP64 (solver modes 1, 2) */
+    uint32_t not_converged;        /* substeps whose solve hit its iteration cap */
+    uint32_t nonfinite_lanes;      /* NaN/Inf particle lanes after the last G2P */
+} apic_step_stats;
+
+/* ---- field identifiers for apic_read_field / apic_write_field ---------- */
+/* Particle fields are SoA float arrays of num_chunks*8 lanes; lanes at and
+ * beyond num_particles are the reference's AoSoA padding lanes
+ * (src/apic.rs:857-898). */
+enum apic_field {
+    APIC_F_POS_X = 0, APIC_F_POS_Y, APIC_F_VEL_X, APIC_F_VEL_Y,
+    APIC_F_CU_X, APIC_F_CU_Y, APIC_F_CV_X, APIC_F_CV_Y, APIC_F_TRES,
+    /* MAC faces (src/apic.rs:736-751): u has (W+1)*H, v has W*(H+1) */
+    APIC_F_U = 16, APIC_F_V, APIC_F_VALID_U /* u8 */, APIC_F_VALID_V /* u8 */,
+    /* cell arrays, W*H floats */
+    APIC_F_DENSITY = 24, APIC_F_SMOOTHED_DENSITY, APIC_F_PRESSURE,
+    /* bit masks as u64 words: bit (i % 64) of word i / 64 is cell or face i */
+    APIC_F_FLUID_BITS = 32, APIC_F_OBSTACLE_BITS, APIC_F_U_OPEN_BITS, APIC_F_V_OPEN_BITS,
+    /* base pressure system in the reference's padded layout (index = cell + W,
+     * W*H + 2W floats); only entries at fluid cells are defined */
+    APIC_F_RESIDUAL = 40, APIC_F_DIAG, APIC_F_INV_DIAG, APIC_F_PLUS_X, APIC_F_PLUS_Y,
+    /* (key, val) pairs of the last Morton sort, num_particles u32 each */
+    APIC_F_SORT_KEYS = 48, APIC_F_SORT_VALS,
+    /* base fluid cell list: padded indices, ascending, fluid_cells u32 */
+    APIC_F_FLUID_LIST = 52,
+    /* force fields (src/apic.rs:725-728), face-sized floats */
+    APIC_F_EXT_FORCE_U = 56, APIC_F_EXT_FORCE_V, APIC_F_POST_FORCE_U, APIC_F_POST_FORCE_V,
+    /* coarse multigrid level l (0-based): id + APIC_F_MG_LEVEL_STRIDE * l.
+     * Coefficients use the padded layout of that level (Wl*Hl + 2Wl). */
+    APIC_F_MG_FLUID_BITS = 64, APIC_F_MG_DIAG, APIC_F_MG_INV_DIAG, APIC_F_MG_PLUS_X,
+    APIC_F_MG_PLUS_Y
+};
+#define APIC_F_MG_LEVEL_STRIDE 256
+
+/* ---- stages, for apic_debug_run_stage (order of src/apic.rs:2429-2474) - */
+enum apic_stage {
+    APIC_STAGE_SORT = 0, /* update_spatial_lookup                 :1043-1111 */
+    APIC_STAGE_P2G,      /* transfer_particles_to_grid            :1218-1497 */
+    APIC_STAGE_FORCES,   /* apply_external_forces                 :1604-1626 */
+    APIC_STAGE_BUILD,    /* build_pressure_system                 :1640-1785 */
+    APIC_STAGE_MG,       /* update_multilevel_grid                :1499-1602 */
+    APIC_STAGE_PCG,      /* solve_pcg                             :1865-1956 */
+    APIC_STAGE_GRAD,     /* apply_pressure_gradient               :1958-2055 */
+    APIC_STAGE_POST,     /* post-force add                        :2453-2458 */
+    APIC_STAGE_EXTRAP,   /* extrapolate_velocity                  :2266-2350 */
+    APIC_STAGE_G2P,      /* transfer_grid_to_particles_and_advect :2057-2264 */
+    APIC_STAGE_VMAX,     /* get_max_particle_velocity             :2412-2427 */
+    APIC_STAGE_COUNT
+};
+
+/* ---- scene generators (host code only; no GPU needed) ------------------ */
+#define APIC_SCENE_REFERENCE_DEFAULT 0 /* Apic::new's 3x3-per-cell block, src/apic.rs:831-849 */
+#define APIC_SCENE_DAM_BREAK         1 /* fluid where x < fluid_x and y < fluid_y */
+#define APIC_SCENE_DAM_BREAK_DISK    2 /* dam break plus a disk with its own velocity */
+#define APIC_SCENE_NOISE             3 /* value-noise mask > threshold, N(0, sigma^2) velocities */
+typedef struct apic_scene_params {
+    uint32_t kind;
+    uint32_t width, height;   /* grid cells */
+    float    cell_size;       /* domain units per cell */
+    uint32_t sub;             /* sub x sub particles per cell, jittered per sub-cell */
+    uint32_t seed;
+    float    fluid_x, fluid_y;          /* dam-break extent (domain units) */
+    float    disk_x, disk_y, disk_r;    /* disk centre and radius */
+    float    disk_vx, disk_vy;          /* disk initial velocity */
+    float    noise_period;              /* value-noise lattice period (domain units) */
+    float    noise_threshold;
+    float    vel_sigma;                 /* per-component velocity std-dev (NOISE) */
+} apic_scene_params;
+
+/* Number of particles the scene holds. */
+int apic_scene_count(const apic_scene_params* p, uint64_t* n_out);
+/* Fill n particles; n must equal apic_scene_count's result. */
+int apic_scene_fill(const apic_scene_params* p, uint64_t n,
+                    float* pos_x, float* pos_y, float* vel_x, float* vel_y);
+
+/* ---- lifecycle --------------------------------------------------------- */
+typedef struct apic_handle apic_handle;
+
+/* Apic::new (src/apic.rs:779-916): grid, 1-cell solid border, the reference's
+ * default dam-break particles, multigrid hierarchy, open-face masks. */
+int apic_create(uint32_t width, uint32_t height, float cell_size,
+                const apic_world_props* props, apic_handle** out);
+int apic_destroy(apic_handle* h);
+/* Text of the last error on this thread (static storage, never NULL). */
+const char* apic_last_error(void);
+/* Number of CUDA devices visible (0 without a GPU). */
+int apic_device_count(int* n_out);
+
+/* ---- the step ---------------------------------------------------------- */
+/* Apic::update (src/apic.rs:2429-2474).  flags: APIC_UPDATE_*. */
+int apic_update(apic_handle* h, uint32_t flags, float frame_deltatime);
+/* Apic::add_radial_force (src/apic.rs:2352-2410). */
+int apic_add_radial_force(apic_handle* h, float world_x, float world_y,
+                          float radius, float strength);
+/* Apic::get_max_particle_velocity (src/apic.rs:2412-2427). */
+int apic_max_particle_velocity(apic_handle* h, float* out);
+/* Apic::is_fluid (src/apic.rs:1015-1022). */
+int apic_is_fluid(apic_handle* h, int32_t i, int32_t j, uint64_t* out);
+/* Apic::update_world (src/apic.rs:918-944): recompute the open-face masks
+ * from the obstacle mask (call after writing APIC_F_OBSTACLE_BITS). */
+int apic_update_world(apic_handle* h);
+
+/* ---- state access (the reference's public fields) ---------------------- */
+int apic_get_info(apic_handle* h, apic_info* out);
+int apic_get_stats(apic_handle* h, apic_step_stats* out);
+/* Element count and element size in bytes of a field. */
+int apic_field_shape(apic_handle* h, int field, uint64_t* count, uint32_t* elem_bytes);
+/* Copy a whole field device->host / host->device; bytes must equal
+ * count*elem_bytes.  Both synchronise the handle's stream. */
+int apic_read_field(apic_handle* h, int field, void* dst, uint64_t bytes);
+int apic_write_field(apic_handle* h, int field, const void* src, uint64_t bytes);
+/* Particle pair field in the reference's AoSoA-8 `Vec2x8` layout: per chunk
+ * 8 x-lanes then 8 y-lanes (num_chunks*16 floats).  which: 0 positions,
+ * 1 velocities, 2 c_u, 3 c_v.  Fills `Vec<Vec2x8>` mirrors directly. */
+int apic_read_vec2x8(apic_handle* h, int which, float* dst, uint64_t floats);
+/* Replace the particle set (scene injection): n particles, C = 0, time
+ * residual = 0; the last AoSoA chunk is padded with the last position and
+ * zero velocity as in src/apic.rs:887-898. */
+int apic_set_particles(apic_handle* h, uint32_t n, const float* pos_x, const float* pos_y,
+                       const float* vel_x, const float* vel_y);
+
+/* ---- pressure solver configuration ------------------------------------- */
+int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterations);
+
+/* ---- measurement -------------------------------------------------------- */
+/* When enabled, each stage of each substep is bracketed by CUDA events on the
+ * handle's stream; apic_get_stage_times returns the summed milliseconds per
+ * apic_stage and the number of launches of each since the last reset. */
+int apic_set_profiling(apic_handle* h, int enabled);
+int apic_get_stage_times(apic_handle* h, double* ms, uint64_t* launches, int n);
+int apic_reset_stage_times(apic_handle* h);
+/* Wait for all work of the handle's stream. */
+int apic_synchronize(apic_handle* h);
+/* The handle's cudaStream_t, for callers that interleave their own work. */
+int apic_get_stream(apic_handle* h, void** stream_out);
+
+/* ---- testing hook ------------------------------------------------------ */
+/* Run one stage of the substep on the current device state with substep dt.
+ * Derived device structures (fluid lists, segment lists) are rebuilt from the
+ * written fields first.  Used by the stage-by-stage parity tests. */
+int apic_debug_run_stage(apic_handle* h, int stage, float dt);
+/* End-of-substep bookkeeping after stage-by-stage runs: prev_deltatime = dt,
+ * timestamp += 1 (src/apic.rs:2465-2467). */
+int apic_debug_finish_substep(apic_handle* h, float dt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* APIC_GPU_H */

@@ -1,0 +1,294 @@
+"""GPU-vs-oracle parity through the C-ABI (needs a GB300).
+
+Lock-step test: the GPU library and the CPU oracle start from the same
+particles and run each stage of every substep in the reference's order
+(src/apic.rs:2429-2474).  After each stage the outputs are compared:
+
+* bit-exact (== on values, so -0 == +0) for every stage whose arithmetic has
+  one defined order: Morton keys and the stable sort permutation, the
+  permuted particles, fluid masks and lists, valid flags, forces, density
+  smoothing and the Laplacian, multigrid coarsening, the pressure gradient,
+  extrapolation and G2P/advection;
+* within a stated tolerance where the reference's own order is schedule
+  dependent: P2G sums (float atomics, here and in the reference) and the PCG
+  solve (FP64-accumulated reductions on the GPU, FP32 serial on the oracle).
+  After those two stages the GPU state is re-synchronised from the oracle so
+  the following stages start from identical inputs.
+"""
+import numpy as np
+import pytest
+
+import apic_gb300 as A
+
+pytestmark = pytest.mark.gpu
+
+P2G_RTOL = 2e-5      # relative to the field's max magnitude (order of float atomics)
+PCG_RTOL = 2e-3      # pressure, relative to max |p| (FP64 vs FP32 reductions in the Krylov loop)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu(gpu_lib):
+    if A.device_count() == 0:
+        pytest.skip("no CUDA device")
+
+
+def eq(a, b, name):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, f"{name}: shape {a.shape} vs {b.shape}"
+    if a.dtype.kind == "f":
+        bad = ~((a == b) | (np.isnan(a) & np.isnan(b)))
+    else:
+        bad = a != b
+    if bad.any():
+        i = int(np.argmax(bad))
+        raise AssertionError(f"{name}: {int(bad.sum())}/{a.size} differ; first at {i}: gpu={a[i]!r} oracle={b[i]!r}")
+
+
+def close(a, b, rtol, name):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    assert a.shape == b.shape, name
+    scale = max(float(np.max(np.abs(b))) if b.size else 0.0, 1e-30)
+    err = np.abs(a - b)
+    worst = float(np.max(err)) if err.size else 0.0
+    assert worst <= rtol * scale, f"{name}: max |diff| {worst:.3e} > {rtol:.1e} * max|ref| {scale:.3e}"
+    return worst / scale
+
+
+def fluid_padded(o):
+    return o.read_field("fluid_list").astype(np.int64)
+
+
+def host_dt(vmax, frame, t, cfl, cs):
+    """Substep size exactly as src/apic.rs:2433-2441 computes it in f32."""
+    f32 = np.float32
+    safe = f32(f32(cfl) * f32(cs)) / f32(vmax) if f32(vmax) > f32(1e-5) else f32(frame)
+    return float(min(safe, f32(f32(frame) - f32(t))))
+
+
+def make_pair(oracle_mod, side, cs, props, scene=None):
+    o = oracle_mod.OracleSim(side, side, cs, props)
+    g = A.Apic(side, side, cs, props)
+    if scene is not None:
+        px, py, vx, vy = A.generate_scene(scene)
+        o.set_particles(px, py, vx, vy)
+        g.set_particles(px, py, vx, vy)
+    return o, g
+
+
+def lockstep_substep(o, g, dt, sort, stats):
+    pf = A.PARTICLE_FIELDS
+    if sort:
+        o.run_stage("sort", dt)
+        g.run_stage("sort", dt)
+        eq(g.read_field("sort_keys"), o.read_field("sort_keys"), "sort keys")
+        eq(g.read_field("sort_vals"), o.read_field("sort_vals"), "sort vals")
+        for f in pf:
+            eq(g.read_field(f), o.read_field(f), f"permuted {f}")
+    # P2G (order-dependent sums): compare within tolerance, then re-sync
+    o.run_stage("p2g", dt)
+    g.run_stage("p2g", dt)
+    eq(g.read_field("fluid_bits"), o.read_field("fluid_bits"), "fluid bits")
+    eq(g.read_field("fluid_list"), o.read_field("fluid_list"), "fluid list")
+    eq(g.read_field("valid_u"), o.read_field("valid_u"), "valid u")
+    eq(g.read_field("valid_v"), o.read_field("valid_v"), "valid v")
+    for f in ("u", "v", "density"):
+        stats.setdefault("p2g_" + f, []).append(close(g.read_field(f), o.read_field(f), P2G_RTOL, "p2g " + f))
+        g.write_field(f, o.read_field(f))
+    o.run_stage("forces", dt)
+    g.run_stage("forces", dt)
+    eq(g.read_field("u"), o.read_field("u"), "forces u")
+    eq(g.read_field("v"), o.read_field("v"), "forces v")
+    o.run_stage("build", dt)
+    g.run_stage("build", dt)
+    eq(g.read_field("smoothed_density"), o.read_field("smoothed_density"), "smoothed density")
+    fl = fluid_padded(o)
+    for f in ("residual", "diag", "inv_diag", "plus_x", "plus_y"):
+        eq(g.read_field(f)[fl], o.read_field(f)[fl], "build " + f)
+    o.run_stage("mg", dt)
+    g.run_stage("mg", dt)
+    levels = o.info().mg_levels
+    for lvl in range(levels):
+        eq(g.read_field(A.mg_field("fluid_bits", lvl)), o.read_field(A.mg_field("fluid_bits", lvl)), f"mg{lvl} bits")
+        bits = o.read_field(A.mg_field("fluid_bits", lvl))
+        raw = np.nonzero(np.unpackbits(bits.view(np.uint8), bitorder="little"))[0]
+        lw = lvl_width(o, lvl)
+        idx = raw + lw
+        for f in ("diag", "inv_diag", "plus_x", "plus_y"):
+            eq(g.read_field(A.mg_field(f, lvl))[idx], o.read_field(A.mg_field(f, lvl))[idx], f"mg{lvl} {f}")
+    o.run_stage("pcg", dt)
+    g.run_stage("pcg", dt)
+    so, sg = o.stats(), g.stats()
+    stats.setdefault("pcg_iters", []).append((sg.pcg_iterations, so.pcg_iterations))
+    cells = fl - o.info().width
+    p_o, p_g = o.read_field("pressure"), g.read_field("pressure")
+    stats.setdefault("pcg_p", []).append(close(p_g[cells], p_o[cells], PCG_RTOL, "pressure"))
+    g.write_field("pressure", p_o)
+    o.run_stage("grad", dt)
+    g.run_stage("grad", dt)
+    for f in ("u", "v", "valid_u", "valid_v"):
+        eq(g.read_field(f), o.read_field(f), "grad " + f)
+    o.run_stage("post", dt)
+    g.run_stage("post", dt)
+    eq(g.read_field("u"), o.read_field("u"), "post u")
+    o.run_stage("extrap", dt)
+    g.run_stage("extrap", dt)
+    for f in ("u", "v", "valid_u", "valid_v"):
+        eq(g.read_field(f), o.read_field(f), "extrap " + f)
+    o.run_stage("g2p", dt)
+    g.run_stage("g2p", dt)
+    for f in pf:
+        eq(g.read_field(f), o.read_field(f), "g2p " + f)
+    o.finish_substep(dt)
+    g.finish_substep(dt)
+
+
+def lvl_width(o, lvl):
+    """Width of coarse level lvl (src/apic.rs:900-908 halves both sides)."""
+    w = o.info().width
+    for _ in range(lvl + 1):
+        w //= 2
+    return w
+
+
+def run_lockstep(o, g, frames, frame_dt, props, cs, forces=None):
+    stats = {}
+    for k in range(frames):
+        if forces and k in forces:
+            for args in forces[k]:
+                o.add_radial_force(*args)
+                g.add_radial_force(*args)
+            for f in ("ext_force_u", "ext_force_v", "post_force_u", "post_force_v"):
+                eq(g.read_field(f), o.read_field(f), f)
+        t = np.float32(0)
+        first = True
+        while t < np.float32(frame_dt):
+            vo = o.get_max_particle_velocity()
+            vg = g.get_max_particle_velocity()
+            assert vg == vo, f"max velocity gpu {vg} oracle {vo}"
+            dt = host_dt(vo, frame_dt, t, props.cfl, cs)
+            lockstep_substep(o, g, dt, first, stats)
+            first = False
+            t = np.float32(t + np.float32(dt))
+        # clear the frame's forces like Apic::update does (src/apic.rs:2470-2473)
+        zu = np.zeros_like(o.read_field("ext_force_u"))
+        zv = np.zeros_like(o.read_field("ext_force_v"))
+        for name, z in (("ext_force_u", zu), ("ext_force_v", zv), ("post_force_u", zu), ("post_force_v", zv)):
+            o.write_field(name, z)
+            g.write_field(name, z)
+    return stats
+
+
+def test_lockstep_reference_default_scene(oracle_mod):
+    props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+    side = 64
+    o, g = make_pair(oracle_mod, side, 1 / side, props)
+    st = run_lockstep(o, g, 6, 1 / 60, props, 1 / side)
+    assert len(st["pcg_p"]) >= 6
+
+
+def test_lockstep_dam_break_with_forces(oracle_mod):
+    props = A.WorldProperties(-9.81, 0.5, 5.0, 1e-5)
+    side = 128
+    cs = 1 / side
+    scene = A.scene_params(A.SCENE_DAM_BREAK, side, cell_size=cs, sub=2, seed=0, fluid_x=0.4, fluid_y=0.6)
+    o, g = make_pair(oracle_mod, side, cs, props, scene)
+    forces = {2: [(0.2, 0.3, 0.05, 150.0)], 3: [(0.25, 0.2, 0.06, -150.0)]}
+    run_lockstep(o, g, 5, 1 / 240, props, cs, forces)
+
+
+def test_lockstep_random_velocities_odd_count(oracle_mod):
+    props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+    side = 64
+    cs = 1 / side
+    scene = A.scene_params(A.SCENE_NOISE, side, cell_size=cs, sub=2, seed=2, noise_period=0.15,
+                           noise_threshold=0.5, vel_sigma=0.5)
+    px, py, vx, vy = A.generate_scene(scene)
+    n = len(px) - (len(px) % 8) - 3  # force a ragged last chunk
+    o = oracle_mod.OracleSim(side, side, cs, props)
+    g = A.Apic(side, side, cs, props)
+    o.set_particles(px[:n], py[:n], vx[:n], vy[:n])
+    g.set_particles(px[:n], py[:n], vx[:n], vy[:n])
+    run_lockstep(o, g, 4, 1 / 60, props, cs)
+
+
+def test_full_update_drift(oracle_mod):
+    """Whole updates with no re-sync: report the drift from the oracle."""
+    props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+    side = 64
+    o, g = make_pair(oracle_mod, side, 1 / side, props)
+    opts = A.DebugOptions()
+    for _ in range(20):
+        o.update(opts, 1 / 60)
+        g.update(opts, 1 / 60)
+    assert g.timestamp == o.info().timestamp
+    n = o.info().num_particles
+    for f in ("pos_x", "pos_y"):
+        d = np.abs(g.read_field(f)[:n].astype(np.float64) - o.read_field(f)[:n])
+        print(f"drift after 20 updates, {f}: max {np.max(d):.3e} mean {np.mean(d):.3e} (cell {1 / side:.3e})")
+        assert np.max(d) < 0.5 / side, f"{f} drift {np.max(d)}"
+
+
+def test_disable_sort_keeps_order(oracle_mod):
+    props = A.WorldProperties()
+    side = 64
+    o, g = make_pair(oracle_mod, side, 1 / side, props)
+    opts = A.DebugOptions(disable_particle_sort=True)
+    x0 = g.read_field("pos_x").copy()
+    g.update(opts, 1 / 60)
+    o.update(opts, 1 / 60)
+    x1 = g.read_field("pos_x")
+    n = o.info().num_particles
+    # no permutation: every particle moved by at most a few cells
+    assert np.max(np.abs(x1[:n] - x0[:n])) < 3 / side
+
+
+def test_empty_and_tiny_grids(gpu_lib):
+    props = A.WorldProperties()
+    g = A.Apic(8, 8, 1 / 8, props)  # the reference seeds no particles on 8x8
+    assert g.num_particles == 0
+    g.update(A.DebugOptions(), 1 / 60)
+    h = A.Apic(64, 64, 1 / 64, props)
+    h.set_particles(np.zeros(0, np.float32), np.zeros(0, np.float32))
+    h.update(A.DebugOptions(), 1 / 60)
+    assert h.num_particles == 0
+
+
+def test_odd_side_rejected(gpu_lib):
+    # src/apic.rs:910 panics when no multigrid level exists; the C-ABI returns an error
+    with pytest.raises(A.ApicError) as ei:
+        A.Apic(66 + 1, 64, 1 / 64, A.WorldProperties())
+    assert ei.value.code == A.ERR_INVALID_ARG
+
+
+def test_nonfinite_particle_is_reported(gpu_lib):
+    props = A.WorldProperties()
+    g = A.Apic(64, 64, 1 / 64, props)
+    x = g.read_field("pos_x")
+    x[5] = np.nan
+    g.write_field("pos_x", x)
+    g.update(A.DebugOptions(), 1 / 60)
+    assert g.stats().nonfinite_lanes > 0
+
+
+@pytest.mark.parametrize("mode", [A.SOLVER_REL_FP32, A.SOLVER_REL_MIXED])
+def test_relative_solver_modes(oracle_mod, mode):
+    props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+    side = 128
+    cs = 1 / side
+    scene = A.scene_params(A.SCENE_DAM_BREAK, side, cell_size=cs, sub=2, seed=0, fluid_x=0.4, fluid_y=0.6)
+    o, g = make_pair(oracle_mod, side, cs, props, scene)
+    for s in (o, g):
+        s.set_solver(mode, 1e-6, 500)
+    opts = A.DebugOptions()
+    for _ in range(8):
+        o.update(opts, 1 / 240)
+        g.update(opts, 1 / 240)
+    sg, so = g.stats(), o.stats()
+    assert sg.pcg_iterations > 0
+    if mode == A.SOLVER_REL_MIXED:
+        assert sg.true_residual_rel <= 1e-6, sg.true_residual_rel
+        assert so.true_residual_rel <= 1e-6, so.true_residual_rel
+    else:
+        assert sg.true_residual_rel <= 1e-4
