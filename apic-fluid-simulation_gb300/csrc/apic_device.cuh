@@ -164,8 +164,9 @@ __device__ __forceinline__ float warp_maxf(float v) {
 }
 
 // Deterministic block sum into partials[blockIdx.x]; returns true in the last
-// block to finish, whose thread 0 receives the total of all partials summed in
-// block order (threadfence reduction; no block waits on another).
+// block to finish, whose thread 0 receives the total of all partials (summed
+// by a fixed strided pattern and tree, so the result does not depend on
+// scheduling; no block waits on another).
 template <int kThreads>
 __device__ __forceinline__ bool block_sum_last(double v, double* partials, uint32_t* counter, double* total) {
     __shared__ double s_w[kThreads / 32];
@@ -185,11 +186,52 @@ __device__ __forceinline__ bool block_sum_last(double v, double* partials, uint3
     __syncthreads();
     if (!s_last) return false;
     __threadfence();
+    const volatile double* vp = partials;
+    double t = 0;
+    for (uint32_t b = threadIdx.x; b < gridDim.x; b += kThreads) t += vp[b];
+    t = warp_sum(t);
+    __syncthreads();
+    if (lane == 0) s_w[warp] = t;
+    __syncthreads();
     if (threadIdx.x == 0) {
-        double t = 0;
-        volatile double* vp = partials;
-        for (uint32_t b = 0; b < gridDim.x; ++b) t += vp[b];
-        *total = t;
+        double a = 0;
+        for (int w = 0; w < kThreads / 32; ++w) a += s_w[w];
+        *total = a;
+        *counter = 0;
+    }
+    return true;
+}
+
+// Same pattern for a maximum of non-negative values (exact in any order).
+template <int kThreads>
+__device__ __forceinline__ bool block_max_last(float v, double* partials, uint32_t* counter, float* total) {
+    __shared__ float s_m[kThreads / 32];
+    __shared__ bool s_last;
+    v = warp_maxf(v);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_m[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float b = 0.0f;
+        for (int w = 0; w < kThreads / 32; ++w) b = fmaxf(b, s_m[w]);
+        partials[blockIdx.x] = double(b);
+        __threadfence();
+        s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    const volatile double* vp = partials;
+    float t = 0.0f;
+    for (uint32_t b = threadIdx.x; b < gridDim.x; b += kThreads) t = fmaxf(t, float(vp[b]));
+    t = warp_maxf(t);
+    __syncthreads();
+    if (lane == 0) s_m[warp] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.0f;
+        for (int w = 0; w < kThreads / 32; ++w) a = fmaxf(a, s_m[w]);
+        *total = a;
         *counter = 0;
     }
     return true;

@@ -63,6 +63,7 @@ struct Ctl {
     uint32_t not_converged;
     uint32_t refinements;
     uint32_t inner_cap;     // iteration cap of the running (inner) solve
+    uint32_t used_iters;    // iterations used by the refinement loop so far
     double dgamma;          // FP64 copies for the relative-tolerance modes
     double bnorm2;          // ||b||^2 of the running solve
     double rnorm2;          // ||r||^2 of the recursive residual
@@ -137,6 +138,7 @@ struct Scene {
     float* corr = nullptr;                    // correction of an inner solve (padded)
     double* p64 = nullptr;                    // FP64 pressure of the refinement loop (padded)
     double* b64 = nullptr;                    // FP64 right-hand side (padded)
+    bool p64_valid = false;                   // p64 holds the refined pressure (mixed mode)
 
     int nlevels = 0;                          // including the base (levels[0])
     Level lv[kMaxLevels];
@@ -149,6 +151,9 @@ struct Scene {
     uint32_t scan_tmp_len = 0;
 
     cudaStream_t stream = nullptr;
+    cudaStream_t cap_stream = nullptr;        // stream used to record graphs
+    cudaGraphExec_t update_exec = nullptr;    // whole Apic::update as one graph
+    cudaGraphExec_t solve_exec = nullptr;     // the pressure solve alone
     int solver_mode = APIC_SOLVER_REFERENCE;
     float rel_tol = 1e-6f;
     uint32_t max_iter = 500;
@@ -186,8 +191,7 @@ cudaError_t launch_post_forces(Scene& s);
 cudaError_t launch_extrapolate(Scene& s);
 cudaError_t launch_smoothed_view(Scene& s, float* out);
 cudaError_t launch_level_lists(Scene& s, int level);
-// solver.cu
-cudaError_t launch_solve(Scene& s);
+// solver.cu: the solve is recorded into graphs (apic_graph.h: build_solve)
 // runtime.cu
 cudaError_t launch_plan_first(Scene& s);
 cudaError_t launch_advance(Scene& s);

@@ -212,6 +212,12 @@ __global__ void __launch_bounds__(256) k_compact_write(const uint32_t* __restric
 __device__ __forceinline__ float smoothed_at(const float* sm, const float* dens, const uint32_t* fluid, uint32_t c) {
     return bit_at(fluid, c) ? sm[c] : dens[c];
 }
+// Same, for a cell index that can fall one row past the grid when a caller
+// opens the solid border (the reference reads past its array there).
+__device__ __forceinline__ float smoothed_guarded(const float* sm, const float* dens, const uint32_t* fluid,
+                                                  uint32_t c, uint32_t cells) {
+    return c < cells ? smoothed_at(sm, dens, fluid, c) : 0.0f;
+}
 
 __global__ void __launch_bounds__(kSegBlock) k_smooth_density(const uint32_t* __restrict__ fluid,
                                                                const uint32_t* __restrict__ seg,
@@ -349,10 +355,11 @@ __global__ void __launch_bounds__(256) k_gradient(uint32_t uf, uint32_t vf, int 
                                                   const float* __restrict__ p, const float* __restrict__ sm,
                                                   const float* __restrict__ dens, const float* __restrict__ post_u,
                                                   const float* __restrict__ post_v, const Ctl* __restrict__ ctl,
-                                                  int do_gradient, int do_post) {
+                                                  const double* __restrict__ p64, int do_gradient, int do_post) {
     uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= uf + vf) return;
     const float target = 9.0f;
+    const uint32_t cells = uint32_t(W) * uint32_t(H);
     const bool post = do_post && ctl->has_post;
     if (f < uf) {
         int x = int(f % uint32_t(W + 1)), y = int(f / uint32_t(W + 1));
@@ -366,10 +373,19 @@ __global__ void __launch_bounds__(256) k_gradient(uint32_t uf, uint32_t vf, int 
                 uint32_t lf = fluid_xy(fluid, x - 1, y, W, H), rf = fluid_xy(fluid, x, y, W, H);
                 float dp = 0.0f;
                 uint32_t li = uint32_t(y * W + x - 1), ri = uint32_t(y * W + x);
-                if (lf && rf) dp = p[ri] - p[li];
-                else if (lf) dp = -p[li] / theta(smoothed_at(sm, dens, fluid, ri), sm[li], target);
-                else if (rf) dp = p[ri] / theta(smoothed_at(sm, dens, fluid, li), sm[ri], target);
-                val -= dp * inv_dx;
+                if (p64) {
+                    // mixed precision: differences of the FP64 refined pressure
+                    double d = 0.0;
+                    if (lf && rf) d = p64[ri + W] - p64[li + W];
+                    else if (lf) d = -p64[li + W] / double(theta(smoothed_guarded(sm, dens, fluid, ri, cells), sm[li], target));
+                    else if (rf) d = p64[ri + W] / double(theta(smoothed_guarded(sm, dens, fluid, li, cells), sm[ri], target));
+                    val -= float(d * double(inv_dx));
+                } else {
+                    if (lf && rf) dp = p[ri] - p[li];
+                    else if (lf) dp = -p[li] / theta(smoothed_guarded(sm, dens, fluid, ri, cells), sm[li], target);
+                    else if (rf) dp = p[ri] / theta(smoothed_guarded(sm, dens, fluid, li, cells), sm[ri], target);
+                    val -= dp * inv_dx;
+                }
             }
         }
         if (post) val += post_u[f] * ctl->dt;
@@ -387,10 +403,18 @@ __global__ void __launch_bounds__(256) k_gradient(uint32_t uf, uint32_t vf, int 
                 uint32_t bf = fluid_xy(fluid, x, y - 1, W, H), tf = fluid_xy(fluid, x, y, W, H);
                 float dp = 0.0f;
                 uint32_t bi = uint32_t((y - 1) * W + x), ti = uint32_t(y * W + x);
-                if (bf && tf) dp = p[ti] - p[bi];
-                else if (bf) dp = -p[bi] / theta(smoothed_at(sm, dens, fluid, ti), sm[bi], target);
-                else if (tf) dp = p[ti] / theta(smoothed_at(sm, dens, fluid, bi), sm[ti], target);
-                val -= dp * inv_dx;
+                if (p64) {
+                    double d = 0.0;
+                    if (bf && tf) d = p64[ti + W] - p64[bi + W];
+                    else if (bf) d = -p64[bi + W] / double(theta(smoothed_guarded(sm, dens, fluid, ti, cells), sm[bi], target));
+                    else if (tf) d = p64[ti + W] / double(theta(smoothed_guarded(sm, dens, fluid, bi, cells), sm[ti], target));
+                    val -= float(d * double(inv_dx));
+                } else {
+                    if (bf && tf) dp = p[ti] - p[bi];
+                    else if (bf) dp = -p[bi] / theta(smoothed_guarded(sm, dens, fluid, ti, cells), sm[bi], target);
+                    else if (tf) dp = p[ti] / theta(smoothed_guarded(sm, dens, fluid, bi, cells), sm[ti], target);
+                    val -= dp * inv_dx;
+                }
             }
         }
         if (post) val += post_v[g] * ctl->dt;
@@ -500,7 +524,8 @@ cudaError_t launch_gradient(Scene& s, bool post) {
     uint32_t nf = s.uf + s.vf;
     k_gradient<<<div_up(nf, 256), 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), 1.0f / s.dx, s.u, s.v,
                                                        s.valid_u, s.valid_v, s.lv[0].fluid, s.obstacle, s.pressure,
-                                                       s.sm_a, s.density, s.post_u, s.post_v, s.ctl, 1, post ? 1 : 0);
+                                                       s.sm_a, s.density, s.post_u, s.post_v, s.ctl,
+                                                       s.p64_valid ? s.p64 : nullptr, 1, post ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -508,7 +533,8 @@ cudaError_t launch_post_forces(Scene& s) {
     uint32_t nf = s.uf + s.vf;
     k_gradient<<<div_up(nf, 256), 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), 1.0f / s.dx, s.u, s.v,
                                                        s.valid_u, s.valid_v, s.lv[0].fluid, s.obstacle, s.pressure,
-                                                       s.sm_a, s.density, s.post_u, s.post_v, s.ctl, 0, 1);
+                                                       s.sm_a, s.density, s.post_u, s.post_v, s.ctl, nullptr,
+                                                       0, 1);
     return cudaGetLastError();
 }
 

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "apic_device.cuh"
+#include "apic_graph.h"
 #include "apic_internal.h"
 
 using namespace apic;
@@ -78,12 +79,24 @@ __device__ void plan(Ctl* ctl) {
 __global__ void k_plan_first(Ctl* ctl) { plan(ctl); }
 
 // End of a substep (src/apic.rs:2463-2467), then plan the next one.
-__global__ void k_advance(Ctl* ctl) {
+__device__ void advance(Ctl* ctl) {
     ctl->t = ctl->t + ctl->dt;
     ctl->prev_dt = ctl->dt;
     ctl->timestamp += 1;
     ctl->substeps += 1;
     plan(ctl);
+}
+__global__ void k_advance(Ctl* ctl) { advance(ctl); }
+
+// Graph forms: the same planning, then the loop / sort conditions.
+__global__ void k_plan_first_g(Ctl* ctl, cudaGraphConditionalHandle h_sort, cudaGraphConditionalHandle h_loop) {
+    plan(ctl);
+    cudaGraphSetConditional(h_sort, (ctl->go && ctl->sort_now) ? 1u : 0u);
+    cudaGraphSetConditional(h_loop, ctl->go ? 1u : 0u);
+}
+__global__ void k_advance_g(Ctl* ctl, cudaGraphConditionalHandle h_loop) {
+    advance(ctl);
+    cudaGraphSetConditional(h_loop, ctl->go ? 1u : 0u);
 }
 
 __global__ void k_set_dt(Ctl* ctl, float dt, uint32_t has_ext, uint32_t has_post) {
@@ -189,8 +202,20 @@ void free_scene(Scene& s) {
     dfree(s.partials); dfree(s.scan_tmp);
     if (s.ev_a) cudaEventDestroy(s.ev_a);
     if (s.ev_b) cudaEventDestroy(s.ev_b);
+    if (s.update_exec) cudaGraphExecDestroy(s.update_exec);
+    if (s.solve_exec) cudaGraphExecDestroy(s.solve_exec);
+    s.update_exec = s.solve_exec = nullptr;
+    if (s.cap_stream) cudaStreamDestroy(s.cap_stream);
+    s.cap_stream = nullptr;
     if (s.stream) cudaStreamDestroy(s.stream);
     s.stream = nullptr;
+}
+
+// Graphs bake in launch shapes and solver settings: rebuild after changes.
+void invalidate_graphs(Scene& s) {
+    if (s.update_exec) cudaGraphExecDestroy(s.update_exec);
+    if (s.solve_exec) cudaGraphExecDestroy(s.solve_exec);
+    s.update_exec = s.solve_exec = nullptr;
 }
 
 // Open-face masks from the obstacle mask (update_world, src/apic.rs:918-944).
@@ -322,14 +347,78 @@ cudaError_t clear_p2g_targets(Scene& s) {
     return cudaGetLastError();
 }
 
-// One substep after planning (src/apic.rs:2446-2461).
-int run_substep(Scene& s, bool sort_now) {
+// Stages before the pressure solve (src/apic.rs:2446-2449).
+cudaError_t enqueue_pre_solve(Scene& s) {
+    cudaError_t e;
+    if ((e = clear_p2g_targets(s)) != cudaSuccess) return e;
+    if ((e = launch_p2g(s)) != cudaSuccess) return e;
+    if ((e = launch_finalize_faces(s, true, true)) != cudaSuccess) return e;
+    if ((e = launch_base_lists(s)) != cudaSuccess) return e;
+    if ((e = launch_build_pressure(s)) != cudaSuccess) return e;
+    return launch_multilevel(s);
+}
+// Stages after it (src/apic.rs:2451-2461), without the end-of-substep bookkeeping.
+cudaError_t enqueue_post_solve(Scene& s) {
+    cudaError_t e;
+    if ((e = launch_gradient(s, true)) != cudaSuccess) return e;
+    if ((e = launch_extrapolate(s)) != cudaSuccess) return e;
+    return launch_g2p(s);
+}
+
+int ensure_solve_graph(Scene& s) {
+    if (s.solve_exec) return APIC_OK;
+    GraphCursor c;
+    CK(cudaGraphCreate(&c.g, 0));
+    cudaError_t e = build_solve(s, c);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&s.solve_exec, c.g, 0);
+    cudaGraphDestroy(c.g);
+    if (e != cudaSuccess) return fail(APIC_ERR_CUDA, std::string("solve graph: ") + cudaGetErrorString(e));
+    return APIC_OK;
+}
+
+// Apic::update as one graph: plan -> IF(sort) -> WHILE(substep due) { stages; advance }.
+int ensure_update_graph(Scene& s) {
+    if (s.update_exec) return APIC_OK;
+    GraphCursor top;
+    CK(cudaGraphCreate(&top.g, 0));
+    cudaGraphConditionalHandle h_sort, h_loop;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h_sort, top.g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h_loop, top.g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess)
+        e = capture_into(s, top, [&]() {
+            k_plan_first_g<<<1, 1, 0, s.stream>>>(s.ctl, h_sort, h_loop);
+            return cudaGetLastError();
+        });
+    GraphCursor sort_body, loop_body;
+    if (e == cudaSuccess) e = add_conditional_with(top, cudaGraphCondTypeIf, h_sort, &sort_body);
+    if (e == cudaSuccess) e = capture_into(s, sort_body, [&]() { return launch_sort(s); });
+    if (e == cudaSuccess) e = add_conditional_with(top, cudaGraphCondTypeWhile, h_loop, &loop_body);
+    if (e == cudaSuccess) e = capture_into(s, loop_body, [&]() { return enqueue_pre_solve(s); });
+    if (e == cudaSuccess) e = build_solve(s, loop_body);
+    if (e == cudaSuccess)
+        e = capture_into(s, loop_body, [&]() {
+            cudaError_t r = enqueue_post_solve(s);
+            if (r != cudaSuccess) return r;
+            k_advance_g<<<1, 1, 0, s.stream>>>(s.ctl, h_loop);
+            return cudaGetLastError();
+        });
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&s.update_exec, top.g, 0);
+    cudaGraphDestroy(top.g);
+    if (e != cudaSuccess) return fail(APIC_ERR_CUDA, std::string("update graph: ") + cudaGetErrorString(e));
+    return APIC_OK;
+}
+
+// One substep launched stage by stage, each bracketed by events when
+// profiling (the graph form cannot hold event nodes inside its loops).
+int run_substep_eager(Scene& s, bool sort_now) {
+    int rc = ensure_solve_graph(s);
+    if (rc) return rc;
     if (sort_now) { StageTimer t(s, APIC_STAGE_SORT); CK(launch_sort(s)); }
     { StageTimer t(s, APIC_STAGE_P2G); CK(clear_p2g_targets(s)); CK(launch_p2g(s)); }
     { StageTimer t(s, APIC_STAGE_FORCES); CK(launch_finalize_faces(s, true, true)); CK(launch_base_lists(s)); }
     { StageTimer t(s, APIC_STAGE_BUILD); CK(launch_build_pressure(s)); }
     { StageTimer t(s, APIC_STAGE_MG); CK(launch_multilevel(s)); }
-    { StageTimer t(s, APIC_STAGE_PCG); CK(launch_solve(s)); }
+    { StageTimer t(s, APIC_STAGE_PCG); CK(cudaGraphLaunch(s.solve_exec, s.stream)); }
     { StageTimer t(s, APIC_STAGE_GRAD); CK(launch_gradient(s, true)); }
     { StageTimer t(s, APIC_STAGE_EXTRAP); CK(launch_extrapolate(s)); }
     { StageTimer t(s, APIC_STAGE_G2P); CK(launch_g2p(s)); }
@@ -418,6 +507,8 @@ int apic_create(uint32_t width, uint32_t height, float cell_size, const apic_wor
 #define AL(ptr, count) if ((e = dalloc(&(ptr), (count))) != cudaSuccess) return bail(fail(APIC_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e)))
     if ((e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking)) != cudaSuccess)
         return bail(fail(APIC_ERR_CUDA, cudaGetErrorString(e)));
+    if ((e = cudaStreamCreateWithFlags(&s.cap_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(fail(APIC_ERR_CUDA, cudaGetErrorString(e)));
     cudaEventCreate(&s.ev_a);
     cudaEventCreate(&s.ev_b);
     AL(s.pp, 1);
@@ -490,6 +581,7 @@ int apic_set_particles(apic_handle* h, uint32_t n, const float* px, const float*
         return fail(APIC_ERR_INVALID_ARG, "grid sides must be even and > 4 (no multigrid level)");
     if (uint64_t(n) + 8 > (1ull << 31)) return fail(APIC_ERR_INVALID_ARG, "too many particles");
     CK(cudaStreamSynchronize(h->s.stream));
+    invalidate_graphs(h->s);
     int rc = load_particles(h, n, px, py, vx, vy);
     if (rc == APIC_OK) CK(cudaStreamSynchronize(h->s.stream));
     return rc;
@@ -499,9 +591,11 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
     if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
     if (mode < APIC_SOLVER_REFERENCE || mode > APIC_SOLVER_REL_MIXED || !(rel_tol > 0.0f) || max_iterations == 0)
         return fail(APIC_ERR_INVALID_ARG, "bad solver configuration");
+    if (h->s.stream) cudaStreamSynchronize(h->s.stream);
     h->s.solver_mode = mode;
     h->s.rel_tol = rel_tol;
     h->s.max_iter = max_iterations;
+    invalidate_graphs(h->s);
     return APIC_OK;
 }
 
@@ -513,19 +607,23 @@ int apic_update(apic_handle* h, uint32_t flags, float frame_dt) {
     s.stats = apic_step_stats{};
     k_begin_update<<<1, 1, 0, st>>>(s.ctl, frame_dt, flags, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
     if (!s.vmax_valid) { CK(launch_vmax(s)); s.vmax_valid = true; }
-    k_plan_first<<<1, 1, 0, st>>>(s.ctl);
-    CK(cudaGetLastError());
-    bool first = true;
-    uint32_t refinements = 0;
-    for (;;) {
-        int rc = sync_ctl(s);
+    if (s.profiling) {
+        // stage-by-stage with host control of the substep loop
+        k_plan_first<<<1, 1, 0, st>>>(s.ctl);
+        CK(cudaGetLastError());
+        bool first = true;
+        for (;;) {
+            int rc = sync_ctl(s);
+            if (rc != APIC_OK) return rc;
+            if (!s.ctl_host->go) break;
+            rc = run_substep_eager(s, first && !(flags & APIC_UPDATE_DISABLE_SORT));
+            if (rc != APIC_OK) return rc;
+            first = false;
+        }
+    } else {
+        int rc = ensure_update_graph(s);
         if (rc != APIC_OK) return rc;
-        if (!s.ctl_host->go) break;
-        bool sort_now = first && !(flags & APIC_UPDATE_DISABLE_SORT);
-        rc = run_substep(s, sort_now);
-        if (rc != APIC_OK) return rc;
-        refinements += s.stats.refinement_steps;
-        first = false;
+        CK(cudaGraphLaunch(s.update_exec, st));
     }
     if (s.has_ext) { CK(cudaMemsetAsync(s.ext_u, 0, sizeof(float) * s.uf, st)); CK(cudaMemsetAsync(s.ext_v, 0, sizeof(float) * s.vf, st)); }
     if (s.has_post) { CK(cudaMemsetAsync(s.post_u, 0, sizeof(float) * s.uf, st)); CK(cudaMemsetAsync(s.post_v, 0, sizeof(float) * s.vf, st)); }
@@ -536,7 +634,7 @@ int apic_update(apic_handle* h, uint32_t flags, float frame_dt) {
     s.stats.substeps = c.substeps;
     s.stats.pcg_iterations = c.pcg_iters;
     s.stats.pcg_iterations_total = c.pcg_iters_total;
-    s.stats.refinement_steps = refinements;
+    s.stats.refinement_steps = c.refinements;
     s.stats.residual_max = bits_to_float(c.max_r_bits);
     s.stats.residual_rel = c.bnorm2 > 0 ? float(std::sqrt(c.rnorm2 / c.bnorm2)) : 0.0f;
     s.stats.true_residual_rel = c.true_rel;
@@ -753,6 +851,7 @@ int apic_write_field(apic_handle* h, int field, const void* src, uint64_t bytes)
     if (!src) return fail(APIC_ERR_INVALID_ARG, "null source");
     CK(cudaMemcpy(d.dev, src, bytes, cudaMemcpyHostToDevice));
     if (field == APIC_F_VEL_X || field == APIC_F_VEL_Y) s.vmax_valid = false;
+    if (field == APIC_F_PRESSURE) s.p64_valid = false;
     if (field == APIC_F_OBSTACLE_BITS) {
         std::memcpy(h->obstacle_host.data(), src, bytes);
         int rc = upload_world(h);
@@ -840,7 +939,9 @@ int apic_debug_run_stage(apic_handle* h, int stage, float dt) {
         case APIC_STAGE_PCG: {
             k_begin_update<<<1, 1, 0, st>>>(s.ctl, 0.0f, 0u, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
             k_set_dt<<<1, 1, 0, st>>>(s.ctl, dt, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
-            CK(launch_solve(s));
+            int rg = ensure_solve_graph(s);
+            if (rg) return rg;
+            CK(cudaGraphLaunch(s.solve_exec, st));
             int rc = sync_ctl(s);
             if (rc) return rc;
             const Ctl& c = *s.ctl_host;
@@ -849,6 +950,7 @@ int apic_debug_run_stage(apic_handle* h, int stage, float dt) {
             s.stats.residual_max = bits_to_float(c.max_r_bits);
             s.stats.true_residual_rel = c.true_rel;
             s.stats.not_converged = c.not_converged;
+            s.stats.refinement_steps = c.refinements;
             break;
         }
         case APIC_STAGE_GRAD: CK(launch_gradient(s, false)); break;

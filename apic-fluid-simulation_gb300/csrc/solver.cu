@@ -27,6 +27,7 @@
 #include <cmath>
 
 #include "apic_device.cuh"
+#include "apic_graph.h"
 #include "apic_internal.h"
 
 namespace apic {
@@ -309,32 +310,14 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* __rest
         mx = fmaxf(mx, fabsf(nr));
         acc += double(nr) * double(nr);
     }
-    double tot;
     if (mode == APIC_SOLVER_REFERENCE) {
-        // max is exact in any order; reuse the sum machinery with a max
-        __shared__ float sm[kSegWarps];
-        __shared__ bool last;
-        float m = warp_maxf(mx);
-        if (lane == 0) sm[threadIdx.x >> 5] = m;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            float b = 0.0f;
-            for (int w = 0; w < kSegWarps; ++w) b = fmaxf(b, sm[w]);
-            partials[blockIdx.x] = double(b);
-            __threadfence();
-            last = atomicAdd(&ctl->red_counter, 1u) == gridDim.x - 1;
-        }
-        __syncthreads();
-        if (last && threadIdx.x == 0) {
-            __threadfence();
-            volatile double* vp = partials;
-            double t = 0;
-            for (uint32_t b = 0; b < gridDim.x; ++b) t = fmax(t, vp[b]);
-            ctl->red_counter = 0;
-            ctl->max_r_bits = __float_as_uint(float(t));
-            if (float(t) < solve_error) ctl->pcg_done = 1;
+        float t;
+        if (block_max_last<kSegBlock>(mx, partials, &ctl->red_counter, &t) && threadIdx.x == 0) {
+            ctl->max_r_bits = __float_as_uint(t);
+            if (t < solve_error) ctl->pcg_done = 1;
         }
     } else {
+        double tot;
         if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
             ctl->rnorm2 = tot;
             double rel = ctl->bnorm2 > 0.0 ? sqrt(tot / ctl->bnorm2) : 0.0;
@@ -457,27 +440,46 @@ __global__ void __launch_bounds__(kSegBlock) k_pressure_to64(Level B, const floa
     }
 }
 
-__global__ void k_set_target(Ctl* ctl, double tol, int from_true) {
-    ctl->pcg_done = 0;
-    if (from_true) {
-        double t = ctl->true_rel > 0.0 ? tol / ctl->true_rel : 1.0;
-        ctl->target_rel = t < 1.0 ? t : 1.0;
-    } else {
-        ctl->target_rel = tol;
-    }
+// ---- loop control (device side; each sets a graph conditional) ------------
+
+// Continue the PCG loop while not converged and under the iteration cap
+// (src/apic.rs:1894-1899); dyn_cap reads the remaining budget of a refinement.
+__global__ void k_pcg_cond(const Ctl* __restrict__ ctl, cudaGraphConditionalHandle h, uint32_t cap, int dyn_cap) {
+    uint32_t c = dyn_cap ? ctl->inner_cap : cap;
+    cudaGraphSetConditional(h, (!ctl->pcg_done && ctl->pcg_iters < c) ? 1u : 0u);
 }
 
-__global__ void k_finish_solve(Ctl* ctl, int mode, uint32_t cap) {
+__global__ void k_finish_solve(Ctl* ctl, uint32_t cap) {
     ctl->pcg_iters_total += ctl->pcg_iters;
     if (ctl->pcg_iters >= cap && !ctl->pcg_done) ctl->not_converged++;
-    (void)mode;
 }
 
-// Mixed mode: iterations summed over the inner solves.
-__global__ void k_set_iters(Ctl* ctl, uint32_t total, uint32_t failed) {
-    ctl->pcg_iters = total;
-    ctl->pcg_iters_total += total;
-    ctl->not_converged += failed;
+__global__ void k_rel_begin(Ctl* ctl, double tol, uint32_t cap) {
+    ctl->target_rel = tol;
+    ctl->inner_cap = cap;
+    ctl->refinements = 0;
+    ctl->used_iters = 0;
+}
+
+// Refinement loop: go on while the FP64 true residual is above tol and
+// iterations remain; the inner solve then targets tol / true residual.
+__global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol, uint32_t cap) {
+    bool cont = ctl->true_rel > tol && ctl->used_iters < cap && ctl->refinements < 32u;
+    if (cont) {
+        ctl->refinements++;
+        ctl->inner_cap = cap - ctl->used_iters;
+        double t = ctl->true_rel > 0.0 ? tol / ctl->true_rel : 1.0;
+        ctl->target_rel = t < 1.0 ? t : 1.0;
+    }
+    cudaGraphSetConditional(h, cont ? 1u : 0u);
+}
+
+__global__ void k_refine_post(Ctl* ctl) { ctl->used_iters += ctl->pcg_iters; }
+
+__global__ void k_refine_end(Ctl* ctl, double tol) {
+    ctl->pcg_iters = ctl->used_iters;
+    ctl->pcg_iters_total += ctl->used_iters;
+    if (ctl->true_rel > tol) ctl->not_converged++;
 }
 
 #undef SEG_LOOP
@@ -511,78 +513,116 @@ static void vcycle(Scene& s) {
     k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 0, 0);
 }
 
-static bool read_done(Scene& s) {
-    cudaMemcpyAsync(&s.ctl_host->pcg_done, &s.ctl->pcg_done, sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream);
-    cudaStreamSynchronize(s.stream);
-    return s.ctl_host->pcg_done != 0;
-}
-
-// One PCG solve into `x` (pressure in the reference layout when p_padded == 0).
-// Iterations run in batches; the host reads the device flag between batches.
-static void pcg(Scene& s, int mode, float* x, int p_padded, uint32_t cap) {
-    cudaStream_t st = s.stream;
+// One PCG iteration (src/apic.rs:1899-1955); x receives alpha * s.
+static void pcg_iteration(Scene& s, int mode, float* x, int p_padded) {
     const Level& B = s.lv[0];
     uint32_t g = seg_grid(B.words);
-    k_pcg_begin<<<1, 1, 0, st>>>(s.ctl);
-    if (mode == APIC_SOLVER_REFERENCE) k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
+    cudaStream_t st = s.stream;
+    k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, s.partials, mode);
+    k_pcg_update<<<g, kSegBlock, 0, st>>>(B, x, p_padded, s.search, s.ap, s.ctl, s.partials, mode, s.props.solve_error);
     vcycle(s);
-    k_pcg_start<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl, s.partials, mode);
-    const uint32_t batch = mode == APIC_SOLVER_REFERENCE ? 2u : 8u;
-    for (uint32_t it = 0; it < cap; ++it) {
-        if (it % batch == 0 && read_done(s)) break;
-        k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, s.partials, mode);
-        k_pcg_update<<<g, kSegBlock, 0, st>>>(B, x, p_padded, s.search, s.ap, s.ctl, s.partials, mode,
-                                              s.props.solve_error);
-        vcycle(s);
-        k_dot_rz<<<g, kSegBlock, 0, st>>>(B, s.ctl, s.partials, mode);
-        k_search<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl);
-    }
+    k_dot_rz<<<g, kSegBlock, 0, st>>>(B, s.ctl, s.partials, mode);
+    k_search<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl);
 }
 
-cudaError_t launch_solve(Scene& s) {
-    cudaStream_t st = s.stream;
+// PCG setup (src/apic.rs:1885-1892) followed by a device-controlled WHILE
+// loop over iterations.
+static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p_padded, uint32_t cap, int dyn_cap,
+                             bool clear_pressure) {
+    const Level& B = s.lv[0];
+    uint32_t g = seg_grid(B.words);
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, c.g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return e;
+    e = capture_into(s, c, [&]() {
+        cudaStream_t st = s.stream;
+        k_pcg_begin<<<1, 1, 0, st>>>(s.ctl);
+        if (clear_pressure) k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
+        vcycle(s);
+        k_pcg_start<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl, s.partials, mode);
+        k_pcg_cond<<<1, 1, 0, st>>>(s.ctl, h, cap, dyn_cap);
+        return cudaGetLastError();
+    });
+    if (e != cudaSuccess) return e;
+    GraphCursor body;
+    e = add_conditional_with(c, cudaGraphCondTypeWhile, h, &body);
+    if (e != cudaSuccess) return e;
+    return capture_into(s, body, [&]() {
+        pcg_iteration(s, mode, x, p_padded);
+        k_pcg_cond<<<1, 1, 0, s.stream>>>(s.ctl, h, cap, dyn_cap);
+        return cudaGetLastError();
+    });
+}
+
+cudaError_t build_solve(Scene& s, GraphCursor& c) {
     const Level& B = s.lv[0];
     uint32_t g = seg_grid(B.words);
     int mode = s.solver_mode;
-    s.stats.refinement_steps = 0;
+    s.p64_valid = false;
+    cudaError_t e;
     if (mode == APIC_SOLVER_REFERENCE) {
-        pcg(s, mode, s.pressure, 0, 100);
-        k_finish_solve<<<1, 1, 0, st>>>(s.ctl, mode, 100);
+        e = build_pcg(s, c, mode, s.pressure, 0, 100, 0, true);
+        if (e != cudaSuccess) return e;
+        return capture_into(s, c, [&]() {
+            k_finish_solve<<<1, 1, 0, s.stream>>>(s.ctl, 100);
+            return cudaGetLastError();
+        });
+    }
+    const double tol = double(s.rel_tol);
+    e = capture_into(s, c, [&]() {
+        cudaStream_t st = s.stream;
+        k_mixed_init<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.ctl);
+        k_bnorm<<<g, kSegBlock, 0, st>>>(B, s.b64, s.ctl, s.partials);
+        k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
+        k_rel_begin<<<1, 1, 0, st>>>(s.ctl, tol, s.max_iter);
         return cudaGetLastError();
-    }
-    // relative-tolerance modes: keep b in FP64 for the true residual
-    k_mixed_init<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.ctl);
-    k_bnorm<<<g, kSegBlock, 0, st>>>(B, s.b64, s.ctl, s.partials);
-    k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
+    });
+    if (e != cudaSuccess) return e;
     if (mode == APIC_SOLVER_REL_FP32) {
-        k_set_target<<<1, 1, 0, st>>>(s.ctl, double(s.rel_tol), 0);
-        pcg(s, mode, s.pressure, 0, s.max_iter);
-        k_finish_solve<<<1, 1, 0, st>>>(s.ctl, mode, s.max_iter);
-    } else {
-        // FP64 iterative refinement: r = b - A p (FP64), FP32 PCG on A d = r, p += d.
-        uint32_t used = 0, refinements = 0, total = 0;
-        for (int outer = 0; outer < 32 && used < s.max_iter; ++outer) {
-            k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 3);
-            cudaMemcpyAsync(s.ctl_host, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
-            cudaStreamSynchronize(st);
-            if (!(s.ctl_host->true_rel > double(s.rel_tol))) break;
-            refinements++;
-            k_set_target<<<1, 1, 0, st>>>(s.ctl, double(s.rel_tol), 1);
-            pcg(s, APIC_SOLVER_REL_FP32, s.corr, 1, s.max_iter - used);
-            k_mixed_accumulate<<<g, kSegBlock, 0, st>>>(B, s.p64, s.corr, s.pressure, s.ctl, 0);
-            cudaMemcpyAsync(s.ctl_host, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
-            cudaStreamSynchronize(st);
-            used += s.ctl_host->pcg_iters;
-            total += s.ctl_host->pcg_iters;
-        }
-        k_mixed_accumulate<<<g, kSegBlock, 0, st>>>(B, s.p64, s.corr, s.pressure, s.ctl, 1);
-        k_set_iters<<<1, 1, 0, st>>>(s.ctl, total, (s.ctl_host->true_rel > double(s.rel_tol)) ? 1u : 0u);
-        s.stats.refinement_steps = refinements;
+        e = build_pcg(s, c, APIC_SOLVER_REL_FP32, s.pressure, 0, s.max_iter, 1, false);
+        if (e != cudaSuccess) return e;
+        // true residual of the FP32 pressure that the projection will use
+        return capture_into(s, c, [&]() {
+            cudaStream_t st = s.stream;
+            k_finish_solve<<<1, 1, 0, st>>>(s.ctl, s.max_iter);
+            k_pressure_to64<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.p64, s.ctl);
+            k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 1);
+            return cudaGetLastError();
+        });
     }
-    // true residual of the FP32 pressure that the projection will use
-    k_pressure_to64<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.p64, s.ctl);
-    k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 1);
-    return cudaGetLastError();
+    // APIC_SOLVER_REL_MIXED: r = b - A p in FP64, FP32 PCG on A d = r, p += d.
+    cudaGraphConditionalHandle hr;
+    e = cudaGraphConditionalHandleCreate(&hr, c.g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return e;
+    e = capture_into(s, c, [&]() {
+        cudaStream_t st = s.stream;
+        k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 3);
+        k_refine_cond<<<1, 1, 0, st>>>(s.ctl, hr, tol, s.max_iter);
+        return cudaGetLastError();
+    });
+    if (e != cudaSuccess) return e;
+    GraphCursor body;
+    e = add_conditional_with(c, cudaGraphCondTypeWhile, hr, &body);
+    if (e != cudaSuccess) return e;
+    e = build_pcg(s, body, APIC_SOLVER_REL_FP32, s.corr, 1, s.max_iter, 1, false);
+    if (e != cudaSuccess) return e;
+    e = capture_into(s, body, [&]() {
+        cudaStream_t st = s.stream;
+        k_mixed_accumulate<<<g, kSegBlock, 0, st>>>(B, s.p64, s.corr, s.pressure, s.ctl, 0);
+        k_refine_post<<<1, 1, 0, st>>>(s.ctl);
+        k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 3);
+        k_refine_cond<<<1, 1, 0, st>>>(s.ctl, hr, tol, s.max_iter);
+        return cudaGetLastError();
+    });
+    if (e != cudaSuccess) return e;
+    // the projection uses the FP64 pressure; its true residual is the one reported
+    s.p64_valid = true;
+    return capture_into(s, c, [&]() {
+        cudaStream_t st = s.stream;
+        k_mixed_accumulate<<<g, kSegBlock, 0, st>>>(B, s.p64, s.corr, s.pressure, s.ctl, 1);
+        k_refine_end<<<1, 1, 0, st>>>(s.ctl, tol);
+        return cudaGetLastError();
+    });
 }
 
 }  // namespace apic

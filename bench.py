@@ -1,0 +1,379 @@
+"""Benchmark of the GB300 APIC/FLIP step: particle-steps/s on the single large scene.
+
+Workload (N=1): 1024 x 1024 MAC grid, dx = 1/1024, dam break x < 0.5, y < 0.5
+at 4 particles per cell (seed 1) plus a disk of radius 0.08 at (0.7, 0.8)
+moving at (0, -2); gravity -9.81, cfl 5, border damping 0.1; one step = one
+Apic::update of dt = 1/480 (one frame, split into CFL substeps as the
+reference does).  The pressure solve runs FP32 MG-PCG inside FP64 iterative
+refinement to a true relative residual of 1e-6 (``--solver`` selects the plain
+FP32 or the reference's own exits).  Inputs are synthetic (deterministic
+hash-jittered particles); the state stays resident in HBM across steps.
+
+Printed JSON line: ``value`` = particles x steps / device time of the timed
+steps (CUDA events on the scene's stream, L2 flushed between steps);
+``e2e`` = the same through the C-ABI with a host force field uploaded from
+pinned memory and the particle state read back every step; ``roofline`` for
+the dominant kernel, ``cpu_baseline`` = the C++ restatement of the reference
+step (OpenMP, all host cores) on a bounded sample of the same workload.
+
+``--impl reference`` times that CPU restatement alone as the reference arm.
+Under torchrun (N > 1) each rank runs an independent replica on its own GPU
+(the single-scene path does not shard), rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "apic-fluid-simulation_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s"
+SIDE = 1024
+FRAME_DT = 1.0 / 480.0
+
+
+def scene_params(A, side=SIDE):
+    return A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=1.0 / side, sub=2, seed=1, fluid_x=0.5,
+                          fluid_y=0.5, disk=(0.7, 0.8, 0.08), disk_v=(0.0, -2.0))
+
+
+def props(A):
+    return A.WorldProperties(gravity=-9.81, border_damping=0.1, cfl=5.0, solve_error=1e-5)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.rows = []
+        if self.proc is None:
+            return
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def summary(self):
+        rows = getattr(self, "rows", [])
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return world, rank, local
+
+
+def dist_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- CPU arm --
+def cpu_restatement_rate(n_steps: int, warmup: int, budget_s: float, side: int = SIDE, threads: int = 0):
+    """Particle-steps/s of the C++ restatement of the reference step (OpenMP)."""
+    import apic_gb300 as A
+    from oracle.oracle import OracleSim
+    threads = threads or os.cpu_count() or 1
+    px, py, vx, vy = A.generate_scene(scene_params(A, side))
+    o = OracleSim(side, side, 1.0 / side, props(A), threads=threads)
+    o.set_particles(px, py, vx, vy)
+    o.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+    opts = A.DebugOptions()
+    for _ in range(warmup):
+        o.update(opts, FRAME_DT)
+    times = []
+    t_start = time.perf_counter()
+    for _ in range(n_steps):
+        t0 = time.perf_counter()
+        o.update(opts, FRAME_DT)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > budget_s:
+            break
+    n = len(px)
+    total = sum(times)
+    return {"value": n * len(times) / total, "steps": len(times), "seconds": total, "threads": threads,
+            "particles": n, "ms_per_step": 1e3 * total / len(times),
+            "p50_ms": 1e3 * float(np.percentile(times, 50)), "p99_ms": 1e3 * float(np.percentile(times, 99))}
+
+
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    r = cpu_restatement_rate(args.steps, args.warmup, budget_s=150.0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": args.gpus,
+        "steps": r["steps"], "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"dam break + disk, {SIDE}x{SIDE} MAC grid, 4 ppc, seed 1, dt=1/480",
+                   "particles": r["particles"], "solver": "FP32 MG-PCG + FP64 refinement to 1e-6"},
+        "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"],
+        "cpu_baseline": {"value": r["value"], "unit": METRIC, "cores": r["threads"], "kind": "port",
+                         "sample": f"{r['steps']} updates after {args.warmup} warm-up updates from t=0"},
+        "e2e": {"value": r["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm --
+def level_fluid_counts(A, sim):
+    info = sim.info()
+    counts = [info.fluid_cells]
+    for lvl in range(info.mg_levels):
+        bits = sim.read_field(A.mg_field("fluid_bits", lvl))
+        counts.append(int(np.unpackbits(bits.view(np.uint8)).sum()))
+    return counts
+
+
+def run_gpu_arm(args, world, rank, local):
+    import apic_gb300 as A
+    from apic_gb300 import build as gpu_build
+    gpu_build.build()
+    import torch
+
+    dev = local
+    torch.cuda.set_device(dev)
+    px, py, vx, vy = A.generate_scene(scene_params(A, args.side))
+    n = len(px)
+    sim = A.Apic(args.side, args.side, 1.0 / args.side, props(A))
+    sim.set_particles(px, py, vx, vy)
+    mode = {"mixed": A.SOLVER_REL_MIXED, "fp32": A.SOLVER_REL_FP32, "reference": A.SOLVER_REFERENCE}[args.solver]
+    sim.set_solver(mode, 1e-6, 500)
+    opts = A.DebugOptions()
+    stream_ptr = ctypes_stream(sim)
+    ext_stream = torch.cuda.ExternalStream(stream_ptr)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
+
+    for _ in range(args.warmup):
+        sim.update(opts, FRAME_DT)
+    sim.synchronize()
+
+    # ---- timed region: K updates, device time per update, L2 flushed in between
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    substeps, iters = 0, 0
+    true_res = []
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clocks:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            starts[k].record(ext_stream)
+            sim.update(opts, FRAME_DT)
+            ends[k].record(ext_stream)
+            st = sim.stats()
+            substeps += st.substeps
+            iters += st.pcg_iterations_total
+            true_res.append(st.true_residual_rel)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    dist_barrier(world)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    dev_s = sum(step_ms) / 1e3
+    dev_s_max = dist_max(dev_s, world)
+    value = world * n * args.steps / dev_s_max
+
+    # ---- e2e through the C-ABI with host buffers (pinned), copies inside the timed region
+    fu = torch.zeros(sim.field_shape(A.FIELDS["ext_force_u"])[0], dtype=torch.float32).pin_memory()
+    fv = torch.zeros(sim.field_shape(A.FIELDS["ext_force_v"])[0], dtype=torch.float32).pin_memory()
+    nc = sim.num_chunks
+    pos_h = torch.empty(nc * 16, dtype=torch.float32).pin_memory()
+    vel_h = torch.empty(nc * 16, dtype=torch.float32).pin_memory()
+    lib = sim._lib
+    e2e_steps = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(e2e_steps):
+        lib.apic_write_field(sim._h, A.FIELDS["ext_force_u"], fu.data_ptr(), fu.numel() * 4)
+        lib.apic_write_field(sim._h, A.FIELDS["ext_force_v"], fv.data_ptr(), fv.numel() * 4)
+        sim.update(opts, FRAME_DT)
+        lib.apic_read_vec2x8(sim._h, 0, A.ctypes.cast(pos_h.data_ptr(), A._FP), nc * 16)
+        lib.apic_read_vec2x8(sim._h, 1, A.ctypes.cast(vel_h.data_ptr(), A._FP), nc * 16)
+    e2e_s = dist_max(time.perf_counter() - te, world)
+    e2e_value = world * n * e2e_steps / e2e_s
+    h2d = (fu.numel() + fv.numel()) * 4
+    d2h = 2 * nc * 16 * 4
+
+    # ---- per-stage device times (events around each stage) for the roofline
+    sim.set_profiling(True)
+    sim.reset_stage_times()
+    prof_steps = max(1, min(args.steps, 5))
+    prof_sub = 0
+    prof_iters = 0
+    for _ in range(prof_steps):
+        sim.update(opts, FRAME_DT)
+        prof_sub += sim.stats().substeps
+        prof_iters += sim.stats().pcg_iterations_total
+    stages = sim.stage_times()
+    sim.set_profiling(False)
+    counts = level_fluid_counts(A, sim)
+    peak, peak_kind = peaks()
+    roof = roofline(stages, prof_sub, prof_iters, n, sim, counts, peak, peak_kind)
+
+    result = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline and world == 1:
+            c = cpu_restatement_rate(n_steps=args.cpu_steps, warmup=1, budget_s=args.cpu_budget, side=args.side)
+            cpu = {"value": c["value"], "unit": METRIC, "cores": c["threads"], "kind": "port",
+                   "sample": f"C++ restatement of the reference step (OpenMP), {c['steps']} updates of the same "
+                             f"scene after 1 warm-up update, {c['seconds']:.1f} s"}
+        result = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dev_s_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"dam break + disk, {args.side}x{args.side} MAC grid, dx=1/{args.side}, 4 ppc, "
+                                   f"seed 1, dt=1/480 per step", "particles": n,
+                       "solver": {"mixed": "FP32 MG-PCG + FP64 refinement, true rel. residual <= 1e-6",
+                                  "fp32": "FP32 MG-PCG to recursive rel. residual 1e-6",
+                                  "reference": "reference exits (max|r| < 1e-5, 100 iterations)"}[args.solver],
+                       "substeps": substeps, "pcg_iterations": iters,
+                       "true_residual_rel_max": max(true_res) if true_res else None,
+                       "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
+            "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
+            "wall_s": wall,
+            "clocks": clocks.summary(),
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": e2e_steps,
+                    "what": "apic_write_field(ext force u,v) from pinned host + apic_update + "
+                            "apic_read_vec2x8(positions, velocities) to pinned host"},
+            "gpu_launches": None,
+            "roofline": roof,
+            "stage_ms_per_step": {k: v[0] / prof_steps for k, v in stages.items() if v[1]},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(result), flush=True)
+    sim.close()
+    return result
+
+
+def ctypes_stream(sim) -> int:
+    import ctypes
+    out = ctypes.c_void_p()
+    sim._lib.apic_get_stream(sim._h, ctypes.byref(out))
+    return int(out.value or 0)
+
+
+def roofline(stages, substeps, iters, n, sim, counts, peak, peak_kind):
+    """Roofline of the stage with the largest device time (HBM bound)."""
+    info = sim.info()
+    W = H = info.width
+    U, V, C = (W + 1) * H, W * (H + 1), W * H
+    npad = info.num_chunks * 8
+    f0 = counts[0]
+    fl = sum(counts[1:])
+    # algorithmic bytes of one launch of each stage (per substep)
+    alg = {
+        "g2p": 48 * npad + 4 * (U + V),
+        "p2g": 36 * n + 8 * (U + V) + 4 * C,
+        "pcg": (132 * f0 + 76 * fl) * (iters / max(substeps, 1)),
+        "extrap": 4 * 10 * (U + V),
+        "grad": 8 * (U + V) + 4 * C,
+        "build": 3 * 8 * f0 + 36 * f0,
+        "forces": 5 * (U + V),
+        "mg": 32 * fl,
+        "sort": (184 - 128 + 16 * 3) * n,
+    }
+    dom = max((k for k in stages if stages[k][1]), key=lambda k: stages[k][0])
+    ms, launches = stages[dom]
+    avg_s = ms / 1e3 / max(launches, 1)
+    achieved = alg.get(dom, 0) / avg_s / 1e9 if avg_s > 0 else 0.0
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+            "algorithmic_bytes_per_launch": alg.get(dom), "avg_launch_ms": avg_s * 1e3}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--solver", default="mixed", choices=["mixed", "fp32", "reference"])
+    ap.add_argument("--side", type=int, default=SIDE)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--cpu-budget", type=float, default=30.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+    else:
+        run_gpu_arm(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

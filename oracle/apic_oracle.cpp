@@ -310,6 +310,8 @@ template <class T> struct Sim : SimBase {
     uint32_t max_iter = 500;
     bool world_ready = false;
     apic_step_stats stats{};
+    std::vector<double> p64;   // refined FP64 pressure of the mixed mode (padded layout)
+    bool p64_valid = false;
 
     bool par() const { return threads > 1; }
     size_t npad() const { return size_t(num_chunks) * 8; }
@@ -1001,8 +1003,12 @@ template <class T> struct Sim : SimBase {
             size_t i = base.fluid[k];
             pressure[i - width] = T(p64[i]);
         }
+        // the mixed mode projects with the FP64 pressure; the plain mode with the FP32 one
         std::vector<double> pf(n, 0.0);
-        for (size_t k = 0; k < fluid_cells; ++k) pf[base.fluid[k]] = double(pressure[base.fluid[k] - width]);
+        if (mixed) pf = p64;
+        else
+            for (size_t k = 0; k < fluid_cells; ++k) pf[base.fluid[k]] = double(pressure[base.fluid[k] - width]);
+        if (mixed) { this->p64 = p64; p64_valid = true; }
         double tr = true_residual(b, pf, &r64);
         stats.true_residual_rel = tr;
         if (mixed && tr > double(rel_tol)) stats.not_converged++;
@@ -1014,6 +1020,7 @@ template <class T> struct Sim : SimBase {
     }
 
     void solve() {
+        p64_valid = false;
         if (solver_mode == APIC_SOLVER_REFERENCE) solve_pcg_reference();
         else solve_pcg_relative(solver_mode == APIC_SOLVER_REL_MIXED);
         stats.pcg_iterations_total += stats.pcg_iterations;
@@ -1034,6 +1041,14 @@ template <class T> struct Sim : SimBase {
                 bool lf = is_fluid(lx, y) == 1, rf = is_fluid(x, y) == 1;
                 T dp = 0;
                 size_t li = size_t(y * W + lx), ri = size_t(y * W + x);
+                if (p64_valid) {  // mixed mode: FP64 pressure differences
+                    double d = 0.0;
+                    if (lf && rf) d = p64[ri + W] - p64[li + W];
+                    else if (lf) d = -p64[li + W] / double(theta(smoothed[ri], smoothed[li], target));
+                    else if (rf) d = p64[ri + W] / double(theta(smoothed[li], smoothed[ri], target));
+                    mac_u[f] -= T(d * double(inv));
+                    continue;
+                }
                 if (lf && rf) dp = pressure[ri] - pressure[li];
                 else if (lf) { T th = theta(smoothed[ri], smoothed[li], target); dp = -pressure[li] / th; }
                 else if (rf) { T th = theta(smoothed[li], smoothed[ri], target); dp = pressure[ri] / th; }
@@ -1049,6 +1064,14 @@ template <class T> struct Sim : SimBase {
                 bool bf = is_fluid(x, by) == 1, tf = is_fluid(x, y) == 1;
                 T dp = 0;
                 size_t bi = size_t(by * W + x), ti = size_t(y * W + x);
+                if (p64_valid) {
+                    double d = 0.0;
+                    if (bf && tf) d = p64[ti + W] - p64[bi + W];
+                    else if (bf) d = -p64[bi + W] / double(theta(smoothed[ti], smoothed[bi], target));
+                    else if (tf) d = p64[ti + W] / double(theta(smoothed[bi], smoothed[ti], target));
+                    mac_v[f] -= T(d * double(inv));
+                    continue;
+                }
                 if (bf && tf) dp = pressure[ti] - pressure[bi];
                 else if (bf) { T th = theta(smoothed[ti], smoothed[bi], target); dp = -pressure[bi] / th; }
                 else if (tf) { T th = theta(smoothed[bi], smoothed[ti], target); dp = pressure[ti] / th; }
@@ -1487,6 +1510,7 @@ int oracle_write_field(oracle_sim* o, int field, const void* src, uint64_t bytes
         if (field == APIC_F_SORT_KEYS || field == APIC_F_SORT_VALS || field == APIC_F_FLUID_LIST)
             return APIC_ERR_INVALID_ARG;
         if (bytes) std::memcpy(r.ptr, src, bytes);
+        if (field == APIC_F_PRESSURE) s.p64_valid = false;
         if (field == APIC_F_FLUID_BITS) s.rebuild_base_lists();
         if (field == APIC_F_OBSTACLE_BITS) s.update_world();
         return APIC_OK;

@@ -214,20 +214,46 @@ def test_lockstep_random_velocities_odd_count(oracle_mod):
 
 
 def test_full_update_drift(oracle_mod):
-    """Whole updates with no re-sync: report the drift from the oracle."""
+    """Whole updates with no re-sync: the drift from the oracle stays small.
+
+    Sorting is disabled so that slot k holds the same particle on both sides
+    (a sort reorders particles whose cells differ by last-bit rounding).
+    """
     props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
     side = 64
     o, g = make_pair(oracle_mod, side, 1 / side, props)
-    opts = A.DebugOptions()
-    for _ in range(20):
+    opts = A.DebugOptions(disable_particle_sort=True)
+    n = o.info().num_particles
+    worst = 0.0
+    for k in range(20):
         o.update(opts, 1 / 60)
         g.update(opts, 1 / 60)
-    assert g.timestamp == o.info().timestamp
-    n = o.info().num_particles
-    for f in ("pos_x", "pos_y"):
-        d = np.abs(g.read_field(f)[:n].astype(np.float64) - o.read_field(f)[:n])
-        print(f"drift after 20 updates, {f}: max {np.max(d):.3e} mean {np.mean(d):.3e} (cell {1 / side:.3e})")
-        assert np.max(d) < 0.5 / side, f"{f} drift {np.max(d)}"
+        if g.timestamp != o.info().timestamp:
+            break  # one side split a frame into one more CFL substep; stop comparing
+        for f in ("pos_x", "pos_y"):
+            d = np.abs(g.read_field(f)[:n].astype(np.float64) - o.read_field(f)[:n])
+            worst = max(worst, float(np.max(d)))
+    print(f"max position drift over {k + 1} updates: {worst:.3e} (cell {1 / side:.3e})")
+    assert worst < 0.25 / side
+
+
+def test_graph_and_staged_paths_agree(gpu_lib):
+    """apic_update as one CUDA graph vs stage-by-stage launches (profiling)."""
+    props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+    side = 64
+    a = A.Apic(side, side, 1 / side, props)
+    b = A.Apic(side, side, 1 / side, props)
+    b.set_profiling(True)
+    opts = A.DebugOptions(disable_particle_sort=True)
+    for _ in range(3):
+        a.update(opts, 1 / 60)
+        b.update(opts, 1 / 60)
+    assert a.timestamp == b.timestamp
+    times = b.stage_times()
+    assert times["pcg"][1] == b.timestamp and times["g2p"][1] == b.timestamp
+    for f in ("pos_x", "pos_y", "vel_x", "vel_y"):
+        d = np.max(np.abs(a.read_field(f).astype(np.float64) - b.read_field(f)))
+        assert d < 1e-4, (f, d)
 
 
 def test_disable_sort_keeps_order(oracle_mod):
