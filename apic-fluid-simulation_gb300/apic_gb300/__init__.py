@@ -30,13 +30,13 @@ FIELDS = {
     "u": 16, "v": 17, "valid_u": 18, "valid_v": 19,
     "density": 24, "smoothed_density": 25, "pressure": 26,
     "fluid_bits": 32, "obstacle_bits": 33, "u_open_bits": 34, "v_open_bits": 35,
-    "residual": 40, "diag": 41, "inv_diag": 42, "plus_x": 43, "plus_y": 44,
+    "residual": 40, "diag": 41, "inv_diag": 42, "plus_x": 43, "plus_y": 44, "error": 45,
     "sort_keys": 48, "sort_vals": 49, "fluid_list": 52,
     "ext_force_u": 56, "ext_force_v": 57, "post_force_u": 58, "post_force_v": 59,
 }
 MG_FIELDS = {"fluid_bits": 64, "diag": 65, "inv_diag": 66, "plus_x": 67, "plus_y": 68}
 MG_LEVEL_STRIDE = 256
-STAGES = ["sort", "p2g", "forces", "build", "mg", "pcg", "grad", "post", "extrap", "g2p", "vmax"]
+STAGES = ["sort", "p2g", "forces", "build", "mg", "pcg", "grad", "post", "extrap", "g2p", "vmax", "vcycle"]
 PARTICLE_FIELDS = ["pos_x", "pos_y", "vel_x", "vel_y", "cu_x", "cu_y", "cv_x", "cv_y", "tres"]
 
 

@@ -141,6 +141,8 @@ struct Scene {
     bool p64_valid = false;                   // p64 holds the refined pressure (mixed mode)
 
     int nlevels = 0;                          // including the base (levels[0])
+    int tail_first = 0;                       // first level of the shared-memory tail (nlevels: none)
+    size_t tail_smem = 0;
     Level lv[kMaxLevels];
     float *cg_s = nullptr, *cg_ap = nullptr, *cg_r = nullptr;  // coarsest level CG
 
@@ -192,6 +194,9 @@ cudaError_t launch_extrapolate(Scene& s);
 cudaError_t launch_smoothed_view(Scene& s, float* out);
 cudaError_t launch_level_lists(Scene& s, int level);
 // solver.cu: the solve is recorded into graphs (apic_graph.h: build_solve)
+// vcycle.cu
+void plan_vcycle(Scene& s);     // pick the coarse levels that run in one CTA
+void enqueue_vcycle(Scene& s);  // z = M^-1 r on s.stream
 // runtime.cu
 cudaError_t launch_plan_first(Scene& s);
 cudaError_t launch_advance(Scene& s);

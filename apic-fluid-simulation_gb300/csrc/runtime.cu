@@ -55,6 +55,7 @@ __global__ void k_begin_update(Ctl* ctl, float frame_dt, uint32_t flags, uint32_
     ctl->has_ext = has_ext;
     ctl->has_post = has_post;
     ctl->status = 0;
+    ctl->pcg_done = 0;
 }
 
 // Substep size (src/apic.rs:2433-2441) and the loop condition (:2432).
@@ -536,6 +537,7 @@ int apic_create(uint32_t width, uint32_t height, float cell_size, const apic_wor
         Level& C = s.lv[s.nlevels - 1];
         AL(s.cg_s, C.padded); AL(s.cg_ap, C.padded); AL(s.cg_r, C.padded);
     }
+    plan_vcycle(s);
     AL(s.ctl, 1);
     AL(s.partials, 2 * kMaxRedBlocks);
     s.scan_tmp_len = 3 * (div_up(max_words, 1024) + 1);
@@ -754,6 +756,7 @@ FieldDesc describe(apic_handle* h, int id, const PartPtrs* pp) {
         case APIC_F_INV_DIAG: F(s.lv[0].inv_diag, padded); return d;
         case APIC_F_PLUS_X: F(s.lv[0].px, padded); return d;
         case APIC_F_PLUS_Y: F(s.lv[0].py, padded); return d;
+        case APIC_F_ERROR: F(s.lv[0].err, padded); return d;
         case APIC_F_SORT_KEYS: d = {s.keys, s.n, 4, kU32, true}; return d;
         case APIC_F_SORT_VALS: d = {s.vals, s.n, 4, kU32, true}; return d;
         case APIC_F_FLUID_LIST: d = {nullptr, 0, 4, kU32, true}; return d;  // derived on read
@@ -961,6 +964,11 @@ int apic_debug_run_stage(apic_handle* h, int stage, float dt) {
             break;
         }
         case APIC_STAGE_VMAX: CK(launch_vmax(s)); s.vmax_valid = true; break;
+        case APIC_STAGE_VCYCLE:
+            k_begin_update<<<1, 1, 0, st>>>(s.ctl, 0.0f, 0u, 0u, 0u);  // clears the solve's done flag
+            enqueue_vcycle(s);
+            CK(cudaGetLastError());
+            break;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown stage");
     }
     CK(cudaStreamSynchronize(st));

@@ -33,7 +33,6 @@
 namespace apic {
 namespace {
 
-constexpr float kOmega = 1.2f;
 constexpr float kSafety = 1e-5f;  // SAFTY, src/apic.rs:8
 
 #define SEG_LOOP(level_idx)                                                        \
@@ -49,178 +48,6 @@ __global__ void k_pcg_begin(Ctl* ctl) {
     ctl->alpha = 0.0f;
     ctl->beta = 0.0f;
     ctl->rnorm2 = 0.0;
-}
-
-// src/apic.rs:471-535 for one colour.  init: first sweep after the level's
-// error was zero-filled (src/apic.rs:1792 and :540); own and not yet swept
-// neighbour values are zero then.
-__global__ void __launch_bounds__(kSegBlock) k_smooth(Level L, int li, const Ctl* __restrict__ ctl, int color, int init) {
-    if (ctl->pcg_done) return;
-    SEG_LOOP(li) {
-        uint32_t word = L.seg[s_];
-        uint32_t bits = L.fluid[word];
-        if (!((bits >> lane) & 1u)) continue;
-        long long raw = (long long)word * 32 + lane;
-        uint32_t x = uint32_t(raw) % L.w, y = uint32_t(raw) / L.w;
-        if (int((x + y) & 1u) != color) continue;
-        uint32_t c = uint32_t(raw) + L.w;
-        float inv = L.inv_diag[c];
-        if (inv != 0.0f) {
-            float old = init ? 0.0f : L.err[c];
-            float sum = L.res[c];
-            if (!(init && color == 0)) {
-                const long long W = L.w;
-                if (fluid_raw(L.fluid, raw + 1, L.cells)) sum = __fmaf_rn(-L.px[c], L.err[c + 1], sum);
-                if (fluid_raw(L.fluid, raw + W, L.cells)) sum = __fmaf_rn(-L.py[c], L.err[c + W], sum);
-                if (fluid_raw(L.fluid, raw - 1, L.cells)) sum = __fmaf_rn(-L.px[c - 1], L.err[c - 1], sum);
-                if (fluid_raw(L.fluid, raw - W, L.cells)) sum = __fmaf_rn(-L.py[c - W], L.err[c - W], sum);
-            }
-            float gs = sum * inv;
-            L.err[c] = old + (kOmega * (gs - old));
-        } else if (init) {
-            L.err[c] = 0.0f;
-        }
-    }
-}
-
-// restrict, src/apic.rs:537-594: coarse residual of each coarse fluid cell.
-__global__ void __launch_bounds__(kSegBlock) k_restrict(Level f, Level c, int lc, const Ctl* __restrict__ ctl) {
-    if (ctl->pcg_done) return;
-    SEG_LOOP(lc) {
-        uint32_t word = c.seg[s_];
-        uint32_t bits = c.fluid[word];
-        if (!((bits >> lane) & 1u)) continue;
-        uint32_t rc = word * 32 + lane;
-        uint32_t cx = rc % c.w, cy = rc / c.w;
-        float sum = 0.0f;
-        for (uint32_t dy = 0; dy < 2; ++dy)
-            for (uint32_t dx = 0; dx < 2; ++dx) {
-                uint32_t fx = cx * 2 + dx, fy = cy * 2 + dy;
-                long long rf = (long long)fy * f.w + fx;
-                if (!fluid_raw(f.fluid, rf, f.cells)) continue;
-                uint32_t pf = uint32_t(rf) + f.w;
-                const long long W = f.w;
-                float b = f.res[pf];
-                float ax = f.diag[pf] * f.err[pf];
-                if (fluid_raw(f.fluid, rf + 1, f.cells)) ax += f.px[pf] * f.err[pf + 1];
-                if (fluid_raw(f.fluid, rf + W, f.cells)) ax += f.py[pf] * f.err[pf + W];
-                if (fluid_raw(f.fluid, rf - 1, f.cells)) ax += f.px[pf - 1] * f.err[pf - 1];
-                if (fluid_raw(f.fluid, rf - W, f.cells)) ax += f.py[pf - W] * f.err[pf - W];
-                sum += b - ax;
-            }
-        c.res[rc + c.w] = sum;
-    }
-}
-
-// prolongate, src/apic.rs:596-616.
-__global__ void __launch_bounds__(kSegBlock) k_prolong(Level c, Level f, int lf, const Ctl* __restrict__ ctl, int base) {
-    if (ctl->pcg_done) return;
-    const uint32_t last = ctl->last_fluid, extra = ctl->pad_count;
-    SEG_LOOP(lf) {
-        uint32_t word = f.seg[s_];
-        uint32_t bits = f.fluid[word];
-        if (!((bits >> lane) & 1u)) continue;
-        uint32_t rf = word * 32 + lane;
-        uint32_t pf = rf + f.w;
-        uint32_t cx = (rf % f.w) / 2, cy = (rf / f.w) / 2;
-        float ec = c.err[cy * c.w + cx + c.w];
-        float e = f.err[pf] + ec;
-        if (base && pf == last)
-            for (uint32_t k = 0; k < extra; ++k) e += ec;
-        f.err[pf] = e;
-    }
-}
-
-// solve_coarse_exact, src/apic.rs:618-704, in one CTA.
-constexpr int kCoarseThreads = 1024;
-__device__ __forceinline__ double cta_sum(double v, double* sh) {
-    v = warp_sum(v);
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[warp] = v;
-    __syncthreads();
-    double t = 0;
-    for (int w = 0; w < kCoarseThreads / 32; ++w) t += sh[w];
-    return t;
-}
-__device__ __forceinline__ float cta_max(float v, float* sh) {
-    v = warp_maxf(v);
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[warp] = v;
-    __syncthreads();
-    float t = 0.0f;
-    for (int w = 0; w < kCoarseThreads / 32; ++w) t = fmaxf(t, sh[w]);
-    return t;
-}
-
-__global__ void __launch_bounds__(kCoarseThreads) k_coarse_solve(Level L, float* __restrict__ cs,
-                                                                 float* __restrict__ cap, float* __restrict__ cr,
-                                                                 const Ctl* __restrict__ ctl) {
-    if (ctl->pcg_done) return;
-    __shared__ double shd[32];
-    __shared__ float shf[32];
-    const long long W = L.w;
-    uint32_t nf = 0;
-    double g = 0;
-    for (uint32_t r = threadIdx.x; r < L.cells; r += kCoarseThreads) {
-        uint32_t c = r + L.w;
-        if (bit_at(L.fluid, r)) {
-            float rv = L.res[c];
-            L.err[c] = 0.0f;
-            cr[c] = rv;
-            cs[c] = rv;
-            g += double(rv * rv);
-            nf++;
-        }
-    }
-    float gamma = float(cta_sum(g, shd));
-    uint32_t nfl = uint32_t(cta_sum(double(nf), shd));
-    if (gamma < 1e-12f) return;
-    uint32_t max_it = min(nfl, 100u);
-    for (uint32_t it = 0; it < max_it; ++it) {
-        __syncthreads();
-        double d = 0;
-        for (uint32_t r = threadIdx.x; r < L.cells; r += kCoarseThreads) {
-            if (!bit_at(L.fluid, r)) continue;
-            uint32_t c = r + L.w;
-            float v = L.diag[c] * cs[c];
-            if (fluid_raw(L.fluid, (long long)r + 1, L.cells)) v = __fmaf_rn(L.px[c], cs[c + 1], v);
-            if (fluid_raw(L.fluid, (long long)r - 1, L.cells)) v = __fmaf_rn(L.px[c - 1], cs[c - 1], v);
-            if (fluid_raw(L.fluid, (long long)r + W, L.cells)) v = __fmaf_rn(L.py[c], cs[c + W], v);
-            if (fluid_raw(L.fluid, (long long)r - W, L.cells)) v = __fmaf_rn(L.py[c - W], cs[c - W], v);
-            cap[c] = v;
-            d += double(cs[c] * v);
-        }
-        float delta = float(cta_sum(d, shd));
-        if (fabsf(delta) < kSafety) break;
-        float alpha = gamma / delta;
-        float me = 0.0f;
-        for (uint32_t r = threadIdx.x; r < L.cells; r += kCoarseThreads) {
-            if (!bit_at(L.fluid, r)) continue;
-            uint32_t c = r + L.w;
-            L.err[c] = L.err[c] + alpha * cs[c];
-            float nr = cr[c] - alpha * cap[c];
-            cr[c] = nr;
-            me = fmaxf(me, fabsf(nr));
-        }
-        float max_err = cta_max(me, shf);
-        if (max_err < 1e-6f) break;
-        double ng = 0;
-        for (uint32_t r = threadIdx.x; r < L.cells; r += kCoarseThreads) {
-            if (!bit_at(L.fluid, r)) continue;
-            uint32_t c = r + L.w;
-            ng += double(cr[c] * cr[c]);
-        }
-        float new_gamma = float(cta_sum(ng, shd));
-        float beta = new_gamma / gamma;
-        gamma = new_gamma;
-        for (uint32_t r = threadIdx.x; r < L.cells; r += kCoarseThreads) {
-            if (!bit_at(L.fluid, r)) continue;
-            uint32_t c = r + L.w;
-            cs[c] = cr[c] + (beta * cs[c]);
-        }
-    }
 }
 
 // ---- PCG kernels on the base level ---------------------------------------
@@ -462,14 +289,17 @@ __global__ void k_rel_begin(Ctl* ctl, double tol, uint32_t cap) {
 }
 
 // Refinement loop: go on while the FP64 true residual is above tol and
-// iterations remain; the inner solve then targets tol / true residual.
+// iterations remain.  Each inner FP32 solve reduces its own right-hand side
+// (the current true residual) by kInnerReduction, or down to tol / 2 of ||b||
+// when that is reached first; FP32 cannot usefully reduce it further.
+constexpr double kInnerReduction = 1e-4;
 __global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol, uint32_t cap) {
     bool cont = ctl->true_rel > tol && ctl->used_iters < cap && ctl->refinements < 32u;
     if (cont) {
         ctl->refinements++;
         ctl->inner_cap = cap - ctl->used_iters;
-        double t = ctl->true_rel > 0.0 ? tol / ctl->true_rel : 1.0;
-        ctl->target_rel = t < 1.0 ? t : 1.0;
+        double t = kInnerReduction * ctl->true_rel;  // target relative to ||b||
+        ctl->target_rel = t > 0.5 * tol ? t : 0.5 * tol;
     }
     cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
@@ -486,33 +316,6 @@ __global__ void k_refine_end(Ctl* ctl, double tol) {
 
 }  // namespace
 
-// One V-cycle: z = M^-1 r in lv[0].err (apply_preconditioner, src/apic.rs:1788-1821).
-static void vcycle(Scene& s) {
-    cudaStream_t st = s.stream;
-    auto grid = [&](int l) { return seg_grid(s.lv[l].words); };
-    Level* L = s.lv;
-    k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 0, 1);
-    k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 1, 1);
-    int last = s.nlevels - 1;
-    if (last >= 1) {
-        k_restrict<<<grid(1), kSegBlock, 0, st>>>(L[0], L[1], 1, s.ctl);
-        for (int l = 1; l < last; ++l) {
-            k_smooth<<<grid(l), kSegBlock, 0, st>>>(L[l], l, s.ctl, 0, 1);
-            k_smooth<<<grid(l), kSegBlock, 0, st>>>(L[l], l, s.ctl, 1, 1);
-            k_restrict<<<grid(l + 1), kSegBlock, 0, st>>>(L[l], L[l + 1], l + 1, s.ctl);
-        }
-        k_coarse_solve<<<1, kCoarseThreads, 0, st>>>(L[last], s.cg_s, s.cg_ap, s.cg_r, s.ctl);
-        for (int l = last - 1; l >= 1; --l) {
-            k_prolong<<<grid(l), kSegBlock, 0, st>>>(L[l + 1], L[l], l, s.ctl, 0);
-            k_smooth<<<grid(l), kSegBlock, 0, st>>>(L[l], l, s.ctl, 1, 0);
-            k_smooth<<<grid(l), kSegBlock, 0, st>>>(L[l], l, s.ctl, 0, 0);
-        }
-        k_prolong<<<grid(0), kSegBlock, 0, st>>>(L[1], L[0], 0, s.ctl, 1);
-    }
-    k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 1, 0);
-    k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 0, 0);
-}
-
 // One PCG iteration (src/apic.rs:1899-1955); x receives alpha * s.
 static void pcg_iteration(Scene& s, int mode, float* x, int p_padded) {
     const Level& B = s.lv[0];
@@ -520,7 +323,7 @@ static void pcg_iteration(Scene& s, int mode, float* x, int p_padded) {
     cudaStream_t st = s.stream;
     k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, s.partials, mode);
     k_pcg_update<<<g, kSegBlock, 0, st>>>(B, x, p_padded, s.search, s.ap, s.ctl, s.partials, mode, s.props.solve_error);
-    vcycle(s);
+    enqueue_vcycle(s);
     k_dot_rz<<<g, kSegBlock, 0, st>>>(B, s.ctl, s.partials, mode);
     k_search<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl);
 }
@@ -538,7 +341,7 @@ static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p
         cudaStream_t st = s.stream;
         k_pcg_begin<<<1, 1, 0, st>>>(s.ctl);
         if (clear_pressure) k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
-        vcycle(s);
+        enqueue_vcycle(s);
         k_pcg_start<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl, s.partials, mode);
         k_pcg_cond<<<1, 1, 0, st>>>(s.ctl, h, cap, dyn_cap);
         return cudaGetLastError();

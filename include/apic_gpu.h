@@ -102,6 +102,7 @@ enum apic_field {
     /* base pressure system in the reference's padded layout (index = cell + W,
      * W*H + 2W floats); only entries at fluid cells are defined */
     APIC_F_RESIDUAL = 40, APIC_F_DIAG, APIC_F_INV_DIAG, APIC_F_PLUS_X, APIC_F_PLUS_Y,
+    APIC_F_ERROR /* base multigrid error (preconditioned residual z) */,
     /* (key, val) pairs of the last Morton sort, num_particles u32 each */
     APIC_F_SORT_KEYS = 48, APIC_F_SORT_VALS,
     /* base fluid cell list: padded indices, ascending, fluid_cells u32 */
@@ -128,6 +129,7 @@ enum apic_stage {
     APIC_STAGE_EXTRAP,   /* extrapolate_velocity                  :2266-2350 */
     APIC_STAGE_G2P,      /* transfer_grid_to_particles_and_advect :2057-2264 */
     APIC_STAGE_VMAX,     /* get_max_particle_velocity             :2412-2427 */
+    APIC_STAGE_VCYCLE,   /* apply_preconditioner alone            :1788-1821 */
     APIC_STAGE_COUNT
 };
 

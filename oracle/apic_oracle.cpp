@@ -982,8 +982,10 @@ template <class T> struct Sim : SimBase {
             if (rel > double(rel_tol)) stats.not_converged++;
             for (size_t k = 0; k < fluid_cells; ++k) p64[base.fluid[k]] = double(x[base.fluid[k]]);
         } else {
+            // Each inner solve reduces its right-hand side (the current true
+            // residual) by 1e-4, or to rel_tol / 2 of ||b|| when that comes first.
             uint32_t used = 0;
-            double inner_tol = 1e-3;
+            const double inner_reduction = 1e-4;
             for (int outer = 0; outer < 32 && used < max_iter; ++outer) {
                 double tr = true_residual(b, p64, &r64);
                 if (tr <= double(rel_tol)) break;
@@ -994,7 +996,8 @@ template <class T> struct Sim : SimBase {
                     x[i] = T(0);
                 }
                 double irel = 0;
-                used += pcg_relative(x, std::max(inner_tol, double(rel_tol) / std::max(tr, 1e-30)), max_iter - used, &irel);
+                double target = std::max(inner_reduction, 0.5 * double(rel_tol) / std::max(tr, 1e-300));
+                used += pcg_relative(x, target, max_iter - used, &irel);
                 for (size_t k = 0; k < fluid_cells; ++k) p64[base.fluid[k]] += double(x[base.fluid[k]]);
             }
             stats.pcg_iterations = used;
@@ -1284,6 +1287,7 @@ template <class T> struct Sim : SimBase {
             case APIC_STAGE_EXTRAP: extrapolate(); break;
             case APIC_STAGE_G2P: g2p(dt); break;
             case APIC_STAGE_VMAX: break;
+            case APIC_STAGE_VCYCLE: precondition(); break;
             default: return APIC_ERR_INVALID_ARG;
         }
         return APIC_OK;
@@ -1324,6 +1328,7 @@ template <class T> struct Sim : SimBase {
             case APIC_F_INV_DIAG: r = ref_of(base.inv_diag, padded, 0); return true;
             case APIC_F_PLUS_X: r = ref_of(base.px, padded, 0); return true;
             case APIC_F_PLUS_Y: r = ref_of(base.py, padded, 0); return true;
+            case APIC_F_ERROR: r = ref_of(base.error, padded, 0); return true;
             case APIC_F_SORT_KEYS: r = ref_of(sort_key, sort_key.size(), 3); return true;
             case APIC_F_SORT_VALS: r = ref_of(sort_val, sort_val.size(), 3); return true;
             case APIC_F_FLUID_LIST: r = ref_of(base.fluid, fluid_cells, 3); return true;

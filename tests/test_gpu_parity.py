@@ -24,6 +24,7 @@ pytestmark = pytest.mark.gpu
 
 P2G_RTOL = 2e-5      # relative to the field's max magnitude (order of float atomics)
 PCG_RTOL = 2e-3      # pressure, relative to max |p| (FP64 vs FP32 reductions in the Krylov loop)
+VCYCLE_RTOL = 1e-5   # z = M^-1 r: smoothing/transfers exact, coarsest CG reductions FP64 vs FP32
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -117,6 +118,11 @@ def lockstep_substep(o, g, dt, sort, stats):
         idx = raw + lw
         for f in ("diag", "inv_diag", "plus_x", "plus_y"):
             eq(g.read_field(A.mg_field(f, lvl))[idx], o.read_field(A.mg_field(f, lvl))[idx], f"mg{lvl} {f}")
+    # one V-cycle on the freshly built system (apply_preconditioner, src/apic.rs:1788-1821)
+    o.run_stage("vcycle", dt)
+    g.run_stage("vcycle", dt)
+    stats.setdefault("vcycle", []).append(close(g.read_field("error")[fl], o.read_field("error")[fl], VCYCLE_RTOL,
+                                                "vcycle z"))
     o.run_stage("pcg", dt)
     g.run_stage("pcg", dt)
     so, sg = o.stats(), g.stats()
@@ -124,7 +130,9 @@ def lockstep_substep(o, g, dt, sort, stats):
     cells = fl - o.info().width
     p_o, p_g = o.read_field("pressure"), g.read_field("pressure")
     stats.setdefault("pcg_p", []).append(close(p_g[cells], p_o[cells], PCG_RTOL, "pressure"))
+    # re-sync; writing the pressure also makes both sides project with this FP32 field
     g.write_field("pressure", p_o)
+    o.write_field("pressure", p_o)
     o.run_stage("grad", dt)
     g.run_stage("grad", dt)
     for f in ("u", "v", "valid_u", "valid_v"):
@@ -188,12 +196,15 @@ def test_lockstep_reference_default_scene(oracle_mod):
     assert len(st["pcg_p"]) >= 6
 
 
-def test_lockstep_dam_break_with_forces(oracle_mod):
+@pytest.mark.parametrize("mode", [A.SOLVER_REFERENCE, A.SOLVER_REL_MIXED])
+def test_lockstep_dam_break_with_forces(oracle_mod, mode):
     props = A.WorldProperties(-9.81, 0.5, 5.0, 1e-5)
     side = 128
     cs = 1 / side
     scene = A.scene_params(A.SCENE_DAM_BREAK, side, cell_size=cs, sub=2, seed=0, fluid_x=0.4, fluid_y=0.6)
     o, g = make_pair(oracle_mod, side, cs, props, scene)
+    for sim in (o, g):
+        sim.set_solver(mode, 1e-6, 500)
     forces = {2: [(0.2, 0.3, 0.05, 150.0)], 3: [(0.25, 0.2, 0.06, -150.0)]}
     run_lockstep(o, g, 5, 1 / 240, props, cs, forces)
 
