@@ -295,6 +295,9 @@ __global__ void k_rel_begin(Ctl* ctl, double tol, uint32_t cap) {
 constexpr double kInnerReduction = 1e-4;
 __global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol, uint32_t cap) {
     bool cont = ctl->true_rel > tol && ctl->used_iters < cap && ctl->refinements < 32u;
+    // an inner solve that could not take a single step (r.z underflows or is
+    // zero) will not make progress on the next round either
+    if (ctl->refinements > 0u && ctl->pcg_iters == 0u) cont = false;
     if (cont) {
         ctl->refinements++;
         ctl->inner_cap = cap - ctl->used_iters;
