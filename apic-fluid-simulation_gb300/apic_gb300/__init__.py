@@ -24,6 +24,7 @@ OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_NONFINITE, ERR_NOT_CONV
 UPDATE_DISABLE_SORT = 0x1
 SOLVER_REFERENCE, SOLVER_REL_FP32, SOLVER_REL_MIXED = 0, 1, 2
 SCENE_REFERENCE_DEFAULT, SCENE_DAM_BREAK, SCENE_DAM_BREAK_DISK, SCENE_NOISE = 0, 1, 2, 3
+OPT_PERSISTENT_SOLVE = 1
 
 FIELDS = {
     "pos_x": 0, "pos_y": 1, "vel_x": 2, "vel_y": 3, "cu_x": 4, "cu_y": 5, "cv_x": 6, "cv_y": 7, "tres": 8,
@@ -101,6 +102,8 @@ SIGNATURES = {
     "apic_set_particles": (ctypes.c_int, [_VP, ctypes.c_uint32, _FP, _FP, _FP, _FP]),
     "apic_set_solver": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_float, ctypes.c_uint32]),
     "apic_set_profiling": (ctypes.c_int, [_VP, ctypes.c_int]),
+    "apic_set_option": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int]),
+    "apic_get_option": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "apic_get_stage_times": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]),
     "apic_reset_stage_times": (ctypes.c_int, [_VP]),
@@ -341,6 +344,14 @@ class Apic:
     @property
     def smoothed_density(self) -> np.ndarray:
         return self.read_field("smoothed_density")
+
+    def set_option(self, option: int, value: int) -> None:
+        _check(self._lib.apic_set_option(self._h, option, value), "apic_set_option")
+
+    def get_option(self, option: int) -> int:
+        v = ctypes.c_int(0)
+        _check(self._lib.apic_get_option(self._h, option, ctypes.byref(v)), "apic_get_option")
+        return v.value
 
     # -- measurement and testing hooks
     def set_profiling(self, on: bool) -> None:

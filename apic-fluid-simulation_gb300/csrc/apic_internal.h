@@ -83,6 +83,12 @@ enum : uint32_t {
     kStatusTimeout = 4u,
 };
 
+// Grid barrier state of the persistent solver (zeroed before each launch).
+struct GridSync {
+    unsigned int count;
+    unsigned int gen;
+};
+
 struct Level {
     uint32_t w = 0, h = 0, cells = 0;
     uint32_t words = 0;     // u32 mask words (even)
@@ -156,6 +162,10 @@ struct Scene {
     cudaStream_t cap_stream = nullptr;        // stream used to record graphs
     cudaGraphExec_t update_exec = nullptr;    // whole Apic::update as one graph
     cudaGraphExec_t solve_exec = nullptr;     // the pressure solve alone
+    GridSync* gsync = nullptr;                // persistent solver barrier
+    int persist_grid = 0;                     // CTAs of the persistent solver (0: unavailable)
+    size_t persist_smem = 0;
+    bool use_persistent = true;               // persistent kernel vs graph of per-phase kernels
     int solver_mode = APIC_SOLVER_REFERENCE;
     float rel_tol = 1e-6f;
     uint32_t max_iter = 500;
@@ -194,6 +204,9 @@ cudaError_t launch_extrapolate(Scene& s);
 cudaError_t launch_smoothed_view(Scene& s, float* out);
 cudaError_t launch_level_lists(Scene& s, int level);
 // solver.cu: the solve is recorded into graphs (apic_graph.h: build_solve)
+// pcg_persistent.cu
+void plan_persistent_solve(Scene& s);
+cudaError_t enqueue_persistent_solve(Scene& s);
 // vcycle.cu
 void plan_vcycle(Scene& s);     // pick the coarse levels that run in one CTA
 void enqueue_vcycle(Scene& s);  // z = M^-1 r on s.stream

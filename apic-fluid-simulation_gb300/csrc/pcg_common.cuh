@@ -1,0 +1,162 @@
+// pcg_common.cuh — per-cell PCG phases on the base level, shared by the graph
+// kernels (solver.cu) and the persistent solver (pcg_persistent.cu).
+//
+// Restates Apic::solve_pcg (src/apic.rs:1865-1956) and apply_matrix_and_dot
+// (:1823-1863).  Each phase visits the base fluid cells through the segment
+// list (one warp per non-zero 32-cell mask word) and returns this thread's
+// contribution to the phase's reduction; callers reduce deterministically.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "apic_device.cuh"
+#include "apic_internal.h"
+
+namespace apic {
+namespace pcg {
+
+#define APIC_BASE_LOOP(B, nseg, warp, nwarps)                                                   \
+    const uint32_t lane_ = threadIdx.x & 31;                                                    \
+    for (uint32_t s_ = (warp); s_ < (nseg); s_ += (nwarps))                                     \
+        if (uint32_t word_ = (B).seg[s_]; ((B).fluid[word_] >> lane_) & 1u)
+
+// pressure = 0 at fluid cells (src/apic.rs:1872-1883).
+__device__ __forceinline__ void ph_clear_pressure(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
+                                                  float* p) {
+    APIC_BASE_LOOP(B, nseg, warp, nwarps) { p[word_ * 32 + lane_] = 0.0f; }
+}
+
+// s = z; returns r.z (src/apic.rs:1887-1888).
+__device__ __forceinline__ double ph_start(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps, float* s) {
+    double acc = 0;
+    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
+        uint32_t c = word_ * 32 + lane_ + B.w;
+        float z = B.err[c], r = B.res[c];
+        s[c] = z;
+        acc += double(r * z);
+    }
+    return acc;
+}
+
+// Ap = A s (FMA chain of :1833-1846); returns s.Ap.
+__device__ __forceinline__ double ph_spmv(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
+                                          const float* s, float* ap) {
+    double acc = 0;
+    const long long W = B.w;
+    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
+        long long raw = (long long)word_ * 32 + lane_;
+        uint32_t c = uint32_t(raw) + B.w;
+        float sc = s[c];
+        float v = B.diag[c] * sc;
+        if (fluid_raw(B.fluid, raw + 1, B.cells)) v = __fmaf_rn(B.px[c], s[c + 1], v);
+        if (fluid_raw(B.fluid, raw - 1, B.cells)) v = __fmaf_rn(B.px[c - 1], s[c - 1], v);
+        if (fluid_raw(B.fluid, raw + W, B.cells)) v = __fmaf_rn(B.py[c], s[c + W], v);
+        if (fluid_raw(B.fluid, raw - W, B.cells)) v = __fmaf_rn(B.py[c - W], s[c - W], v);
+        ap[c] = v;
+        acc += double(v * sc);
+    }
+    return acc;
+}
+
+// x += alpha s (x = pressure in cell layout, or a padded vector);
+// r = fma(-alpha, Ap, r) (:1910-1928).  Returns max|r| and sum r^2.
+__device__ __forceinline__ void ph_update(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps, float alpha,
+                                          float* x, int x_padded, const float* s, const float* ap, float* max_r,
+                                          double* r2) {
+    float mx = 0.0f;
+    double acc = 0;
+    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
+        uint32_t raw = word_ * 32 + lane_;
+        uint32_t c = raw + B.w;
+        uint32_t xi = x_padded ? c : raw;
+        x[xi] = x[xi] + alpha * s[c];
+        float nr = __fmaf_rn(-alpha, ap[c], B.res[c]);
+        B.res[c] = nr;
+        mx = fmaxf(mx, fabsf(nr));
+        acc += double(nr) * double(nr);
+    }
+    *max_r = mx;
+    *r2 = acc;
+}
+
+// r.z after the preconditioner (:1936).
+__device__ __forceinline__ double ph_rz(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps) {
+    double acc = 0;
+    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
+        uint32_t c = word_ * 32 + lane_ + B.w;
+        acc += double(B.res[c] * B.err[c]);
+    }
+    return acc;
+}
+
+// s = z + beta s (:1945-1954).
+__device__ __forceinline__ void ph_search(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps, float beta,
+                                          float* s) {
+    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
+        uint32_t c = word_ * 32 + lane_ + B.w;
+        s[c] = B.err[c] + (beta * s[c]);
+    }
+}
+
+// ---- FP64 refinement (APIC_SOLVER_REL_MIXED) ---------------------------------
+
+// b64 = res, p64 = 0; returns ||b||^2.
+__device__ __forceinline__ double ph_mixed_init(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
+                                                double* b64, double* p64) {
+    double bb = 0;
+    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
+        uint32_t c = word_ * 32 + lane_ + B.w;
+        double b = double(B.res[c]);
+        b64[c] = b;
+        p64[c] = 0.0;
+        bb += b * b;
+    }
+    return bb;
+}
+
+// r64 = b64 - A p64 in FP64; flags bit 0: res = float(r64), bit 1: x = 0.
+// Returns ||r64||^2.
+__device__ __forceinline__ double ph_true_residual(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
+                                                   const double* b64, const double* p64, float* x, int flags) {
+    double rr = 0;
+    const long long W = B.w;
+    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
+        long long raw = (long long)word_ * 32 + lane_;
+        uint32_t c = uint32_t(raw) + B.w;
+        double v = double(B.diag[c]) * p64[c];
+        if (fluid_raw(B.fluid, raw + 1, B.cells)) v += double(B.px[c]) * p64[c + 1];
+        if (fluid_raw(B.fluid, raw - 1, B.cells)) v += double(B.px[c - 1]) * p64[c - 1];
+        if (fluid_raw(B.fluid, raw + W, B.cells)) v += double(B.py[c]) * p64[c + W];
+        if (fluid_raw(B.fluid, raw - W, B.cells)) v += double(B.py[c - W]) * p64[c - W];
+        double r = b64[c] - v;
+        rr += r * r;
+        if (flags & 1) B.res[c] = float(r);
+        if (flags & 2) x[c] = 0.0f;
+    }
+    return rr;
+}
+
+// p64 += x, or (finalize) pressure = float(p64).
+__device__ __forceinline__ void ph_accumulate(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
+                                              double* p64, const float* x, float* pressure, int finalize) {
+    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
+        uint32_t raw = word_ * 32 + lane_;
+        uint32_t c = raw + B.w;
+        if (!finalize) p64[c] += double(x[c]);
+        else pressure[raw] = float(p64[c]);
+    }
+}
+
+// p64 = pressure (the FP32 pressure the projection uses, for its true residual).
+__device__ __forceinline__ void ph_pressure_to64(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
+                                                 const float* pressure, double* p64) {
+    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
+        uint32_t raw = word_ * 32 + lane_;
+        p64[raw + B.w] = double(pressure[raw]);
+    }
+}
+
+#undef APIC_BASE_LOOP
+
+}  // namespace pcg
+}  // namespace apic

@@ -200,7 +200,7 @@ void free_scene(Scene& s) {
     dfree(s.ctl);
     if (s.ctl_host) cudaFreeHost(s.ctl_host);
     s.ctl_host = nullptr;
-    dfree(s.partials); dfree(s.scan_tmp);
+    dfree(s.partials); dfree(s.scan_tmp); dfree(s.gsync);
     if (s.ev_a) cudaEventDestroy(s.ev_a);
     if (s.ev_b) cudaEventDestroy(s.ev_b);
     if (s.update_exec) cudaGraphExecDestroy(s.update_exec);
@@ -419,7 +419,11 @@ int run_substep_eager(Scene& s, bool sort_now) {
     { StageTimer t(s, APIC_STAGE_FORCES); CK(launch_finalize_faces(s, true, true)); CK(launch_base_lists(s)); }
     { StageTimer t(s, APIC_STAGE_BUILD); CK(launch_build_pressure(s)); }
     { StageTimer t(s, APIC_STAGE_MG); CK(launch_multilevel(s)); }
-    { StageTimer t(s, APIC_STAGE_PCG); CK(cudaGraphLaunch(s.solve_exec, s.stream)); }
+    {
+        StageTimer t(s, APIC_STAGE_PCG);
+        if (s.use_persistent && s.persist_grid > 0) CK(enqueue_persistent_solve(s));
+        else CK(cudaGraphLaunch(s.solve_exec, s.stream));
+    }
     { StageTimer t(s, APIC_STAGE_GRAD); CK(launch_gradient(s, true)); }
     { StageTimer t(s, APIC_STAGE_EXTRAP); CK(launch_extrapolate(s)); }
     { StageTimer t(s, APIC_STAGE_G2P); CK(launch_g2p(s)); }
@@ -538,6 +542,8 @@ int apic_create(uint32_t width, uint32_t height, float cell_size, const apic_wor
         AL(s.cg_s, C.padded); AL(s.cg_ap, C.padded); AL(s.cg_r, C.padded);
     }
     plan_vcycle(s);
+    AL(s.gsync, 1);
+    plan_persistent_solve(s);
     AL(s.ctl, 1);
     AL(s.partials, 2 * kMaxRedBlocks);
     s.scan_tmp_len = 3 * (div_up(max_words, 1024) + 1);
@@ -642,6 +648,7 @@ int apic_update(apic_handle* h, uint32_t flags, float frame_dt) {
     s.stats.true_residual_rel = c.true_rel;
     s.stats.not_converged = c.not_converged;
     s.stats.nonfinite_lanes = c.nonfinite;
+    if (c.status & kStatusTimeout) return fail(APIC_ERR_TIMEOUT, "a bounded device wait gave up (persistent solver barrier)");
     if (c.status & kStatusBadStep) return fail(APIC_ERR_NONFINITE, "substep size is not positive (non-finite velocities)");
     return APIC_OK;
 }
@@ -890,6 +897,28 @@ int apic_read_vec2x8(apic_handle* h, int which, float* dst, uint64_t floats) {
     return APIC_OK;
 }
 
+int apic_set_option(apic_handle* h, int option, int value) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    Scene& s = h->s;
+    if (s.stream) cudaStreamSynchronize(s.stream);
+    switch (option) {
+        case APIC_OPT_PERSISTENT_SOLVE:
+            if (value && s.persist_grid == 0) return fail(APIC_ERR_UNSUPPORTED, "cooperative launch unavailable");
+            s.use_persistent = value != 0;
+            invalidate_graphs(s);
+            return APIC_OK;
+        default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
+    }
+}
+
+int apic_get_option(apic_handle* h, int option, int* value) {
+    if (valid_handle(h) || !value) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    switch (option) {
+        case APIC_OPT_PERSISTENT_SOLVE: *value = (h->s.use_persistent && h->s.persist_grid > 0) ? 1 : 0; return APIC_OK;
+        default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
+    }
+}
+
 int apic_set_profiling(apic_handle* h, int enabled) {
     if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
     h->s.profiling = enabled != 0;
@@ -942,9 +971,13 @@ int apic_debug_run_stage(apic_handle* h, int stage, float dt) {
         case APIC_STAGE_PCG: {
             k_begin_update<<<1, 1, 0, st>>>(s.ctl, 0.0f, 0u, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
             k_set_dt<<<1, 1, 0, st>>>(s.ctl, dt, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
-            int rg = ensure_solve_graph(s);
-            if (rg) return rg;
-            CK(cudaGraphLaunch(s.solve_exec, st));
+            if (s.use_persistent && s.persist_grid > 0) {
+                CK(enqueue_persistent_solve(s));
+            } else {
+                int rg = ensure_solve_graph(s);
+                if (rg) return rg;
+                CK(cudaGraphLaunch(s.solve_exec, st));
+            }
             int rc = sync_ctl(s);
             if (rc) return rc;
             const Ctl& c = *s.ctl_host;

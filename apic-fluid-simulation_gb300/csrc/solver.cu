@@ -29,17 +29,15 @@
 #include "apic_device.cuh"
 #include "apic_graph.h"
 #include "apic_internal.h"
+#include "pcg_common.cuh"
 
 namespace apic {
 namespace {
 
 constexpr float kSafety = 1e-5f;  // SAFTY, src/apic.rs:8
 
-#define SEG_LOOP(level_idx)                                                        \
-    const uint32_t nseg = ctl->seg_count[level_idx];                               \
-    const int lane = threadIdx.x & 31;                                             \
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;                         \
-    for (uint32_t s_ = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s_ < nseg; s_ += nwarps)
+__device__ __forceinline__ uint32_t gwarp() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ uint32_t gnwarps() { return (gridDim.x * blockDim.x) >> 5; }
 
 __global__ void k_pcg_begin(Ctl* ctl) {
     ctl->pcg_done = 0;
@@ -50,27 +48,15 @@ __global__ void k_pcg_begin(Ctl* ctl) {
     ctl->rnorm2 = 0.0;
 }
 
-// ---- PCG kernels on the base level ---------------------------------------
+// ---- PCG kernels on the base level (phases in pcg_common.cuh) --------------
 
-__global__ void __launch_bounds__(kSegBlock) k_clear_pressure(Level B, float* __restrict__ p, const Ctl* __restrict__ ctl) {
-    SEG_LOOP(0) {
-        uint32_t word = B.seg[s_];
-        if ((B.fluid[word] >> lane) & 1u) p[word * 32 + lane] = 0.0f;
-    }
+__global__ void __launch_bounds__(kSegBlock) k_clear_pressure(Level B, float* p, const Ctl* ctl) {
+    pcg::ph_clear_pressure(B, ctl->seg_count[0], gwarp(), gnwarps(), p);
 }
 
 // s = z and gamma = r.z (src/apic.rs:1887-1892).
-__global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* __restrict__ s, Ctl* __restrict__ ctl,
-                                                         double* __restrict__ partials, int mode) {
-    double acc = 0;
-    SEG_LOOP(0) {
-        uint32_t word = B.seg[s_];
-        if (!((B.fluid[word] >> lane) & 1u)) continue;
-        uint32_t c = word * 32 + lane + B.w;
-        float z = B.err[c], r = B.res[c];
-        s[c] = z;
-        acc += double(r * z);
-    }
+__global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl* ctl, double* partials, int mode) {
+    double acc = pcg::ph_start(B, ctl->seg_count[0], gwarp(), gnwarps(), s);
     double tot;
     if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
         float gamma = float(tot);
@@ -81,62 +67,29 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* __restr
 }
 
 // Ap = A s and delta = s.Ap (apply_matrix_and_dot, src/apic.rs:1823-1863).
-__global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* __restrict__ s, float* __restrict__ ap,
-                                                        Ctl* __restrict__ ctl, double* __restrict__ partials,
+__global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s, float* ap, Ctl* ctl, double* partials,
                                                         int mode) {
     if (ctl->pcg_done) return;
-    double acc = 0;
-    const long long W = B.w;
-    SEG_LOOP(0) {
-        uint32_t word = B.seg[s_];
-        if (!((B.fluid[word] >> lane) & 1u)) continue;
-        long long raw = (long long)word * 32 + lane;
-        uint32_t c = uint32_t(raw) + B.w;
-        float sc = s[c];
-        float v = B.diag[c] * sc;
-        if (fluid_raw(B.fluid, raw + 1, B.cells)) v = __fmaf_rn(B.px[c], s[c + 1], v);
-        if (fluid_raw(B.fluid, raw - 1, B.cells)) v = __fmaf_rn(B.px[c - 1], s[c - 1], v);
-        if (fluid_raw(B.fluid, raw + W, B.cells)) v = __fmaf_rn(B.py[c], s[c + W], v);
-        if (fluid_raw(B.fluid, raw - W, B.cells)) v = __fmaf_rn(B.py[c - W], s[c - W], v);
-        ap[c] = v;
-        acc += double(v * sc);
-    }
+    double acc = pcg::ph_spmv(B, ctl->seg_count[0], gwarp(), gnwarps(), s, ap);
     double tot;
     if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
         float delta = float(tot);
         ctl->pcg_iters++;
-        if (mode == APIC_SOLVER_REFERENCE) {
-            if (fabsf(delta) < kSafety) { ctl->pcg_done = 1; return; }
-            ctl->alpha = ctl->gamma / delta;
-        } else {
-            if (!(delta != 0.0f) || !isfinite(delta)) { ctl->pcg_done = 1; return; }
-            ctl->alpha = ctl->gamma / delta;
-        }
+        bool stop = mode == APIC_SOLVER_REFERENCE ? fabsf(delta) < kSafety : (!(delta != 0.0f) || !isfinite(delta));
+        if (stop) ctl->pcg_done = 1;
+        else ctl->alpha = ctl->gamma / delta;
     }
 }
 
 // p += alpha s, r = fma(-alpha, Ap, r), max|r| (src/apic.rs:1907-1932);
-// relative modes reduce ||r||^2 instead.  Relative modes accumulate into x.
-__global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* __restrict__ p, int p_padded,
-                                                          const float* __restrict__ s, const float* __restrict__ ap,
-                                                          Ctl* __restrict__ ctl, double* __restrict__ partials,
-                                                          int mode, float solve_error) {
+// relative modes reduce ||r||^2 instead.
+__global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int p_padded, const float* s,
+                                                          const float* ap, Ctl* ctl, double* partials, int mode,
+                                                          float solve_error) {
     if (ctl->pcg_done) return;
-    const float alpha = ctl->alpha;
-    double acc = 0;
-    float mx = 0.0f;
-    SEG_LOOP(0) {
-        uint32_t word = B.seg[s_];
-        if (!((B.fluid[word] >> lane) & 1u)) continue;
-        uint32_t raw = word * 32 + lane;
-        uint32_t c = raw + B.w;
-        uint32_t pi = p_padded ? c : raw;
-        p[pi] = p[pi] + alpha * s[c];
-        float nr = __fmaf_rn(-alpha, ap[c], B.res[c]);
-        B.res[c] = nr;
-        mx = fmaxf(mx, fabsf(nr));
-        acc += double(nr) * double(nr);
-    }
+    float mx;
+    double acc;
+    pcg::ph_update(B, ctl->seg_count[0], gwarp(), gnwarps(), ctl->alpha, p, p_padded, s, ap, &mx, &acc);
     if (mode == APIC_SOLVER_REFERENCE) {
         float t;
         if (block_max_last<kSegBlock>(mx, partials, &ctl->red_counter, &t) && threadIdx.x == 0) {
@@ -154,16 +107,9 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* __rest
 }
 
 // gamma' = r.z, beta (src/apic.rs:1934-1943).
-__global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* __restrict__ ctl, double* __restrict__ partials,
-                                                      int mode) {
+__global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, double* partials, int mode) {
     if (ctl->pcg_done) return;
-    double acc = 0;
-    SEG_LOOP(0) {
-        uint32_t word = B.seg[s_];
-        if (!((B.fluid[word] >> lane) & 1u)) continue;
-        uint32_t c = word * 32 + lane + B.w;
-        acc += double(B.res[c] * B.err[c]);
-    }
+    double acc = pcg::ph_rz(B, ctl->seg_count[0], gwarp(), gnwarps());
     double tot;
     if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
         float ng = float(tot);
@@ -173,98 +119,39 @@ __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* __restrict__
     }
 }
 
-// s = z + beta s (src/apic.rs:1945-1954); counts the iteration cap.
-__global__ void __launch_bounds__(kSegBlock) k_search(Level B, float* __restrict__ s, const Ctl* __restrict__ ctl) {
+// s = z + beta s (src/apic.rs:1945-1954).
+__global__ void __launch_bounds__(kSegBlock) k_search(Level B, float* s, const Ctl* ctl) {
     if (ctl->pcg_done) return;
-    const float beta = ctl->beta;
-    SEG_LOOP(0) {
-        uint32_t word = B.seg[s_];
-        if (!((B.fluid[word] >> lane) & 1u)) continue;
-        uint32_t c = word * 32 + lane + B.w;
-        s[c] = B.err[c] + (beta * s[c]);
-    }
+    pcg::ph_search(B, ctl->seg_count[0], gwarp(), gnwarps(), ctl->beta, s);
 }
 
 // ---- FP64 refinement helpers (APIC_SOLVER_REL_MIXED) ----------------------
 
-// b64 = res (FP64 copy of the right-hand side), p64 = 0.
-__global__ void __launch_bounds__(kSegBlock) k_mixed_init(Level B, double* __restrict__ b64, double* __restrict__ p64,
-                                                          const Ctl* __restrict__ ctl) {
-    SEG_LOOP(0) {
-        uint32_t word = B.seg[s_];
-        if (!((B.fluid[word] >> lane) & 1u)) continue;
-        uint32_t c = word * 32 + lane + B.w;
-        b64[c] = double(B.res[c]);
-        p64[c] = 0.0;
-    }
-}
-
-// r64 = b64 - A p64 in FP64 and the true relative residual; flags bit 0:
-// res = float(r64), bit 1: x = 0 (start of an inner correction solve).
-__global__ void __launch_bounds__(kSegBlock) k_true_residual(Level B, const double* __restrict__ b64,
-                                                             const double* __restrict__ p64, float* __restrict__ x,
-                                                             Ctl* __restrict__ ctl, double* __restrict__ partials,
-                                                             int flags) {
-    double rr = 0;
-    const long long W = B.w;
-    SEG_LOOP(0) {
-        uint32_t word = B.seg[s_];
-        if (!((B.fluid[word] >> lane) & 1u)) continue;
-        long long raw = (long long)word * 32 + lane;
-        uint32_t c = uint32_t(raw) + B.w;
-        double v = double(B.diag[c]) * p64[c];
-        if (fluid_raw(B.fluid, raw + 1, B.cells)) v += double(B.px[c]) * p64[c + 1];
-        if (fluid_raw(B.fluid, raw - 1, B.cells)) v += double(B.px[c - 1]) * p64[c - 1];
-        if (fluid_raw(B.fluid, raw + W, B.cells)) v += double(B.py[c]) * p64[c + W];
-        if (fluid_raw(B.fluid, raw - W, B.cells)) v += double(B.py[c - W]) * p64[c - W];
-        double r = b64[c] - v;
-        rr += r * r;
-        if (flags & 1) B.res[c] = float(r);
-        if (flags & 2) x[c] = 0.0f;
-    }
-    double tot;
-    if (block_sum_last<kSegBlock>(rr, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
-        ctl->true_rel = ctl->bnorm2 > 0.0 ? sqrt(tot / ctl->bnorm2) : 0.0;
-    }
-}
-
-__global__ void __launch_bounds__(kSegBlock) k_bnorm(Level B, const double* __restrict__ b64, Ctl* __restrict__ ctl,
-                                                     double* __restrict__ partials) {
-    double bb = 0;
-    SEG_LOOP(0) {
-        uint32_t word = B.seg[s_];
-        if (!((B.fluid[word] >> lane) & 1u)) continue;
-        uint32_t c = word * 32 + lane + B.w;
-        bb += b64[c] * b64[c];
-    }
+// b64 = res, p64 = 0 and ||b||^2.
+__global__ void __launch_bounds__(kSegBlock) k_mixed_init(Level B, double* b64, double* p64, Ctl* ctl,
+                                                          double* partials) {
+    double bb = pcg::ph_mixed_init(B, ctl->seg_count[0], gwarp(), gnwarps(), b64, p64);
     double tot;
     if (block_sum_last<kSegBlock>(bb, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) ctl->bnorm2 = tot;
 }
 
-// p64 += x; optionally pressure = float(p64) at the end.
-__global__ void __launch_bounds__(kSegBlock) k_mixed_accumulate(Level B, double* __restrict__ p64,
-                                                                const float* __restrict__ x,
-                                                                float* __restrict__ pressure,
-                                                                const Ctl* __restrict__ ctl, int finalize) {
-    SEG_LOOP(0) {
-        uint32_t word = B.seg[s_];
-        if (!((B.fluid[word] >> lane) & 1u)) continue;
-        uint32_t raw = word * 32 + lane;
-        uint32_t c = raw + B.w;
-        if (!finalize) p64[c] += double(x[c]);
-        else pressure[raw] = float(p64[c]);
-    }
+// True relative residual of p64 (flags: see pcg::ph_true_residual).
+__global__ void __launch_bounds__(kSegBlock) k_true_residual(Level B, const double* b64, const double* p64, float* x,
+                                                             Ctl* ctl, double* partials, int flags) {
+    double rr = pcg::ph_true_residual(B, ctl->seg_count[0], gwarp(), gnwarps(), b64, p64, x, flags);
+    double tot;
+    if (block_sum_last<kSegBlock>(rr, partials, &ctl->red_counter, &tot) && threadIdx.x == 0)
+        ctl->true_rel = ctl->bnorm2 > 0.0 ? sqrt(tot / ctl->bnorm2) : 0.0;
 }
 
-// Pressure as FP64 field (for the true residual of modes 1 and 2).
-__global__ void __launch_bounds__(kSegBlock) k_pressure_to64(Level B, const float* __restrict__ pressure,
-                                                             double* __restrict__ p64, const Ctl* __restrict__ ctl) {
-    SEG_LOOP(0) {
-        uint32_t word = B.seg[s_];
-        if (!((B.fluid[word] >> lane) & 1u)) continue;
-        uint32_t raw = word * 32 + lane;
-        p64[raw + B.w] = double(pressure[raw]);
-    }
+__global__ void __launch_bounds__(kSegBlock) k_mixed_accumulate(Level B, double* p64, const float* x, float* pressure,
+                                                                const Ctl* ctl, int finalize) {
+    pcg::ph_accumulate(B, ctl->seg_count[0], gwarp(), gnwarps(), p64, x, pressure, finalize);
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_pressure_to64(Level B, const float* pressure, double* p64,
+                                                             const Ctl* ctl) {
+    pcg::ph_pressure_to64(B, ctl->seg_count[0], gwarp(), gnwarps(), pressure, p64);
 }
 
 // ---- loop control (device side; each sets a graph conditional) ------------
@@ -315,7 +202,6 @@ __global__ void k_refine_end(Ctl* ctl, double tol) {
     if (ctl->true_rel > tol) ctl->not_converged++;
 }
 
-#undef SEG_LOOP
 
 }  // namespace
 
@@ -361,6 +247,8 @@ static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p
 }
 
 cudaError_t build_solve(Scene& s, GraphCursor& c) {
+    if (s.use_persistent && s.persist_grid > 0)
+        return capture_into(s, c, [&]() { return enqueue_persistent_solve(s); });
     const Level& B = s.lv[0];
     uint32_t g = seg_grid(B.words);
     int mode = s.solver_mode;
@@ -377,8 +265,7 @@ cudaError_t build_solve(Scene& s, GraphCursor& c) {
     const double tol = double(s.rel_tol);
     e = capture_into(s, c, [&]() {
         cudaStream_t st = s.stream;
-        k_mixed_init<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.ctl);
-        k_bnorm<<<g, kSegBlock, 0, st>>>(B, s.b64, s.ctl, s.partials);
+        k_mixed_init<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.ctl, s.partials);
         k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
         k_rel_begin<<<1, 1, 0, st>>>(s.ctl, tol, s.max_iter);
         return cudaGetLastError();

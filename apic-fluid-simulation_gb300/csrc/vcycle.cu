@@ -28,329 +28,44 @@
 
 #include "apic_device.cuh"
 #include "apic_internal.h"
+#include "vcycle_common.cuh"
 
 namespace apic {
+using namespace vc;
 namespace {
 
-constexpr float kOmega = 1.2f;
-constexpr int kTailThreads = 1024;
-constexpr size_t kTailSmemBudget = 200 * 1024;
+__device__ __forceinline__ uint32_t gwarp() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ uint32_t gnwarps() { return (gridDim.x * blockDim.x) >> 5; }
 
-// ---- per-cell arithmetic shared by the global and the shared-memory kernels
-
-// One SOR update (src/apic.rs:487-507) of padded cell c with raw index raw.
-// nb(padded, raw) returns a neighbour's current error; neighbours that are not
-// fluid are skipped (their reference contribution is zero).
-template <class NB>
-__device__ __forceinline__ float sor_cell(const uint32_t* bits, uint32_t w, uint32_t cells, const float* inv_d,
-                                          const float* px, const float* py, const float* res, long long raw,
-                                          uint32_t c, float old, bool neighbours, NB nb) {
-    float inv = inv_d[c];
-    if (inv == 0.0f) return old;
-    float sum = res[c];
-    if (neighbours) {
-        const long long W = w;
-        if (fluid_raw(bits, raw + 1, cells)) sum = __fmaf_rn(-px[c], nb(c + 1, raw + 1), sum);
-        if (fluid_raw(bits, raw + W, cells)) sum = __fmaf_rn(-py[c], nb(c + w, raw + W), sum);
-        if (fluid_raw(bits, raw - 1, cells)) sum = __fmaf_rn(-px[c - 1], nb(c - 1, raw - 1), sum);
-        if (fluid_raw(bits, raw - W, cells)) sum = __fmaf_rn(-py[c - w], nb(c - w, raw - W), sum);
-    }
-    float gs = sum * inv;
-    return old + (kOmega * (gs - old));
-}
-
-// Coarse residual of coarse cell (cx, cy) from its fine children (:549-583).
-__device__ __forceinline__ float restrict_cell(const uint32_t* fb, uint32_t fw, uint32_t fcells, const float* fd,
-                                               const float* fpx, const float* fpy, const float* fr, const float* fe,
-                                               uint32_t cx, uint32_t cy) {
-    float sum = 0.0f;
-    const long long W = fw;
-    for (uint32_t dy = 0; dy < 2; ++dy)
-        for (uint32_t dx = 0; dx < 2; ++dx) {
-            long long rf = (long long)(cy * 2 + dy) * fw + (cx * 2 + dx);
-            if (!fluid_raw(fb, rf, fcells)) continue;
-            uint32_t pf = uint32_t(rf) + fw;
-            float b = fr[pf];
-            float ax = fd[pf] * fe[pf];
-            if (fluid_raw(fb, rf + 1, fcells)) ax += fpx[pf] * fe[pf + 1];
-            if (fluid_raw(fb, rf + W, fcells)) ax += fpy[pf] * fe[pf + fw];
-            if (fluid_raw(fb, rf - 1, fcells)) ax += fpx[pf - 1] * fe[pf - 1];
-            if (fluid_raw(fb, rf - W, fcells)) ax += fpy[pf - fw] * fe[pf - fw];
-            sum += b - ax;
-        }
-    return sum;
-}
-
-__device__ __forceinline__ bool is_red(uint32_t raw, uint32_t w) { return (((raw % w) + (raw / w)) & 1u) == 0u; }
-
-// e + ec, plus ec again `reps` times (the padded base list, :611-615).
-__device__ __forceinline__ float prolonged(float e, float ec, uint32_t reps) {
-    e = e + ec;
-    for (uint32_t k = 0; k < reps; ++k) e = e + ec;
-    return e;
-}
-
-#define SEG_LOOP(level_idx)                                                        \
-    const uint32_t nseg = ctl->seg_count[level_idx];                               \
-    const int lane = threadIdx.x & 31;                                             \
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;                         \
-    for (uint32_t s_ = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s_ < nseg; s_ += nwarps)
-
-// One colour sweep on a level held in global memory.  init: first sweep after
-// the level's error was zero-filled (own and unswept values are zero).
-__global__ void __launch_bounds__(kSegBlock) k_smooth(Level L, int li, const Ctl* __restrict__ ctl, int color, int init) {
+__global__ void __launch_bounds__(kSegBlock) k_smooth(Level L, int li, const Ctl* ctl, int color, int init) {
     if (ctl->pcg_done) return;
-    SEG_LOOP(li) {
-        uint32_t word = L.seg[s_];
-        if (!((L.fluid[word] >> lane) & 1u)) continue;
-        uint32_t raw = word * 32 + lane;
-        if (int(!is_red(raw, L.w)) != color) continue;
-        uint32_t c = raw + L.w;
-        float old = init ? 0.0f : L.err[c];
-        const float* e = L.err;
-        L.err[c] = sor_cell(L.fluid, L.w, L.cells, L.inv_diag, L.px, L.py, L.res, raw, c, old, !(init && color == 0),
-                            [e](uint32_t p, long long) { return e[p]; });
-    }
+    ph_smooth(L, ctl->seg_count[li], gwarp(), gnwarps(), color, init);
 }
 
 // Restriction only (into the first tail level or the coarsest level).
-__global__ void __launch_bounds__(kSegBlock) k_restrict(Level f, Level c, int lc, const Ctl* __restrict__ ctl) {
+__global__ void __launch_bounds__(kSegBlock) k_restrict(Level f, Level c, int lc, const Ctl* ctl) {
     if (ctl->pcg_done) return;
-    SEG_LOOP(lc) {
-        uint32_t word = c.seg[s_];
-        if (!((c.fluid[word] >> lane) & 1u)) continue;
-        uint32_t rc = word * 32 + lane;
-        c.res[rc + c.w] = restrict_cell(f.fluid, f.w, f.cells, f.diag, f.px, f.py, f.res, f.err, rc % c.w, rc / c.w);
-    }
+    ph_restrict(f, c, ctl->seg_count[lc], gwarp(), gnwarps(), false);
 }
 
 // Restriction fused with the coarse level's first (red) sweep.
-__global__ void __launch_bounds__(kSegBlock) k_restrict_red(Level f, Level c, int lc, const Ctl* __restrict__ ctl) {
+__global__ void __launch_bounds__(kSegBlock) k_restrict_red(Level f, Level c, int lc, const Ctl* ctl) {
     if (ctl->pcg_done) return;
-    SEG_LOOP(lc) {
-        uint32_t word = c.seg[s_];
-        if (!((c.fluid[word] >> lane) & 1u)) continue;
-        uint32_t rc = word * 32 + lane;
-        uint32_t cp = rc + c.w;
-        float r = restrict_cell(f.fluid, f.w, f.cells, f.diag, f.px, f.py, f.res, f.err, rc % c.w, rc / c.w);
-        c.res[cp] = r;
-        if (is_red(rc, c.w)) {
-            float inv = c.inv_diag[cp];
-            c.err[cp] = inv != 0.0f ? 0.0f + (kOmega * (r * inv - 0.0f)) : 0.0f;
-        }
-    }
+    ph_restrict(f, c, ctl->seg_count[lc], gwarp(), gnwarps(), true);
 }
 
-// Prolongation fused with the black sweep: black cells take their prolonged
-// error as the old value, red neighbours are read as prolonged values.
-__global__ void __launch_bounds__(kSegBlock) k_prolong_black(Level c, Level f, int lf, const Ctl* __restrict__ ctl,
-                                                             int base) {
+// Prolongation fused with the black sweep.
+__global__ void __launch_bounds__(kSegBlock) k_prolong_black(Level c, Level f, int lf, const Ctl* ctl, int base) {
     if (ctl->pcg_done) return;
-    const uint32_t last = base ? ctl->last_fluid : 0xFFFFFFFFu;
-    const uint32_t extra = base ? ctl->pad_count : 0u;
-    const float* fe = f.err;
-    const float* ce = c.err;
-    const uint32_t fw = f.w, cw = c.w;
-    auto coarse_e = [=](long long rf) {
-        uint32_t r = uint32_t(rf);
-        return ce[((r / fw) / 2) * cw + (r % fw) / 2 + cw];
-    };
-    SEG_LOOP(lf) {
-        uint32_t word = f.seg[s_];
-        if (!((f.fluid[word] >> lane) & 1u)) continue;
-        uint32_t raw = word * 32 + lane;
-        if (is_red(raw, fw)) continue;
-        uint32_t p = raw + fw;
-        float old = prolonged(fe[p], coarse_e(raw), p == last ? extra : 0u);
-        f.err[p] = sor_cell(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, raw, p, old, true,
-                            [=](uint32_t q, long long rq) { return prolonged(fe[q], coarse_e(rq), q == last ? extra : 0u); });
-    }
+    ph_prolong(c, f, ctl->seg_count[lf], gwarp(), gnwarps(), 1, base ? ctl->last_fluid : 0xFFFFFFFFu,
+               base ? ctl->pad_count : 0u);
 }
 
 // Prolongation fused with the final red sweep (black neighbours are final).
-__global__ void __launch_bounds__(kSegBlock) k_prolong_red(Level c, Level f, int lf, const Ctl* __restrict__ ctl, int base) {
+__global__ void __launch_bounds__(kSegBlock) k_prolong_red(Level c, Level f, int lf, const Ctl* ctl, int base) {
     if (ctl->pcg_done) return;
-    const uint32_t last = base ? ctl->last_fluid : 0xFFFFFFFFu;
-    const uint32_t extra = base ? ctl->pad_count : 0u;
-    const float* fe = f.err;
-    const float* ce = c.err;
-    const uint32_t fw = f.w, cw = c.w;
-    SEG_LOOP(lf) {
-        uint32_t word = f.seg[s_];
-        if (!((f.fluid[word] >> lane) & 1u)) continue;
-        uint32_t raw = word * 32 + lane;
-        if (!is_red(raw, fw)) continue;
-        uint32_t p = raw + fw;
-        float ec = ce[((raw / fw) / 2) * cw + (raw % fw) / 2 + cw];
-        float old = prolonged(fe[p], ec, p == last ? extra : 0u);
-        f.err[p] = sor_cell(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, raw, p, old, true,
-                            [fe](uint32_t q, long long) { return fe[q]; });
-    }
-}
-
-// ---- CTA-wide helpers -------------------------------------------------------
-__device__ __forceinline__ double cta_sum(double v, double* sh) {
-    v = warp_sum(v);
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[warp] = v;
-    __syncthreads();
-    double t = 0;
-    for (int w = 0; w < int(blockDim.x / 32); ++w) t += sh[w];
-    return t;
-}
-__device__ __forceinline__ float cta_max(float v, float* sh) {
-    v = warp_maxf(v);
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[warp] = v;
-    __syncthreads();
-    float t = 0.0f;
-    for (int w = 0; w < int(blockDim.x / 32); ++w) t = fmaxf(t, sh[w]);
-    return t;
-}
-
-// Plain CG on the coarsest level (solve_coarse_exact, :618-704) by one CTA.
-// Arrays may live in global or shared memory.
-__device__ void cta_coarse_cg(const uint32_t* bits, uint32_t w, uint32_t cells, const float* diag, const float* px,
-                              const float* py, const float* res, float* err, float* cs, float* cap, float* cr) {
-    __shared__ double shd[32];
-    __shared__ float shf[32];
-    const long long W = w;
-    uint32_t nf = 0;
-    double g = 0;
-    for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
-        if (!bit_at(bits, r)) continue;
-        uint32_t c = r + w;
-        float rv = res[c];
-        err[c] = 0.0f;
-        cr[c] = rv;
-        cs[c] = rv;
-        g += double(rv * rv);
-        nf++;
-    }
-    float gamma = float(cta_sum(g, shd));
-    uint32_t nfl = uint32_t(cta_sum(double(nf), shd));
-    if (gamma < 1e-12f) return;
-    uint32_t max_it = min(nfl, 100u);
-    for (uint32_t it = 0; it < max_it; ++it) {
-        __syncthreads();
-        double d = 0;
-        for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
-            if (!bit_at(bits, r)) continue;
-            uint32_t c = r + w;
-            float v = diag[c] * cs[c];
-            if (fluid_raw(bits, (long long)r + 1, cells)) v = __fmaf_rn(px[c], cs[c + 1], v);
-            if (fluid_raw(bits, (long long)r - 1, cells)) v = __fmaf_rn(px[c - 1], cs[c - 1], v);
-            if (fluid_raw(bits, (long long)r + W, cells)) v = __fmaf_rn(py[c], cs[c + w], v);
-            if (fluid_raw(bits, (long long)r - W, cells)) v = __fmaf_rn(py[c - w], cs[c - w], v);
-            cap[c] = v;
-            d += double(cs[c] * v);
-        }
-        float delta = float(cta_sum(d, shd));
-        if (fabsf(delta) < 1e-5f) break;
-        float alpha = gamma / delta;
-        float me = 0.0f;
-        for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
-            if (!bit_at(bits, r)) continue;
-            uint32_t c = r + w;
-            err[c] = err[c] + alpha * cs[c];
-            float nr = cr[c] - alpha * cap[c];
-            cr[c] = nr;
-            me = fmaxf(me, fabsf(nr));
-        }
-        if (cta_max(me, shf) < 1e-6f) break;
-        double ng = 0;
-        for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
-            if (!bit_at(bits, r)) continue;
-            uint32_t c = r + w;
-            ng += double(cr[c] * cr[c]);
-        }
-        float new_gamma = float(cta_sum(ng, shd));
-        float beta = new_gamma / gamma;
-        gamma = new_gamma;
-        for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
-            if (!bit_at(bits, r)) continue;
-            uint32_t c = r + w;
-            cs[c] = cr[c] + (beta * cs[c]);
-        }
-    }
-    __syncthreads();
-}
-
-// The same CG run by one warp (shuffles only, no block barriers) for a
-// coarsest level of at most 32 * kWarpCgCells cells; the other warps wait.
-constexpr uint32_t kWarpCgCells = 8;
-__device__ void warp_coarse_cg(const uint32_t* bits, uint32_t w, uint32_t cells, const float* diag, const float* px,
-                               const float* py, const float* res, float* err, float* cs, float* cap, float* cr) {
-    if (threadIdx.x < 32) {
-        const long long W = w;
-        const uint32_t lane = threadIdx.x;
-        auto wsum = [](double v) {
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            return v;
-        };
-        double g = 0, nf = 0;
-        for (uint32_t r = lane; r < cells; r += 32) {
-            if (!bit_at(bits, r)) continue;
-            uint32_t c = r + w;
-            float rv = res[c];
-            err[c] = 0.0f;
-            cr[c] = rv;
-            cs[c] = rv;
-            g += double(rv * rv);
-            nf += 1.0;
-        }
-        float gamma = float(wsum(g));
-        uint32_t nfl = uint32_t(wsum(nf));
-        if (!(gamma < 1e-12f)) {
-            uint32_t max_it = min(nfl, 100u);
-            for (uint32_t it = 0; it < max_it; ++it) {
-                __syncwarp();
-                double d = 0;
-                for (uint32_t r = lane; r < cells; r += 32) {
-                    if (!bit_at(bits, r)) continue;
-                    uint32_t c = r + w;
-                    float v = diag[c] * cs[c];
-                    if (fluid_raw(bits, (long long)r + 1, cells)) v = __fmaf_rn(px[c], cs[c + 1], v);
-                    if (fluid_raw(bits, (long long)r - 1, cells)) v = __fmaf_rn(px[c - 1], cs[c - 1], v);
-                    if (fluid_raw(bits, (long long)r + W, cells)) v = __fmaf_rn(py[c], cs[c + w], v);
-                    if (fluid_raw(bits, (long long)r - W, cells)) v = __fmaf_rn(py[c - w], cs[c - w], v);
-                    cap[c] = v;
-                    d += double(cs[c] * v);
-                }
-                float delta = float(wsum(d));
-                if (fabsf(delta) < 1e-5f) break;
-                float alpha = gamma / delta;
-                float me = 0.0f;
-                for (uint32_t r = lane; r < cells; r += 32) {
-                    if (!bit_at(bits, r)) continue;
-                    uint32_t c = r + w;
-                    err[c] = err[c] + alpha * cs[c];
-                    float nr = cr[c] - alpha * cap[c];
-                    cr[c] = nr;
-                    me = fmaxf(me, fabsf(nr));
-                }
-                if (warp_maxf(me) < 1e-6f) break;
-                double ng = 0;
-                for (uint32_t r = lane; r < cells; r += 32) {
-                    if (!bit_at(bits, r)) continue;
-                    uint32_t c = r + w;
-                    ng += double(cr[c] * cr[c]);
-                }
-                float new_gamma = float(wsum(ng));
-                float beta = new_gamma / gamma;
-                gamma = new_gamma;
-                __syncwarp();
-                for (uint32_t r = lane; r < cells; r += 32) {
-                    if (!bit_at(bits, r)) continue;
-                    uint32_t c = r + w;
-                    cs[c] = cr[c] + (beta * cs[c]);
-                }
-            }
-        }
-    }
-    __syncthreads();
+    ph_prolong(c, f, ctl->seg_count[lf], gwarp(), gnwarps(), 0, base ? ctl->last_fluid : 0xFFFFFFFFu,
+               base ? ctl->pad_count : 0u);
 }
 
 __global__ void __launch_bounds__(kTailThreads) k_coarse_solve(Level L, float* __restrict__ cs, float* __restrict__ cap,
@@ -359,107 +74,13 @@ __global__ void __launch_bounds__(kTailThreads) k_coarse_solve(Level L, float* _
     cta_coarse_cg(L.fluid, L.w, L.cells, L.diag, L.px, L.py, L.res, L.err, cs, cap, cr);
 }
 
-// ---- the coarse tail in shared memory ----------------------------------------
-struct TailLevel {
-    uint32_t w, cells, words, padded;
-    const uint32_t* fluid;
-    const float *diag, *inv, *px, *py;
-    float* res;   // global residual (read for the first tail level)
-    float* err;   // global error (written back for the first tail level)
-    uint32_t o_bits, o_diag, o_inv, o_px, o_py, o_res, o_err;  // shared offsets, 4-byte units
-};
-struct TailParams {
-    int n;                      // tail levels; lv[n - 1] is the coarsest
-    uint32_t o_cs, o_cap, o_cr;  // coarse CG vectors
-    TailLevel lv[kMaxLevels];
-};
-
-struct SmemLevel {
-    uint32_t w, cells;
-    uint32_t* bits;
-    float *diag, *inv, *px, *py, *res, *err;
-};
-
-__device__ __forceinline__ SmemLevel smem_level(uint32_t* sm, const TailLevel& t) {
-    float* f = reinterpret_cast<float*>(sm);
-    return SmemLevel{t.w, t.cells, sm + t.o_bits, f + t.o_diag, f + t.o_inv, f + t.o_px, f + t.o_py, f + t.o_res,
-                     f + t.o_err};
-}
-
-__device__ void cta_sweep(const SmemLevel& L, int color, int init) {
-    const float* e = L.err;
-    for (uint32_t r = threadIdx.x; r < L.cells; r += blockDim.x) {
-        if (!bit_at(L.bits, r) || int(!is_red(r, L.w)) != color) continue;
-        uint32_t c = r + L.w;
-        float old = init ? 0.0f : L.err[c];
-        L.err[c] = sor_cell(L.bits, L.w, L.cells, L.inv, L.px, L.py, L.res, r, c, old, !(init && color == 0),
-                            [e](uint32_t p, long long) { return e[p]; });
-    }
-    __syncthreads();
-}
-
-__global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(TailParams tp, const Ctl* __restrict__ ctl) {
+__global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(TailParams tp, const Ctl* ctl) {
     if (ctl->pcg_done) return;
     extern __shared__ uint32_t sm[];
-    // load masks and coefficients of every tail level, and the first level's residual
-    for (int l = 0; l < tp.n; ++l) {
-        const TailLevel& t = tp.lv[l];
-        SmemLevel L = smem_level(sm, t);
-        for (uint32_t i = threadIdx.x; i < t.words; i += blockDim.x) L.bits[i] = t.fluid[i];
-        for (uint32_t i = threadIdx.x; i < t.padded; i += blockDim.x) {
-            L.diag[i] = t.diag[i];
-            L.inv[i] = t.inv[i];
-            L.px[i] = t.px[i];
-            L.py[i] = t.py[i];
-            if (l == 0) L.res[i] = t.res[i];
-        }
-    }
-    __syncthreads();
-    // descend: pre-smooth and restrict (the error of each level starts at zero)
-    for (int l = 0; l + 1 < tp.n; ++l) {
-        SmemLevel f = smem_level(sm, tp.lv[l]);
-        SmemLevel c = smem_level(sm, tp.lv[l + 1]);
-        cta_sweep(f, 0, 1);
-        cta_sweep(f, 1, 1);
-        for (uint32_t rc = threadIdx.x; rc < c.cells; rc += blockDim.x)
-            if (bit_at(c.bits, rc))
-                c.res[rc + c.w] = restrict_cell(f.bits, f.w, f.cells, f.diag, f.px, f.py, f.res, f.err, rc % c.w,
-                                                rc / c.w);
-        __syncthreads();
-    }
-    {
-        SmemLevel L = smem_level(sm, tp.lv[tp.n - 1]);
-        float* fs = reinterpret_cast<float*>(sm);
-        if (L.cells <= 32 * kWarpCgCells)
-            warp_coarse_cg(L.bits, L.w, L.cells, L.diag, L.px, L.py, L.res, L.err, fs + tp.o_cs, fs + tp.o_cap,
-                           fs + tp.o_cr);
-        else
-            cta_coarse_cg(L.bits, L.w, L.cells, L.diag, L.px, L.py, L.res, L.err, fs + tp.o_cs, fs + tp.o_cap,
-                          fs + tp.o_cr);
-    }
-    // ascend: prolongate and post-smooth (black, then red)
-    for (int l = tp.n - 2; l >= 0; --l) {
-        SmemLevel f = smem_level(sm, tp.lv[l]);
-        SmemLevel c = smem_level(sm, tp.lv[l + 1]);
-        for (uint32_t r = threadIdx.x; r < f.cells; r += blockDim.x)
-            if (bit_at(f.bits, r)) {
-                uint32_t cx = (r % f.w) / 2, cy = (r / f.w) / 2;
-                f.err[r + f.w] = f.err[r + f.w] + c.err[cy * c.w + cx + c.w];
-            }
-        __syncthreads();
-        cta_sweep(f, 1, 0);
-        cta_sweep(f, 0, 0);
-    }
-    // hand the first tail level's error back to the level above
-    {
-        const TailLevel& t = tp.lv[0];
-        SmemLevel L = smem_level(sm, t);
-        for (uint32_t r = threadIdx.x; r < t.cells; r += blockDim.x)
-            if (bit_at(L.bits, r)) t.err[r + t.w] = L.err[r + t.w];
-    }
+    cta_tail(tp, sm, true);
 }
 
-#undef SEG_LOOP
+
 
 size_t tail_level_bytes(const Level& L) { return 4ull * (L.words + 6ull * L.padded); }
 
@@ -501,27 +122,8 @@ void enqueue_vcycle(Scene& s) {
     for (int l = 1; l <= last; ++l) {
         if (l == s.tail_first) {
             k_restrict<<<grid(l), kSegBlock, 0, st>>>(L[l - 1], L[l], l, s.ctl);
-            TailParams tp;
-            tp.n = s.nlevels - l;
             uint32_t off = 0;
-            for (int k = 0; k < tp.n; ++k) {
-                const Level& v = L[l + k];
-                TailLevel& t = tp.lv[k];
-                t.w = v.w; t.cells = v.cells; t.words = v.words; t.padded = v.padded;
-                t.fluid = v.fluid; t.diag = v.diag; t.inv = v.inv_diag; t.px = v.px; t.py = v.py;
-                t.res = v.res; t.err = v.err;
-                t.o_bits = off; off += v.words;
-                t.o_diag = off; off += v.padded;
-                t.o_inv = off; off += v.padded;
-                t.o_px = off; off += v.padded;
-                t.o_py = off; off += v.padded;
-                t.o_res = off; off += v.padded;
-                t.o_err = off; off += v.padded;
-            }
-            uint32_t cp = L[last].padded;
-            tp.o_cs = off; off += cp;
-            tp.o_cap = off; off += cp;
-            tp.o_cr = off; off += cp;
+            TailParams tp = make_tail_params(s, l, &off);
             k_vcycle_tail<<<1, kTailThreads, size_t(off) * 4, st>>>(tp, s.ctl);
             break;
         }

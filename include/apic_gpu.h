@@ -207,6 +207,15 @@ int apic_set_particles(apic_handle* h, uint32_t n, const float* pos_x, const flo
 /* ---- pressure solver configuration ------------------------------------- */
 int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterations);
 
+/* ---- execution options --------------------------------------------------- */
+/* 1 (default where cooperative launch is possible): the whole pressure solve
+ * runs as one persistent cooperative kernel (one CTA per SM, grid barriers
+ * between phases).  0: a CUDA graph of per-phase kernels with device-side
+ * WHILE loops.  Both compute the same iterations. */
+#define APIC_OPT_PERSISTENT_SOLVE 1
+int apic_set_option(apic_handle* h, int option, int value);
+int apic_get_option(apic_handle* h, int option, int* value);
+
 /* ---- measurement -------------------------------------------------------- */
 /* When enabled, each stage of each substep is bracketed by CUDA events on the
  * handle's stream; apic_get_stage_times returns the summed milliseconds per

@@ -329,3 +329,38 @@ def test_relative_solver_modes(oracle_mod, mode):
         assert so.true_residual_rel <= 1e-6, so.true_residual_rel
     else:
         assert sg.true_residual_rel <= 1e-4
+
+
+@pytest.mark.parametrize("mode", [A.SOLVER_REFERENCE, A.SOLVER_REL_FP32, A.SOLVER_REL_MIXED])
+def test_persistent_solver_matches_graph_solver(gpu_lib, mode):
+    """The one-kernel persistent solve and the graph of per-phase kernels run
+    the same iterations; only the reduction grouping differs."""
+    props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+    side = 256
+    cs = 1 / side
+    scene = A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=cs, sub=2, seed=1, fluid_x=0.5, fluid_y=0.5,
+                           disk=(0.7, 0.8, 0.08), disk_v=(0.0, -2.0))
+    px, py, vx, vy = A.generate_scene(scene)
+    sims = []
+    for persistent in (0, 1):
+        g = A.Apic(side, side, cs, props)
+        g.set_particles(px, py, vx, vy)
+        g.set_solver(mode, 1e-6, 500)
+        if persistent and g.get_option(A.OPT_PERSISTENT_SOLVE) == 0:
+            pytest.skip("cooperative launch unavailable")
+        g.set_option(A.OPT_PERSISTENT_SOLVE, persistent)
+        assert g.get_option(A.OPT_PERSISTENT_SOLVE) == persistent
+        sims.append(g)
+    opts = A.DebugOptions(disable_particle_sort=True)
+    for k in range(6):
+        for g in sims:
+            g.update(opts, 1 / 480)
+        a, b = sims[0].stats(), sims[1].stats()
+        assert abs(int(a.pcg_iterations) - int(b.pcg_iterations)) <= 1, (k, a.pcg_iterations, b.pcg_iterations)
+        if mode == A.SOLVER_REL_MIXED:
+            assert b.true_residual_rel <= 1e-6 and a.true_residual_rel <= 1e-6
+    pa, pb = sims[0].read_field("pressure"), sims[1].read_field("pressure")
+    scale = float(np.max(np.abs(pa))) or 1.0
+    assert float(np.max(np.abs(pa - pb))) <= 1e-3 * scale
+    for f in ("pos_x", "pos_y"):
+        assert float(np.max(np.abs(sims[0].read_field(f) - sims[1].read_field(f)))) < 1e-3 * cs
