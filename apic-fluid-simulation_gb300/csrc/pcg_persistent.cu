@@ -65,8 +65,11 @@ __device__ __noinline__ bool grid_barrier(GridSync* gs, Ctl* ctl) {
             __threadfence();
             atomicAdd(&gs->gen, 1u);
         } else {
+            // bounded wait; leave at once if another CTA already gave up
+            volatile unsigned* vstatus = &ctl->status;
             unsigned long long spins = 0;
             while (*vgen == g) {
+                if ((*vstatus & kStatusTimeout) != 0u) break;
                 if (++spins > kSpinLimit) {
                     atomicOr(&ctl->status, kStatusTimeout);
                     break;
