@@ -110,6 +110,8 @@ SIGNATURES = {
     "apic_synchronize": (ctypes.c_int, [_VP]),
     "apic_get_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
     "apic_debug_run_stage": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_float]),
+    "apic_morton_sort_noalloc": (ctypes.c_int, [_VP, _VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                                ctypes.c_float, _VP, _VP, _VP]),
     "apic_debug_finish_substep": (ctypes.c_int, [_VP, ctypes.c_float]),
 }
 

@@ -187,6 +187,11 @@ struct Scene {
 cudaError_t launch_sort(Scene& s);
 // Exclusive scan of data[0..n) in place; tmp holds div_up(n, 1024) words.
 cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t n, uint32_t* tmp, cudaStream_t st);
+cudaError_t radix_sort_pairs_in(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* hist,
+                                uint32_t* scan_tmp, uint32_t n, int bits, cudaStream_t st);
+int morton_key_bits(uint32_t width, uint32_t height);
+// runtime.cu: record the calling thread's last error text (apic_last_error)
+void set_last_error(const char* msg);
 // particles.cu
 cudaError_t launch_p2g(Scene& s);
 cudaError_t launch_g2p(Scene& s);

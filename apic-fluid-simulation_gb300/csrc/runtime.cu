@@ -447,6 +447,8 @@ int valid_handle(apic_handle* h) {
 
 // ---- scene generators live in scene.cpp ----------------------------------
 
+void apic::set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
 extern "C" {
 
 const char* apic_last_error(void) { return g_last_error.c_str(); }

@@ -228,4 +228,39 @@ cudaError_t launch_sort(Scene& s) {
     return launch_permute(s);
 }
 
+// Stable LSD sort of (keys, vals)[0..n) over the low `bits` key bits, with all
+// intermediate storage supplied by the caller: keys_alt/vals_alt (n words
+// each), hist (256 * ceil(n / 2048) words) and scan_tmp (ceil(hist / 1024)
+// words).  The sorted pairs end in keys/vals.
+cudaError_t radix_sort_pairs_in(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* hist,
+                                uint32_t* scan_tmp, uint32_t n, int bits, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    uint32_t nb = div_up(n, kSortTile);
+    uint32_t* k_in = keys;
+    uint32_t* v_in = vals;
+    uint32_t* k_out = keys_alt;
+    uint32_t* v_out = vals_alt;
+    for (int shift = 0; shift < bits; shift += 8) {
+        k_sort_hist<<<nb, kSortThreads, 0, st>>>(k_in, n, shift, hist);
+        cudaError_t e = exclusive_scan_u32(hist, 256u * nb, scan_tmp, st);
+        if (e != cudaSuccess) return e;
+        k_sort_scatter<<<nb, kSortThreads, 0, st>>>(k_in, v_in, n, shift, hist, k_out, v_out);
+        std::swap(k_in, k_out);
+        std::swap(v_in, v_out);
+    }
+    if (k_in != keys) {
+        cudaMemcpyAsync(keys, k_in, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(vals, v_in, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+    }
+    return cudaGetLastError();
+}
+
+// Bit length of the largest Morton key of a width x height grid.
+int morton_key_bits(uint32_t width, uint32_t height) {
+    Scene probe;
+    probe.W = width;
+    probe.H = height;
+    return key_bits(probe);
+}
+
 }  // namespace apic

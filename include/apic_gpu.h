@@ -228,6 +228,23 @@ int apic_synchronize(apic_handle* h);
 /* The handle's cudaStream_t, for callers that interleave their own work. */
 int apic_get_stream(apic_handle* h, void** stream_out);
 
+/* ---- Morton sort without device allocation ------------------------------ */
+/* No counterpart in the reference.  Computes the same Morton keys and stable
+ * sort permutation as the handle's sort stage, for callers that cannot
+ * allocate device memory: code recording work into a stream capture (where
+ * cudaMalloc is not allowed) and applications whose device memory belongs to
+ * another runtime or a fixed budget.  pos_x/pos_y: n device floats;
+ * keys_out/vals_out: n device u32 (sorted keys; original slot of each).
+ * Every intermediate buffer lives in one fixed device array inside the
+ * library (about 8.5 MiB, held by every GPU that loads it until exit), so n is
+ * limited to 1,048,576; larger n returns APIC_ERR_INVALID_ARG.  The first call
+ * on a device looks up that array's device address (do it before any stream
+ * capture).  Work is enqueued on `stream` (NULL: default stream); calls whose
+ * work overlaps on the GPU share the array and race.  Nothing in the array has
+ * to start at zero: every word is written before it is read. */
+int apic_morton_sort_noalloc(const float* pos_x, const float* pos_y, uint32_t n, uint32_t width, uint32_t height,
+                             float cell_size, uint32_t* keys_out, uint32_t* vals_out, void* stream);
+
 /* ---- testing hook ------------------------------------------------------ */
 /* Run one stage of the substep on the current device state with substep dt.
  * Derived device structures (fluid lists, segment lists) are rebuilt from the
