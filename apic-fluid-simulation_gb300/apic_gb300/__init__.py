@@ -63,7 +63,7 @@ class StatsC(ctypes.Structure):
                 ("pcg_iterations_total", ctypes.c_uint32), ("refinement_steps", ctypes.c_uint32),
                 ("residual_max", ctypes.c_float), ("residual_rel", ctypes.c_float),
                 ("true_residual_rel", ctypes.c_double), ("not_converged", ctypes.c_uint32),
-                ("nonfinite_lanes", ctypes.c_uint32)]
+                ("nonfinite_lanes", ctypes.c_uint32), ("kernel_launches", ctypes.c_uint64)]
 
 
 class SceneParamsC(ctypes.Structure):

@@ -69,6 +69,20 @@ inline cudaError_t add_conditional_with(GraphCursor& c, cudaGraphConditionalNode
     return cudaSuccess;
 }
 
+// Kernel nodes directly in a graph (conditional bodies are separate graphs).
+inline uint32_t count_kernel_nodes(cudaGraph_t g) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return 0;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return 0;
+    uint32_t k = 0;
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
+
 // Solver graph builder (solver.cu): appends the whole pressure solve of the
 // scene's solver mode to the cursor's graph.
 cudaError_t build_solve(Scene& s, GraphCursor& c);

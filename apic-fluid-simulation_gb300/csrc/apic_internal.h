@@ -64,6 +64,8 @@ struct Ctl {
     uint32_t refinements;
     uint32_t inner_cap;     // iteration cap of the running (inner) solve
     uint32_t used_iters;    // iterations used by the refinement loop so far
+    uint32_t refinements_total;  // refinements summed over the substeps of an update
+    uint32_t sorted;        // the update ran the Morton sort
     double dgamma;          // FP64 copies for the relative-tolerance modes
     double bnorm2;          // ||b||^2 of the running solve
     double rnorm2;          // ||r||^2 of the recursive residual
@@ -165,7 +167,9 @@ struct Scene {
     GridSync* gsync = nullptr;                // persistent solver barrier
     int persist_grid = 0;                     // CTAs of the persistent solver (0: unavailable)
     size_t persist_smem = 0;
-    bool use_persistent = true;               // persistent kernel vs graph of per-phase kernels
+    bool use_persistent = false;              // persistent kernel vs graph of per-phase kernels
+    // kernel nodes per execution of each graph body (launch accounting)
+    uint32_t kn_top = 0, kn_sort = 0, kn_loop = 0, kn_pcg = 0, kn_refine = 0;
     int solver_mode = APIC_SOLVER_REFERENCE;
     float rel_tol = 1e-6f;
     uint32_t max_iter = 500;

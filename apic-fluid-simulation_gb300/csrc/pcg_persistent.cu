@@ -334,6 +334,7 @@ __device__ bool solve(Ctx& c) {
         ctl->pcg_iters = used;
         ctl->pcg_iters_total += used;
         ctl->refinements = refinements;
+        ctl->refinements_total += refinements;
         ctl->rnorm2 = rn2;
         ctl->bnorm2 = bnorm2;
         ctl->true_rel = tr;

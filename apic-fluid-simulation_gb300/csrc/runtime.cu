@@ -56,6 +56,8 @@ __global__ void k_begin_update(Ctl* ctl, float frame_dt, uint32_t flags, uint32_
     ctl->has_post = has_post;
     ctl->status = 0;
     ctl->pcg_done = 0;
+    ctl->refinements_total = 0;
+    ctl->sorted = 0;
 }
 
 // Substep size (src/apic.rs:2433-2441) and the loop condition (:2432).
@@ -73,6 +75,7 @@ __device__ void plan(Ctl* ctl) {
     ctl->dt = step;
     ctl->go = 1;
     ctl->sort_now = (!(ctl->flags & APIC_UPDATE_DISABLE_SORT) && t == 0.0f) ? 1u : 0u;
+    if (ctl->sort_now) ctl->sorted = 1;
     ctl->vmax_bits = 0;    // the coming G2P reduces the next maximum
     ctl->nonfinite = 0;
 }
@@ -403,7 +406,12 @@ int ensure_update_graph(Scene& s) {
             k_advance_g<<<1, 1, 0, s.stream>>>(s.ctl, h_loop);
             return cudaGetLastError();
         });
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&s.update_exec, top.g, 0);
+    if (e == cudaSuccess) {
+        s.kn_top = count_kernel_nodes(top.g);
+        s.kn_sort = count_kernel_nodes(sort_body.g);
+        s.kn_loop = count_kernel_nodes(loop_body.g);
+        e = cudaGraphInstantiate(&s.update_exec, top.g, 0);
+    }
     cudaGraphDestroy(top.g);
     if (e != cudaSuccess) return fail(APIC_ERR_CUDA, std::string("update graph: ") + cudaGetErrorString(e));
     return APIC_OK;
@@ -650,6 +658,9 @@ int apic_update(apic_handle* h, uint32_t flags, float frame_dt) {
     s.stats.true_residual_rel = c.true_rel;
     s.stats.not_converged = c.not_converged;
     s.stats.nonfinite_lanes = c.nonfinite;
+    if (!s.profiling)
+        s.stats.kernel_launches = uint64_t(s.kn_top) + (c.sorted ? s.kn_sort : 0u) + uint64_t(c.substeps) * s.kn_loop +
+                                  uint64_t(c.pcg_iters_total) * s.kn_pcg + uint64_t(c.refinements_total) * s.kn_refine;
     if (c.status & kStatusTimeout) return fail(APIC_ERR_TIMEOUT, "a bounded device wait gave up (persistent solver barrier)");
     if (c.status & kStatusBadStep) return fail(APIC_ERR_NONFINITE, "substep size is not positive (non-finite velocities)");
     return APIC_OK;

@@ -197,6 +197,7 @@ __global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol
 __global__ void k_refine_post(Ctl* ctl) { ctl->used_iters += ctl->pcg_iters; }
 
 __global__ void k_refine_end(Ctl* ctl, double tol) {
+    ctl->refinements_total += ctl->refinements;
     ctl->pcg_iters = ctl->used_iters;
     ctl->pcg_iters_total += ctl->used_iters;
     if (ctl->true_rel > tol) ctl->not_converged++;
@@ -239,14 +240,17 @@ static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p
     GraphCursor body;
     e = add_conditional_with(c, cudaGraphCondTypeWhile, h, &body);
     if (e != cudaSuccess) return e;
-    return capture_into(s, body, [&]() {
+    e = capture_into(s, body, [&]() {
         pcg_iteration(s, mode, x, p_padded);
         k_pcg_cond<<<1, 1, 0, s.stream>>>(s.ctl, h, cap, dyn_cap);
         return cudaGetLastError();
     });
+    s.kn_pcg = count_kernel_nodes(body.g);
+    return e;
 }
 
 cudaError_t build_solve(Scene& s, GraphCursor& c) {
+    s.kn_pcg = s.kn_refine = 0;
     if (s.use_persistent && s.persist_grid > 0)
         return capture_into(s, c, [&]() { return enqueue_persistent_solve(s); });
     const Level& B = s.lv[0];
@@ -308,6 +312,7 @@ cudaError_t build_solve(Scene& s, GraphCursor& c) {
         return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
+    s.kn_refine = count_kernel_nodes(body.g);
     // the projection uses the FP64 pressure; its true residual is the one reported
     s.p64_valid = true;
     return capture_into(s, c, [&]() {

@@ -205,6 +205,8 @@ def run_gpu_arm(args, world, rank, local):
     sim.set_particles(px, py, vx, vy)
     mode = {"mixed": A.SOLVER_REL_MIXED, "fp32": A.SOLVER_REL_FP32, "reference": A.SOLVER_REFERENCE}[args.solver]
     sim.set_solver(mode, 1e-6, 500)
+    if args.persistent:
+        sim.set_option(A.OPT_PERSISTENT_SOLVE, 1)
     opts = A.DebugOptions()
     stream_ptr = ctypes_stream(sim)
     ext_stream = torch.cuda.ExternalStream(stream_ptr)
@@ -217,8 +219,10 @@ def run_gpu_arm(args, world, rank, local):
     # ---- timed region: K updates, device time per update, L2 flushed in between
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    substeps, iters = 0, 0
+    substeps, iters, launches = 0, 0, 0
     true_res = []
+    if args.eager:  # stage-by-stage launches (what an ncu launch list can see)
+        sim.set_profiling(True)
     dist_barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(dev) as clocks:
@@ -232,10 +236,13 @@ def run_gpu_arm(args, world, rank, local):
             st = sim.stats()
             substeps += st.substeps
             iters += st.pcg_iterations_total
+            launches += st.kernel_launches
             true_res.append(st.true_residual_rel)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     dist_barrier(world)
+    if args.eager:
+        sim.set_profiling(False)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     dev_s = sum(step_ms) / 1e3
     dev_s_max = dist_max(dev_s, world)
@@ -297,7 +304,9 @@ def run_gpu_arm(args, world, rank, local):
                                   "reference": "reference exits (max|r| < 1e-5, 100 iterations)"}[args.solver],
                        "substeps": substeps, "pcg_iterations": iters,
                        "true_residual_rel_max": max(true_res) if true_res else None,
-                       "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
+                       "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
+                       "solve_form": "persistent kernel" if args.persistent else "graph of per-phase kernels",
+                       "launch": "stage by stage" if args.eager else "one CUDA graph per update"},
             "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
             "wall_s": wall,
             "clocks": clocks.summary(),
@@ -305,7 +314,7 @@ def run_gpu_arm(args, world, rank, local):
                     "steps": e2e_steps,
                     "what": "apic_write_field(ext force u,v) from pinned host + apic_update + "
                             "apic_read_vec2x8(positions, velocities) to pinned host"},
-            "gpu_launches": None,
+            "gpu_launches": launches if not args.eager else None,
             "roofline": roof,
             "stage_ms_per_step": {k: v[0] / prof_steps for k, v in stages.items() if v[1]},
             "cpu_baseline": cpu,
@@ -360,6 +369,10 @@ def main():
     ap.add_argument("--solver", default="mixed", choices=["mixed", "fp32", "reference"])
     ap.add_argument("--side", type=int, default=SIDE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--eager", action="store_true",
+                    help="launch the stages one by one in the timed region (for ncu launch lists)")
+    ap.add_argument("--persistent", action="store_true",
+                    help="run the pressure solve as one persistent cooperative kernel")
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--cpu-budget", type=float, default=30.0)
     args = ap.parse_args()

@@ -84,6 +84,7 @@ typedef struct apic_step_stats {
     double   true_residual_rel;    /* ||b - A p||_2 / ||b||_2 in FP64 (solver modes 1, 2) */
     uint32_t not_converged;        /* substeps whose solve hit its iteration cap */
     uint32_t nonfinite_lanes;      /* NaN/Inf particle lanes after the last G2P */
+    uint64_t kernel_launches;      /* kernels the last update's graph launched (0 when profiling) */
 } apic_step_stats;
 
 /* ---- field identifiers for apic_read_field / apic_write_field ---------- */
@@ -208,10 +209,10 @@ int apic_set_particles(apic_handle* h, uint32_t n, const float* pos_x, const flo
 int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterations);
 
 /* ---- execution options --------------------------------------------------- */
-/* 1 (default where cooperative launch is possible): the whole pressure solve
- * runs as one persistent cooperative kernel (one CTA per SM, grid barriers
- * between phases).  0: a CUDA graph of per-phase kernels with device-side
- * WHILE loops.  Both compute the same iterations. */
+/* 1: the whole pressure solve runs as one persistent cooperative kernel (one
+ * CTA per SM, grid barriers between phases; needs cooperative launch).
+ * 0 (default): a CUDA graph of per-phase kernels with device-side WHILE
+ * loops.  Both compute the same iterations. */
 #define APIC_OPT_PERSISTENT_SOLVE 1
 int apic_set_option(apic_handle* h, int option, int value);
 int apic_get_option(apic_handle* h, int option, int* value);
