@@ -65,6 +65,7 @@ struct Ctl {
     uint32_t inner_cap;     // iteration cap of the running (inner) solve
     uint32_t used_iters;    // iterations used by the refinement loop so far
     uint32_t refinements_total;  // refinements summed over the substeps of an update
+    uint32_t cond;          // last loop decision of a control kernel (eager runs read it)
     uint32_t sorted;        // the update ran the Morton sort
     double dgamma;          // FP64 copies for the relative-tolerance modes
     double bnorm2;          // ||b||^2 of the running solve
@@ -163,7 +164,6 @@ struct Scene {
     cudaStream_t stream = nullptr;
     cudaStream_t cap_stream = nullptr;        // stream used to record graphs
     cudaGraphExec_t update_exec = nullptr;    // whole Apic::update as one graph
-    cudaGraphExec_t solve_exec = nullptr;     // the pressure solve alone
     GridSync* gsync = nullptr;                // persistent solver barrier
     int persist_grid = 0;                     // CTAs of the persistent solver (0: unavailable)
     size_t persist_smem = 0;
@@ -216,6 +216,9 @@ cudaError_t launch_level_lists(Scene& s, int level);
 // pcg_persistent.cu
 void plan_persistent_solve(Scene& s);
 cudaError_t enqueue_persistent_solve(Scene& s);
+// solver.cu: the same solve launched kernel by kernel with host loop control
+// (profiling runs, so every kernel is a separate launch)
+cudaError_t run_solve_eager(Scene& s);
 // vcycle.cu
 void plan_vcycle(Scene& s);     // pick the coarse levels that run in one CTA
 void enqueue_vcycle(Scene& s);  // z = M^-1 r on s.stream

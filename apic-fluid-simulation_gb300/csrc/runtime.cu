@@ -207,8 +207,7 @@ void free_scene(Scene& s) {
     if (s.ev_a) cudaEventDestroy(s.ev_a);
     if (s.ev_b) cudaEventDestroy(s.ev_b);
     if (s.update_exec) cudaGraphExecDestroy(s.update_exec);
-    if (s.solve_exec) cudaGraphExecDestroy(s.solve_exec);
-    s.update_exec = s.solve_exec = nullptr;
+    s.update_exec = nullptr;
     if (s.cap_stream) cudaStreamDestroy(s.cap_stream);
     s.cap_stream = nullptr;
     if (s.stream) cudaStreamDestroy(s.stream);
@@ -218,8 +217,7 @@ void free_scene(Scene& s) {
 // Graphs bake in launch shapes and solver settings: rebuild after changes.
 void invalidate_graphs(Scene& s) {
     if (s.update_exec) cudaGraphExecDestroy(s.update_exec);
-    if (s.solve_exec) cudaGraphExecDestroy(s.solve_exec);
-    s.update_exec = s.solve_exec = nullptr;
+    s.update_exec = nullptr;
 }
 
 // Open-face masks from the obstacle mask (update_world, src/apic.rs:918-944).
@@ -369,17 +367,6 @@ cudaError_t enqueue_post_solve(Scene& s) {
     return launch_g2p(s);
 }
 
-int ensure_solve_graph(Scene& s) {
-    if (s.solve_exec) return APIC_OK;
-    GraphCursor c;
-    CK(cudaGraphCreate(&c.g, 0));
-    cudaError_t e = build_solve(s, c);
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&s.solve_exec, c.g, 0);
-    cudaGraphDestroy(c.g);
-    if (e != cudaSuccess) return fail(APIC_ERR_CUDA, std::string("solve graph: ") + cudaGetErrorString(e));
-    return APIC_OK;
-}
-
 // Apic::update as one graph: plan -> IF(sort) -> WHILE(substep due) { stages; advance }.
 int ensure_update_graph(Scene& s) {
     if (s.update_exec) return APIC_OK;
@@ -420,18 +407,12 @@ int ensure_update_graph(Scene& s) {
 // One substep launched stage by stage, each bracketed by events when
 // profiling (the graph form cannot hold event nodes inside its loops).
 int run_substep_eager(Scene& s, bool sort_now) {
-    int rc = ensure_solve_graph(s);
-    if (rc) return rc;
     if (sort_now) { StageTimer t(s, APIC_STAGE_SORT); CK(launch_sort(s)); }
     { StageTimer t(s, APIC_STAGE_P2G); CK(clear_p2g_targets(s)); CK(launch_p2g(s)); }
     { StageTimer t(s, APIC_STAGE_FORCES); CK(launch_finalize_faces(s, true, true)); CK(launch_base_lists(s)); }
     { StageTimer t(s, APIC_STAGE_BUILD); CK(launch_build_pressure(s)); }
     { StageTimer t(s, APIC_STAGE_MG); CK(launch_multilevel(s)); }
-    {
-        StageTimer t(s, APIC_STAGE_PCG);
-        if (s.use_persistent && s.persist_grid > 0) CK(enqueue_persistent_solve(s));
-        else CK(cudaGraphLaunch(s.solve_exec, s.stream));
-    }
+    { StageTimer t(s, APIC_STAGE_PCG); CK(run_solve_eager(s)); }
     { StageTimer t(s, APIC_STAGE_GRAD); CK(launch_gradient(s, true)); }
     { StageTimer t(s, APIC_STAGE_EXTRAP); CK(launch_extrapolate(s)); }
     { StageTimer t(s, APIC_STAGE_G2P); CK(launch_g2p(s)); }
@@ -984,13 +965,7 @@ int apic_debug_run_stage(apic_handle* h, int stage, float dt) {
         case APIC_STAGE_PCG: {
             k_begin_update<<<1, 1, 0, st>>>(s.ctl, 0.0f, 0u, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
             k_set_dt<<<1, 1, 0, st>>>(s.ctl, dt, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
-            if (s.use_persistent && s.persist_grid > 0) {
-                CK(enqueue_persistent_solve(s));
-            } else {
-                int rg = ensure_solve_graph(s);
-                if (rg) return rg;
-                CK(cudaGraphLaunch(s.solve_exec, st));
-            }
+            CK(run_solve_eager(s));
             int rc = sync_ctl(s);
             if (rc) return rc;
             const Ctl& c = *s.ctl_host;

@@ -180,7 +180,7 @@ __global__ void k_rel_begin(Ctl* ctl, double tol, uint32_t cap) {
 // (the current true residual) by kInnerReduction, or down to tol / 2 of ||b||
 // when that is reached first; FP32 cannot usefully reduce it further.
 constexpr double kInnerReduction = 1e-4;
-__global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol, uint32_t cap) {
+__global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol, uint32_t cap, int graph) {
     bool cont = ctl->true_rel > tol && ctl->used_iters < cap && ctl->refinements < 32u;
     // an inner solve that could not take a single step (r.z underflows or is
     // zero) will not make progress on the next round either
@@ -191,7 +191,8 @@ __global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol
         double t = kInnerReduction * ctl->true_rel;  // target relative to ||b||
         ctl->target_rel = t > 0.5 * tol ? t : 0.5 * tol;
     }
-    cudaGraphSetConditional(h, cont ? 1u : 0u);
+    ctl->cond = cont ? 1u : 0u;
+    if (graph) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 
 __global__ void k_refine_post(Ctl* ctl) { ctl->used_iters += ctl->pcg_iters; }
@@ -294,7 +295,7 @@ cudaError_t build_solve(Scene& s, GraphCursor& c) {
     e = capture_into(s, c, [&]() {
         cudaStream_t st = s.stream;
         k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 3);
-        k_refine_cond<<<1, 1, 0, st>>>(s.ctl, hr, tol, s.max_iter);
+        k_refine_cond<<<1, 1, 0, st>>>(s.ctl, hr, tol, s.max_iter, 1);
         return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
@@ -308,7 +309,7 @@ cudaError_t build_solve(Scene& s, GraphCursor& c) {
         k_mixed_accumulate<<<g, kSegBlock, 0, st>>>(B, s.p64, s.corr, s.pressure, s.ctl, 0);
         k_refine_post<<<1, 1, 0, st>>>(s.ctl);
         k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 3);
-        k_refine_cond<<<1, 1, 0, st>>>(s.ctl, hr, tol, s.max_iter);
+        k_refine_cond<<<1, 1, 0, st>>>(s.ctl, hr, tol, s.max_iter, 1);
         return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
@@ -321,6 +322,73 @@ cudaError_t build_solve(Scene& s, GraphCursor& c) {
         k_refine_end<<<1, 1, 0, st>>>(s.ctl, tol);
         return cudaGetLastError();
     });
+}
+
+// ---- eager form (profiling): same kernels, host-side loop control ----------
+
+static cudaError_t read_ctl(Scene& s) {
+    cudaError_t e = cudaMemcpyAsync(s.ctl_host, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s.stream);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s.stream);
+}
+
+// PCG setup and iterations until the device flags convergence or the cap.
+static cudaError_t eager_pcg(Scene& s, int mode, float* x, int p_padded, uint32_t cap, bool clear_pressure) {
+    const Level& B = s.lv[0];
+    uint32_t g = seg_grid(B.words);
+    cudaStream_t st = s.stream;
+    k_pcg_begin<<<1, 1, 0, st>>>(s.ctl);
+    if (clear_pressure) k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
+    enqueue_vcycle(s);
+    k_pcg_start<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl, s.partials, mode);
+    for (;;) {
+        cudaError_t e = read_ctl(s);
+        if (e != cudaSuccess) return e;
+        if (s.ctl_host->pcg_done || s.ctl_host->pcg_iters >= cap) break;
+        pcg_iteration(s, mode, x, p_padded);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t run_solve_eager(Scene& s) {
+    if (s.use_persistent && s.persist_grid > 0) return enqueue_persistent_solve(s);
+    const Level& B = s.lv[0];
+    uint32_t g = seg_grid(B.words);
+    cudaStream_t st = s.stream;
+    int mode = s.solver_mode;
+    s.p64_valid = false;
+    cudaError_t e;
+    if (mode == APIC_SOLVER_REFERENCE) {
+        if ((e = eager_pcg(s, mode, s.pressure, 0, 100, true)) != cudaSuccess) return e;
+        k_finish_solve<<<1, 1, 0, st>>>(s.ctl, 100);
+        return cudaGetLastError();
+    }
+    const double tol = double(s.rel_tol);
+    k_mixed_init<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.ctl, s.partials);
+    k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
+    k_rel_begin<<<1, 1, 0, st>>>(s.ctl, tol, s.max_iter);
+    if (mode == APIC_SOLVER_REL_FP32) {
+        if ((e = eager_pcg(s, mode, s.pressure, 0, s.max_iter, false)) != cudaSuccess) return e;
+        k_finish_solve<<<1, 1, 0, st>>>(s.ctl, s.max_iter);
+        k_pressure_to64<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.p64, s.ctl);
+        k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 1);
+        return cudaGetLastError();
+    }
+    k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 3);
+    k_refine_cond<<<1, 1, 0, st>>>(s.ctl, 0, tol, s.max_iter, 0);
+    for (;;) {
+        if ((e = read_ctl(s)) != cudaSuccess) return e;
+        if (!s.ctl_host->cond) break;
+        if ((e = eager_pcg(s, APIC_SOLVER_REL_FP32, s.corr, 1, s.ctl_host->inner_cap, false)) != cudaSuccess) return e;
+        k_mixed_accumulate<<<g, kSegBlock, 0, st>>>(B, s.p64, s.corr, s.pressure, s.ctl, 0);
+        k_refine_post<<<1, 1, 0, st>>>(s.ctl);
+        k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 3);
+        k_refine_cond<<<1, 1, 0, st>>>(s.ctl, 0, tol, s.max_iter, 0);
+    }
+    s.p64_valid = true;
+    k_mixed_accumulate<<<g, kSegBlock, 0, st>>>(B, s.p64, s.corr, s.pressure, s.ctl, 1);
+    k_refine_end<<<1, 1, 0, st>>>(s.ctl, tol);
+    return cudaGetLastError();
 }
 
 }  // namespace apic

@@ -248,12 +248,15 @@ def test_full_update_drift(oracle_mod):
     assert worst < 0.25 / side
 
 
-def test_graph_and_staged_paths_agree(gpu_lib):
-    """apic_update as one CUDA graph vs stage-by-stage launches (profiling)."""
+@pytest.mark.parametrize("mode", [A.SOLVER_REFERENCE, A.SOLVER_REL_MIXED])
+def test_graph_and_staged_paths_agree(gpu_lib, mode):
+    """apic_update as one CUDA graph vs kernel-by-kernel launches (profiling)."""
     props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
     side = 64
     a = A.Apic(side, side, 1 / side, props)
     b = A.Apic(side, side, 1 / side, props)
+    for g in (a, b):
+        g.set_solver(mode, 1e-6, 500)
     b.set_profiling(True)
     opts = A.DebugOptions(disable_particle_sort=True)
     for _ in range(3):
