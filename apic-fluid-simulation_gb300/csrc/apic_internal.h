@@ -168,6 +168,7 @@ struct Scene {
     int persist_grid = 0;                     // CTAs of the persistent solver (0: unavailable)
     size_t persist_smem = 0;
     bool use_persistent = false;              // persistent kernel vs graph of per-phase kernels
+    bool fused_vcycle = true;                 // one kernel per level and direction in the V-cycle
     // kernel nodes per execution of each graph body (launch accounting)
     uint32_t kn_top = 0, kn_sort = 0, kn_loop = 0, kn_pcg = 0, kn_refine = 0;
     int solver_mode = APIC_SOLVER_REFERENCE;

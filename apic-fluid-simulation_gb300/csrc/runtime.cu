@@ -901,6 +901,10 @@ int apic_set_option(apic_handle* h, int option, int value) {
             s.use_persistent = value != 0;
             invalidate_graphs(s);
             return APIC_OK;
+        case APIC_OPT_FUSED_VCYCLE:
+            s.fused_vcycle = value != 0;
+            invalidate_graphs(s);
+            return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }
@@ -909,6 +913,7 @@ int apic_get_option(apic_handle* h, int option, int* value) {
     if (valid_handle(h) || !value) return fail(APIC_ERR_INVALID_ARG, "null argument");
     switch (option) {
         case APIC_OPT_PERSISTENT_SOLVE: *value = (h->s.use_persistent && h->s.persist_grid > 0) ? 1 : 0; return APIC_OK;
+        case APIC_OPT_FUSED_VCYCLE: *value = h->s.fused_vcycle ? 1 : 0; return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }

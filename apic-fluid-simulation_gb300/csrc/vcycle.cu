@@ -68,6 +68,19 @@ __global__ void __launch_bounds__(kSegBlock) k_prolong_red(Level c, Level f, int
                base ? ctl->pad_count : 0u);
 }
 
+// Fused descent: finish fine level's pre-smoothing, restrict, coarse red sweep.
+__global__ void __launch_bounds__(kSegBlock) k_down(Level f, Level c, int lc, const Ctl* ctl, int base, int with_red) {
+    if (ctl->pcg_done) return;
+    ph_down(f, c, ctl->seg_count[lc], gwarp(), gnwarps(), base != 0, with_red != 0);
+}
+
+// Fused ascent: prolongation with both post-smoothing sweeps.
+__global__ void __launch_bounds__(kSegBlock) k_up(Level c, Level f, int lf, const Ctl* ctl, int base) {
+    if (ctl->pcg_done) return;
+    ph_up(c, f, ctl->seg_count[lf], gwarp(), gnwarps(), base ? ctl->last_fluid : 0xFFFFFFFFu,
+          base ? ctl->pad_count : 0u);
+}
+
 __global__ void __launch_bounds__(kTailThreads) k_coarse_solve(Level L, float* __restrict__ cs, float* __restrict__ cap,
                                                                float* __restrict__ cr, const Ctl* __restrict__ ctl) {
     if (ctl->pcg_done) return;
@@ -105,8 +118,36 @@ void plan_vcycle(Scene& s) {
     }
 }
 
-// One V-cycle on s.stream: z = M^-1 r in lv[0].err.
+static void enqueue_vcycle_unfused(Scene& s);
+
+// One V-cycle on s.stream: z = M^-1 r in lv[0].err.  Fused form: one kernel
+// per level down (k_down) and up (k_up) around the coarse tail.
 void enqueue_vcycle(Scene& s) {
+    if (!s.fused_vcycle || s.nlevels < 2) {
+        enqueue_vcycle_unfused(s);
+        return;
+    }
+    cudaStream_t st = s.stream;
+    Level* L = s.lv;
+    auto grid = [&](int l) { return seg_grid(L[l].words); };
+    const int last = s.nlevels - 1;
+    const int deepest = s.tail_first < s.nlevels ? s.tail_first : last;  // solved by the tail or the coarse CG
+    for (int l = 0; l < deepest; ++l)
+        k_down<<<grid(l + 1), kSegBlock, 0, st>>>(L[l], L[l + 1], l + 1, s.ctl, l == 0 ? 1 : 0,
+                                                   l + 1 < deepest ? 1 : 0);
+    if (s.tail_first < s.nlevels) {
+        uint32_t off = 0;
+        TailParams tp = make_tail_params(s, s.tail_first, &off);
+        k_vcycle_tail<<<1, kTailThreads, size_t(off) * 4, st>>>(tp, s.ctl);
+    } else {
+        k_coarse_solve<<<1, kTailThreads, 0, st>>>(L[last], s.cg_s, s.cg_ap, s.cg_r, s.ctl);
+    }
+    for (int l = deepest - 1; l >= 0; --l)
+        k_up<<<grid(l), kSegBlock, 0, st>>>(L[l + 1], L[l], l, s.ctl, l == 0 ? 1 : 0);
+}
+
+// Two kernels per sweep and per transfer (the reference's sequence launch by launch).
+static void enqueue_vcycle_unfused(Scene& s) {
     cudaStream_t st = s.stream;
     Level* L = s.lv;
     auto grid = [&](int l) { return seg_grid(L[l].words); };

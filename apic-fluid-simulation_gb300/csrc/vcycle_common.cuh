@@ -41,9 +41,11 @@ __device__ __forceinline__ float sor_cell(const uint32_t* bits, uint32_t w, uint
 }
 
 // Coarse residual of coarse cell (cx, cy) from its fine children (:549-583).
-__device__ __forceinline__ float restrict_cell(const uint32_t* fb, uint32_t fw, uint32_t fcells, const float* fd,
-                                               const float* fpx, const float* fpy, const float* fr, const float* fe,
-                                               uint32_t cx, uint32_t cy) {
+// E(padded, raw) gives the fine error of a fluid cell.
+template <class E>
+__device__ __forceinline__ float restrict_cell_fn(const uint32_t* fb, uint32_t fw, uint32_t fcells, const float* fd,
+                                                  const float* fpx, const float* fpy, const float* fr, E fe,
+                                                  uint32_t cx, uint32_t cy) {
     float sum = 0.0f;
     const long long W = fw;
     for (uint32_t dy = 0; dy < 2; ++dy)
@@ -52,14 +54,20 @@ __device__ __forceinline__ float restrict_cell(const uint32_t* fb, uint32_t fw, 
             if (!fluid_raw(fb, rf, fcells)) continue;
             uint32_t pf = uint32_t(rf) + fw;
             float b = fr[pf];
-            float ax = fd[pf] * fe[pf];
-            if (fluid_raw(fb, rf + 1, fcells)) ax += fpx[pf] * fe[pf + 1];
-            if (fluid_raw(fb, rf + W, fcells)) ax += fpy[pf] * fe[pf + fw];
-            if (fluid_raw(fb, rf - 1, fcells)) ax += fpx[pf - 1] * fe[pf - 1];
-            if (fluid_raw(fb, rf - W, fcells)) ax += fpy[pf - fw] * fe[pf - fw];
+            float ax = fd[pf] * fe(pf, rf);
+            if (fluid_raw(fb, rf + 1, fcells)) ax += fpx[pf] * fe(pf + 1, rf + 1);
+            if (fluid_raw(fb, rf + W, fcells)) ax += fpy[pf] * fe(pf + fw, rf + W);
+            if (fluid_raw(fb, rf - 1, fcells)) ax += fpx[pf - 1] * fe(pf - 1, rf - 1);
+            if (fluid_raw(fb, rf - W, fcells)) ax += fpy[pf - fw] * fe(pf - fw, rf - W);
             sum += b - ax;
         }
     return sum;
+}
+
+__device__ __forceinline__ float restrict_cell(const uint32_t* fb, uint32_t fw, uint32_t fcells, const float* fd,
+                                               const float* fpx, const float* fpy, const float* fr, const float* fe,
+                                               uint32_t cx, uint32_t cy) {
+    return restrict_cell_fn(fb, fw, fcells, fd, fpx, fpy, fr, [fe](uint32_t p, long long) { return fe[p]; }, cx, cy);
 }
 
 __device__ __forceinline__ bool is_red(uint32_t raw, uint32_t w) { return (((raw % w) + (raw / w)) & 1u) == 0u; }
@@ -360,6 +368,91 @@ __device__ __forceinline__ void cta_tail_load_coeffs(const TailParams& tp, uint3
             L.py[i] = t.py[i];
         }
     }
+}
+
+// ---- fused sweeps: one kernel per level and direction ----------------------
+// The values a sweep would read from cells that another thread updates in
+// the same launch are recomputed locally from their own inputs, with the same
+// float operations, so the result equals the two-sweep sequence bit for bit.
+
+// First red sweep value of a cell whose error was zero-filled.
+__device__ __forceinline__ float red_init_value(const Level& L, uint32_t p) {
+    float inv = L.inv_diag[p];
+    return inv != 0.0f ? 0.0f + (kOmega * (L.res[p] * inv - 0.0f)) : 0.0f;
+}
+
+// Error of fine cell q after the two pre-smoothing sweeps (red then black,
+// from zero).  base: red values are computed on the fly from the residual;
+// otherwise they are already in L.err.
+__device__ __forceinline__ float pre_smoothed(const Level& L, uint32_t q, long long rq, bool base) {
+    if (is_red(uint32_t(rq), L.w)) return base ? red_init_value(L, q) : L.err[q];
+    const float* e = L.err;
+    if (base)
+        return sor_cell(L.fluid, L.w, L.cells, L.inv_diag, L.px, L.py, L.res, rq, q, 0.0f, true,
+                        [&L](uint32_t p, long long) { return red_init_value(L, p); });
+    return sor_cell(L.fluid, L.w, L.cells, L.inv_diag, L.px, L.py, L.res, rq, q, 0.0f, true,
+                    [e](uint32_t p, long long) { return e[p]; });
+}
+
+// Descent from fine level f to coarse level c, over coarse fluid cells:
+// finish f's pre-smoothing for the 2x2 children (written back), restrict to
+// c's residual and, with_red, run c's first red sweep.
+__device__ __forceinline__ void ph_down(const Level& f, const Level& c, uint32_t nseg_c, uint32_t warp,
+                                        uint32_t nwarps, bool base, bool with_red) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t s = warp; s < nseg_c; s += nwarps) {
+        uint32_t word = c.seg[s];
+        if (!((c.fluid[word] >> lane) & 1u)) continue;
+        uint32_t rc = word * 32 + lane;
+        uint32_t cx = rc % c.w, cy = rc / c.w;
+        for (uint32_t dy = 0; dy < 2; ++dy)
+            for (uint32_t dx = 0; dx < 2; ++dx) {
+                long long rf = (long long)(cy * 2 + dy) * f.w + (cx * 2 + dx);
+                if (!fluid_raw(f.fluid, rf, f.cells)) continue;
+                uint32_t pf = uint32_t(rf) + f.w;
+                if (base || !is_red(uint32_t(rf), f.w)) f.err[pf] = pre_smoothed(f, pf, rf, base);
+            }
+        float r = restrict_cell_fn(f.fluid, f.w, f.cells, f.diag, f.px, f.py, f.res,
+                                   [&f, base](uint32_t p, long long rp) { return pre_smoothed(f, p, rp, base); },
+                                   cx, cy);
+        uint32_t cp = rc + c.w;
+        c.res[cp] = r;
+        if (with_red && is_red(rc, c.w)) {
+            float inv = c.inv_diag[cp];
+            c.err[cp] = inv != 0.0f ? 0.0f + (kOmega * (r * inv - 0.0f)) : 0.0f;
+        }
+    }
+}
+
+// Ascent into fine level f from coarse level c: prolongation plus the black
+// and red post-sweeps in one pass.  Returns this thread's r.z over its final
+// values (used on the base level).
+__device__ __forceinline__ double ph_up(const Level& c, const Level& f, uint32_t nseg_f, uint32_t warp,
+                                        uint32_t nwarps, uint32_t last, uint32_t extra) {
+    const uint32_t lane = threadIdx.x & 31;
+    const float* fe = f.err;
+    const float* ce = c.err;
+    const uint32_t fw = f.w, cw = c.w;
+    auto pro = [=](uint32_t q, long long rq) {
+        uint32_t r = uint32_t(rq);
+        return prolonged(fe[q], ce[((r / fw) / 2) * cw + (r % fw) / 2 + cw], q == last ? extra : 0u);
+    };
+    auto black_new = [&](uint32_t q, long long rq) {
+        return sor_cell(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, rq, q, pro(q, rq), true, pro);
+    };
+    double rz = 0.0;
+    for (uint32_t s = warp; s < nseg_f; s += nwarps) {
+        uint32_t word = f.seg[s];
+        if (!((f.fluid[word] >> lane) & 1u)) continue;
+        uint32_t raw = word * 32 + lane;
+        uint32_t p = raw + fw;
+        float z;
+        if (!is_red(raw, fw)) z = black_new(p, raw);
+        else z = sor_cell(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, raw, p, pro(p, raw), true, black_new);
+        f.err[p] = z;
+        rz += double(f.res[p] * z);
+    }
+    return rz;
 }
 
 // The coarse tail (levels held in shared memory) by one CTA.  load_coeffs:

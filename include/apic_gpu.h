@@ -214,6 +214,11 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
  * 0 (default): a CUDA graph of per-phase kernels with device-side WHILE
  * loops.  Both compute the same iterations. */
 #define APIC_OPT_PERSISTENT_SOLVE 1
+/* 1 (default): the V-cycle runs one kernel per level going down and one going
+ * up (values another thread updates in the same kernel are recomputed
+ * locally).  0: one kernel per sweep and per transfer.  Same results bit for
+ * bit. */
+#define APIC_OPT_FUSED_VCYCLE 2
 int apic_set_option(apic_handle* h, int option, int value);
 int apic_get_option(apic_handle* h, int option, int* value);
 
