@@ -104,6 +104,7 @@ struct Level {
     float* py = nullptr;
     float* res = nullptr;
     float* err = nullptr;
+    float* err2 = nullptr;  // second error array of the fused V-cycle (never updated in place)
 };
 
 // Particle field order, matching apic_field ids 0..8.

@@ -198,7 +198,7 @@ void free_scene(Scene& s) {
     for (int l = 0; l < s.nlevels; ++l) {
         Level& L = s.lv[l];
         dfree(L.fluid); dfree(L.seg); dfree(L.diag); dfree(L.inv_diag); dfree(L.px); dfree(L.py);
-        dfree(L.res); dfree(L.err);
+        dfree(L.res); dfree(L.err); dfree(L.err2);
     }
     dfree(s.ctl);
     if (s.ctl_host) cudaFreeHost(s.ctl_host);
@@ -526,7 +526,7 @@ int apic_create(uint32_t width, uint32_t height, float cell_size, const apic_wor
         max_words = std::max(max_words, L.words);
         AL(L.fluid, L.words); AL(L.seg, L.words);
         AL(L.diag, L.padded); AL(L.inv_diag, L.padded); AL(L.px, L.padded); AL(L.py, L.padded);
-        AL(L.res, L.padded); AL(L.err, L.padded);
+        AL(L.res, L.padded); AL(L.err, L.padded); AL(L.err2, L.padded);
     }
     {
         Level& C = s.lv[s.nlevels - 1];

@@ -74,10 +74,13 @@ __global__ void __launch_bounds__(kSegBlock) k_down(Level f, Level c, int lc, co
     ph_down(f, c, ctl->seg_count[lc], gwarp(), gnwarps(), base != 0, with_red != 0);
 }
 
-// Fused ascent: prolongation with both post-smoothing sweeps.
-__global__ void __launch_bounds__(kSegBlock) k_up(Level c, Level f, int lf, const Ctl* ctl, int base) {
+// Fused ascent: prolongation with both post-smoothing sweeps.  c_fin: the
+// coarse level's final error; f_pre / f_fin: this level's pre-smoothed and
+// final error arrays.
+__global__ void __launch_bounds__(kSegBlock) k_up(const float* c_fin, uint32_t cw, Level f, const float* f_pre,
+                                                  float* f_fin, int lf, const Ctl* ctl, int base) {
     if (ctl->pcg_done) return;
-    ph_up(c, f, ctl->seg_count[lf], gwarp(), gnwarps(), base ? ctl->last_fluid : 0xFFFFFFFFu,
+    ph_up(c_fin, cw, f, f_pre, f_fin, ctl->seg_count[lf], gwarp(), gnwarps(), base ? ctl->last_fluid : 0xFFFFFFFFu,
           base ? ctl->pad_count : 0u);
 }
 
@@ -142,8 +145,13 @@ void enqueue_vcycle(Scene& s) {
     } else {
         k_coarse_solve<<<1, kTailThreads, 0, st>>>(L[last], s.cg_s, s.cg_ap, s.cg_r, s.ctl);
     }
+    // pre-smoothed error: base in err2, other levels in err; final error:
+    // base in err (what PCG reads), mid levels in err2, the deepest level in
+    // err (written by the tail or the coarse CG)
+    auto pre = [&](int l) { return l == 0 ? L[0].err2 : L[l].err; };
+    auto fin = [&](int l) { return (l == 0 || l == deepest) ? L[l].err : L[l].err2; };
     for (int l = deepest - 1; l >= 0; --l)
-        k_up<<<grid(l), kSegBlock, 0, st>>>(L[l + 1], L[l], l, s.ctl, l == 0 ? 1 : 0);
+        k_up<<<grid(l), kSegBlock, 0, st>>>(fin(l + 1), L[l + 1].w, L[l], pre(l), fin(l), l, s.ctl, l == 0 ? 1 : 0);
 }
 
 // Two kernels per sweep and per transfer (the reference's sequence launch by launch).

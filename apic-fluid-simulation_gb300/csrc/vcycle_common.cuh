@@ -383,7 +383,7 @@ __device__ __forceinline__ float red_init_value(const Level& L, uint32_t p) {
 
 // Error of fine cell q after the two pre-smoothing sweeps (red then black,
 // from zero).  base: red values are computed on the fly from the residual;
-// otherwise they are already in L.err.
+// otherwise they are already in L.err (written by the descent into L).
 __device__ __forceinline__ float pre_smoothed(const Level& L, uint32_t q, long long rq, bool base) {
     if (is_red(uint32_t(rq), L.w)) return base ? red_init_value(L, q) : L.err[q];
     const float* e = L.err;
@@ -395,11 +395,14 @@ __device__ __forceinline__ float pre_smoothed(const Level& L, uint32_t q, long l
 }
 
 // Descent from fine level f to coarse level c, over coarse fluid cells:
-// finish f's pre-smoothing for the 2x2 children (written back), restrict to
-// c's residual and, with_red, run c's first red sweep.
+// store f's pre-smoothed error for the 2x2 children in f_pre (the base keeps
+// it apart in err2; other levels in err, whose red cells the previous
+// descent already set), restrict to c's residual and, with_red, run c's first
+// red sweep into c.err.  No value read in this launch is written in it.
 __device__ __forceinline__ void ph_down(const Level& f, const Level& c, uint32_t nseg_c, uint32_t warp,
                                         uint32_t nwarps, bool base, bool with_red) {
     const uint32_t lane = threadIdx.x & 31;
+    float* f_pre = base ? f.err2 : f.err;
     for (uint32_t s = warp; s < nseg_c; s += nwarps) {
         uint32_t word = c.seg[s];
         if (!((c.fluid[word] >> lane) & 1u)) continue;
@@ -410,7 +413,7 @@ __device__ __forceinline__ void ph_down(const Level& f, const Level& c, uint32_t
                 long long rf = (long long)(cy * 2 + dy) * f.w + (cx * 2 + dx);
                 if (!fluid_raw(f.fluid, rf, f.cells)) continue;
                 uint32_t pf = uint32_t(rf) + f.w;
-                if (base || !is_red(uint32_t(rf), f.w)) f.err[pf] = pre_smoothed(f, pf, rf, base);
+                if (base || !is_red(uint32_t(rf), f.w)) f_pre[pf] = pre_smoothed(f, pf, rf, base);
             }
         float r = restrict_cell_fn(f.fluid, f.w, f.cells, f.diag, f.px, f.py, f.res,
                                    [&f, base](uint32_t p, long long rp) { return pre_smoothed(f, p, rp, base); },
@@ -424,18 +427,19 @@ __device__ __forceinline__ void ph_down(const Level& f, const Level& c, uint32_t
     }
 }
 
-// Ascent into fine level f from coarse level c: prolongation plus the black
-// and red post-sweeps in one pass.  Returns this thread's r.z over its final
-// values (used on the base level).
-__device__ __forceinline__ double ph_up(const Level& c, const Level& f, uint32_t nseg_f, uint32_t warp,
-                                        uint32_t nwarps, uint32_t last, uint32_t extra) {
+// Ascent into fine level f from the coarse level's final error c_fin:
+// prolongation plus the black and red post-sweeps in one pass, reading the
+// pre-smoothed error f_pre and writing the final error f_fin (a different
+// array, so neighbours always read pre-sweep values).  Returns this thread's
+// r.z over its final values (used on the base level).
+__device__ __forceinline__ double ph_up(const float* c_fin, uint32_t cw, const Level& f, const float* f_pre,
+                                        float* f_fin, uint32_t nseg_f, uint32_t warp, uint32_t nwarps, uint32_t last,
+                                        uint32_t extra) {
     const uint32_t lane = threadIdx.x & 31;
-    const float* fe = f.err;
-    const float* ce = c.err;
-    const uint32_t fw = f.w, cw = c.w;
+    const uint32_t fw = f.w;
     auto pro = [=](uint32_t q, long long rq) {
         uint32_t r = uint32_t(rq);
-        return prolonged(fe[q], ce[((r / fw) / 2) * cw + (r % fw) / 2 + cw], q == last ? extra : 0u);
+        return prolonged(f_pre[q], c_fin[((r / fw) / 2) * cw + (r % fw) / 2 + cw], q == last ? extra : 0u);
     };
     auto black_new = [&](uint32_t q, long long rq) {
         return sor_cell(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, rq, q, pro(q, rq), true, pro);
@@ -449,7 +453,7 @@ __device__ __forceinline__ double ph_up(const Level& c, const Level& f, uint32_t
         float z;
         if (!is_red(raw, fw)) z = black_new(p, raw);
         else z = sor_cell(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, raw, p, pro(p, raw), true, black_new);
-        f.err[p] = z;
+        f_fin[p] = z;
         rz += double(f.res[p] * z);
     }
     return rz;
