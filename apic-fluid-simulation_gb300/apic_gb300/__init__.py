@@ -21,11 +21,13 @@ LIB_PATH = os.path.join(_PKG_ROOT, "lib", "libapic_gpu.so")
 
 # ---- constants (include/apic_gpu.h) ---------------------------------------
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_NONFINITE, ERR_NOT_CONVERGED, ERR_NO_DEVICE = range(8)
+ERR_UNSUPPORTED = 8
 UPDATE_DISABLE_SORT = 0x1
 SOLVER_REFERENCE, SOLVER_REL_FP32, SOLVER_REL_MIXED = 0, 1, 2
 SCENE_REFERENCE_DEFAULT, SCENE_DAM_BREAK, SCENE_DAM_BREAK_DISK, SCENE_NOISE = 0, 1, 2, 3
 OPT_PERSISTENT_SOLVE = 1
 OPT_FUSED_VCYCLE = 2
+OPT_CLUSTER_VCYCLE = 3
 
 FIELDS = {
     "pos_x": 0, "pos_y": 1, "vel_x": 2, "vel_y": 3, "cu_x": 4, "cu_y": 5, "cv_x": 6, "cv_y": 7, "tres": 8,

@@ -202,6 +202,83 @@ __device__ __forceinline__ bool block_sum_last(double v, double* partials, uint3
     return true;
 }
 
+// ---- double-float sums ---------------------------------------------------
+// An unevaluated sum hi + lo of two floats (about 48 significant bits).  Sums
+// of FP32 products accumulate in this form with FP32 instructions only:
+// GB300 issues FP64 at a small fraction of the FP32 rate, and an FP64 add per
+// cell plus five per warp shuffle level cost more than the sweep itself.
+// Additions use Knuth's TwoSum for the high parts (exact error term) and
+// fold the low parts in (the "sloppy" double-float add of Dekker/Bailey);
+// -fmad=false keeps every operation as written.
+struct F2 {
+    float hi, lo;
+};
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+    float s = a.hi + b.hi;
+    float v = s - a.hi;
+    float e = (a.hi - (s - v)) + (b.hi - v);
+    e = e + (a.lo + b.lo);
+    float hi = s + e;
+    return F2{hi, e - (hi - s)};
+}
+__device__ __forceinline__ F2 f2_add(F2 a, float b) { return f2_add(a, F2{b, 0.0f}); }
+// a * a exactly (the FMA returns the rounding error of the product).
+__device__ __forceinline__ F2 f2_square(float a) {
+    float p = a * a;
+    return F2{p, __fmaf_rn(a, a, -p)};
+}
+__device__ __forceinline__ double f2_value(F2 a) {
+    return isfinite(a.hi) ? double(a.hi) + double(a.lo) : double(a.hi);
+}
+__device__ __forceinline__ F2 warp_sum(F2 v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        F2 w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+        v = f2_add(v, w);
+    }
+    return v;
+}
+
+// block_sum_last for double-float sums; partials holds one F2 per block in
+// the 8 bytes of a double.
+template <int kThreads>
+__device__ __forceinline__ bool block_sum_last(F2 v, double* partials, uint32_t* counter, double* total) {
+    __shared__ F2 s_f[kThreads / 32];
+    __shared__ bool s_last_f;
+    float2* part = reinterpret_cast<float2*>(partials);
+    v = warp_sum(v);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_f[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        F2 b{0.0f, 0.0f};
+        for (int w = 0; w < kThreads / 32; ++w) b = f2_add(b, s_f[w]);
+        part[blockIdx.x] = make_float2(b.hi, b.lo);
+        __threadfence();
+        uint32_t prev = atomicAdd(counter, 1u);
+        s_last_f = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last_f) return false;
+    __threadfence();
+    F2 t{0.0f, 0.0f};
+    for (uint32_t b = threadIdx.x; b < gridDim.x; b += kThreads) {
+        float2 q = __ldcg(part + b);  // from L2: written by other blocks
+        t = f2_add(t, F2{q.x, q.y});
+    }
+    t = warp_sum(t);
+    __syncthreads();
+    if (lane == 0) s_f[warp] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        F2 a{0.0f, 0.0f};
+        for (int w = 0; w < kThreads / 32; ++w) a = f2_add(a, s_f[w]);
+        *total = f2_value(a);
+        *counter = 0;
+    }
+    return true;
+}
+
 // Same pattern for a maximum of non-negative values (exact in any order).
 template <int kThreads>
 __device__ __forceinline__ bool block_max_last(float v, double* partials, uint32_t* counter, float* total) {

@@ -169,7 +169,12 @@ struct Scene {
     int persist_grid = 0;                     // CTAs of the persistent solver (0: unavailable)
     size_t persist_smem = 0;
     bool use_persistent = false;              // persistent kernel vs graph of per-phase kernels
-    bool fused_vcycle = true;                 // one kernel per level and direction in the V-cycle
+    bool fused_vcycle = false;                // one kernel per level and direction in the V-cycle
+    // middle levels [cluster_first, tail_first) of the V-cycle run in one
+    // thread-block cluster (cluster_first == tail_first: none)
+    uint32_t cluster_max_cells = 65536;       // largest level handed to the cluster (0: never)
+    int cluster_size = 0;                     // CTAs per cluster (0: clusters unavailable)
+    int cluster_first = 0;
     // kernel nodes per execution of each graph body (launch accounting)
     uint32_t kn_top = 0, kn_sort = 0, kn_loop = 0, kn_pcg = 0, kn_refine = 0;
     int solver_mode = APIC_SOLVER_REFERENCE;
@@ -222,7 +227,8 @@ cudaError_t enqueue_persistent_solve(Scene& s);
 // (profiling runs, so every kernel is a separate launch)
 cudaError_t run_solve_eager(Scene& s);
 // vcycle.cu
-void plan_vcycle(Scene& s);     // pick the coarse levels that run in one CTA
+void plan_vcycle(Scene& s);     // pick the coarse levels that run in one CTA / one cluster
+void plan_vcycle_cluster(Scene& s);  // re-pick the cluster's levels after cluster_max_cells changed
 void enqueue_vcycle(Scene& s);  // z = M^-1 r on s.stream
 // runtime.cu
 cudaError_t launch_plan_first(Scene& s);

@@ -26,22 +26,23 @@ __device__ __forceinline__ void ph_clear_pressure(const Level& B, uint32_t nseg,
     APIC_BASE_LOOP(B, nseg, warp, nwarps) { p[word_ * 32 + lane_] = 0.0f; }
 }
 
-// s = z; returns r.z (src/apic.rs:1887-1888).
-__device__ __forceinline__ double ph_start(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps, float* s) {
-    double acc = 0;
+// s = z; returns r.z (src/apic.rs:1887-1888).  Dot products sum the FP32
+// products in double-float (F2, apic_device.cuh).
+__device__ __forceinline__ F2 ph_start(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps, float* s) {
+    F2 acc{0.0f, 0.0f};
     APIC_BASE_LOOP(B, nseg, warp, nwarps) {
         uint32_t c = word_ * 32 + lane_ + B.w;
         float z = B.err[c], r = B.res[c];
         s[c] = z;
-        acc += double(r * z);
+        acc = f2_add(acc, r * z);
     }
     return acc;
 }
 
 // Ap = A s (FMA chain of :1833-1846); returns s.Ap.
-__device__ __forceinline__ double ph_spmv(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
-                                          const float* s, float* ap) {
-    double acc = 0;
+__device__ __forceinline__ F2 ph_spmv(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
+                                      const float* s, float* ap) {
+    F2 acc{0.0f, 0.0f};
     const long long W = B.w;
     APIC_BASE_LOOP(B, nseg, warp, nwarps) {
         long long raw = (long long)word_ * 32 + lane_;
@@ -53,18 +54,19 @@ __device__ __forceinline__ double ph_spmv(const Level& B, uint32_t nseg, uint32_
         if (fluid_raw(B.fluid, raw + W, B.cells)) v = __fmaf_rn(B.py[c], s[c + W], v);
         if (fluid_raw(B.fluid, raw - W, B.cells)) v = __fmaf_rn(B.py[c - W], s[c - W], v);
         ap[c] = v;
-        acc += double(v * sc);
+        acc = f2_add(acc, v * sc);
     }
     return acc;
 }
 
 // x += alpha s (x = pressure in cell layout, or a padded vector);
-// r = fma(-alpha, Ap, r) (:1910-1928).  Returns max|r| and sum r^2.
+// r = fma(-alpha, Ap, r) (:1910-1928).  Returns max|r| and sum r^2 (each
+// square exact, summed in double-float).
 __device__ __forceinline__ void ph_update(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps, float alpha,
                                           float* x, int x_padded, const float* s, const float* ap, float* max_r,
-                                          double* r2) {
+                                          F2* r2) {
     float mx = 0.0f;
-    double acc = 0;
+    F2 acc{0.0f, 0.0f};
     APIC_BASE_LOOP(B, nseg, warp, nwarps) {
         uint32_t raw = word_ * 32 + lane_;
         uint32_t c = raw + B.w;
@@ -73,18 +75,18 @@ __device__ __forceinline__ void ph_update(const Level& B, uint32_t nseg, uint32_
         float nr = __fmaf_rn(-alpha, ap[c], B.res[c]);
         B.res[c] = nr;
         mx = fmaxf(mx, fabsf(nr));
-        acc += double(nr) * double(nr);
+        acc = f2_add(acc, f2_square(nr));
     }
     *max_r = mx;
     *r2 = acc;
 }
 
 // r.z after the preconditioner (:1936).
-__device__ __forceinline__ double ph_rz(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps) {
-    double acc = 0;
+__device__ __forceinline__ F2 ph_rz(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps) {
+    F2 acc{0.0f, 0.0f};
     APIC_BASE_LOOP(B, nseg, warp, nwarps) {
         uint32_t c = word_ * 32 + lane_ + B.w;
-        acc += double(B.res[c] * B.err[c]);
+        acc = f2_add(acc, B.res[c] * B.err[c]);
     }
     return acc;
 }

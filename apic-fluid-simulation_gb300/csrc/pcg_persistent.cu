@@ -137,6 +137,8 @@ __device__ __forceinline__ bool grid_sum(Ctx& c, double v, double& out) {
     c.slot ^= 1;
     return true;
 }
+// Double-float per-thread sums (the phases' dot products) enter as doubles.
+__device__ __forceinline__ bool grid_sum(Ctx& c, F2 v, double& out) { return grid_sum(c, f2_value(v), out); }
 
 __device__ __forceinline__ bool grid_max(Ctx& c, float v, float& out) {
     float b = block_max_bcast(v);
@@ -236,7 +238,7 @@ __device__ bool pcg_loop(Ctx& c, int mode, float* x, int x_padded, uint32_t cap,
         }
         float alpha = gamma / delta;
         float mx;
-        double r2;
+        F2 r2;
         pcg::ph_update(B, n0, c.warp, c.nwarps, alpha, x, x_padded, c.a.search, c.a.ap, &mx, &r2);
         if (ref) {
             float m;

@@ -905,6 +905,14 @@ int apic_set_option(apic_handle* h, int option, int value) {
             s.fused_vcycle = value != 0;
             invalidate_graphs(s);
             return APIC_OK;
+        case APIC_OPT_CLUSTER_VCYCLE:
+            if (value < 0) return fail(APIC_ERR_INVALID_ARG, "cluster level size must be >= 0");
+            if (value > 0 && s.cluster_size == 0)
+                return fail(APIC_ERR_UNSUPPORTED, "thread-block clusters unavailable for this grid or GPU");
+            s.cluster_max_cells = uint32_t(value);
+            plan_vcycle_cluster(s);
+            invalidate_graphs(s);
+            return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }
@@ -914,6 +922,9 @@ int apic_get_option(apic_handle* h, int option, int* value) {
     switch (option) {
         case APIC_OPT_PERSISTENT_SOLVE: *value = (h->s.use_persistent && h->s.persist_grid > 0) ? 1 : 0; return APIC_OK;
         case APIC_OPT_FUSED_VCYCLE: *value = h->s.fused_vcycle ? 1 : 0; return APIC_OK;
+        case APIC_OPT_CLUSTER_VCYCLE:
+            *value = h->s.cluster_size > 0 ? int(h->s.cluster_max_cells) : 0;
+            return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }

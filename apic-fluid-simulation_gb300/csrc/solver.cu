@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kSegBlock) k_clear_pressure(Level B, float* p,
 
 // s = z and gamma = r.z (src/apic.rs:1887-1892).
 __global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl* ctl, double* partials, int mode) {
-    double acc = pcg::ph_start(B, ctl->seg_count[0], gwarp(), gnwarps(), s);
+    F2 acc = pcg::ph_start(B, ctl->seg_count[0], gwarp(), gnwarps(), s);
     double tot;
     if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
         float gamma = float(tot);
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl*
 __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s, float* ap, Ctl* ctl, double* partials,
                                                         int mode) {
     if (ctl->pcg_done) return;
-    double acc = pcg::ph_spmv(B, ctl->seg_count[0], gwarp(), gnwarps(), s, ap);
+    F2 acc = pcg::ph_spmv(B, ctl->seg_count[0], gwarp(), gnwarps(), s, ap);
     double tot;
     if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
         float delta = float(tot);
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int
                                                           float solve_error) {
     if (ctl->pcg_done) return;
     float mx;
-    double acc;
+    F2 acc;
     pcg::ph_update(B, ctl->seg_count[0], gwarp(), gnwarps(), ctl->alpha, p, p_padded, s, ap, &mx, &acc);
     if (mode == APIC_SOLVER_REFERENCE) {
         float t;
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int
 // gamma' = r.z, beta (src/apic.rs:1934-1943).
 __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, double* partials, int mode) {
     if (ctl->pcg_done) return;
-    double acc = pcg::ph_rz(B, ctl->seg_count[0], gwarp(), gnwarps());
+    F2 acc = pcg::ph_rz(B, ctl->seg_count[0], gwarp(), gnwarps());
     double tot;
     if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
         float ng = float(tot);

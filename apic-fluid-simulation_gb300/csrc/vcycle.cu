@@ -20,10 +20,16 @@
 //   * all levels that fit in shared memory (the coarse tail, including the
 //     coarsest CG) run in ONE cooperative CTA: coefficients are loaded from L2
 //     once per V-cycle and every sweep is a __syncthreads()-separated phase
-//     (k_vcycle_tail).
+//     (k_vcycle_tail);
+//   * the middle levels above the tail (a few thousand to some tens of
+//     thousands of fluid cells: too small to fill the GPU, so each of their
+//     launches costs mostly its latency) run in ONE thread-block cluster
+//     together with the tail (k_vcycle_mid): the same phases, separated by
+//     the cluster's hardware barrier instead of kernel boundaries.
 // On the base level the last fluid cell receives the coarse correction once
 // more per duplicate that pads the reference's fluid list to a multiple of 8
 // (:1487-1494, iterated by prolongate :611-615).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "apic_device.cuh"
@@ -96,6 +102,74 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(TailParams tp, con
     cta_tail(tp, sm, true);
 }
 
+// Middle levels lv[0..n) (V-cycle levels first..first+n-1) and the coarse
+// tail, by one thread-block cluster.  On entry lv[0] holds its restricted
+// residual and its first red sweep (k_restrict_red); on exit its error is
+// final.  Every phase is the graph kernels' phase with the cluster's warps as
+// the grid; a cluster barrier (release/acquire at cluster scope, so global
+// writes before it are visible to every CTA after it) separates phases, and
+// CTA 0 runs the shared-memory tail while the others wait.  pcg_done is read
+// once and is the same for every CTA, so all of them reach every barrier.
+constexpr int kMaxMidLevels = 8;
+struct MidParams {
+    int first, n;
+    Level lv[kMaxMidLevels + 1];  // lv[n]: the first tail level
+};
+
+__global__ void __launch_bounds__(kTailThreads, 1) k_vcycle_mid(MidParams mp, TailParams tp, const Ctl* ctl) {
+    if (ctl->pcg_done) return;
+    extern __shared__ uint32_t sm[];
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t wpb = blockDim.x >> 5;
+    const uint32_t warp = cl.block_rank() * wpb + (threadIdx.x >> 5);
+    const uint32_t nwarps = cl.num_blocks() * wpb;
+    const int n = mp.n;
+    for (int k = 0; k < n; ++k) {
+        const int li = mp.first + k;
+        ph_smooth(mp.lv[k], ctl->seg_count[li], warp, nwarps, 1, 1);
+        cl.sync();
+        ph_restrict(mp.lv[k], mp.lv[k + 1], ctl->seg_count[li + 1], warp, nwarps, k + 1 < n);
+        cl.sync();
+    }
+    if (cl.block_rank() == 0) cta_tail(tp, sm, true);
+    cl.sync();
+    for (int k = n - 1; k >= 0; --k) {
+        const uint32_t nseg = ctl->seg_count[mp.first + k];
+        ph_prolong(mp.lv[k + 1], mp.lv[k], nseg, warp, nwarps, 1, 0xFFFFFFFFu, 0u);
+        cl.sync();
+        ph_prolong(mp.lv[k + 1], mp.lv[k], nseg, warp, nwarps, 0, 0xFFFFFFFFu, 0u);
+        if (k > 0) cl.sync();
+    }
+}
+
+cudaLaunchConfig_t mid_config(uint32_t ctas, size_t smem, cudaStream_t st, cudaLaunchAttribute* attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas, 1, 1);
+    cfg.blockDim = dim3(kTailThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = ctas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
+void launch_mid(Scene& s, cudaStream_t st) {
+    MidParams mp;
+    mp.first = s.cluster_first;
+    mp.n = s.tail_first - s.cluster_first;
+    for (int k = 0; k <= mp.n; ++k) mp.lv[k] = s.lv[s.cluster_first + k];
+    uint32_t off = 0;
+    TailParams tp = make_tail_params(s, s.tail_first, &off);
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = mid_config(uint32_t(s.cluster_size), size_t(off) * 4, st, attr);
+    cudaLaunchKernelEx(&cfg, k_vcycle_mid, mp, tp, static_cast<const Ctl*>(s.ctl));
+}
+
 
 
 size_t tail_level_bytes(const Level& L) { return 4ull * (L.words + 6ull * L.padded); }
@@ -118,6 +192,35 @@ void plan_vcycle(Scene& s) {
     if (s.tail_first < s.nlevels) {
         s.tail_smem = bytes;
         cudaFuncSetAttribute(k_vcycle_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTailSmemBudget));
+    }
+    // largest cluster of 1024-thread CTAs with the tail's shared memory that
+    // the GPU can hold
+    s.cluster_size = 0;
+    if (s.tail_first >= 2 && s.tail_first < s.nlevels) {
+        cudaFuncSetAttribute(k_vcycle_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTailSmemBudget));
+        cudaFuncSetAttribute(k_vcycle_mid, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        for (uint32_t ctas : {16u, 8u, 4u}) {
+            cudaLaunchAttribute attr[1];
+            cudaLaunchConfig_t cfg = mid_config(ctas, s.tail_smem, nullptr, attr);
+            int clusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&clusters, k_vcycle_mid, &cfg) == cudaSuccess && clusters > 0) {
+                s.cluster_size = int(ctas);
+                break;
+            }
+        }
+        cudaGetLastError();  // a refused size leaves an error behind
+    }
+    plan_vcycle_cluster(s);
+}
+
+// Middle levels for the cluster: the levels just above the tail with at most
+// cluster_max_cells cells each (never the base level).
+void plan_vcycle_cluster(Scene& s) {
+    s.cluster_first = s.tail_first;
+    if (s.cluster_size == 0 || s.cluster_max_cells == 0 || s.tail_first >= s.nlevels) return;
+    for (int l = s.tail_first - 1; l >= 1 && s.tail_first - l <= kMaxMidLevels; --l) {
+        if (s.lv[l].cells > s.cluster_max_cells) break;
+        s.cluster_first = l;
     }
 }
 
@@ -167,8 +270,14 @@ static void enqueue_vcycle_unfused(Scene& s) {
         k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 0, 0);
         return;
     }
+    const bool cluster = s.cluster_first < s.tail_first && s.tail_first < s.nlevels;
     int deepest_mid = 0;  // deepest level smoothed by the global kernels
     for (int l = 1; l <= last; ++l) {
+        if (cluster && l == s.cluster_first) {
+            k_restrict_red<<<grid(l), kSegBlock, 0, st>>>(L[l - 1], L[l], l, s.ctl);
+            launch_mid(s, st);
+            break;
+        }
         if (l == s.tail_first) {
             k_restrict<<<grid(l), kSegBlock, 0, st>>>(L[l - 1], L[l], l, s.ctl);
             uint32_t off = 0;

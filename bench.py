@@ -207,7 +207,10 @@ def run_gpu_arm(args, world, rank, local):
     sim.set_solver(mode, 1e-6, 500)
     if args.persistent:
         sim.set_option(A.OPT_PERSISTENT_SOLVE, 1)
-    sim.set_option(A.OPT_FUSED_VCYCLE, 0 if args.unfused_vcycle else 1)
+    sim.set_option(A.OPT_FUSED_VCYCLE, 1 if args.fused_vcycle else 0)
+    if args.cluster_cells is not None:
+        sim.set_option(A.OPT_CLUSTER_VCYCLE, args.cluster_cells)
+    cluster_cells = sim.get_option(A.OPT_CLUSTER_VCYCLE)
     opts = A.DebugOptions()
     stream_ptr = ctypes_stream(sim)
     ext_stream = torch.cuda.ExternalStream(stream_ptr)
@@ -307,8 +310,10 @@ def run_gpu_arm(args, world, rank, local):
                        "true_residual_rel_max": max(true_res) if true_res else None,
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
                        "solve_form": "persistent kernel" if args.persistent else "graph of per-phase kernels",
-                       "vcycle": "one kernel per level per direction" if not args.unfused_vcycle
-                       else "one kernel per sweep and transfer",
+                       "vcycle": "one kernel per level per direction" if args.fused_vcycle
+                       else "one kernel per sweep and transfer" + (
+                           f"; levels of <= {cluster_cells} cells in one thread-block cluster"
+                           if cluster_cells else ""),
                        "launch": "stage by stage" if args.eager else "one CUDA graph per update"},
             "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
             "wall_s": wall,
@@ -376,8 +381,10 @@ def main():
                     help="launch the stages one by one in the timed region (for ncu launch lists)")
     ap.add_argument("--persistent", action="store_true",
                     help="run the pressure solve as one persistent cooperative kernel")
-    ap.add_argument("--unfused-vcycle", action="store_true",
-                    help="run the V-cycle as separate sweep / restrict / prolong kernels")
+    ap.add_argument("--fused-vcycle", action="store_true",
+                    help="run the V-cycle as one kernel per level and direction")
+    ap.add_argument("--cluster-cells", type=int, default=None,
+                    help="largest multigrid level run inside the thread-block cluster (0: none)")
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--cpu-budget", type=float, default=30.0)
     args = ap.parse_args()

@@ -214,11 +214,19 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
  * 0 (default): a CUDA graph of per-phase kernels with device-side WHILE
  * loops.  Both compute the same iterations. */
 #define APIC_OPT_PERSISTENT_SOLVE 1
-/* 1 (default): the V-cycle runs one kernel per level going down and one going
- * up (values another thread updates in the same kernel are recomputed
- * locally).  0: one kernel per sweep and per transfer.  Same results bit for
+/* 1: the V-cycle runs one kernel per level going down and one going up
+ * (values another thread updates in the same kernel are recomputed locally).
+ * 0 (default, faster on GB300: the recomputation costs more than the launches
+ * it saves): one kernel per sweep and per transfer.  Same results bit for
  * bit. */
 #define APIC_OPT_FUSED_VCYCLE 2
+/* Largest multigrid level (in cells) whose sweeps and transfers run inside
+ * one thread-block cluster together with the shared-memory coarse levels,
+ * instead of one kernel each; 0 turns the cluster off.  Default 65536.
+ * Setting a non-zero value fails with APIC_ERR_UNSUPPORTED when the GPU
+ * cannot hold a cluster of 1024-thread CTAs; apic_get_option reports 0 then.
+ * Same results bit for bit.  Applies when APIC_OPT_FUSED_VCYCLE is 0. */
+#define APIC_OPT_CLUSTER_VCYCLE 3
 int apic_set_option(apic_handle* h, int option, int value);
 int apic_get_option(apic_handle* h, int option, int* value);
 

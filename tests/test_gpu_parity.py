@@ -392,3 +392,55 @@ def test_fused_vcycle_equals_unfused(gpu_lib, side):
         g.run_stage("vcycle", 1 / 480)
         out.append(g.read_field("error")[fl])
     eq(out[0], out[1], "fused vs unfused V-cycle")
+
+
+@pytest.mark.parametrize("side,cells", [(256, 65536), (1024, 65536), (1024, 1 << 20), (2048, 1 << 20)])
+def test_cluster_vcycle_equals_unfused(gpu_lib, side, cells):
+    """Middle levels inside one thread-block cluster give the same z = M^-1 r, bit for bit."""
+    props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+    cs = 1 / side
+    scene = A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=cs, sub=2, seed=1, fluid_x=0.5, fluid_y=0.5,
+                           disk=(0.7, 0.8, 0.08), disk_v=(0.0, -2.0))
+    g = A.Apic(side, side, cs, props)
+    if g.get_option(A.OPT_CLUSTER_VCYCLE) == 0:
+        pytest.skip("thread-block clusters unavailable")
+    px, py, vx, vy = A.generate_scene(scene)
+    g.set_particles(px, py, vx, vy)
+    for _ in range(3):
+        g.update(A.DebugOptions(), 1 / 480)
+    g.run_stage("mg", 1 / 480)
+    fl = g.read_field("fluid_list").astype(np.int64)
+    out = []
+    for value in (cells, 0, cells):
+        g.set_option(A.OPT_CLUSTER_VCYCLE, value)
+        assert g.get_option(A.OPT_CLUSTER_VCYCLE) == value
+        g.run_stage("vcycle", 1 / 480)
+        out.append(g.read_field("error")[fl])
+    eq(out[0], out[1], "cluster vs per-kernel V-cycle")
+    eq(out[2], out[1], "cluster V-cycle, second run")
+    # whole updates through the graph agree with the per-kernel form too
+    sims = []
+    for value in (cells, 0):
+        h = A.Apic(side, side, cs, props)
+        h.set_particles(px, py, vx, vy)
+        h.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+        h.set_option(A.OPT_CLUSTER_VCYCLE, value)
+        for _ in range(2):
+            h.update(A.DebugOptions(disable_particle_sort=True), 1 / 480)
+        sims.append(h)
+    # P2G's float atomics make two runs differ in the last bits, so an
+    # iteration count may differ by one
+    its = [h.stats().pcg_iterations_total for h in sims]
+    assert abs(its[0] - its[1]) <= 2, its
+    for h in sims:
+        assert float(h.stats().true_residual_rel) <= 1e-6
+
+
+def test_cluster_option_rejected_without_middle_levels(gpu_lib):
+    """A grid whose multigrid levels all fit the shared-memory tail has no cluster levels."""
+    g = A.Apic(64, 64, 1 / 64, A.WorldProperties(-9.81, 0.1, 5.0, 1e-5))
+    assert g.get_option(A.OPT_CLUSTER_VCYCLE) == 0
+    with pytest.raises(A.ApicError) as ei:
+        g.set_option(A.OPT_CLUSTER_VCYCLE, 65536)
+    assert ei.value.code == A.ERR_UNSUPPORTED
+    g.set_option(A.OPT_CLUSTER_VCYCLE, 0)
