@@ -20,6 +20,16 @@ namespace pcg {
     for (uint32_t s_ = (warp); s_ < (nseg); s_ += (nwarps))                                     \
         if (uint32_t word_ = (B).seg[s_]; ((B).fluid[word_] >> lane_) & 1u)
 
+// The same loop over every lane of a segment inside the grid: the body runs
+// without waiting for the mask word, so its loads issue at once, and tests
+// fluid_ before it stores or accumulates.  All reads of a cell in [0, cells)
+// and of its neighbours stay inside the padded arrays.
+#define APIC_BASE_ALL(B, nseg, warp, nwarps)                                                    \
+    const uint32_t lane_ = threadIdx.x & 31;                                                    \
+    for (uint32_t s_ = (warp); s_ < (nseg); s_ += (nwarps))                                     \
+        if (const uint32_t word_ = (B).seg[s_], raw_ = word_ * 32 + lane_; raw_ < (B).cells)    \
+            if (const bool fluid_ = (((B).fluid[word_] >> lane_) & 1u) != 0u; true)
+
 // pressure = 0 at fluid cells (src/apic.rs:1872-1883).
 __device__ __forceinline__ void ph_clear_pressure(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
                                                   float* p) {
@@ -30,9 +40,10 @@ __device__ __forceinline__ void ph_clear_pressure(const Level& B, uint32_t nseg,
 // products in double-float (F2, apic_device.cuh).
 __device__ __forceinline__ F2 ph_start(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps, float* s) {
     F2 acc{0.0f, 0.0f};
-    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
-        uint32_t c = word_ * 32 + lane_ + B.w;
-        float z = B.err[c], r = B.res[c];
+    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+        const uint32_t c = raw_ + B.w;
+        const float z = B.err[c], r = B.res[c];
+        if (!fluid_) continue;
         s[c] = z;
         acc = f2_add(acc, r * z);
     }
@@ -44,15 +55,23 @@ __device__ __forceinline__ F2 ph_spmv(const Level& B, uint32_t nseg, uint32_t wa
                                       const float* s, float* ap) {
     F2 acc{0.0f, 0.0f};
     const long long W = B.w;
-    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
-        long long raw = (long long)word_ * 32 + lane_;
-        uint32_t c = uint32_t(raw) + B.w;
-        float sc = s[c];
+    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+        const long long raw = raw_;
+        const uint32_t c = raw_ + B.w;
+        const bool fr = fluid_raw(B.fluid, raw + 1, B.cells), fl = fluid_raw(B.fluid, raw - 1, B.cells);
+        const bool fu = fluid_raw(B.fluid, raw + W, B.cells), fd = fluid_raw(B.fluid, raw - W, B.cells);
+        const float sc = s[c], sr = s[c + 1], sl = s[c - 1], su = s[c + W], sd = s[c - W];
+        const float pxc = B.px[c], pxl = B.px[c - 1], pyc = B.py[c], pyd = B.py[c - W];
         float v = B.diag[c] * sc;
-        if (fluid_raw(B.fluid, raw + 1, B.cells)) v = __fmaf_rn(B.px[c], s[c + 1], v);
-        if (fluid_raw(B.fluid, raw - 1, B.cells)) v = __fmaf_rn(B.px[c - 1], s[c - 1], v);
-        if (fluid_raw(B.fluid, raw + W, B.cells)) v = __fmaf_rn(B.py[c], s[c + W], v);
-        if (fluid_raw(B.fluid, raw - W, B.cells)) v = __fmaf_rn(B.py[c - W], s[c - W], v);
+        float t = __fmaf_rn(pxc, sr, v);
+        v = fr ? t : v;
+        t = __fmaf_rn(pxl, sl, v);
+        v = fl ? t : v;
+        t = __fmaf_rn(pyc, su, v);
+        v = fu ? t : v;
+        t = __fmaf_rn(pyd, sd, v);
+        v = fd ? t : v;
+        if (!fluid_) continue;
         ap[c] = v;
         acc = f2_add(acc, v * sc);
     }
@@ -67,12 +86,13 @@ __device__ __forceinline__ void ph_update(const Level& B, uint32_t nseg, uint32_
                                           F2* r2) {
     float mx = 0.0f;
     F2 acc{0.0f, 0.0f};
-    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
-        uint32_t raw = word_ * 32 + lane_;
-        uint32_t c = raw + B.w;
-        uint32_t xi = x_padded ? c : raw;
-        x[xi] = x[xi] + alpha * s[c];
-        float nr = __fmaf_rn(-alpha, ap[c], B.res[c]);
+    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+        const uint32_t c = raw_ + B.w;
+        const uint32_t xi = x_padded ? c : raw_;
+        const float nx = x[xi] + alpha * s[c];
+        const float nr = __fmaf_rn(-alpha, ap[c], B.res[c]);
+        if (!fluid_) continue;
+        x[xi] = nx;
         B.res[c] = nr;
         mx = fmaxf(mx, fabsf(nr));
         acc = f2_add(acc, f2_square(nr));
@@ -84,9 +104,10 @@ __device__ __forceinline__ void ph_update(const Level& B, uint32_t nseg, uint32_
 // r.z after the preconditioner (:1936).
 __device__ __forceinline__ F2 ph_rz(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps) {
     F2 acc{0.0f, 0.0f};
-    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
-        uint32_t c = word_ * 32 + lane_ + B.w;
-        acc = f2_add(acc, B.res[c] * B.err[c]);
+    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+        const uint32_t c = raw_ + B.w;
+        const float rz = B.res[c] * B.err[c];
+        if (fluid_) acc = f2_add(acc, rz);
     }
     return acc;
 }
@@ -94,9 +115,10 @@ __device__ __forceinline__ F2 ph_rz(const Level& B, uint32_t nseg, uint32_t warp
 // s = z + beta s (:1945-1954).
 __device__ __forceinline__ void ph_search(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps, float beta,
                                           float* s) {
-    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
-        uint32_t c = word_ * 32 + lane_ + B.w;
-        s[c] = B.err[c] + (beta * s[c]);
+    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+        const uint32_t c = raw_ + B.w;
+        const float v = B.err[c] + (beta * s[c]);
+        if (fluid_) s[c] = v;
     }
 }
 

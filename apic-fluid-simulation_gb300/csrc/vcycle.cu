@@ -125,6 +125,9 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_vcycle_mid(MidParams mp, Ta
     const uint32_t warp = cl.block_rank() * wpb + (threadIdx.x >> 5);
     const uint32_t nwarps = cl.num_blocks() * wpb;
     const int n = mp.n;
+    // CTA 0 starts copying the tail's coefficients now; they arrive while the
+    // middle levels run
+    if (cl.block_rank() == 0) cta_tail_issue_coeffs(tp, sm);
     for (int k = 0; k < n; ++k) {
         const int li = mp.first + k;
         ph_smooth(mp.lv[k], ctl->seg_count[li], warp, nwarps, 1, 1);
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_vcycle_mid(MidParams mp, Ta
         ph_restrict(mp.lv[k], mp.lv[k + 1], ctl->seg_count[li + 1], warp, nwarps, k + 1 < n);
         cl.sync();
     }
-    if (cl.block_rank() == 0) cta_tail(tp, sm, true);
+    if (cl.block_rank() == 0) cta_tail(tp, sm, false);
     cl.sync();
     for (int k = n - 1; k >= 0; --k) {
         const uint32_t nseg = ctl->seg_count[mp.first + k];

@@ -70,6 +70,70 @@ __device__ __forceinline__ float restrict_cell(const uint32_t* fb, uint32_t fw, 
     return restrict_cell_fn(fb, fw, fcells, fd, fpx, fpy, fr, [fe](uint32_t p, long long) { return fe[p]; }, cx, cy);
 }
 
+// Branch-free forms of sor_cell / restrict_cell for the sweeps whose
+// neighbour values are plain loads.  Every load is issued up front, without
+// waiting for the fluid tests: all neighbours of a cell with raw index in
+// [0, cells) have padded indices inside [0, cells + 2w), the extent of every
+// level array.  Non-fluid neighbours (and children) are then dropped by
+// selects, which yields the same floats as skipping them.  nb / fe must be
+// safe to call for any such neighbour.
+template <class NB>
+__device__ __forceinline__ float sor_cell_all(const uint32_t* bits, uint32_t w, uint32_t cells, const float* inv_d,
+                                              const float* px, const float* py, const float* res, long long raw,
+                                              uint32_t c, float old, bool neighbours, NB nb) {
+    const float inv = inv_d[c];
+    float sum = res[c];
+    if (neighbours) {
+        const long long W = w;
+        const bool fr = fluid_raw(bits, raw + 1, cells), fu = fluid_raw(bits, raw + W, cells);
+        const bool fl = fluid_raw(bits, raw - 1, cells), fd = fluid_raw(bits, raw - W, cells);
+        const float pxc = px[c], pyc = py[c], pxl = px[c - 1], pyd = py[c - w];
+        const float er = nb(c + 1, raw + 1), eu = nb(c + w, raw + W), el = nb(c - 1, raw - 1), ed = nb(c - w, raw - W);
+        float t = __fmaf_rn(-pxc, er, sum);
+        sum = fr ? t : sum;
+        t = __fmaf_rn(-pyc, eu, sum);
+        sum = fu ? t : sum;
+        t = __fmaf_rn(-pxl, el, sum);
+        sum = fl ? t : sum;
+        t = __fmaf_rn(-pyd, ed, sum);
+        sum = fd ? t : sum;
+    }
+    const float gs = sum * inv;
+    const float nv = old + (kOmega * (gs - old));
+    return inv == 0.0f ? old : nv;
+}
+
+// Coarse residual of coarse cell (cx, cy) (any cell of the coarse grid).
+__device__ __forceinline__ float restrict_cell_all(const uint32_t* fb, uint32_t fw, uint32_t fcells, const float* fd,
+                                                   const float* fpx, const float* fpy, const float* fr,
+                                                   const float* fe, uint32_t cx, uint32_t cy) {
+    float sum = 0.0f;
+    const long long W = fw;
+#pragma unroll
+    for (uint32_t dy = 0; dy < 2; ++dy)
+#pragma unroll
+        for (uint32_t dx = 0; dx < 2; ++dx) {
+            const long long rf = (long long)(cy * 2 + dy) * fw + (cx * 2 + dx);
+            const uint32_t pf = uint32_t(rf) + fw;
+            const bool f0 = fluid_raw(fb, rf, fcells);
+            const bool fr_ = fluid_raw(fb, rf + 1, fcells), fu = fluid_raw(fb, rf + W, fcells);
+            const bool fl = fluid_raw(fb, rf - 1, fcells), fdn = fluid_raw(fb, rf - W, fcells);
+            const float b = fr[pf];
+            float ax = fd[pf] * fe[pf];
+            float t = ax + fpx[pf] * fe[pf + 1];
+            ax = fr_ ? t : ax;
+            t = ax + fpy[pf] * fe[pf + fw];
+            ax = fu ? t : ax;
+            t = ax + fpx[pf - 1] * fe[pf - 1];
+            ax = fl ? t : ax;
+            t = ax + fpy[pf - fw] * fe[pf - fw];
+            ax = fdn ? t : ax;
+            t = sum + (b - ax);
+            sum = f0 ? t : sum;
+        }
+    return sum;
+}
+
 __device__ __forceinline__ bool is_red(uint32_t raw, uint32_t w) { return (((raw % w) + (raw / w)) & 1u) == 0u; }
 
 // e + ec, plus ec again `reps` times (the padded base list, :611-615).
@@ -274,11 +338,12 @@ __device__ __forceinline__ SmemLevel smem_level(uint32_t* sm, const TailLevel& t
 __device__ __forceinline__ void cta_sweep(const SmemLevel& L, int color, int init) {
     const float* e = L.err;
     for (uint32_t r = threadIdx.x; r < L.cells; r += blockDim.x) {
-        if (!bit_at(L.bits, r) || int(!is_red(r, L.w)) != color) continue;
-        uint32_t c = r + L.w;
-        float old = init ? 0.0f : L.err[c];
-        L.err[c] = sor_cell(L.bits, L.w, L.cells, L.inv, L.px, L.py, L.res, r, c, old, !(init && color == 0),
-                            [e](uint32_t p, long long) { return e[p]; });
+        if (int(!is_red(r, L.w)) != color) continue;
+        const uint32_t c = r + L.w;
+        const float old = init ? 0.0f : e[c];
+        const float v = sor_cell_all(L.bits, L.w, L.cells, L.inv, L.px, L.py, L.res, r, c, old,
+                                     !(init && color == 0), [e](uint32_t p, long long) { return e[p]; });
+        if (bit_at(L.bits, r)) L.err[c] = v;
     }
     __syncthreads();
 }
@@ -290,19 +355,22 @@ __device__ __forceinline__ void cta_sweep(const SmemLevel& L, int color, int ini
 // Each phase visits every fluid cell of the level once (one warp per segment).
 
 // One colour sweep; init: first sweep after the level's error was zero-filled.
+// Every lane of the colour computes (its loads do not wait for the mask word)
+// and only fluid cells store.
 __device__ __forceinline__ void ph_smooth(const Level& L, uint32_t nseg, uint32_t warp, uint32_t nwarps, int color,
                                           int init) {
     const uint32_t lane = threadIdx.x & 31;
+    const float* e = L.err;
     for (uint32_t s = warp; s < nseg; s += nwarps) {
-        uint32_t word = L.seg[s];
-        if (!((L.fluid[word] >> lane) & 1u)) continue;
-        uint32_t raw = word * 32 + lane;
-        if (int(!is_red(raw, L.w)) != color) continue;
-        uint32_t c = raw + L.w;
-        float old = init ? 0.0f : L.err[c];
-        const float* e = L.err;
-        L.err[c] = sor_cell(L.fluid, L.w, L.cells, L.inv_diag, L.px, L.py, L.res, raw, c, old, !(init && color == 0),
-                            [e](uint32_t p, long long) { return e[p]; });
+        const uint32_t word = L.seg[s];
+        const uint32_t raw = word * 32 + lane;
+        if (raw >= L.cells || int(!is_red(raw, L.w)) != color) continue;
+        const bool fluid = (L.fluid[word] >> lane) & 1u;
+        const uint32_t c = raw + L.w;
+        const float old = init ? 0.0f : e[c];
+        const float v = sor_cell_all(L.fluid, L.w, L.cells, L.inv_diag, L.px, L.py, L.res, raw, c, old,
+                                     !(init && color == 0), [e](uint32_t p, long long) { return e[p]; });
+        if (fluid) L.err[c] = v;
     }
 }
 
@@ -311,16 +379,17 @@ __device__ __forceinline__ void ph_restrict(const Level& f, const Level& c, uint
                                             uint32_t nwarps, bool with_red) {
     const uint32_t lane = threadIdx.x & 31;
     for (uint32_t s = warp; s < nseg_c; s += nwarps) {
-        uint32_t word = c.seg[s];
-        if (!((c.fluid[word] >> lane) & 1u)) continue;
-        uint32_t rc = word * 32 + lane;
-        uint32_t cp = rc + c.w;
-        float r = restrict_cell(f.fluid, f.w, f.cells, f.diag, f.px, f.py, f.res, f.err, rc % c.w, rc / c.w);
+        const uint32_t word = c.seg[s];
+        const uint32_t rc = word * 32 + lane;
+        if (rc >= c.cells) continue;
+        const bool fluid = (c.fluid[word] >> lane) & 1u;
+        const uint32_t cp = rc + c.w;
+        const float r = restrict_cell_all(f.fluid, f.w, f.cells, f.diag, f.px, f.py, f.res, f.err, rc % c.w,
+                                          rc / c.w);
+        const float inv = c.inv_diag[cp];
+        if (!fluid) continue;
         c.res[cp] = r;
-        if (with_red && is_red(rc, c.w)) {
-            float inv = c.inv_diag[cp];
-            c.err[cp] = inv != 0.0f ? 0.0f + (kOmega * (r * inv - 0.0f)) : 0.0f;
-        }
+        if (with_red && is_red(rc, c.w)) c.err[cp] = inv != 0.0f ? 0.0f + (kOmega * (r * inv - 0.0f)) : 0.0f;
     }
 }
 
@@ -333,41 +402,64 @@ __device__ __forceinline__ void ph_prolong(const Level& c, const Level& f, uint3
     const float* fe = f.err;
     const float* ce = c.err;
     const uint32_t fw = f.w, cw = c.w;
+    const long long fcells = f.cells;
+    // coarse error under fine raw index rf; rf outside the grid (a neighbour
+    // whose value a select drops) is clamped so the load stays in bounds
     auto coarse_e = [=](long long rf) {
-        uint32_t r = uint32_t(rf);
+        const uint32_t r = uint32_t(rf < 0 ? 0 : (rf >= fcells ? fcells - 1 : rf));
         return ce[((r / fw) / 2) * cw + (r % fw) / 2 + cw];
     };
     for (uint32_t s = warp; s < nseg_f; s += nwarps) {
-        uint32_t word = f.seg[s];
-        if (!((f.fluid[word] >> lane) & 1u)) continue;
-        uint32_t raw = word * 32 + lane;
-        if (int(!is_red(raw, fw)) != color) continue;
-        uint32_t p = raw + fw;
-        float old = prolonged(fe[p], coarse_e(raw), p == last ? extra : 0u);
+        const uint32_t word = f.seg[s];
+        const uint32_t raw = word * 32 + lane;
+        if (raw >= f.cells || int(!is_red(raw, fw)) != color) continue;
+        const bool fluid = (f.fluid[word] >> lane) & 1u;
+        const uint32_t p = raw + fw;
+        const float old = prolonged(fe[p], coarse_e(raw), p == last ? extra : 0u);
+        float v;
         if (color == 1)
-            f.err[p] = sor_cell(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, raw, p, old, true,
-                                [=](uint32_t q, long long rq) {
-                                    return prolonged(fe[q], coarse_e(rq), q == last ? extra : 0u);
-                                });
+            v = sor_cell_all(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, raw, p, old, true,
+                             [=](uint32_t q, long long rq) {
+                                 return prolonged(fe[q], coarse_e(rq), q == last ? extra : 0u);
+                             });
         else
-            f.err[p] = sor_cell(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, raw, p, old, true,
-                                [fe](uint32_t q, long long) { return fe[q]; });
+            v = sor_cell_all(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, raw, p, old, true,
+                             [fe](uint32_t q, long long) { return fe[q]; });
+        if (fluid) f.err[p] = v;
+    }
+}
+
+// Asynchronous 4-byte copy global -> shared (cp.async, sm_80+): the copies
+// of a whole array set are issued back to back and complete together at
+// cp_async_wait_all, so loading costs about one L2 round trip instead of one
+// per loop iteration.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const uint32_t sa = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Start copying every tail level's mask and coefficients into shared memory
+// (complete after cp_async_wait_all).
+__device__ __forceinline__ void cta_tail_issue_coeffs(const TailParams& tp, uint32_t* sm) {
+    for (int l = 0; l < tp.n; ++l) {
+        const TailLevel& t = tp.lv[l];
+        SmemLevel L = smem_level(sm, t);
+        for (uint32_t i = threadIdx.x; i < t.words; i += blockDim.x) cp_async4(L.bits + i, t.fluid + i);
+        for (uint32_t i = threadIdx.x; i < t.padded; i += blockDim.x) {
+            cp_async4(L.diag + i, t.diag + i);
+            cp_async4(L.inv + i, t.inv + i);
+            cp_async4(L.px + i, t.px + i);
+            cp_async4(L.py + i, t.py + i);
+        }
     }
 }
 
 // Copy every tail level's mask and coefficients into shared memory.
 __device__ __forceinline__ void cta_tail_load_coeffs(const TailParams& tp, uint32_t* sm) {
-    for (int l = 0; l < tp.n; ++l) {
-        const TailLevel& t = tp.lv[l];
-        SmemLevel L = smem_level(sm, t);
-        for (uint32_t i = threadIdx.x; i < t.words; i += blockDim.x) L.bits[i] = t.fluid[i];
-        for (uint32_t i = threadIdx.x; i < t.padded; i += blockDim.x) {
-            L.diag[i] = t.diag[i];
-            L.inv[i] = t.inv[i];
-            L.px[i] = t.px[i];
-            L.py[i] = t.py[i];
-        }
-    }
+    cta_tail_issue_coeffs(tp, sm);
+    cp_async_wait_all();
+    __syncthreads();
 }
 
 // ---- fused sweeps: one kernel per level and direction ----------------------
@@ -462,23 +554,28 @@ __device__ __forceinline__ double ph_up(const float* c_fin, uint32_t cw, const L
 // The coarse tail (levels held in shared memory) by one CTA.  load_coeffs:
 // copy masks and coefficients first (otherwise they are already resident);
 // the first level's residual is always copied in and its error copied out.
+// load_coeffs false: the coefficients are resident or their copies were
+// issued earlier by this CTA (cta_tail_issue_coeffs); the wait below covers
+// those too.
 __device__ __forceinline__ void cta_tail(const TailParams& tp, uint32_t* sm, bool load_coeffs) {
-    if (load_coeffs) cta_tail_load_coeffs(tp, sm);
+    if (load_coeffs) cta_tail_issue_coeffs(tp, sm);
     {
         const TailLevel& t = tp.lv[0];
         SmemLevel L = smem_level(sm, t);
-        for (uint32_t i = threadIdx.x; i < t.padded; i += blockDim.x) L.res[i] = __ldcg(t.res + i);
+        for (uint32_t i = threadIdx.x; i < t.padded; i += blockDim.x) cp_async4(L.res + i, t.res + i);
     }
+    cp_async_wait_all();
     __syncthreads();
     for (int l = 0; l + 1 < tp.n; ++l) {
         SmemLevel f = smem_level(sm, tp.lv[l]);
         SmemLevel c = smem_level(sm, tp.lv[l + 1]);
         cta_sweep(f, 0, 1);
         cta_sweep(f, 1, 1);
-        for (uint32_t rc = threadIdx.x; rc < c.cells; rc += blockDim.x)
-            if (bit_at(c.bits, rc))
-                c.res[rc + c.w] = restrict_cell(f.bits, f.w, f.cells, f.diag, f.px, f.py, f.res, f.err, rc % c.w,
-                                                rc / c.w);
+        for (uint32_t rc = threadIdx.x; rc < c.cells; rc += blockDim.x) {
+            const float r = restrict_cell_all(f.bits, f.w, f.cells, f.diag, f.px, f.py, f.res, f.err, rc % c.w,
+                                              rc / c.w);
+            if (bit_at(c.bits, rc)) c.res[rc + c.w] = r;
+        }
         __syncthreads();
     }
     {
