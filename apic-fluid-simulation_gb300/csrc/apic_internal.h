@@ -56,6 +56,7 @@ struct Ctl {
     float gamma;            // r.z of the current iteration (FP32, as the reference)
     float alpha;
     float beta;
+    uint32_t beta_valid;    // beta belongs to this solve (the search direction is z + beta s)
     uint32_t max_r_bits;    // max |r| (float bits)
     uint32_t pcg_done;
     uint32_t pcg_iters;
@@ -229,7 +230,9 @@ cudaError_t run_solve_eager(Scene& s);
 // vcycle.cu
 void plan_vcycle(Scene& s);     // pick the coarse levels that run in one CTA / one cluster
 void plan_vcycle_cluster(Scene& s);  // re-pick the cluster's levels after cluster_max_cells changed
-void enqueue_vcycle(Scene& s);  // z = M^-1 r on s.stream
+// z = M^-1 r on s.stream; base_red_done: the base level's first red sweep
+// was already written (by k_pcg_update)
+void enqueue_vcycle(Scene& s, bool base_red_done = false);
 // runtime.cu
 cudaError_t launch_plan_first(Scene& s);
 cudaError_t launch_advance(Scene& s);

@@ -101,6 +101,80 @@ __device__ __forceinline__ void ph_update(const Level& B, uint32_t nseg, uint32_
     *r2 = acc;
 }
 
+// ---- graph-path forms with the search update folded in -----------------------
+// The search direction of an iteration, s' = z + beta s (:1945-1954), is not
+// written by a kernel of its own: the SpMV evaluates it at the five stencil
+// points from z and the previous s, and the update kernel, the last to read
+// the previous s, stores it.  Both round exactly as the separate update would.
+// With beta_valid == 0 (first iteration of a solve) s already holds z.
+
+// s' at padded index q.
+__device__ __forceinline__ float search_at(const float* z, const float* s, float beta, bool beta_valid, uint32_t q) {
+    return beta_valid ? z[q] + (beta * s[q]) : s[q];
+}
+
+// Ap' = A s' (the FMA chain of :1833-1846); returns s'.Ap'.
+__device__ __forceinline__ F2 ph_spmv_search(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
+                                             const float* s, float beta, bool beta_valid, float* ap) {
+    F2 acc{0.0f, 0.0f};
+    const long long W = B.w;
+    const float* z = B.err;
+    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+        const long long raw = raw_;
+        const uint32_t c = raw_ + B.w;
+        const bool fr = fluid_raw(B.fluid, raw + 1, B.cells), fl = fluid_raw(B.fluid, raw - 1, B.cells);
+        const bool fu = fluid_raw(B.fluid, raw + W, B.cells), fd = fluid_raw(B.fluid, raw - W, B.cells);
+        const float sc = search_at(z, s, beta, beta_valid, c);
+        const float sr = search_at(z, s, beta, beta_valid, c + 1), sl = search_at(z, s, beta, beta_valid, c - 1);
+        const float su = search_at(z, s, beta, beta_valid, c + uint32_t(W));
+        const float sd = search_at(z, s, beta, beta_valid, c - uint32_t(W));
+        const float pxc = B.px[c], pxl = B.px[c - 1], pyc = B.py[c], pyd = B.py[c - W];
+        float v = B.diag[c] * sc;
+        float t = __fmaf_rn(pxc, sr, v);
+        v = fr ? t : v;
+        t = __fmaf_rn(pxl, sl, v);
+        v = fl ? t : v;
+        t = __fmaf_rn(pyc, su, v);
+        v = fu ? t : v;
+        t = __fmaf_rn(pyd, sd, v);
+        v = fd ? t : v;
+        if (!fluid_) continue;
+        ap[c] = v;
+        acc = f2_add(acc, v * sc);
+    }
+    return acc;
+}
+
+// x += alpha s', r = fma(-alpha, Ap, r) (:1910-1928), s = s'; and on red
+// cells the preconditioner's first sweep from zero error, which needs only
+// the cell's new residual: z = 0 + omega (r / diag - 0) (smooth_level
+// :487-507 with every neighbour still zero).  Returns max|r| and sum r^2.
+__device__ __forceinline__ void ph_update_search(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
+                                                 float alpha, float beta, bool beta_valid, float* x, int x_padded,
+                                                 float* s, const float* ap, float* max_r, F2* r2) {
+    constexpr float kOmegaSor = 1.2f;
+    float mx = 0.0f;
+    F2 acc{0.0f, 0.0f};
+    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+        const uint32_t c = raw_ + B.w;
+        const uint32_t xi = x_padded ? c : raw_;
+        const float sc = search_at(B.err, s, beta, beta_valid, c);
+        const float nx = x[xi] + alpha * sc;
+        const float nr = __fmaf_rn(-alpha, ap[c], B.res[c]);
+        const float inv = B.inv_diag[c];
+        if (!fluid_) continue;
+        s[c] = sc;
+        x[xi] = nx;
+        B.res[c] = nr;
+        if ((((raw_ % B.w) + (raw_ / B.w)) & 1u) == 0u)
+            B.err[c] = inv != 0.0f ? 0.0f + (kOmegaSor * (nr * inv - 0.0f)) : 0.0f;
+        mx = fmaxf(mx, fabsf(nr));
+        acc = f2_add(acc, f2_square(nr));
+    }
+    *max_r = mx;
+    *r2 = acc;
+}
+
 // r.z after the preconditioner (:1936).
 __device__ __forceinline__ F2 ph_rz(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps) {
     F2 acc{0.0f, 0.0f};

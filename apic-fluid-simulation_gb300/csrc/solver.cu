@@ -45,6 +45,7 @@ __global__ void k_pcg_begin(Ctl* ctl) {
     ctl->gamma = 0.0f;
     ctl->alpha = 0.0f;
     ctl->beta = 0.0f;
+    ctl->beta_valid = 0;
     ctl->rnorm2 = 0.0;
 }
 
@@ -66,11 +67,12 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl*
     }
 }
 
-// Ap = A s and delta = s.Ap (apply_matrix_and_dot, src/apic.rs:1823-1863).
+// s' = z + beta s, Ap = A s' and delta = s'.Ap (apply_matrix_and_dot,
+// src/apic.rs:1823-1863; the search update :1945-1954 is folded in).
 __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s, float* ap, Ctl* ctl, double* partials,
                                                         int mode) {
     if (ctl->pcg_done) return;
-    F2 acc = pcg::ph_spmv(B, ctl->seg_count[0], gwarp(), gnwarps(), s, ap);
+    F2 acc = pcg::ph_spmv_search(B, ctl->seg_count[0], gwarp(), gnwarps(), s, ctl->beta, ctl->beta_valid != 0, ap);
     double tot;
     if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
         float delta = float(tot);
@@ -81,15 +83,17 @@ __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s,
     }
 }
 
-// p += alpha s, r = fma(-alpha, Ap, r), max|r| (src/apic.rs:1907-1932);
-// relative modes reduce ||r||^2 instead.
-__global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int p_padded, const float* s,
+// p += alpha s', r = fma(-alpha, Ap, r), max|r| (src/apic.rs:1907-1932),
+// s = s', and the V-cycle's first red sweep on the base level; relative
+// modes reduce ||r||^2 instead of max|r|.
+__global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int p_padded, float* s,
                                                           const float* ap, Ctl* ctl, double* partials, int mode,
                                                           float solve_error) {
     if (ctl->pcg_done) return;
     float mx;
     F2 acc;
-    pcg::ph_update(B, ctl->seg_count[0], gwarp(), gnwarps(), ctl->alpha, p, p_padded, s, ap, &mx, &acc);
+    pcg::ph_update_search(B, ctl->seg_count[0], gwarp(), gnwarps(), ctl->alpha, ctl->beta, ctl->beta_valid != 0, p,
+                          p_padded, s, ap, &mx, &acc);
     if (mode == APIC_SOLVER_REFERENCE) {
         float t;
         if (block_max_last<kSegBlock>(mx, partials, &ctl->red_counter, &t) && threadIdx.x == 0) {
@@ -115,15 +119,11 @@ __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, double*
         float ng = float(tot);
         if (mode == APIC_SOLVER_REFERENCE ? (ng < kSafety) : !(ng != 0.0f)) { ctl->pcg_done = 1; return; }
         ctl->beta = ng / ctl->gamma;
+        ctl->beta_valid = 1;
         ctl->gamma = ng;
     }
 }
 
-// s = z + beta s (src/apic.rs:1945-1954).
-__global__ void __launch_bounds__(kSegBlock) k_search(Level B, float* s, const Ctl* ctl) {
-    if (ctl->pcg_done) return;
-    pcg::ph_search(B, ctl->seg_count[0], gwarp(), gnwarps(), ctl->beta, s);
-}
 
 // ---- FP64 refinement helpers (APIC_SOLVER_REL_MIXED) ----------------------
 
@@ -207,16 +207,18 @@ __global__ void k_refine_end(Ctl* ctl, double tol) {
 
 }  // namespace
 
-// One PCG iteration (src/apic.rs:1899-1955); x receives alpha * s.
+// One PCG iteration (src/apic.rs:1899-1955); x receives alpha * s.  The
+// search update that ends the reference's iteration happens at the start of
+// the next one (inside k_spmv_dot / k_pcg_update), and k_pcg_update also
+// runs the V-cycle's first base-level sweep.
 static void pcg_iteration(Scene& s, int mode, float* x, int p_padded) {
     const Level& B = s.lv[0];
     uint32_t g = seg_grid(B.words);
     cudaStream_t st = s.stream;
     k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, s.partials, mode);
     k_pcg_update<<<g, kSegBlock, 0, st>>>(B, x, p_padded, s.search, s.ap, s.ctl, s.partials, mode, s.props.solve_error);
-    enqueue_vcycle(s);
+    enqueue_vcycle(s, true);
     k_dot_rz<<<g, kSegBlock, 0, st>>>(B, s.ctl, s.partials, mode);
-    k_search<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl);
 }
 
 // PCG setup (src/apic.rs:1885-1892) followed by a device-controlled WHILE

@@ -227,15 +227,17 @@ void plan_vcycle_cluster(Scene& s) {
     }
 }
 
-static void enqueue_vcycle_unfused(Scene& s);
+static void enqueue_vcycle_unfused(Scene& s, bool base_red_done);
 
 // One V-cycle on s.stream: z = M^-1 r in lv[0].err.  Fused form: one kernel
 // per level down (k_down) and up (k_up) around the coarse tail.
-void enqueue_vcycle(Scene& s) {
+void enqueue_vcycle(Scene& s, bool base_red_done) {
     if (!s.fused_vcycle || s.nlevels < 2) {
-        enqueue_vcycle_unfused(s);
+        enqueue_vcycle_unfused(s, base_red_done);
         return;
     }
+    // the fused descent recomputes the base level's red sweep from the
+    // residual, so a sweep already written changes nothing
     cudaStream_t st = s.stream;
     Level* L = s.lv;
     auto grid = [&](int l) { return seg_grid(L[l].words); };
@@ -261,12 +263,12 @@ void enqueue_vcycle(Scene& s) {
 }
 
 // Two kernels per sweep and per transfer (the reference's sequence launch by launch).
-static void enqueue_vcycle_unfused(Scene& s) {
+static void enqueue_vcycle_unfused(Scene& s, bool base_red_done) {
     cudaStream_t st = s.stream;
     Level* L = s.lv;
     auto grid = [&](int l) { return seg_grid(L[l].words); };
     const int last = s.nlevels - 1;
-    k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 0, 1);
+    if (!base_red_done) k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 0, 1);
     k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 1, 1);
     if (last < 1) {
         k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 1, 0);
