@@ -28,6 +28,7 @@ SCENE_REFERENCE_DEFAULT, SCENE_DAM_BREAK, SCENE_DAM_BREAK_DISK, SCENE_NOISE = 0,
 OPT_PERSISTENT_SOLVE = 1
 OPT_FUSED_VCYCLE = 2
 OPT_CLUSTER_VCYCLE = 3
+OPT_PDL = 4
 
 FIELDS = {
     "pos_x": 0, "pos_y": 1, "vel_x": 2, "vel_y": 3, "cu_x": 4, "cu_y": 5, "cv_x": 6, "cv_y": 7, "tres": 8,
@@ -66,7 +67,8 @@ class StatsC(ctypes.Structure):
                 ("pcg_iterations_total", ctypes.c_uint32), ("refinement_steps", ctypes.c_uint32),
                 ("residual_max", ctypes.c_float), ("residual_rel", ctypes.c_float),
                 ("true_residual_rel", ctypes.c_double), ("not_converged", ctypes.c_uint32),
-                ("nonfinite_lanes", ctypes.c_uint32), ("kernel_launches", ctypes.c_uint64)]
+                ("nonfinite_lanes", ctypes.c_uint32), ("kernel_launches", ctypes.c_uint64),
+                ("solve_ms", ctypes.c_double)]
 
 
 class SceneParamsC(ctypes.Structure):

@@ -151,6 +151,22 @@ __device__ __forceinline__ uint32_t fluid_xy(const uint32_t* m, int i, int j, in
     return bit_at(m, uint32_t(j * W + i));
 }
 
+// Programmatic dependent launch (sm_90+): wait until the kernel this one
+// depends on has completed and its writes are visible (returns at once when
+// the kernel was launched without the attribute), then let the next kernel's
+// CTAs be scheduled.
+__device__ __forceinline__ void pdl_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// The GPU's global nanosecond timer (PTX %globaltimer).
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // ---- reductions ----
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

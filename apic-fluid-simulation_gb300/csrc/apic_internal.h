@@ -57,6 +57,8 @@ struct Ctl {
     float alpha;
     float beta;
     uint32_t beta_valid;    // beta belongs to this solve (the search direction is z + beta s)
+    unsigned long long solve_t0;  // %globaltimer at the start of the running solve (ns)
+    unsigned long long solve_ns;  // summed solve time of this update (ns)
     uint32_t max_r_bits;    // max |r| (float bits)
     uint32_t pcg_done;
     uint32_t pcg_iters;
@@ -176,6 +178,7 @@ struct Scene {
     uint32_t cluster_max_cells = 65536;       // largest level handed to the cluster (0: never)
     int cluster_size = 0;                     // CTAs per cluster (0: clusters unavailable)
     int cluster_first = 0;
+    bool use_pdl = true;                      // programmatic dependent launch inside the PCG loop
     // kernel nodes per execution of each graph body (launch accounting)
     uint32_t kn_top = 0, kn_sort = 0, kn_loop = 0, kn_pcg = 0, kn_refine = 0;
     int solver_mode = APIC_SOLVER_REFERENCE;
@@ -239,6 +242,27 @@ cudaError_t launch_advance(Scene& s);
 
 // helpers shared by the launchers
 inline uint32_t div_up(uint64_t a, uint64_t b) { return uint32_t((a + b - 1) / b); }
+
+// Launch kern on st.  pdl: programmatic dependent launch, so the kernel's
+// CTAs are scheduled while the previous kernel on the stream drains instead
+// of after it; the kernel must call pdl_wait() (apic_device.cuh) before it
+// reads anything the previous kernel writes.  Only for a launch whose
+// predecessor on the stream (within the same capture) is a kernel.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                          Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
 uint32_t seg_grid(uint32_t words);     // blocks for a segment kernel over `words` words
 
 }  // namespace apic

@@ -58,6 +58,7 @@ __global__ void k_begin_update(Ctl* ctl, float frame_dt, uint32_t flags, uint32_
     ctl->pcg_done = 0;
     ctl->refinements_total = 0;
     ctl->sorted = 0;
+    ctl->solve_ns = 0;
 }
 
 // Substep size (src/apic.rs:2433-2441) and the loop condition (:2432).
@@ -639,6 +640,7 @@ int apic_update(apic_handle* h, uint32_t flags, float frame_dt) {
     s.stats.true_residual_rel = c.true_rel;
     s.stats.not_converged = c.not_converged;
     s.stats.nonfinite_lanes = c.nonfinite;
+    s.stats.solve_ms = double(c.solve_ns) * 1e-6;
     if (!s.profiling)
         s.stats.kernel_launches = uint64_t(s.kn_top) + (c.sorted ? s.kn_sort : 0u) + uint64_t(c.substeps) * s.kn_loop +
                                   uint64_t(c.pcg_iters_total) * s.kn_pcg + uint64_t(c.refinements_total) * s.kn_refine;
@@ -913,6 +915,10 @@ int apic_set_option(apic_handle* h, int option, int value) {
             plan_vcycle_cluster(s);
             invalidate_graphs(s);
             return APIC_OK;
+        case APIC_OPT_PDL:
+            s.use_pdl = value != 0;
+            invalidate_graphs(s);
+            return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }
@@ -925,6 +931,7 @@ int apic_get_option(apic_handle* h, int option, int* value) {
         case APIC_OPT_CLUSTER_VCYCLE:
             *value = h->s.cluster_size > 0 ? int(h->s.cluster_max_cells) : 0;
             return APIC_OK;
+        case APIC_OPT_PDL: *value = h->s.use_pdl ? 1 : 0; return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }

@@ -39,7 +39,8 @@ constexpr float kSafety = 1e-5f;  // SAFTY, src/apic.rs:8
 __device__ __forceinline__ uint32_t gwarp() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
 __device__ __forceinline__ uint32_t gnwarps() { return (gridDim.x * blockDim.x) >> 5; }
 
-__global__ void k_pcg_begin(Ctl* ctl) {
+__global__ void k_pcg_begin(Ctl* ctl, int stamp) {
+    if (stamp) ctl->solve_t0 = global_ns();
     ctl->pcg_done = 0;
     ctl->pcg_iters = 0;
     ctl->gamma = 0.0f;
@@ -57,6 +58,7 @@ __global__ void __launch_bounds__(kSegBlock) k_clear_pressure(Level B, float* p,
 
 // s = z and gamma = r.z (src/apic.rs:1887-1892).
 __global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl* ctl, double* partials, int mode) {
+    pdl_wait();
     F2 acc = pcg::ph_start(B, ctl->seg_count[0], gwarp(), gnwarps(), s);
     double tot;
     if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
@@ -71,6 +73,7 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl*
 // src/apic.rs:1823-1863; the search update :1945-1954 is folded in).
 __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s, float* ap, Ctl* ctl, double* partials,
                                                         int mode) {
+    pdl_wait();
     if (ctl->pcg_done) return;
     F2 acc = pcg::ph_spmv_search(B, ctl->seg_count[0], gwarp(), gnwarps(), s, ctl->beta, ctl->beta_valid != 0, ap);
     double tot;
@@ -89,6 +92,7 @@ __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s,
 __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int p_padded, float* s,
                                                           const float* ap, Ctl* ctl, double* partials, int mode,
                                                           float solve_error) {
+    pdl_wait();
     if (ctl->pcg_done) return;
     float mx;
     F2 acc;
@@ -112,6 +116,7 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int
 
 // gamma' = r.z, beta (src/apic.rs:1934-1943).
 __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, double* partials, int mode) {
+    pdl_wait();
     if (ctl->pcg_done) return;
     F2 acc = pcg::ph_rz(B, ctl->seg_count[0], gwarp(), gnwarps());
     double tot;
@@ -130,6 +135,7 @@ __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, double*
 // b64 = res, p64 = 0 and ||b||^2.
 __global__ void __launch_bounds__(kSegBlock) k_mixed_init(Level B, double* b64, double* p64, Ctl* ctl,
                                                           double* partials) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->solve_t0 = global_ns();  // the relative-mode solve starts here
     double bb = pcg::ph_mixed_init(B, ctl->seg_count[0], gwarp(), gnwarps(), b64, p64);
     double tot;
     if (block_sum_last<kSegBlock>(bb, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) ctl->bnorm2 = tot;
@@ -159,11 +165,13 @@ __global__ void __launch_bounds__(kSegBlock) k_pressure_to64(Level B, const floa
 // Continue the PCG loop while not converged and under the iteration cap
 // (src/apic.rs:1894-1899); dyn_cap reads the remaining budget of a refinement.
 __global__ void k_pcg_cond(const Ctl* __restrict__ ctl, cudaGraphConditionalHandle h, uint32_t cap, int dyn_cap) {
+    pdl_wait();
     uint32_t c = dyn_cap ? ctl->inner_cap : cap;
     cudaGraphSetConditional(h, (!ctl->pcg_done && ctl->pcg_iters < c) ? 1u : 0u);
 }
 
 __global__ void k_finish_solve(Ctl* ctl, uint32_t cap) {
+    ctl->solve_ns += global_ns() - ctl->solve_t0;
     ctl->pcg_iters_total += ctl->pcg_iters;
     if (ctl->pcg_iters >= cap && !ctl->pcg_done) ctl->not_converged++;
 }
@@ -198,6 +206,7 @@ __global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol
 __global__ void k_refine_post(Ctl* ctl) { ctl->used_iters += ctl->pcg_iters; }
 
 __global__ void k_refine_end(Ctl* ctl, double tol) {
+    ctl->solve_ns += global_ns() - ctl->solve_t0;
     ctl->refinements_total += ctl->refinements;
     ctl->pcg_iters = ctl->used_iters;
     ctl->pcg_iters_total += ctl->used_iters;
@@ -215,10 +224,12 @@ static void pcg_iteration(Scene& s, int mode, float* x, int p_padded) {
     const Level& B = s.lv[0];
     uint32_t g = seg_grid(B.words);
     cudaStream_t st = s.stream;
+    const bool pdl = s.use_pdl;
     k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, s.partials, mode);
-    k_pcg_update<<<g, kSegBlock, 0, st>>>(B, x, p_padded, s.search, s.ap, s.ctl, s.partials, mode, s.props.solve_error);
+    launch(pdl, k_pcg_update, g, kSegBlock, 0, st, B, x, p_padded, s.search, s.ap, s.ctl, s.partials, mode,
+           s.props.solve_error);
     enqueue_vcycle(s, true);
-    k_dot_rz<<<g, kSegBlock, 0, st>>>(B, s.ctl, s.partials, mode);
+    launch(pdl, k_dot_rz, g, kSegBlock, 0, st, B, s.ctl, s.partials, mode);
 }
 
 // PCG setup (src/apic.rs:1885-1892) followed by a device-controlled WHILE
@@ -232,11 +243,12 @@ static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p
     if (e != cudaSuccess) return e;
     e = capture_into(s, c, [&]() {
         cudaStream_t st = s.stream;
-        k_pcg_begin<<<1, 1, 0, st>>>(s.ctl);
+        // only the reference-mode solve clears the pressure, and it starts here
+        k_pcg_begin<<<1, 1, 0, st>>>(s.ctl, clear_pressure ? 1 : 0);
         if (clear_pressure) k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
         enqueue_vcycle(s);
-        k_pcg_start<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl, s.partials, mode);
-        k_pcg_cond<<<1, 1, 0, st>>>(s.ctl, h, cap, dyn_cap);
+        launch(s.use_pdl, k_pcg_start, g, kSegBlock, 0, st, B, s.search, s.ctl, s.partials, mode);
+        launch(s.use_pdl, k_pcg_cond, 1, 1, 0, st, s.ctl, h, cap, dyn_cap);
         return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
@@ -245,7 +257,7 @@ static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p
     if (e != cudaSuccess) return e;
     e = capture_into(s, body, [&]() {
         pcg_iteration(s, mode, x, p_padded);
-        k_pcg_cond<<<1, 1, 0, s.stream>>>(s.ctl, h, cap, dyn_cap);
+        launch(s.use_pdl, k_pcg_cond, 1, 1, 0, s.stream, s.ctl, h, cap, dyn_cap);
         return cudaGetLastError();
     });
     s.kn_pcg = count_kernel_nodes(body.g);
@@ -339,7 +351,7 @@ static cudaError_t eager_pcg(Scene& s, int mode, float* x, int p_padded, uint32_
     const Level& B = s.lv[0];
     uint32_t g = seg_grid(B.words);
     cudaStream_t st = s.stream;
-    k_pcg_begin<<<1, 1, 0, st>>>(s.ctl);
+    k_pcg_begin<<<1, 1, 0, st>>>(s.ctl, clear_pressure ? 1 : 0);
     if (clear_pressure) k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
     enqueue_vcycle(s);
     k_pcg_start<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl, s.partials, mode);

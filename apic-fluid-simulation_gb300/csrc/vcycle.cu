@@ -44,24 +44,28 @@ __device__ __forceinline__ uint32_t gwarp() { return (blockIdx.x * blockDim.x + 
 __device__ __forceinline__ uint32_t gnwarps() { return (gridDim.x * blockDim.x) >> 5; }
 
 __global__ void __launch_bounds__(kSegBlock) k_smooth(Level L, int li, const Ctl* ctl, int color, int init) {
+    pdl_wait();
     if (ctl->pcg_done) return;
     ph_smooth(L, ctl->seg_count[li], gwarp(), gnwarps(), color, init);
 }
 
 // Restriction only (into the first tail level or the coarsest level).
 __global__ void __launch_bounds__(kSegBlock) k_restrict(Level f, Level c, int lc, const Ctl* ctl) {
+    pdl_wait();
     if (ctl->pcg_done) return;
     ph_restrict(f, c, ctl->seg_count[lc], gwarp(), gnwarps(), false);
 }
 
 // Restriction fused with the coarse level's first (red) sweep.
 __global__ void __launch_bounds__(kSegBlock) k_restrict_red(Level f, Level c, int lc, const Ctl* ctl) {
+    pdl_wait();
     if (ctl->pcg_done) return;
     ph_restrict(f, c, ctl->seg_count[lc], gwarp(), gnwarps(), true);
 }
 
 // Prolongation fused with the black sweep.
 __global__ void __launch_bounds__(kSegBlock) k_prolong_black(Level c, Level f, int lf, const Ctl* ctl, int base) {
+    pdl_wait();
     if (ctl->pcg_done) return;
     ph_prolong(c, f, ctl->seg_count[lf], gwarp(), gnwarps(), 1, base ? ctl->last_fluid : 0xFFFFFFFFu,
                base ? ctl->pad_count : 0u);
@@ -69,6 +73,7 @@ __global__ void __launch_bounds__(kSegBlock) k_prolong_black(Level c, Level f, i
 
 // Prolongation fused with the final red sweep (black neighbours are final).
 __global__ void __launch_bounds__(kSegBlock) k_prolong_red(Level c, Level f, int lf, const Ctl* ctl, int base) {
+    pdl_wait();
     if (ctl->pcg_done) return;
     ph_prolong(c, f, ctl->seg_count[lf], gwarp(), gnwarps(), 0, base ? ctl->last_fluid : 0xFFFFFFFFu,
                base ? ctl->pad_count : 0u);
@@ -92,11 +97,13 @@ __global__ void __launch_bounds__(kSegBlock) k_up(const float* c_fin, uint32_t c
 
 __global__ void __launch_bounds__(kTailThreads) k_coarse_solve(Level L, float* __restrict__ cs, float* __restrict__ cap,
                                                                float* __restrict__ cr, const Ctl* __restrict__ ctl) {
+    pdl_wait();
     if (ctl->pcg_done) return;
     cta_coarse_cg(L.fluid, L.w, L.cells, L.diag, L.px, L.py, L.res, L.err, cs, cap, cr);
 }
 
 __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(TailParams tp, const Ctl* ctl) {
+    pdl_wait();
     if (ctl->pcg_done) return;
     extern __shared__ uint32_t sm[];
     cta_tail(tp, sm, true);
@@ -117,6 +124,7 @@ struct MidParams {
 };
 
 __global__ void __launch_bounds__(kTailThreads, 1) k_vcycle_mid(MidParams mp, TailParams tp, const Ctl* ctl) {
+    pdl_wait();
     if (ctl->pcg_done) return;
     extern __shared__ uint32_t sm[];
     namespace cg = cooperative_groups;
@@ -168,8 +176,13 @@ void launch_mid(Scene& s, cudaStream_t st) {
     for (int k = 0; k <= mp.n; ++k) mp.lv[k] = s.lv[s.cluster_first + k];
     uint32_t off = 0;
     TailParams tp = make_tail_params(s, s.tail_first, &off);
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     cudaLaunchConfig_t cfg = mid_config(uint32_t(s.cluster_size), size_t(off) * 4, st, attr);
+    if (s.use_pdl) {
+        attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[1].val.programmaticStreamSerializationAllowed = 1;
+        cfg.numAttrs = 2;
+    }
     cudaLaunchKernelEx(&cfg, k_vcycle_mid, mp, tp, static_cast<const Ctl*>(s.ctl));
 }
 
@@ -268,43 +281,44 @@ static void enqueue_vcycle_unfused(Scene& s, bool base_red_done) {
     Level* L = s.lv;
     auto grid = [&](int l) { return seg_grid(L[l].words); };
     const int last = s.nlevels - 1;
-    if (!base_red_done) k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 0, 1);
-    k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 1, 1);
+    const bool pdl = s.use_pdl;
+    if (!base_red_done) launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 0, 1);
+    launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 1, 1);
     if (last < 1) {
-        k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 1, 0);
-        k_smooth<<<grid(0), kSegBlock, 0, st>>>(L[0], 0, s.ctl, 0, 0);
+        launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 1, 0);
+        launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 0, 0);
         return;
     }
     const bool cluster = s.cluster_first < s.tail_first && s.tail_first < s.nlevels;
     int deepest_mid = 0;  // deepest level smoothed by the global kernels
     for (int l = 1; l <= last; ++l) {
         if (cluster && l == s.cluster_first) {
-            k_restrict_red<<<grid(l), kSegBlock, 0, st>>>(L[l - 1], L[l], l, s.ctl);
+            launch(pdl, k_restrict_red, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
             launch_mid(s, st);
             break;
         }
         if (l == s.tail_first) {
-            k_restrict<<<grid(l), kSegBlock, 0, st>>>(L[l - 1], L[l], l, s.ctl);
+            launch(pdl, k_restrict, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
             uint32_t off = 0;
             TailParams tp = make_tail_params(s, l, &off);
-            k_vcycle_tail<<<1, kTailThreads, size_t(off) * 4, st>>>(tp, s.ctl);
+            launch(pdl, k_vcycle_tail, 1, kTailThreads, size_t(off) * 4, st, tp, s.ctl);
             break;
         }
         if (l == last) {
-            k_restrict<<<grid(l), kSegBlock, 0, st>>>(L[l - 1], L[l], l, s.ctl);
-            k_coarse_solve<<<1, kTailThreads, 0, st>>>(L[l], s.cg_s, s.cg_ap, s.cg_r, s.ctl);
+            launch(pdl, k_restrict, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
+            launch(pdl, k_coarse_solve, 1, kTailThreads, 0, st, L[l], s.cg_s, s.cg_ap, s.cg_r, s.ctl);
             break;
         }
-        k_restrict_red<<<grid(l), kSegBlock, 0, st>>>(L[l - 1], L[l], l, s.ctl);
-        k_smooth<<<grid(l), kSegBlock, 0, st>>>(L[l], l, s.ctl, 1, 1);
+        launch(pdl, k_restrict_red, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
+        launch(pdl, k_smooth, grid(l), kSegBlock, 0, st, L[l], l, s.ctl, 1, 1);
         deepest_mid = l;
     }
     for (int l = deepest_mid; l >= 1; --l) {
-        k_prolong_black<<<grid(l), kSegBlock, 0, st>>>(L[l + 1], L[l], l, s.ctl, 0);
-        k_prolong_red<<<grid(l), kSegBlock, 0, st>>>(L[l + 1], L[l], l, s.ctl, 0);
+        launch(pdl, k_prolong_black, grid(l), kSegBlock, 0, st, L[l + 1], L[l], l, s.ctl, 0);
+        launch(pdl, k_prolong_red, grid(l), kSegBlock, 0, st, L[l + 1], L[l], l, s.ctl, 0);
     }
-    k_prolong_black<<<grid(0), kSegBlock, 0, st>>>(L[1], L[0], 0, s.ctl, 1);
-    k_prolong_red<<<grid(0), kSegBlock, 0, st>>>(L[1], L[0], 0, s.ctl, 1);
+    launch(pdl, k_prolong_black, grid(0), kSegBlock, 0, st, L[1], L[0], 0, s.ctl, 1);
+    launch(pdl, k_prolong_red, grid(0), kSegBlock, 0, st, L[1], L[0], 0, s.ctl, 1);
 }
 
 }  // namespace apic

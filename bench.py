@@ -211,6 +211,8 @@ def run_gpu_arm(args, world, rank, local):
     if args.cluster_cells is not None:
         sim.set_option(A.OPT_CLUSTER_VCYCLE, args.cluster_cells)
     cluster_cells = sim.get_option(A.OPT_CLUSTER_VCYCLE)
+    if args.no_pdl:
+        sim.set_option(A.OPT_PDL, 0)
     opts = A.DebugOptions()
     stream_ptr = ctypes_stream(sim)
     ext_stream = torch.cuda.ExternalStream(stream_ptr)
@@ -223,7 +225,7 @@ def run_gpu_arm(args, world, rank, local):
     # ---- timed region: K updates, device time per update, L2 flushed in between
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    substeps, iters, launches = 0, 0, 0
+    substeps, iters, launches, solve_ms = 0, 0, 0, 0.0
     true_res = []
     if args.eager:  # stage-by-stage launches (what an ncu launch list can see)
         sim.set_profiling(True)
@@ -241,6 +243,7 @@ def run_gpu_arm(args, world, rank, local):
             substeps += st.substeps
             iters += st.pcg_iterations_total
             launches += st.kernel_launches
+            solve_ms += st.solve_ms
             true_res.append(st.true_residual_rel)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
@@ -287,16 +290,19 @@ def run_gpu_arm(args, world, rank, local):
     sim.set_profiling(False)
     counts = level_fluid_counts(A, sim)
     peak, peak_kind = peaks()
-    roof = roofline(stages, prof_sub, prof_iters, n, sim, counts, peak, peak_kind)
+    roof = roofline(iters, solve_ms, args.steps, counts, peak, peak_kind) if solve_ms > 0 and not args.eager else None
 
     result = None
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline and world == 1:
-            c = cpu_restatement_rate(n_steps=args.cpu_steps, warmup=1, budget_s=args.cpu_budget, side=args.side)
+            # the same updates as the timed GPU region: warm-up updates, then the timed ones
+            c = cpu_restatement_rate(n_steps=args.cpu_steps or args.steps, warmup=args.warmup,
+                                     budget_s=args.cpu_budget, side=args.side)
             cpu = {"value": c["value"], "unit": METRIC, "cores": c["threads"], "kind": "port",
-                   "sample": f"C++ restatement of the reference step (OpenMP), {c['steps']} updates of the same "
-                             f"scene after 1 warm-up update, {c['seconds']:.1f} s"}
+                   "sample": f"C++ restatement of the reference step (OpenMP, {c['threads']} threads), updates "
+                             f"{args.warmup + 1}..{args.warmup + c['steps']} of the same scene (the GPU's timed "
+                             f"updates), {c['seconds']:.1f} s"}
         result = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dev_s_max / args.steps, "higher_is_better": True,
@@ -314,7 +320,8 @@ def run_gpu_arm(args, world, rank, local):
                        else "one kernel per sweep and transfer" + (
                            f"; levels of <= {cluster_cells} cells in one thread-block cluster"
                            if cluster_cells else ""),
-                       "launch": "stage by stage" if args.eager else "one CUDA graph per update"},
+                       "launch": ("stage by stage" if args.eager else "one CUDA graph per update")
+                       + ("" if args.no_pdl else "; programmatic dependent launch in the PCG loop")},
             "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
             "wall_s": wall,
             "clocks": clocks.summary(),
@@ -339,33 +346,48 @@ def ctypes_stream(sim) -> int:
     return int(out.value or 0)
 
 
-def roofline(stages, substeps, iters, n, sim, counts, peak, peak_kind):
-    """Roofline of the stage with the largest device time (HBM bound)."""
-    info = sim.info()
-    W = H = info.width
-    U, V, C = (W + 1) * H, W * (H + 1), W * H
-    npad = info.num_chunks * 8
+# Algorithmic bytes of one PCG iteration per fluid cell (each array read or
+# written once per pass; neighbour reads hit cached lines):
+#   base level: SpMV with the search update 24 B, update + first red sweep
+#   38 B, black sweep 22 B, restriction 20 B, prolongation + black sweep 23 B,
+#   prolongation + red sweep 23 B, r.z 8 B = 158 B;
+#   coarser levels: sweeps, restriction, prolongations = 88 B.
+SOLVE_BYTES_BASE = 158
+SOLVE_BYTES_COARSE = 88
+
+
+def solve_traffic():
+    """DRAM bytes per PCG iteration from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "solve_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["dram_bytes_per_iteration"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def roofline(iters, solve_ms, steps, counts, peak, peak_kind):
+    """Roofline of the pressure solve, the dominant part of a step.
+
+    The solve is a CUDA graph of per-phase kernels inside device-side WHILE
+    loops, so CUDA events cannot bracket it; its first and last kernels read
+    the GPU's global nanosecond timer instead (apic_step_stats.solve_ms),
+    summed here over the timed updates.  achieved = algorithmic bytes of the
+    iterations run / that time.
+    """
     f0 = counts[0]
     fl = sum(counts[1:])
-    # algorithmic bytes of one launch of each stage (per substep)
-    alg = {
-        "g2p": 48 * npad + 4 * (U + V),
-        "p2g": 36 * n + 8 * (U + V) + 4 * C,
-        "pcg": (132 * f0 + 76 * fl) * (iters / max(substeps, 1)),
-        "extrap": 4 * 10 * (U + V),
-        "grad": 8 * (U + V) + 4 * C,
-        "build": 3 * 8 * f0 + 36 * f0,
-        "forces": 5 * (U + V),
-        "mg": 32 * fl,
-        "sort": (184 - 128 + 16 * 3) * n,
-    }
-    dom = max((k for k in stages if stages[k][1]), key=lambda k: stages[k][0])
-    ms, launches = stages[dom]
-    avg_s = ms / 1e3 / max(launches, 1)
-    achieved = alg.get(dom, 0) / avg_s / 1e9 if avg_s > 0 else 0.0
-    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-            "algorithmic_bytes_per_launch": alg.get(dom), "avg_launch_ms": avg_s * 1e3}
+    per_iter = SOLVE_BYTES_BASE * f0 + SOLVE_BYTES_COARSE * fl
+    sec = solve_ms / 1e3
+    achieved = per_iter * iters / sec / 1e9
+    traffic = solve_traffic()
+    return {"bound": "hbm", "kernel": "pressure solve: MG-preconditioned CG (k_spmv_dot, k_pcg_update, "
+                                      "V-cycle kernels, k_dot_rz per iteration)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "traffic": traffic, "traffic_unit": "DRAM bytes per PCG iteration" if traffic else None,
+            "algorithmic_bytes_per_iteration": per_iter, "iterations": iters,
+            "us_per_iteration": solve_ms * 1e3 / max(iters, 1), "solve_ms_per_step": solve_ms / steps}
 
 
 def main():
@@ -385,7 +407,9 @@ def main():
                     help="run the V-cycle as one kernel per level and direction")
     ap.add_argument("--cluster-cells", type=int, default=None,
                     help="largest multigrid level run inside the thread-block cluster (0: none)")
-    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--no-pdl", action="store_true",
+                    help="launch the PCG loop's kernels in plain stream order")
+    ap.add_argument("--cpu-steps", type=int, default=0, help="CPU sample updates (default: --steps)")
     ap.add_argument("--cpu-budget", type=float, default=30.0)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -85,6 +85,9 @@ typedef struct apic_step_stats {
     uint32_t not_converged;        /* substeps whose solve hit its iteration cap */
     uint32_t nonfinite_lanes;      /* NaN/Inf particle lanes after the last G2P */
     uint64_t kernel_launches;      /* kernels the last update's graph launched (0 when profiling) */
+    double   solve_ms;             /* device time of the last update's pressure solves, read from
+                                      the GPU's global nanosecond timer by the solve's first and
+                                      last kernels (0 for the persistent solver) */
 } apic_step_stats;
 
 /* ---- field identifiers for apic_read_field / apic_write_field ---------- */
@@ -227,6 +230,10 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
  * cannot hold a cluster of 1024-thread CTAs; apic_get_option reports 0 then.
  * Same results bit for bit.  Applies when APIC_OPT_FUSED_VCYCLE is 0. */
 #define APIC_OPT_CLUSTER_VCYCLE 3
+/* 1 (default): kernels inside the PCG loop use programmatic dependent launch
+ * (each is scheduled while its predecessor drains and waits on the device
+ * for its results); 0: plain stream order.  Same results bit for bit. */
+#define APIC_OPT_PDL 4
 int apic_set_option(apic_handle* h, int option, int value);
 int apic_get_option(apic_handle* h, int option, int* value);
 
