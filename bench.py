@@ -13,8 +13,9 @@ Printed JSON line: ``value`` = particles x steps / device time of the timed
 steps (CUDA events on the scene's stream, L2 flushed between steps);
 ``e2e`` = the same through the C-ABI with a host force field uploaded from
 pinned memory and the particle state read back every step; ``roofline`` for
-the dominant kernel, ``cpu_baseline`` = the C++ restatement of the reference
-step (OpenMP, all host cores) on a bounded sample of the same workload.
+the pressure solve (the dominant part of a step, timed inside the update
+graph by the device's global timer), ``cpu_baseline`` = the C++ restatement
+of the reference step (OpenMP, all host cores) over the same updates.
 
 ``--impl reference`` times that CPU restatement alone as the reference arm.
 Under torchrun (N > 1) each rank runs an independent replica on its own GPU
