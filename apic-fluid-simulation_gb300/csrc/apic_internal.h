@@ -234,8 +234,10 @@ cudaError_t run_solve_eager(Scene& s);
 void plan_vcycle(Scene& s);     // pick the coarse levels that run in one CTA / one cluster
 void plan_vcycle_cluster(Scene& s);  // re-pick the cluster's levels after cluster_max_cells changed
 // z = M^-1 r on s.stream; base_red_done: the base level's first red sweep
-// was already written (by k_pcg_update)
-void enqueue_vcycle(Scene& s, bool base_red_done = false);
+// was already written (by k_pcg_update); rz_mode >= 0: the last kernel also
+// reduces r.z and finishes the PCG iteration for that solver mode (returns
+// false when this V-cycle form cannot, and the caller must).
+bool enqueue_vcycle(Scene& s, bool base_red_done = false, int rz_mode = -1);
 // runtime.cu
 cudaError_t launch_plan_first(Scene& s);
 cudaError_t launch_advance(Scene& s);

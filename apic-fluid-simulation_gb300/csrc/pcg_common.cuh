@@ -175,6 +175,20 @@ __device__ __forceinline__ void ph_update_search(const Level& B, uint32_t nseg, 
     *r2 = acc;
 }
 
+// gamma' = r.z ends the iteration (:1934-1943): beta, or the exit when r.z
+// is below SAFTY (reference mode) or zero.  Run by one thread with the total.
+__device__ __forceinline__ void finish_rz(Ctl* ctl, double tot, int mode) {
+    constexpr float kSafetyRz = 1e-5f;  // SAFTY, src/apic.rs:8
+    const float ng = float(tot);
+    if (mode == APIC_SOLVER_REFERENCE ? (ng < kSafetyRz) : !(ng != 0.0f)) {
+        ctl->pcg_done = 1;
+        return;
+    }
+    ctl->beta = ng / ctl->gamma;
+    ctl->beta_valid = 1;
+    ctl->gamma = ng;
+}
+
 // r.z after the preconditioner (:1936).
 __device__ __forceinline__ F2 ph_rz(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps) {
     F2 acc{0.0f, 0.0f};

@@ -120,13 +120,8 @@ __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, double*
     if (ctl->pcg_done) return;
     F2 acc = pcg::ph_rz(B, ctl->seg_count[0], gwarp(), gnwarps());
     double tot;
-    if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
-        float ng = float(tot);
-        if (mode == APIC_SOLVER_REFERENCE ? (ng < kSafety) : !(ng != 0.0f)) { ctl->pcg_done = 1; return; }
-        ctl->beta = ng / ctl->gamma;
-        ctl->beta_valid = 1;
-        ctl->gamma = ng;
-    }
+    if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0)
+        pcg::finish_rz(ctl, tot, mode);
 }
 
 
@@ -228,8 +223,8 @@ static void pcg_iteration(Scene& s, int mode, float* x, int p_padded) {
     k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, s.partials, mode);
     launch(pdl, k_pcg_update, g, kSegBlock, 0, st, B, x, p_padded, s.search, s.ap, s.ctl, s.partials, mode,
            s.props.solve_error);
-    enqueue_vcycle(s, true);
-    launch(pdl, k_dot_rz, g, kSegBlock, 0, st, B, s.ctl, s.partials, mode);
+    // the V-cycle's last kernel also reduces r.z and sets beta (k_dot_rz's work)
+    if (!enqueue_vcycle(s, true, mode)) launch(pdl, k_dot_rz, g, kSegBlock, 0, st, B, s.ctl, s.partials, mode);
 }
 
 // PCG setup (src/apic.rs:1885-1892) followed by a device-controlled WHILE

@@ -34,6 +34,7 @@
 
 #include "apic_device.cuh"
 #include "apic_internal.h"
+#include "pcg_common.cuh"
 #include "vcycle_common.cuh"
 
 namespace apic {
@@ -69,6 +70,19 @@ __global__ void __launch_bounds__(kSegBlock) k_prolong_black(Level c, Level f, i
     if (ctl->pcg_done) return;
     ph_prolong(c, f, ctl->seg_count[lf], gwarp(), gnwarps(), 1, base ? ctl->last_fluid : 0xFFFFFFFFu,
                base ? ctl->pad_count : 0u);
+}
+
+// Base-level prolongation fused with the final red sweep, which also reduces
+// r.z over every fluid cell (red cells' new z, black cells' final z) and
+// finishes the PCG iteration (k_dot_rz's work).
+__global__ void __launch_bounds__(kSegBlock) k_prolong_red_rz(Level c, Level B, Ctl* ctl, double* partials,
+                                                              int mode) {
+    pdl_wait();
+    if (ctl->pcg_done) return;
+    const F2 acc = ph_prolong_red_rz(c, B, ctl->seg_count[0], gwarp(), gnwarps(), ctl->last_fluid, ctl->pad_count);
+    double tot;
+    if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0)
+        pcg::finish_rz(ctl, tot, mode);
 }
 
 // Prolongation fused with the final red sweep (black neighbours are final).
@@ -240,14 +254,14 @@ void plan_vcycle_cluster(Scene& s) {
     }
 }
 
-static void enqueue_vcycle_unfused(Scene& s, bool base_red_done);
+static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode);
 
 // One V-cycle on s.stream: z = M^-1 r in lv[0].err.  Fused form: one kernel
 // per level down (k_down) and up (k_up) around the coarse tail.
-void enqueue_vcycle(Scene& s, bool base_red_done) {
+bool enqueue_vcycle(Scene& s, bool base_red_done, int rz_mode) {
     if (!s.fused_vcycle || s.nlevels < 2) {
-        enqueue_vcycle_unfused(s, base_red_done);
-        return;
+        enqueue_vcycle_unfused(s, base_red_done, rz_mode);
+        return rz_mode < 0 || s.nlevels >= 2;
     }
     // the fused descent recomputes the base level's red sweep from the
     // residual, so a sweep already written changes nothing
@@ -273,10 +287,11 @@ void enqueue_vcycle(Scene& s, bool base_red_done) {
     auto fin = [&](int l) { return (l == 0 || l == deepest) ? L[l].err : L[l].err2; };
     for (int l = deepest - 1; l >= 0; --l)
         k_up<<<grid(l), kSegBlock, 0, st>>>(fin(l + 1), L[l + 1].w, L[l], pre(l), fin(l), l, s.ctl, l == 0 ? 1 : 0);
+    return rz_mode < 0;
 }
 
 // Two kernels per sweep and per transfer (the reference's sequence launch by launch).
-static void enqueue_vcycle_unfused(Scene& s, bool base_red_done) {
+static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode) {
     cudaStream_t st = s.stream;
     Level* L = s.lv;
     auto grid = [&](int l) { return seg_grid(L[l].words); };
@@ -318,7 +333,10 @@ static void enqueue_vcycle_unfused(Scene& s, bool base_red_done) {
         launch(pdl, k_prolong_red, grid(l), kSegBlock, 0, st, L[l + 1], L[l], l, s.ctl, 0);
     }
     launch(pdl, k_prolong_black, grid(0), kSegBlock, 0, st, L[1], L[0], 0, s.ctl, 1);
-    launch(pdl, k_prolong_red, grid(0), kSegBlock, 0, st, L[1], L[0], 0, s.ctl, 1);
+    if (rz_mode >= 0)
+        launch(pdl, k_prolong_red_rz, grid(0), kSegBlock, 0, st, L[1], L[0], s.ctl, s.partials, rz_mode);
+    else
+        launch(pdl, k_prolong_red, grid(0), kSegBlock, 0, st, L[1], L[0], 0, s.ctl, 1);
 }
 
 }  // namespace apic

@@ -429,6 +429,38 @@ __device__ __forceinline__ void ph_prolong(const Level& c, const Level& f, uint3
     }
 }
 
+// ph_prolong's red pass on the base level, also returning this thread's share
+// of r.z over every fluid cell: red cells' new z, black cells' z as the
+// black pass left it (final).  The products are those of pcg::ph_rz.
+__device__ __forceinline__ F2 ph_prolong_red_rz(const Level& c, const Level& f, uint32_t nseg_f, uint32_t warp,
+                                                uint32_t nwarps, uint32_t last, uint32_t extra) {
+    const uint32_t lane = threadIdx.x & 31;
+    const float* fe = f.err;
+    const float* ce = c.err;
+    const uint32_t fw = f.w, cw = c.w;
+    F2 acc{0.0f, 0.0f};
+    for (uint32_t s = warp; s < nseg_f; s += nwarps) {
+        const uint32_t word = f.seg[s];
+        const uint32_t raw = word * 32 + lane;
+        if (raw >= f.cells) continue;
+        const bool fluid = (f.fluid[word] >> lane) & 1u;
+        const uint32_t p = raw + fw;
+        float z;
+        if (is_red(raw, fw)) {
+            const float ec = ce[((raw / fw) / 2) * cw + (raw % fw) / 2 + cw];
+            const float old = prolonged(fe[p], ec, p == last ? extra : 0u);
+            z = sor_cell_all(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, raw, p, old, true,
+                             [fe](uint32_t q, long long) { return fe[q]; });
+            if (fluid) f.err[p] = z;
+        } else {
+            z = fe[p];
+        }
+        const float rz = f.res[p] * z;
+        if (fluid) acc = f2_add(acc, rz);
+    }
+    return acc;
+}
+
 // Asynchronous 4-byte copy global -> shared (cp.async, sm_80+): the copies
 // of a whole array set are issued back to back and complete together at
 // cp_async_wait_all, so loading costs about one L2 round trip instead of one
