@@ -179,6 +179,12 @@ struct Scene {
     int cluster_size = 0;                     // CTAs per cluster (0: clusters unavailable)
     int cluster_first = 0;
     bool use_pdl = true;                      // programmatic dependent launch inside the PCG loop
+    // levels [dsm_first, dsm_tail) of the V-cycle held in a cluster's
+    // distributed shared memory, dsm_tail.. in CTA 0 (dsm_first == nlevels: none)
+    bool use_dsm = true;
+    int dsm_first = 0, dsm_tail = 0;
+    size_t dsm_smem = 0;
+    uint32_t dsm_off = 0;
     // kernel nodes per execution of each graph body (launch accounting)
     uint32_t kn_top = 0, kn_sort = 0, kn_loop = 0, kn_pcg = 0, kn_refine = 0;
     int solver_mode = APIC_SOLVER_REFERENCE;
@@ -233,6 +239,9 @@ cudaError_t run_solve_eager(Scene& s);
 // vcycle.cu
 void plan_vcycle(Scene& s);     // pick the coarse levels that run in one CTA / one cluster
 void plan_vcycle_cluster(Scene& s);  // re-pick the cluster's levels after cluster_max_cells changed
+// vcycle_dsm.cu
+void plan_vcycle_dsm(Scene& s);
+void launch_vcycle_dsm(Scene& s, cudaStream_t st);
 // z = M^-1 r on s.stream; base_red_done: the base level's first red sweep
 // was already written (by k_pcg_update); rz_mode >= 0: the last kernel also
 // reduces r.z and finishes the PCG iteration for that solver mode (returns

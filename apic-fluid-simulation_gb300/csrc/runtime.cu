@@ -919,6 +919,10 @@ int apic_set_option(apic_handle* h, int option, int value) {
             s.use_pdl = value != 0;
             invalidate_graphs(s);
             return APIC_OK;
+        case APIC_OPT_DSM_VCYCLE:
+            s.use_dsm = value != 0;
+            invalidate_graphs(s);
+            return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }
@@ -932,6 +936,9 @@ int apic_get_option(apic_handle* h, int option, int* value) {
             *value = h->s.cluster_size > 0 ? int(h->s.cluster_max_cells) : 0;
             return APIC_OK;
         case APIC_OPT_PDL: *value = h->s.use_pdl ? 1 : 0; return APIC_OK;
+        case APIC_OPT_DSM_VCYCLE:
+            *value = (h->s.use_dsm && h->s.dsm_first < h->s.dsm_tail) ? 1 : 0;
+            return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }

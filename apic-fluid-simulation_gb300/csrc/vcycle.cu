@@ -241,6 +241,7 @@ void plan_vcycle(Scene& s) {
         cudaGetLastError();  // a refused size leaves an error behind
     }
     plan_vcycle_cluster(s);
+    plan_vcycle_dsm(s);
 }
 
 // Middle levels for the cluster: the levels just above the tail with at most
@@ -304,9 +305,15 @@ static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode) {
         launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 0, 0);
         return;
     }
-    const bool cluster = s.cluster_first < s.tail_first && s.tail_first < s.nlevels;
+    const bool dsm = s.use_dsm && s.dsm_first < s.dsm_tail && s.dsm_tail < s.nlevels;
+    const bool cluster = !dsm && s.cluster_first < s.tail_first && s.tail_first < s.nlevels;
     int deepest_mid = 0;  // deepest level smoothed by the global kernels
     for (int l = 1; l <= last; ++l) {
+        if (dsm && l == s.dsm_first) {
+            launch(pdl, k_restrict_red, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
+            launch_vcycle_dsm(s, st);
+            break;
+        }
         if (cluster && l == s.cluster_first) {
             launch(pdl, k_restrict_red, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
             launch_mid(s, st);

@@ -214,6 +214,9 @@ def run_gpu_arm(args, world, rank, local):
     cluster_cells = sim.get_option(A.OPT_CLUSTER_VCYCLE)
     if args.no_pdl:
         sim.set_option(A.OPT_PDL, 0)
+    if args.no_dsm:
+        sim.set_option(A.OPT_DSM_VCYCLE, 0)
+    dsm = sim.get_option(A.OPT_DSM_VCYCLE)
     opts = A.DebugOptions()
     stream_ptr = ctypes_stream(sim)
     ext_stream = torch.cuda.ExternalStream(stream_ptr)
@@ -319,6 +322,7 @@ def run_gpu_arm(args, world, rank, local):
                        "solve_form": "persistent kernel" if args.persistent else "graph of per-phase kernels",
                        "vcycle": "one kernel per level per direction" if args.fused_vcycle
                        else "one kernel per sweep and transfer" + (
+                           "; coarse levels in one cluster's distributed shared memory" if dsm else
                            f"; levels of <= {cluster_cells} cells in one thread-block cluster"
                            if cluster_cells else ""),
                        "launch": ("stage by stage" if args.eager else "one CUDA graph per update")
@@ -408,6 +412,8 @@ def main():
                     help="run the V-cycle as one kernel per level and direction")
     ap.add_argument("--cluster-cells", type=int, default=None,
                     help="largest multigrid level run inside the thread-block cluster (0: none)")
+    ap.add_argument("--no-dsm", action="store_true",
+                    help="keep the middle multigrid levels in global memory instead of a cluster's shared memory")
     ap.add_argument("--no-pdl", action="store_true",
                     help="launch the PCG loop's kernels in plain stream order")
     ap.add_argument("--cpu-steps", type=int, default=0, help="CPU sample updates (default: --steps)")

@@ -234,6 +234,13 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
  * (each is scheduled while its predecessor drains and waits on the device
  * for its results); 0: plain stream order.  Same results bit for bit. */
 #define APIC_OPT_PDL 4
+/* 1 (default where the level sizes allow): the multigrid levels from the
+ * largest that fits down to 32 rows live in the distributed shared memory of
+ * one 16-CTA thread-block cluster (each CTA owns a band of rows) and the
+ * coarser ones in its first CTA; overrides APIC_OPT_CLUSTER_VCYCLE.  0: off.
+ * apic_get_option reports 0 where no level qualifies.  Same results bit for
+ * bit. */
+#define APIC_OPT_DSM_VCYCLE 5
 int apic_set_option(apic_handle* h, int option, int value);
 int apic_get_option(apic_handle* h, int option, int* value);
 

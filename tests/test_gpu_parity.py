@@ -404,6 +404,7 @@ def test_cluster_vcycle_equals_unfused(gpu_lib, side, cells):
     g = A.Apic(side, side, cs, props)
     if g.get_option(A.OPT_CLUSTER_VCYCLE) == 0:
         pytest.skip("thread-block clusters unavailable")
+    g.set_option(A.OPT_DSM_VCYCLE, 0)  # the distributed form replaces this one when on
     px, py, vx, vy = A.generate_scene(scene)
     g.set_particles(px, py, vx, vy)
     for _ in range(3):
@@ -424,6 +425,7 @@ def test_cluster_vcycle_equals_unfused(gpu_lib, side, cells):
         h = A.Apic(side, side, cs, props)
         h.set_particles(px, py, vx, vy)
         h.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+        h.set_option(A.OPT_DSM_VCYCLE, 0)
         h.set_option(A.OPT_CLUSTER_VCYCLE, value)
         for _ in range(2):
             h.update(A.DebugOptions(disable_particle_sort=True), 1 / 480)
@@ -444,3 +446,48 @@ def test_cluster_option_rejected_without_middle_levels(gpu_lib):
         g.set_option(A.OPT_CLUSTER_VCYCLE, 65536)
     assert ei.value.code == A.ERR_UNSUPPORTED
     g.set_option(A.OPT_CLUSTER_VCYCLE, 0)
+
+
+@pytest.mark.parametrize("side", [256, 1024, 2048])
+def test_dsm_vcycle_equals_global(gpu_lib, side):
+    """Levels held in a cluster's distributed shared memory give the same z = M^-1 r, bit for bit."""
+    props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+    cs = 1 / side
+    scene = A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=cs, sub=2, seed=1, fluid_x=0.5, fluid_y=0.5,
+                           disk=(0.7, 0.8, 0.08), disk_v=(0.0, -2.0))
+    g = A.Apic(side, side, cs, props)
+    if g.get_option(A.OPT_DSM_VCYCLE) == 0:
+        pytest.skip("no level qualifies for the distributed form on this GPU")
+    px, py, vx, vy = A.generate_scene(scene)
+    g.set_particles(px, py, vx, vy)
+    for _ in range(3):
+        g.update(A.DebugOptions(), 1 / 480)
+    g.run_stage("mg", 1 / 480)
+    fl = g.read_field("fluid_list").astype(np.int64)
+    out = []
+    for dsm, cluster in ((1, 65536), (0, 0), (1, 65536)):
+        g.set_option(A.OPT_DSM_VCYCLE, dsm)
+        g.set_option(A.OPT_CLUSTER_VCYCLE, cluster)
+        g.run_stage("vcycle", 1 / 480)
+        out.append(g.read_field("error")[fl])
+    eq(out[0], out[1], "distributed vs per-kernel V-cycle")
+    eq(out[2], out[1], "distributed V-cycle, second run")
+    # whole updates through the graph, both solver families
+    for mode in (A.SOLVER_REFERENCE, A.SOLVER_REL_MIXED):
+        sims = []
+        for dsm in (1, 0):
+            h = A.Apic(side, side, cs, props)
+            h.set_particles(px, py, vx, vy)
+            h.set_solver(mode, 1e-6, 500)
+            h.set_option(A.OPT_DSM_VCYCLE, dsm)
+            for _ in range(2):
+                h.update(A.DebugOptions(disable_particle_sort=True), 1 / 480)
+            sims.append(h)
+        its = [h.stats().pcg_iterations_total for h in sims]
+        assert abs(its[0] - its[1]) <= 2, its
+        if mode == A.SOLVER_REL_MIXED:
+            for h in sims:
+                assert float(h.stats().true_residual_rel) <= 1e-6
+        pa, pb = sims[0].read_field("pressure"), sims[1].read_field("pressure")
+        scale = float(np.max(np.abs(pa))) or 1.0
+        assert float(np.max(np.abs(pa - pb))) <= 1e-3 * scale
