@@ -130,6 +130,8 @@ struct Scene {
     float* part[NPF] = {};                 // allocation A of each field
     float* part_alt[NPF] = {};             // allocation B of each field
     PartPtrs* pp = nullptr;                // device table: which allocation is current
+    float* vec_stage = nullptr;            // Vec2x8 staging for host reads (allocated on first use)
+    uint32_t vec_stage_floats = 0;
     uint32_t* keys = nullptr;
     uint32_t* vals = nullptr;
     uint32_t* keys_alt = nullptr;
@@ -218,6 +220,7 @@ cudaError_t launch_p2g(Scene& s);
 cudaError_t launch_g2p(Scene& s);
 cudaError_t launch_vmax(Scene& s);
 cudaError_t launch_permute(Scene& s);
+cudaError_t launch_pack_vec2x8(Scene& s, int which, float* out);  // which: 0 pos, 1 vel, 2 C_u, 3 C_v
 // grid.cu
 cudaError_t launch_finalize_faces(Scene& s, bool forces, bool gravity);
 cudaError_t launch_base_lists(Scene& s);

@@ -261,6 +261,23 @@ cudaError_t launch_vmax(Scene& s) {
     return cudaGetLastError();
 }
 
+// Interleave two SoA particle fields into the reference's Vec2x8 layout
+// (per chunk: 8 x lanes then 8 y lanes), for one contiguous copy to the host.
+__global__ void __launch_bounds__(256) k_pack_vec2x8(const PartPtrs* __restrict__ pp, int fx, int fy, uint32_t nchunks,
+                                                     float* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nchunks * 16u) return;
+    const uint32_t c = i >> 4, j = i & 15u;
+    out[i] = j < 8u ? pp->f[fx][c * 8u + j] : pp->f[fy][c * 8u + (j - 8u)];
+}
+
+cudaError_t launch_pack_vec2x8(Scene& s, int which, float* out) {
+    if (s.nchunks == 0) return cudaSuccess;
+    k_pack_vec2x8<<<div_up(uint64_t(s.nchunks) * 16, 256), 256, 0, s.stream>>>(s.pp, 2 * which, 2 * which + 1,
+                                                                             s.nchunks, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_permute(Scene& s) {
     if (s.npad == 0) return cudaSuccess;
     k_permute<<<div_up(s.npad, 256), 256, 0, s.stream>>>(s.pp, s.vals, s.n, s.npad);

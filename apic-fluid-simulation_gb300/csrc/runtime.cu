@@ -201,6 +201,9 @@ void free_scene(Scene& s) {
         dfree(L.fluid); dfree(L.seg); dfree(L.diag); dfree(L.inv_diag); dfree(L.px); dfree(L.py);
         dfree(L.res); dfree(L.err); dfree(L.err2);
     }
+    dfree(s.vec_stage);
+    s.vec_stage = nullptr;
+    s.vec_stage_floats = 0;
     dfree(s.ctl);
     if (s.ctl_host) cudaFreeHost(s.ctl_host);
     s.ctl_host = nullptr;
@@ -882,14 +885,20 @@ int apic_read_vec2x8(apic_handle* h, int which, float* dst, uint64_t floats) {
     if (floats != uint64_t(s.nchunks) * 16) return fail(APIC_ERR_INVALID_ARG, "size mismatch");
     if (floats == 0) return APIC_OK;
     if (!dst) return fail(APIC_ERR_INVALID_ARG, "null destination");
+    // per chunk: 8 x lanes then 8 y lanes (ultraviolet::Vec2x8 {x: f32x8, y:
+    // f32x8}), interleaved on the device, then one contiguous copy
+    if (s.vec_stage_floats < floats) {
+        CK(cudaStreamSynchronize(s.stream));
+        dfree(s.vec_stage);
+        s.vec_stage = nullptr;
+        s.vec_stage_floats = 0;
+        if (dalloc(&s.vec_stage, floats) != cudaSuccess)
+            return fail(APIC_ERR_OOM, "out of device memory (Vec2x8 staging)");
+        s.vec_stage_floats = uint32_t(floats);
+    }
+    CK(launch_pack_vec2x8(s, which, s.vec_stage));
+    CK(cudaMemcpyAsync(dst, s.vec_stage, floats * sizeof(float), cudaMemcpyDeviceToHost, s.stream));
     CK(cudaStreamSynchronize(s.stream));
-    PartPtrs pp = read_ptrs(s);
-    int fx = 2 * which, fy = 2 * which + 1;
-    // per chunk: 8 x lanes then 8 y lanes (ultraviolet::Vec2x8 {x: f32x8, y: f32x8})
-    CK(cudaMemcpy2D(dst, 16 * sizeof(float), pp.f[fx], 8 * sizeof(float), 8 * sizeof(float), s.nchunks,
-                    cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy2D(dst + 8, 16 * sizeof(float), pp.f[fy], 8 * sizeof(float), 8 * sizeof(float), s.nchunks,
-                    cudaMemcpyDeviceToHost));
     return APIC_OK;
 }
 

@@ -470,6 +470,11 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// 16-byte form (both addresses 16-byte aligned), through L2 only.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const uint32_t sa = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
 
 // Start copying every tail level's mask and coefficients into shared memory
 // (complete after cp_async_wait_all).
@@ -588,10 +593,13 @@ __device__ __forceinline__ double ph_up(const float* c_fin, uint32_t cw, const L
 // the first level's residual is always copied in and its error copied out.
 // load_coeffs false: the coefficients are resident or their copies were
 // issued earlier by this CTA (cta_tail_issue_coeffs); the wait below covers
-// those too.
-__device__ __forceinline__ void cta_tail(const TailParams& tp, uint32_t* sm, bool load_coeffs) {
+// those too.  global_io false: the first level's residual is already in
+// shared memory and its error stays there (a cluster's other CTAs exchange
+// them through distributed shared memory).
+__device__ __forceinline__ void cta_tail(const TailParams& tp, uint32_t* sm, bool load_coeffs,
+                                         bool global_io = true) {
     if (load_coeffs) cta_tail_issue_coeffs(tp, sm);
-    {
+    if (global_io) {
         const TailLevel& t = tp.lv[0];
         SmemLevel L = smem_level(sm, t);
         for (uint32_t i = threadIdx.x; i < t.padded; i += blockDim.x) cp_async4(L.res + i, t.res + i);
@@ -631,6 +639,10 @@ __device__ __forceinline__ void cta_tail(const TailParams& tp, uint32_t* sm, boo
         __syncthreads();
         cta_sweep(f, 1, 0);
         cta_sweep(f, 0, 0);
+    }
+    if (!global_io) {
+        __syncthreads();
+        return;
     }
     const TailLevel& t = tp.lv[0];
     SmemLevel L = smem_level(sm, t);

@@ -166,9 +166,10 @@ __device__ __forceinline__ void dsm_sweep(const View& v, const cg::cluster_group
 // Restriction of fine view f into the coarse cells of this CTA's coarse rows
 // (their children are this CTA's fine rows): restrict_cell_all's arithmetic.
 // Coarse view c (with_red: also its first red sweep) or, when c is null, the
-// global first tail level.
+// first tail level's residual in CTA 0's shared memory (tail_res, padded
+// layout, mapped into this CTA's address space).
 __device__ __forceinline__ void dsm_restrict(const View& f, const cg::cluster_group& cl, const View* c,
-                                             const DsmParams& p, uint32_t rank, bool with_red) {
+                                             const DsmParams& p, float* tail_res, uint32_t rank, bool with_red) {
     const int wc = f.w >> 1;
     const int rc = f.R >> 1;
     const int yc0 = int(rank) * rc;
@@ -210,23 +211,24 @@ __device__ __forceinline__ void dsm_restrict(const View& f, const cg::cluster_gr
                 c->err[co] = inv != 0.0f ? 0.0f + (kOmega * (sum * inv - 0.0f)) : 0.0f;
             }
         } else if (bit_at(p.tfluid, uint32_t(craw))) {
-            p.tres[craw + wc] = sum;
+            tail_res[craw + wc] = sum;  // CTA 0's shared memory
         }
     }
 }
 
 // Prolongation from the coarse level into own fine cells of one colour,
 // fused with that colour's post-sweep (ph_prolong's arithmetic).  Coarse
-// error from view c, or (c null) from the global first tail level.
+// error from view c, or (c null) from the first tail level's error in CTA 0's
+// shared memory (tail_err, padded layout).
 __device__ __forceinline__ void dsm_prolong(const View& f, const cg::cluster_group& cl, const View* c,
-                                            const DsmParams& p, int color) {
+                                            const float* tail_err, int color) {
     const int wc = f.w >> 1;
     // coarse error under fine cell (x, y); outside the grid (a neighbour
     // whose value a select drops) reads 0
     auto coarse_e = [&](int x, int y) -> float {
         if (y < 0 || y >= f.h) return 0.0f;
         const int craw = (y >> 1) * wc + (x >> 1);
-        return c ? err_raw(*c, cl, craw) : p.terr[craw + wc];
+        return c ? err_raw(*c, cl, craw) : tail_err[craw + wc];
     };
     const int half = f.w >> 1;
     const int n = f.R * half;
@@ -264,20 +266,22 @@ __device__ __forceinline__ void dsm_load(const DsmParams& p, uint8_t* sm, uint32
             if (g >= 0 && g < words) cp_async4(flw + j, L.fluid + g);
             else flw[j] = 0u;
         }
-        for (int i = threadIdx.x; i < nh; i += blockDim.x) {
-            // padded index base + i + w lies in [0, cells + 2w) for rows -1 .. h
+        // 16-byte copies: base + w = y0 * w is a multiple of 32 floats and
+        // the arrays start 256-byte aligned; padded index base + i + w lies
+        // in [0, cells + 2w) for rows -1 .. h
+        for (int i = 4 * threadIdx.x; i < nh; i += 4 * blockDim.x) {
             const size_t g = size_t(base + i + L.w);
-            cp_async4(const_cast<float*>(v.diag) + i, L.diag + g);
-            cp_async4(const_cast<float*>(v.inv) + i, L.inv + g);
-            cp_async4(const_cast<float*>(v.px) + i, L.px + g);
-            cp_async4(const_cast<float*>(v.py) + i, L.py + g);
+            cp_async16(const_cast<float*>(v.diag) + i, L.diag + g);
+            cp_async16(const_cast<float*>(v.inv) + i, L.inv + g);
+            cp_async16(const_cast<float*>(v.px) + i, L.px + g);
+            cp_async16(const_cast<float*>(v.py) + i, L.py + g);
         }
         if (k == 0) {
             const int no = L.R * L.w;
-            for (int i = threadIdx.x; i < no; i += blockDim.x) {
+            for (int i = 4 * threadIdx.x; i < no; i += 4 * blockDim.x) {
                 const size_t g = size_t(v.lo + i + L.w);
-                cp_async4(v.res + i, L.res + g);
-                cp_async4(v.err + i, L.err + g);
+                cp_async16(v.res + i, L.res + g);
+                cp_async16(v.err + i, L.err + g);
             }
         }
     }
@@ -292,6 +296,9 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_vcycle_dsm(DsmParams p, Tai
     const uint32_t rank = cl.block_rank();
     uint8_t* dsm = smem + dsm_off;
     uint32_t* tail_sm = reinterpret_cast<uint32_t*>(smem);
+    // the first tail level's residual and error live in CTA 0's shared memory
+    float* tail_res = cl.map_shared_rank(reinterpret_cast<float*>(tail_sm) + tp.lv[0].o_res, 0);
+    const float* tail_err = cl.map_shared_rank(reinterpret_cast<float*>(tail_sm) + tp.lv[0].o_err, 0);
     if (rank == 0) cta_tail_issue_coeffs(tp, tail_sm);
     dsm_load(p, dsm, rank);
     cp_async_wait_all();
@@ -307,25 +314,25 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_vcycle_dsm(DsmParams p, Tai
         cl.sync();
         if (k + 1 < n) {
             const View c = view_of(p.lv[k + 1], dsm, rank);
-            dsm_restrict(f, cl, &c, p, rank, true);
+            dsm_restrict(f, cl, &c, p, tail_res, rank, true);
         } else {
-            dsm_restrict(f, cl, nullptr, p, rank, false);
+            dsm_restrict(f, cl, nullptr, p, tail_res, rank, false);
         }
         cl.sync();
     }
-    if (rank == 0) cta_tail(tp, tail_sm, false);
+    if (rank == 0) cta_tail(tp, tail_sm, false, false);
     cl.sync();
     for (int k = n - 1; k >= 0; --k) {
         const View f = view_of(p.lv[k], dsm, rank);
         if (k + 1 < n) {
             const View c = view_of(p.lv[k + 1], dsm, rank);
-            dsm_prolong(f, cl, &c, p, 1);
+            dsm_prolong(f, cl, &c, tail_err, 1);
             cl.sync();
-            dsm_prolong(f, cl, &c, p, 0);
+            dsm_prolong(f, cl, &c, tail_err, 0);
         } else {
-            dsm_prolong(f, cl, nullptr, p, 1);
+            dsm_prolong(f, cl, nullptr, tail_err, 1);
             cl.sync();
-            dsm_prolong(f, cl, nullptr, p, 0);
+            dsm_prolong(f, cl, nullptr, tail_err, 0);
         }
         cl.sync();  // the next (finer) level reads this one's final error
     }

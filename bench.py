@@ -259,26 +259,40 @@ def run_gpu_arm(args, world, rank, local):
     dev_s_max = dist_max(dev_s, world)
     value = world * n * args.steps / dev_s_max
 
-    # ---- e2e through the C-ABI with host buffers (pinned), copies inside the timed region
-    fu = torch.zeros(sim.field_shape(A.FIELDS["ext_force_u"])[0], dtype=torch.float32).pin_memory()
-    fv = torch.zeros(sim.field_shape(A.FIELDS["ext_force_v"])[0], dtype=torch.float32).pin_memory()
-    nc = sim.num_chunks
+    # ---- e2e through the C-ABI with host buffers (pinned), copies inside the
+    # timed region: a second scene from the same start, over the same updates
+    # (warm-up updates, then the timed ones), so e2e and value cover the same
+    # part of the flow
+    sim2 = A.Apic(args.side, args.side, 1.0 / args.side, props(A))
+    sim2.set_particles(px, py, vx, vy)
+    sim2.set_solver(mode, 1e-6, 500)
+    for opt in (A.OPT_PERSISTENT_SOLVE, A.OPT_FUSED_VCYCLE, A.OPT_CLUSTER_VCYCLE, A.OPT_PDL, A.OPT_DSM_VCYCLE):
+        v = sim.get_option(opt)
+        if sim2.get_option(opt) != v:
+            sim2.set_option(opt, v)
+    for _ in range(args.warmup):
+        sim2.update(opts, FRAME_DT)
+    fu = torch.zeros(sim2.field_shape(A.FIELDS["ext_force_u"])[0], dtype=torch.float32).pin_memory()
+    fv = torch.zeros(sim2.field_shape(A.FIELDS["ext_force_v"])[0], dtype=torch.float32).pin_memory()
+    nc = sim2.num_chunks
     pos_h = torch.empty(nc * 16, dtype=torch.float32).pin_memory()
     vel_h = torch.empty(nc * 16, dtype=torch.float32).pin_memory()
-    lib = sim._lib
-    e2e_steps = max(2, min(args.steps, 5))
+    lib = sim2._lib
+    e2e_steps = args.steps
     torch.cuda.synchronize()
+    dist_barrier(world)
     te = time.perf_counter()
     for _ in range(e2e_steps):
-        lib.apic_write_field(sim._h, A.FIELDS["ext_force_u"], fu.data_ptr(), fu.numel() * 4)
-        lib.apic_write_field(sim._h, A.FIELDS["ext_force_v"], fv.data_ptr(), fv.numel() * 4)
-        sim.update(opts, FRAME_DT)
-        lib.apic_read_vec2x8(sim._h, 0, A.ctypes.cast(pos_h.data_ptr(), A._FP), nc * 16)
-        lib.apic_read_vec2x8(sim._h, 1, A.ctypes.cast(vel_h.data_ptr(), A._FP), nc * 16)
+        lib.apic_write_field(sim2._h, A.FIELDS["ext_force_u"], fu.data_ptr(), fu.numel() * 4)
+        lib.apic_write_field(sim2._h, A.FIELDS["ext_force_v"], fv.data_ptr(), fv.numel() * 4)
+        sim2.update(opts, FRAME_DT)
+        lib.apic_read_vec2x8(sim2._h, 0, A.ctypes.cast(pos_h.data_ptr(), A._FP), nc * 16)
+        lib.apic_read_vec2x8(sim2._h, 1, A.ctypes.cast(vel_h.data_ptr(), A._FP), nc * 16)
     e2e_s = dist_max(time.perf_counter() - te, world)
     e2e_value = world * n * e2e_steps / e2e_s
     h2d = (fu.numel() + fv.numel()) * 4
     d2h = 2 * nc * 16 * 4
+    sim2.close()
 
     # ---- per-stage device times (events around each stage) for the roofline
     sim.set_profiling(True)
@@ -333,7 +347,8 @@ def run_gpu_arm(args, world, rank, local):
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps,
                     "what": "apic_write_field(ext force u,v) from pinned host + apic_update + "
-                            "apic_read_vec2x8(positions, velocities) to pinned host"},
+                            "apic_read_vec2x8(positions, velocities) to pinned host, wall clock, on a second "
+                            "scene over the same updates as the timed region"},
             "gpu_launches": launches if not args.eager else None,
             "roofline": roof,
             "stage_ms_per_step": {k: v[0] / prof_steps for k, v in stages.items() if v[1]},

@@ -491,3 +491,22 @@ def test_dsm_vcycle_equals_global(gpu_lib, side):
         pa, pb = sims[0].read_field("pressure"), sims[1].read_field("pressure")
         scale = float(np.max(np.abs(pa))) or 1.0
         assert float(np.max(np.abs(pa - pb))) <= 1e-3 * scale
+
+
+def test_read_vec2x8_layout(gpu_lib):
+    """apic_read_vec2x8 returns the reference's Vec2x8 chunks (8 x lanes, then 8 y lanes) of every field pair."""
+    side = 64
+    g = A.Apic(side, side, 1 / side, A.WorldProperties(-9.81, 0.1, 5.0, 1e-5))
+    rng = np.random.default_rng(7)
+    n = 1001  # ragged last chunk
+    px = rng.uniform(0.1, 0.9, n).astype(np.float32)
+    py = rng.uniform(0.1, 0.9, n).astype(np.float32)
+    g.set_particles(px, py, rng.normal(size=n).astype(np.float32), rng.normal(size=n).astype(np.float32))
+    g.update(A.DebugOptions(), 1 / 480)
+    pairs = [("pos_x", "pos_y"), ("vel_x", "vel_y"), ("cu_x", "cu_y"), ("cv_x", "cv_y")]
+    for which, (fx, fy) in enumerate(pairs):
+        out = g.read_vec2x8(which)
+        x, y = g.read_field(fx), g.read_field(fy)
+        chunks = out.reshape(-1, 16)
+        eq(chunks[:, :8].ravel(), x, f"Vec2x8 x lanes ({fx})")
+        eq(chunks[:, 8:].ravel(), y, f"Vec2x8 y lanes ({fy})")
