@@ -28,9 +28,12 @@
 namespace apic {
 
 constexpr int kMaxLevels = 20;        // base + coarse levels
-constexpr int kSegBlock = 256;        // threads per block of segment kernels
+#ifndef APIC_SEG_BLOCK
+#define APIC_SEG_BLOCK 256
+#endif
+constexpr int kSegBlock = APIC_SEG_BLOCK;  // threads per block of segment kernels
 constexpr int kSegWarps = kSegBlock / 32;
-constexpr int kMaxRedBlocks = 1216;   // 152 SMs x 8: grid of reduction kernels
+constexpr int kMaxRedBlocks = 152 * (2048 / kSegBlock);  // one full wave on 152 SMs: grid of reduction kernels
 constexpr int kSortTile = 2048;       // keys per block in the radix sort
 constexpr int kSortThreads = 256;
 

@@ -250,9 +250,9 @@ __device__ __forceinline__ void dsm_prolong(const View& f, const cg::cluster_gro
     }
 }
 
-// Copy this CTA's rows (plus halo) of every distributed level into shared
-// memory; the first level also brings its residual and first red sweep.
-__device__ __forceinline__ void dsm_load(const DsmParams& p, uint8_t* sm, uint32_t rank) {
+// Start copying this CTA's rows (plus halo) of every distributed level's mask
+// and coefficients into shared memory (they do not change during a solve).
+__device__ __forceinline__ void dsm_load_coeffs(const DsmParams& p, uint8_t* sm, uint32_t rank) {
     for (int k = 0; k < p.n; ++k) {
         const DsmLevel& L = p.lv[k];
         const View v = view_of(L, sm, rank);
@@ -276,21 +276,24 @@ __device__ __forceinline__ void dsm_load(const DsmParams& p, uint8_t* sm, uint32
             cp_async16(const_cast<float*>(v.px) + i, L.px + g);
             cp_async16(const_cast<float*>(v.py) + i, L.py + g);
         }
-        if (k == 0) {
-            const int no = L.R * L.w;
-            for (int i = 4 * threadIdx.x; i < no; i += 4 * blockDim.x) {
-                const size_t g = size_t(v.lo + i + L.w);
-                cp_async16(v.res + i, L.res + g);
-                cp_async16(v.err + i, L.err + g);
-            }
-        }
+    }
+}
+
+// Start copying the first level's residual and first red sweep (written by
+// the kernel before this one).
+__device__ __forceinline__ void dsm_load_first(const DsmParams& p, uint8_t* sm, uint32_t rank) {
+    const DsmLevel& L = p.lv[0];
+    const View v = view_of(L, sm, rank);
+    const int no = L.R * L.w;
+    for (int i = 4 * threadIdx.x; i < no; i += 4 * blockDim.x) {
+        const size_t g = size_t(v.lo + i + L.w);
+        cp_async16(v.res + i, L.res + g);
+        cp_async16(v.err + i, L.err + g);
     }
 }
 
 __global__ void __launch_bounds__(kTailThreads, 1) k_vcycle_dsm(DsmParams p, TailParams tp, uint32_t dsm_off,
                                                                const Ctl* ctl) {
-    pdl_wait();
-    if (ctl->pcg_done) return;  // the same value in every CTA: all reach every barrier
     extern __shared__ __align__(16) uint8_t smem[];
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t rank = cl.block_rank();
@@ -299,8 +302,16 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_vcycle_dsm(DsmParams p, Tai
     // the first tail level's residual and error live in CTA 0's shared memory
     float* tail_res = cl.map_shared_rank(reinterpret_cast<float*>(tail_sm) + tp.lv[0].o_res, 0);
     const float* tail_err = cl.map_shared_rank(reinterpret_cast<float*>(tail_sm) + tp.lv[0].o_err, 0);
+    // masks and coefficients were written by the multigrid setup, before the
+    // solve: their copies start while the previous kernel drains
     if (rank == 0) cta_tail_issue_coeffs(tp, tail_sm);
-    dsm_load(p, dsm, rank);
+    dsm_load_coeffs(p, dsm, rank);
+    pdl_wait();
+    if (ctl->pcg_done) {  // the same value in every CTA: all reach every barrier
+        cp_async_wait_all();
+        return;
+    }
+    dsm_load_first(p, dsm, rank);
     cp_async_wait_all();
     __syncthreads();
     cl.sync();
