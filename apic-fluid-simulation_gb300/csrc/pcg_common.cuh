@@ -24,10 +24,15 @@ namespace pcg {
 // without waiting for the mask word, so its loads issue at once, and tests
 // fluid_ before it stores or accumulates.  All reads of a cell in [0, cells)
 // and of its neighbours stay inside the padded arrays.
-#define APIC_BASE_ALL(B, nseg, warp, nwarps)                                                    \
-    const uint32_t lane_ = threadIdx.x & 31;                                                    \
-    for (uint32_t s_ = (warp); s_ < (nseg); s_ += (nwarps))                                     \
-        if (const uint32_t word_ = (B).seg[s_], raw_ = word_ * 32 + lane_; raw_ < (B).cells)    \
+#define APIC_BASE_ALL(B, nseg, warp, nwarps) APIC_BASE_ALL_W0(B, nseg, warp, nwarps, 0xFFFFFFFFu)
+// w0: the warp's first segment word when the caller loaded it early (before
+// waiting on the previous kernel), else 0xFFFFFFFF.
+#define APIC_BASE_ALL_W0(B, nseg, warp, nwarps, w0)                                                  \
+    const uint32_t lane_ = threadIdx.x & 31;                                                         \
+    for (uint32_t s_ = (warp); s_ < (nseg); s_ += (nwarps))                                          \
+        if (const uint32_t word_ = (s_ == (warp) && (w0) != 0xFFFFFFFFu) ? (w0) : (B).seg[s_],       \
+            raw_ = word_ * 32 + lane_;                                                               \
+            raw_ < (B).cells)                                                                        \
             if (const bool fluid_ = (((B).fluid[word_] >> lane_) & 1u) != 0u; true)
 
 // pressure = 0 at fluid cells (src/apic.rs:1872-1883).
@@ -115,11 +120,12 @@ __device__ __forceinline__ float search_at(const float* z, const float* s, float
 
 // Ap' = A s' (the FMA chain of :1833-1846); returns s'.Ap'.
 __device__ __forceinline__ F2 ph_spmv_search(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
-                                             const float* s, float beta, bool beta_valid, float* ap) {
+                                             const float* s, float beta, bool beta_valid, float* ap,
+                                             uint32_t w0 = 0xFFFFFFFFu) {
     F2 acc{0.0f, 0.0f};
     const long long W = B.w;
     const float* z = B.err;
-    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+    APIC_BASE_ALL_W0(B, nseg, warp, nwarps, w0) {
         const long long raw = raw_;
         const uint32_t c = raw_ + B.w;
         const bool fr = fluid_raw(B.fluid, raw + 1, B.cells), fl = fluid_raw(B.fluid, raw - 1, B.cells);
@@ -151,11 +157,12 @@ __device__ __forceinline__ F2 ph_spmv_search(const Level& B, uint32_t nseg, uint
 // :487-507 with every neighbour still zero).  Returns max|r| and sum r^2.
 __device__ __forceinline__ void ph_update_search(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
                                                  float alpha, float beta, bool beta_valid, float* x, int x_padded,
-                                                 float* s, const float* ap, float* max_r, F2* r2) {
+                                                 float* s, const float* ap, float* max_r, F2* r2,
+                                                 uint32_t w0 = 0xFFFFFFFFu) {
     constexpr float kOmegaSor = 1.2f;
     float mx = 0.0f;
     F2 acc{0.0f, 0.0f};
-    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+    APIC_BASE_ALL_W0(B, nseg, warp, nwarps, w0) {
         const uint32_t c = raw_ + B.w;
         const uint32_t xi = x_padded ? c : raw_;
         const float sc = search_at(B.err, s, beta, beta_valid, c);

@@ -73,9 +73,13 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl*
 // src/apic.rs:1823-1863; the search update :1945-1954 is folded in).
 __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s, float* ap, Ctl* ctl, double* partials,
                                                         int mode) {
+    // the base segment list is written by the substep's setup: load this
+    // warp's first word before waiting on the previous kernel
+    const uint32_t nseg = ctl->seg_count[0];
+    const uint32_t w0 = gwarp() < nseg ? B.seg[gwarp()] : 0xFFFFFFFFu;
     pdl_wait();
     if (ctl->pcg_done) return;
-    F2 acc = pcg::ph_spmv_search(B, ctl->seg_count[0], gwarp(), gnwarps(), s, ctl->beta, ctl->beta_valid != 0, ap);
+    F2 acc = pcg::ph_spmv_search(B, nseg, gwarp(), gnwarps(), s, ctl->beta, ctl->beta_valid != 0, ap, w0);
     double tot;
     if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
         float delta = float(tot);
@@ -92,12 +96,14 @@ __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s,
 __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int p_padded, float* s,
                                                           const float* ap, Ctl* ctl, double* partials, int mode,
                                                           float solve_error) {
+    const uint32_t nseg = ctl->seg_count[0];
+    const uint32_t w0 = gwarp() < nseg ? B.seg[gwarp()] : 0xFFFFFFFFu;
     pdl_wait();
     if (ctl->pcg_done) return;
     float mx;
     F2 acc;
-    pcg::ph_update_search(B, ctl->seg_count[0], gwarp(), gnwarps(), ctl->alpha, ctl->beta, ctl->beta_valid != 0, p,
-                          p_padded, s, ap, &mx, &acc);
+    pcg::ph_update_search(B, nseg, gwarp(), gnwarps(), ctl->alpha, ctl->beta, ctl->beta_valid != 0, p, p_padded, s,
+                          ap, &mx, &acc, w0);
     if (mode == APIC_SOLVER_REFERENCE) {
         float t;
         if (block_max_last<kSegBlock>(mx, partials, &ctl->red_counter, &t) && threadIdx.x == 0) {

@@ -44,32 +44,48 @@ namespace {
 __device__ __forceinline__ uint32_t gwarp() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
 __device__ __forceinline__ uint32_t gnwarps() { return (gridDim.x * blockDim.x) >> 5; }
 
+// Segment lists and their lengths are written by the multigrid setup, never
+// by the kernel just before: each warp loads its first segment word before
+// waiting on that kernel (programmatic dependent launch).
+__device__ __forceinline__ uint32_t early_word(const uint32_t* seg, uint32_t nseg) {
+    const uint32_t s = gwarp();
+    return s < nseg ? seg[s] : kNoWord;
+}
+
 __global__ void __launch_bounds__(kSegBlock) k_smooth(Level L, int li, const Ctl* ctl, int color, int init) {
+    const uint32_t nseg = ctl->seg_count[li];
+    const uint32_t w0 = early_word(L.seg, nseg);
     pdl_wait();
     if (ctl->pcg_done) return;
-    ph_smooth(L, ctl->seg_count[li], gwarp(), gnwarps(), color, init);
+    ph_smooth(L, nseg, gwarp(), gnwarps(), color, init, w0);
 }
 
 // Restriction only (into the first tail level or the coarsest level).
 __global__ void __launch_bounds__(kSegBlock) k_restrict(Level f, Level c, int lc, const Ctl* ctl) {
+    const uint32_t nseg = ctl->seg_count[lc];
+    const uint32_t w0 = early_word(c.seg, nseg);
     pdl_wait();
     if (ctl->pcg_done) return;
-    ph_restrict(f, c, ctl->seg_count[lc], gwarp(), gnwarps(), false);
+    ph_restrict(f, c, nseg, gwarp(), gnwarps(), false, w0);
 }
 
 // Restriction fused with the coarse level's first (red) sweep.
 __global__ void __launch_bounds__(kSegBlock) k_restrict_red(Level f, Level c, int lc, const Ctl* ctl) {
+    const uint32_t nseg = ctl->seg_count[lc];
+    const uint32_t w0 = early_word(c.seg, nseg);
     pdl_wait();
     if (ctl->pcg_done) return;
-    ph_restrict(f, c, ctl->seg_count[lc], gwarp(), gnwarps(), true);
+    ph_restrict(f, c, nseg, gwarp(), gnwarps(), true, w0);
 }
 
 // Prolongation fused with the black sweep.
 __global__ void __launch_bounds__(kSegBlock) k_prolong_black(Level c, Level f, int lf, const Ctl* ctl, int base) {
+    const uint32_t nseg = ctl->seg_count[lf];
+    const uint32_t w0 = early_word(f.seg, nseg);
+    const uint32_t last = base ? ctl->last_fluid : 0xFFFFFFFFu, extra = base ? ctl->pad_count : 0u;
     pdl_wait();
     if (ctl->pcg_done) return;
-    ph_prolong(c, f, ctl->seg_count[lf], gwarp(), gnwarps(), 1, base ? ctl->last_fluid : 0xFFFFFFFFu,
-               base ? ctl->pad_count : 0u);
+    ph_prolong(c, f, nseg, gwarp(), gnwarps(), 1, last, extra, w0);
 }
 
 // Base-level prolongation fused with the final red sweep, which also reduces
@@ -77,9 +93,12 @@ __global__ void __launch_bounds__(kSegBlock) k_prolong_black(Level c, Level f, i
 // finishes the PCG iteration (k_dot_rz's work).
 __global__ void __launch_bounds__(kSegBlock) k_prolong_red_rz(Level c, Level B, Ctl* ctl, double* partials,
                                                               int mode) {
+    const uint32_t nseg = ctl->seg_count[0];
+    const uint32_t w0 = early_word(B.seg, nseg);
+    const uint32_t last = ctl->last_fluid, extra = ctl->pad_count;
     pdl_wait();
     if (ctl->pcg_done) return;
-    const F2 acc = ph_prolong_red_rz(c, B, ctl->seg_count[0], gwarp(), gnwarps(), ctl->last_fluid, ctl->pad_count);
+    const F2 acc = ph_prolong_red_rz(c, B, nseg, gwarp(), gnwarps(), last, extra, w0);
     double tot;
     if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0)
         pcg::finish_rz(ctl, tot, mode);
@@ -87,10 +106,12 @@ __global__ void __launch_bounds__(kSegBlock) k_prolong_red_rz(Level c, Level B, 
 
 // Prolongation fused with the final red sweep (black neighbours are final).
 __global__ void __launch_bounds__(kSegBlock) k_prolong_red(Level c, Level f, int lf, const Ctl* ctl, int base) {
+    const uint32_t nseg = ctl->seg_count[lf];
+    const uint32_t w0 = early_word(f.seg, nseg);
+    const uint32_t last = base ? ctl->last_fluid : 0xFFFFFFFFu, extra = base ? ctl->pad_count : 0u;
     pdl_wait();
     if (ctl->pcg_done) return;
-    ph_prolong(c, f, ctl->seg_count[lf], gwarp(), gnwarps(), 0, base ? ctl->last_fluid : 0xFFFFFFFFu,
-               base ? ctl->pad_count : 0u);
+    ph_prolong(c, f, nseg, gwarp(), gnwarps(), 0, last, extra, w0);
 }
 
 // Fused descent: finish fine level's pre-smoothing, restrict, coarse red sweep.

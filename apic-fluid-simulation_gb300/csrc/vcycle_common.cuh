@@ -14,6 +14,8 @@ namespace apic {
 namespace vc {
 
 constexpr float kOmega = 1.2f;
+// "no preloaded segment word" (phases load seg[warp] themselves)
+constexpr uint32_t kNoWord = 0xFFFFFFFFu;
 constexpr int kTailThreads = 1024;
 constexpr size_t kTailSmemBudget = 200 * 1024;
 
@@ -357,12 +359,14 @@ __device__ __forceinline__ void cta_sweep(const SmemLevel& L, int color, int ini
 // One colour sweep; init: first sweep after the level's error was zero-filled.
 // Every lane of the colour computes (its loads do not wait for the mask word)
 // and only fluid cells store.
+// w0: this warp's first segment word if the caller loaded it early
+// (before waiting on the previous kernel), else kNoWord.
 __device__ __forceinline__ void ph_smooth(const Level& L, uint32_t nseg, uint32_t warp, uint32_t nwarps, int color,
-                                          int init) {
+                                          int init, uint32_t w0 = kNoWord) {
     const uint32_t lane = threadIdx.x & 31;
     const float* e = L.err;
     for (uint32_t s = warp; s < nseg; s += nwarps) {
-        const uint32_t word = L.seg[s];
+        const uint32_t word = (s == warp && w0 != kNoWord) ? w0 : L.seg[s];
         const uint32_t raw = word * 32 + lane;
         if (raw >= L.cells || int(!is_red(raw, L.w)) != color) continue;
         const bool fluid = (L.fluid[word] >> lane) & 1u;
@@ -376,10 +380,10 @@ __device__ __forceinline__ void ph_smooth(const Level& L, uint32_t nseg, uint32_
 
 // Restriction into coarse level c; with_red also runs c's first (red) sweep.
 __device__ __forceinline__ void ph_restrict(const Level& f, const Level& c, uint32_t nseg_c, uint32_t warp,
-                                            uint32_t nwarps, bool with_red) {
+                                            uint32_t nwarps, bool with_red, uint32_t w0 = kNoWord) {
     const uint32_t lane = threadIdx.x & 31;
     for (uint32_t s = warp; s < nseg_c; s += nwarps) {
-        const uint32_t word = c.seg[s];
+        const uint32_t word = (s == warp && w0 != kNoWord) ? w0 : c.seg[s];
         const uint32_t rc = word * 32 + lane;
         if (rc >= c.cells) continue;
         const bool fluid = (c.fluid[word] >> lane) & 1u;
@@ -397,7 +401,8 @@ __device__ __forceinline__ void ph_restrict(const Level& f, const Level& c, uint
 // reads red neighbours as prolonged values, red (0) reads final black ones.
 // last / extra: the base level's duplicated last fluid cell (else ~0u / 0).
 __device__ __forceinline__ void ph_prolong(const Level& c, const Level& f, uint32_t nseg_f, uint32_t warp,
-                                           uint32_t nwarps, int color, uint32_t last, uint32_t extra) {
+                                           uint32_t nwarps, int color, uint32_t last, uint32_t extra,
+                                           uint32_t w0 = kNoWord) {
     const uint32_t lane = threadIdx.x & 31;
     const float* fe = f.err;
     const float* ce = c.err;
@@ -410,7 +415,7 @@ __device__ __forceinline__ void ph_prolong(const Level& c, const Level& f, uint3
         return ce[((r / fw) / 2) * cw + (r % fw) / 2 + cw];
     };
     for (uint32_t s = warp; s < nseg_f; s += nwarps) {
-        const uint32_t word = f.seg[s];
+        const uint32_t word = (s == warp && w0 != kNoWord) ? w0 : f.seg[s];
         const uint32_t raw = word * 32 + lane;
         if (raw >= f.cells || int(!is_red(raw, fw)) != color) continue;
         const bool fluid = (f.fluid[word] >> lane) & 1u;
@@ -433,14 +438,15 @@ __device__ __forceinline__ void ph_prolong(const Level& c, const Level& f, uint3
 // of r.z over every fluid cell: red cells' new z, black cells' z as the
 // black pass left it (final).  The products are those of pcg::ph_rz.
 __device__ __forceinline__ F2 ph_prolong_red_rz(const Level& c, const Level& f, uint32_t nseg_f, uint32_t warp,
-                                                uint32_t nwarps, uint32_t last, uint32_t extra) {
+                                                uint32_t nwarps, uint32_t last, uint32_t extra,
+                                                uint32_t w0 = kNoWord) {
     const uint32_t lane = threadIdx.x & 31;
     const float* fe = f.err;
     const float* ce = c.err;
     const uint32_t fw = f.w, cw = c.w;
     F2 acc{0.0f, 0.0f};
     for (uint32_t s = warp; s < nseg_f; s += nwarps) {
-        const uint32_t word = f.seg[s];
+        const uint32_t word = (s == warp && w0 != kNoWord) ? w0 : f.seg[s];
         const uint32_t raw = word * 32 + lane;
         if (raw >= f.cells) continue;
         const bool fluid = (f.fluid[word] >> lane) & 1u;
