@@ -82,6 +82,30 @@ class SceneParamsC(ctypes.Structure):
                 ("vel_sigma", ctypes.c_float)]
 
 
+class ServerRoundC(ctypes.Structure):
+    _fields_ = [("admitted", ctypes.c_uint32), ("stepped", ctypes.c_uint32), ("completed", ctypes.c_uint32),
+                ("active", ctypes.c_uint32), ("queued", ctypes.c_uint32), ("round_ms", ctypes.c_double),
+                ("memory_used", ctypes.c_uint64)]
+
+
+class RequestInfoC(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("finished", ctypes.c_uint32), ("steps_done", ctypes.c_uint32),
+                ("particles", ctypes.c_uint64), ("substeps", ctypes.c_uint64), ("pcg_iterations", ctypes.c_uint64),
+                ("max_true_residual", ctypes.c_double), ("submit_ms", ctypes.c_double),
+                ("admit_ms", ctypes.c_double), ("done_ms", ctypes.c_double), ("bytes", ctypes.c_uint64),
+                ("result_floats", ctypes.c_uint64)]
+
+
+class ServerStatsC(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("active", ctypes.c_uint64), ("queued", ctypes.c_uint64), ("rounds", ctypes.c_uint64),
+                ("particle_substeps", ctypes.c_uint64), ("particle_updates", ctypes.c_uint64),
+                ("busy_ms", ctypes.c_double), ("elapsed_ms", ctypes.c_double),
+                ("step_p50_ms", ctypes.c_double), ("step_p99_ms", ctypes.c_double),
+                ("request_p50_ms", ctypes.c_double), ("request_p99_ms", ctypes.c_double),
+                ("memory_used", ctypes.c_uint64), ("memory_peak", ctypes.c_uint64)]
+
+
 # Every symbol that include/apic_gpu.h declares, with its ctypes signature.
 _VP = ctypes.c_void_p
 _FP = ctypes.POINTER(ctypes.c_float)
@@ -119,6 +143,19 @@ SIGNATURES = {
     "apic_morton_sort_noalloc": (ctypes.c_int, [_VP, _VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                                 ctypes.c_float, _VP, _VP, _VP]),
     "apic_debug_finish_substep": (ctypes.c_int, [_VP, ctypes.c_float]),
+    "apic_update_batch": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
+                                         ctypes.POINTER(ctypes.c_int)]),
+    "apic_scene_bytes": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
+                                        ctypes.POINTER(ctypes.c_uint64)]),
+    "apic_server_create": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_VP)]),
+    "apic_server_destroy": (ctypes.c_int, [_VP]),
+    "apic_server_submit": (ctypes.c_int, [_VP, ctypes.POINTER(SceneParamsC), ctypes.POINTER(WorldPropsC),
+                                          ctypes.c_uint32, ctypes.c_float, ctypes.c_int, ctypes.c_float,
+                                          ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]),
+    "apic_server_step": (ctypes.c_int, [_VP, ctypes.POINTER(ServerRoundC)]),
+    "apic_server_request": (ctypes.c_int, [_VP, ctypes.c_uint64, ctypes.POINTER(RequestInfoC)]),
+    "apic_server_result_positions": (ctypes.c_int, [_VP, ctypes.c_uint64, _FP, ctypes.c_uint64]),
+    "apic_server_get_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ServerStatsC)]),
 }
 
 _lib = None
@@ -384,3 +421,74 @@ class Apic:
 
     def finish_substep(self, dt: float) -> None:
         _check(self._lib.apic_debug_finish_substep(self._h, dt), "apic_debug_finish_substep")
+
+
+# ---- batched and served scenes (no counterpart in the reference) -------------
+
+def update_batch(sims, debug_options: DebugOptions | None = None, frame_deltatime: float = 1 / 60) -> list[int]:
+    """One update of every scene in `sims`, enqueued side by side (apic_update_batch)."""
+    lib = load_library()
+    flags = UPDATE_DISABLE_SORT if (debug_options is not None and debug_options.disable_particle_sort) else 0
+    arr = (_VP * len(sims))(*[s._h for s in sims])
+    status = (ctypes.c_int * len(sims))()
+    _check(lib.apic_update_batch(arr, len(sims), flags, frame_deltatime, status), "apic_update_batch")
+    return list(status)
+
+
+def scene_bytes(width: int, height: int, particles: int) -> int:
+    out = ctypes.c_uint64(0)
+    _check(load_library().apic_scene_bytes(width, height, particles, ctypes.byref(out)), "apic_scene_bytes")
+    return out.value
+
+
+class Server:
+    """Continuous-batching request loop over independent scenes (apic_server_*)."""
+
+    def __init__(self, memory_budget_bytes: int, max_active: int, keep_results: bool = False):
+        self._lib = load_library()
+        h = _VP()
+        _check(self._lib.apic_server_create(memory_budget_bytes, max_active, 1 if keep_results else 0,
+                                            ctypes.byref(h)), "apic_server_create")
+        self._h = h
+
+    def submit(self, scene: SceneParamsC, props: WorldProperties, steps: int, frame_deltatime: float,
+               solver: int = SOLVER_REL_MIXED, rel_tol: float = 1e-6, max_iterations: int = 500) -> int:
+        wp = WorldPropsC(props.gravity, props.border_damping, props.cfl, props.solve_error)
+        out = ctypes.c_uint64(0)
+        _check(self._lib.apic_server_submit(self._h, ctypes.byref(scene), ctypes.byref(wp), steps, frame_deltatime,
+                                            solver, rel_tol, max_iterations, ctypes.byref(out)),
+               "apic_server_submit")
+        return out.value
+
+    def step(self) -> ServerRoundC:
+        rd = ServerRoundC()
+        _check(self._lib.apic_server_step(self._h, ctypes.byref(rd)), "apic_server_step")
+        return rd
+
+    def request(self, rid: int) -> RequestInfoC:
+        info = RequestInfoC()
+        _check(self._lib.apic_server_request(self._h, rid, ctypes.byref(info)), "apic_server_request")
+        return info
+
+    def result_positions(self, rid: int) -> np.ndarray:
+        info = self.request(rid)
+        out = np.zeros(info.result_floats, np.float32)
+        _check(self._lib.apic_server_result_positions(self._h, rid, _fptr(out), out.size),
+               "apic_server_result_positions")
+        return out.reshape(-1, 2, 8)
+
+    def stats(self) -> ServerStatsC:
+        st = ServerStatsC()
+        _check(self._lib.apic_server_get_stats(self._h, ctypes.byref(st)), "apic_server_get_stats")
+        return st
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.apic_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

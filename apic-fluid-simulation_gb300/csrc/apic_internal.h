@@ -257,6 +257,13 @@ bool enqueue_vcycle(Scene& s, bool base_red_done = false, int rz_mode = -1);
 cudaError_t launch_plan_first(Scene& s);
 cudaError_t launch_advance(Scene& s);
 
+// runtime.cu: Apic::update split in two, so several scenes can be enqueued
+// before any is waited on (apic_update_batch, the request server)
+int update_launch(apic_handle* h, uint32_t flags, float frame_dt);
+int create_scene(uint32_t width, uint32_t height, float cell_size, const apic_world_props* props,
+                 bool default_particles, apic_handle** out);
+int update_finish(apic_handle* h);
+
 // helpers shared by the launchers
 inline uint32_t div_up(uint64_t a, uint64_t b) { return uint32_t((a + b - 1) / b); }
 

@@ -456,6 +456,16 @@ int apic_device_count(int* n_out) {
 }
 
 int apic_create(uint32_t width, uint32_t height, float cell_size, const apic_world_props* props, apic_handle** out) {
+    return apic::create_scene(width, height, cell_size, props, true, out);
+}
+
+}  // extern "C"
+
+// Apic::new; default_particles false leaves the scene empty (callers that
+// set their own particles next, such as the request server, then never hold
+// the default block's memory).
+int apic::create_scene(uint32_t width, uint32_t height, float cell_size, const apic_world_props* props,
+                       bool default_particles, apic_handle** out) {
     if (!out || !props) return fail(APIC_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
     if (width == 0 || height == 0 || !(cell_size > 0.0f) || !std::isfinite(cell_size))
@@ -469,7 +479,7 @@ int apic_create(uint32_t width, uint32_t height, float cell_size, const apic_wor
     for (uint32_t y = 0; y < height; ++y)
         for (uint32_t x = 0; x < width; ++x) {
             bool border = x == 0 || x == width - 1 || y == 0 || y == height - 1;
-            if (!border && x > 4 && x < width - 4 && y > 4 && y < height / 2)
+            if (default_particles && !border && x > 4 && x < width - 4 && y > 4 && y < height / 2)
                 for (int py = 0; py < 3; ++py)
                     for (int px = 0; px < 3; ++px) {
                         ix.push_back((float(x) + (float(px) + 0.5f) / 3.0f) * cell_size);
@@ -568,6 +578,8 @@ int apic_create(uint32_t width, uint32_t height, float cell_size, const apic_wor
     return APIC_OK;
 }
 
+extern "C" {
+
 int apic_destroy(apic_handle* h) {
     if (!h) return APIC_OK;
     if (h->s.stream) cudaStreamSynchronize(h->s.stream);
@@ -602,7 +614,14 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
     return APIC_OK;
 }
 
-int apic_update(apic_handle* h, uint32_t flags, float frame_dt) {
+}  // extern "C"
+
+namespace apic {
+
+// First half of Apic::update: everything up to the copy of the control block
+// back to the host is enqueued on the scene's stream; nothing waits (except
+// in profiling mode, whose host-driven loop reads the device state).
+int update_launch(apic_handle* h, uint32_t flags, float frame_dt) {
     if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
     Scene& s = h->s;
     if (!std::isfinite(frame_dt)) return fail(APIC_ERR_INVALID_ARG, "frame_deltatime must be finite");
@@ -631,8 +650,14 @@ int apic_update(apic_handle* h, uint32_t flags, float frame_dt) {
     if (s.has_ext) { CK(cudaMemsetAsync(s.ext_u, 0, sizeof(float) * s.uf, st)); CK(cudaMemsetAsync(s.ext_v, 0, sizeof(float) * s.vf, st)); }
     if (s.has_post) { CK(cudaMemsetAsync(s.post_u, 0, sizeof(float) * s.uf, st)); CK(cudaMemsetAsync(s.post_v, 0, sizeof(float) * s.vf, st)); }
     s.has_ext = s.has_post = false;
-    int rc = sync_ctl(s);
-    if (rc != APIC_OK) return rc;
+    CK(cudaMemcpyAsync(s.ctl_host, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    return APIC_OK;
+}
+
+// Second half: wait for the scene's stream and publish the step statistics.
+int update_finish(apic_handle* h) {
+    Scene& s = h->s;
+    CK(cudaStreamSynchronize(s.stream));
     const Ctl& c = *s.ctl_host;
     s.stats.substeps = c.substeps;
     s.stats.pcg_iterations = c.pcg_iters;
@@ -649,6 +674,38 @@ int apic_update(apic_handle* h, uint32_t flags, float frame_dt) {
                                   uint64_t(c.pcg_iters_total) * s.kn_pcg + uint64_t(c.refinements_total) * s.kn_refine;
     if (c.status & kStatusTimeout) return fail(APIC_ERR_TIMEOUT, "a bounded device wait gave up (persistent solver barrier)");
     if (c.status & kStatusBadStep) return fail(APIC_ERR_NONFINITE, "substep size is not positive (non-finite velocities)");
+    return APIC_OK;
+}
+
+}  // namespace apic
+
+extern "C" {
+
+int apic_update(apic_handle* h, uint32_t flags, float frame_dt) {
+    int rc = update_launch(h, flags, frame_dt);
+    if (rc != APIC_OK) return rc;
+    return update_finish(h);
+}
+
+int apic_update_batch(apic_handle* const* handles, uint32_t count, uint32_t flags, float frame_dt, int* status) {
+    if (count && !handles) return fail(APIC_ERR_INVALID_ARG, "null handle array");
+    for (uint32_t i = 0; i < count; ++i)
+        if (valid_handle(handles[i])) return fail(APIC_ERR_INVALID_ARG, "invalid handle in batch");
+    // every scene's update is enqueued on its own stream before any is waited
+    // on, so the GPU runs the scenes' kernels side by side
+    std::vector<int> rc(count, APIC_OK);
+    for (uint32_t i = 0; i < count; ++i) rc[i] = update_launch(handles[i], flags, frame_dt);
+    int first = APIC_OK;
+    std::string first_msg;
+    for (uint32_t i = 0; i < count; ++i) {
+        if (rc[i] == APIC_OK) rc[i] = update_finish(handles[i]);
+        if (status) status[i] = rc[i];
+        if (rc[i] != APIC_OK && first == APIC_OK) {
+            first = rc[i];
+            first_msg = apic_last_error();
+        }
+    }
+    if (first != APIC_OK) return fail(first, "apic_update_batch: " + first_msg);
     return APIC_OK;
 }
 

@@ -273,6 +273,62 @@ int apic_get_stream(apic_handle* h, void** stream_out);
 int apic_morton_sort_noalloc(const float* pos_x, const float* pos_y, uint32_t n, uint32_t width, uint32_t height,
                              float cell_size, uint32_t* keys_out, uint32_t* vals_out, void* stream);
 
+/* ---- batched and served scenes ------------------------------------------ */
+/* No counterpart in the reference, which simulates one scene per process.
+ * One Apic::update of each of `count` scenes: every update is enqueued on its
+ * scene's own stream before any is waited on, so the GPU runs the scenes'
+ * kernels side by side (a small scene alone leaves most SMs idle).  Each
+ * scene computes exactly what apic_update computes for it.  status (may be
+ * NULL): per-scene result; the return value is the first failure. */
+int apic_update_batch(apic_handle* const* handles, uint32_t count, uint32_t flags, float frame_deltatime,
+                      int* status);
+
+/* Estimated device bytes of a scene (upper bound used for admission). */
+int apic_scene_bytes(uint32_t width, uint32_t height, uint64_t particles, uint64_t* bytes_out);
+
+/* Continuous-batching request server: requests (scene, step count, dt) are
+ * queued on submission; each apic_server_step admits queued requests in
+ * arrival order while the active set is below max_active and their
+ * estimated memory fits memory_budget_bytes, runs one update of every
+ * active scene (as apic_update_batch), and retires scenes that reached their
+ * step count.  State stays on the device between rounds.  keep_results: copy
+ * each finished scene's positions (Vec2x8 layout) to the host before its
+ * device memory is released. */
+typedef struct apic_server apic_server;
+typedef struct apic_server_round {
+    uint32_t admitted, stepped, completed, active, queued;
+    double   round_ms;       /* wall time of this round's updates */
+    uint64_t memory_used;    /* estimated bytes of the active scenes */
+} apic_server_round;
+typedef struct apic_request_info {
+    int      status;         /* APIC_OK, or why the request failed */
+    uint32_t finished;
+    uint32_t steps_done;
+    uint64_t particles, substeps, pcg_iterations;
+    double   max_true_residual;           /* over its updates (mixed / FP32 relative modes) */
+    double   submit_ms, admit_ms, done_ms; /* since server creation; -1 when not yet */
+    uint64_t bytes;          /* admission estimate */
+    uint64_t result_floats;  /* kept positions (0: none) */
+} apic_request_info;
+typedef struct apic_server_stats {
+    uint64_t submitted, completed, failed, active, queued, rounds;
+    uint64_t particle_substeps, particle_updates;
+    double   busy_ms, elapsed_ms;
+    double   step_p50_ms, step_p99_ms;        /* per scene-step: its round's wall time */
+    double   request_p50_ms, request_p99_ms;  /* completion minus submission */
+    uint64_t memory_used, memory_peak;
+} apic_server_stats;
+int apic_server_create(uint64_t memory_budget_bytes, uint32_t max_active, uint32_t keep_results,
+                       apic_server** out);
+int apic_server_destroy(apic_server* sv);
+int apic_server_submit(apic_server* sv, const apic_scene_params* scene, const apic_world_props* props,
+                       uint32_t steps, float frame_deltatime, int solver_mode, float rel_tol,
+                       uint32_t max_iterations, uint64_t* id_out);
+int apic_server_step(apic_server* sv, apic_server_round* out);
+int apic_server_request(apic_server* sv, uint64_t id, apic_request_info* out);
+int apic_server_result_positions(apic_server* sv, uint64_t id, float* dst, uint64_t floats);
+int apic_server_get_stats(apic_server* sv, apic_server_stats* out);
+
 /* ---- testing hook ------------------------------------------------------ */
 /* Run one stage of the substep on the current device state with substep dt.
  * Derived device structures (fluid lists, segment lists) are rebuilt from the

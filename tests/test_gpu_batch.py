@@ -1,0 +1,139 @@
+"""Batched and served scenes through the C-ABI (needs a GB300).
+
+A scene updated inside a batch, or as one request among others in the
+continuous-batching server, runs exactly the kernels it runs alone; the only
+difference between two runs is the order of P2G's float atomics, so results
+agree within a small tolerance (the same bound the drift test uses).
+"""
+import numpy as np
+import pytest
+
+import apic_gb300 as A
+
+pytestmark = pytest.mark.gpu
+
+PROPS = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+POS_TOL_CELLS = 1e-3  # max |position difference| in cells after the run
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu(gpu_lib):
+    if A.device_count() == 0:
+        pytest.skip("no CUDA device")
+
+
+def dam_break(side, seed, frac):
+    f = float(np.sqrt(frac))
+    return A.scene_params(A.SCENE_DAM_BREAK, side, cell_size=1.0 / side, sub=2, seed=seed, fluid_x=f, fluid_y=f)
+
+
+def disk_drop(side, seed):
+    return A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=1.0 / side, sub=2, seed=seed, fluid_x=0.3,
+                          fluid_y=0.3, disk=(0.6, 0.7, 0.1), disk_v=(0.0, -2.0))
+
+
+def alone(scene, steps, dt):
+    """The scene through the plain single-scene path."""
+    g = A.Apic(scene.width, scene.height, scene.cell_size, PROPS)
+    px, py, vx, vy = A.generate_scene(scene)
+    g.set_particles(px, py, vx, vy)
+    g.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+    for _ in range(steps):
+        g.update(A.DebugOptions(), dt)
+    return g
+
+
+def test_update_batch_matches_alone(gpu_lib):
+    scenes = [dam_break(64, 11, 0.3), disk_drop(96, 12), dam_break(128, 13, 0.5), dam_break(256, 14, 0.25)]
+    steps, dt = 6, 1 / 240
+    sims = []
+    for sc in scenes:
+        g = A.Apic(sc.width, sc.height, sc.cell_size, PROPS)
+        px, py, vx, vy = A.generate_scene(sc)
+        g.set_particles(px, py, vx, vy)
+        g.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+        sims.append(g)
+    for _ in range(steps):
+        status = A.update_batch(sims, A.DebugOptions(), dt)
+        assert status == [A.OK] * len(sims)
+        for g in sims:
+            assert g.stats().substeps >= 1
+            assert float(g.stats().true_residual_rel) <= 1e-6
+    for sc, g in zip(scenes, sims):
+        ref = alone(sc, steps, dt)
+        d = np.max(np.abs(g.read_vec2x8(0) - ref.read_vec2x8(0)))
+        assert float(d) < POS_TOL_CELLS * sc.cell_size, (sc.width, float(d))
+
+
+def test_update_batch_rejects_bad_input(gpu_lib):
+    with pytest.raises(A.ApicError) as ei:
+        A.update_batch([A.Apic(64, 64, 1 / 64, PROPS), type("X", (), {"_h": None})()], None, 1 / 240)
+    assert ei.value.code == A.ERR_INVALID_ARG
+
+
+def test_server_results_same_alone_and_in_mix(gpu_lib):
+    reqs = [(dam_break(64, 21, 0.4), 5), (disk_drop(128, 22), 3), (dam_break(96, 23, 0.2), 7),
+            (dam_break(128, 24, 0.5), 4), (disk_drop(64, 25), 6), (dam_break(192, 26, 0.3), 2)]
+    dt = 1 / 240
+    # room for about two of these scenes at a time: admission must queue the rest
+    budget = 2 * max(A.scene_bytes(sc.width, sc.height, len(A.generate_scene(sc)[0])) for sc, _ in reqs)
+    sv = A.Server(budget, max_active=4, keep_results=True)
+    ids = [sv.submit(sc, PROPS, steps, dt) for sc, steps in reqs]
+    max_stepped, rounds, waited = 0, 0, False
+    while True:
+        rd = sv.step()
+        rounds += 1
+        max_stepped = max(max_stepped, rd.stepped)
+        waited = waited or (rd.queued > 0 and rd.active > 0)
+        assert rd.memory_used <= budget
+        if rd.active == 0 and rd.queued == 0:
+            break
+        assert rounds < 200
+    st = sv.stats()
+    assert st.completed == len(reqs) and st.failed == 0
+    assert st.memory_peak <= budget
+    assert max_stepped <= 4  # max_active
+    assert waited  # the budget held requests back while others ran
+    assert st.step_p99_ms >= st.step_p50_ms > 0.0
+    assert st.request_p99_ms >= st.request_p50_ms > 0.0
+    total = 0
+    for rid, (sc, steps) in zip(ids, reqs):
+        info = sv.request(rid)
+        assert info.status == A.OK and info.finished and info.steps_done == steps
+        assert info.admit_ms >= info.submit_ms and info.done_ms >= info.admit_ms
+        assert info.max_true_residual <= 1e-6
+        total += info.particles * info.substeps
+        ref = alone(sc, steps, dt)
+        d = np.max(np.abs(sv.result_positions(rid) - ref.read_vec2x8(0)))
+        assert float(d) < POS_TOL_CELLS * sc.cell_size, (rid, float(d))
+    assert st.particle_substeps == total
+    sv.close()
+
+
+def test_server_rejects_scene_over_budget(gpu_lib):
+    sv = A.Server(1 << 20, max_active=2)
+    with pytest.raises(A.ApicError) as ei:
+        sv.submit(dam_break(256, 1, 0.5), PROPS, 3, 1 / 240)
+    assert ei.value.code == A.ERR_OOM
+    sv.close()
+
+
+def test_scene_bytes_bounds_server_scenes(gpu_lib):
+    """The admission estimate bounds what an admitted scene holds on the device."""
+    import torch
+    sv = A.Server(1 << 40, max_active=1, keep_results=True)
+    # a first request loads the library's kernels and module data, which are
+    # not part of a scene's footprint
+    sv.submit(dam_break(128, 5, 0.3), PROPS, 1, 1 / 240)
+    sv.step()
+    for side, frac in ((128, 0.3), (512, 0.6), (1024, 0.6)):
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        rid = sv.submit(dam_break(side, 5, frac), PROPS, 2, 1 / 240)
+        sv.step()  # admits the scene and runs its first update
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        used, est = free0 - free1, sv.request(rid).bytes
+        assert used <= est, (side, used, est)
+        sv.step()  # last update: positions kept, device memory released
+    sv.close()
