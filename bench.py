@@ -410,7 +410,187 @@ def roofline(iters, solve_ms, steps, counts, peak, peak_kind):
             "us_per_iteration": solve_ms * 1e3 / max(iters, 1), "solve_ms_per_step": solve_ms / steps}
 
 
+# ---------------------------------------------------------- batched / served --
+def batched_scenes(A, count, seed=3, lo=64, hi=512):
+    """Config 4: sides log-uniform in [lo, hi] rounded to a multiple of 8, dam
+    break filling a square of a uniform [0.2, 0.6] share of the domain, 4 ppc."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        side = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi))) / 8.0)) * 8
+        f = float(np.sqrt(rng.uniform(0.2, 0.6)))
+        out.append(A.scene_params(A.SCENE_DAM_BREAK, side, cell_size=1.0 / side, sub=2, seed=seed * 100000 + i,
+                                  fluid_x=f, fluid_y=f))
+    return out
+
+
+def make_sims(A, scenes, dsm=True):
+    sims = []
+    for sc in scenes:
+        g = A.Apic(sc.width, sc.height, sc.cell_size, props(A))
+        px, py, vx, vy = A.generate_scene(sc)
+        g.set_particles(px, py, vx, vy)
+        g.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+        if not dsm:
+            g.set_option(A.OPT_DSM_VCYCLE, 0)
+        sims.append(g)
+    return sims
+
+
+def run_batched(args):
+    """Config 4: many uneven scenes, one batched update per round, against the
+    plain path (one scene's update after another) over the same updates."""
+    import apic_gb300 as A
+    from apic_gb300 import build as gpu_build
+    gpu_build.build()
+    import torch
+    torch.cuda.set_device(0)
+    scenes = batched_scenes(A, args.scenes)
+    dt = 1.0 / 240.0
+    # plain: fresh scenes, the first `cmp` updates one scene at a time
+    cmp_steps = args.compare_steps
+    sims = make_sims(A, scenes, not args.no_dsm)
+    counts = [g.num_particles for g in sims]
+    n_tot = sum(counts)
+    for g in sims:  # warm-up: graph capture and first-touch of every scene
+        g.update(A.DebugOptions(), dt)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sub_plain = 0
+    for _ in range(cmp_steps):
+        for g, n in zip(sims, counts):
+            g.update(A.DebugOptions(), dt)
+            sub_plain += n * g.stats().substeps
+    plain_s = time.perf_counter() - t0
+    for g in sims:
+        g.close()
+    # batched: fresh scenes, the same updates, then the rest of the run
+    sims = make_sims(A, scenes, not args.no_dsm)
+    A.update_batch(sims, A.DebugOptions(), dt)
+    torch.cuda.synchronize()
+    round_ms, sub_cmp, sub_all, res_max = [], 0, 0, 0.0
+    with ClockSampler(0) as clocks:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            tr = time.perf_counter()
+            A.update_batch(sims, A.DebugOptions(), dt)
+            round_ms.append((time.perf_counter() - tr) * 1e3)
+            stats = [g.stats() for g in sims]
+            sub = sum(n * st.substeps for n, st in zip(counts, stats))
+            res_max = max(res_max, max(float(st.true_residual_rel) for st in stats))
+            sub_all += sub
+            if k < cmp_steps:
+                sub_cmp += sub
+                if k == cmp_steps - 1:
+                    cmp_s = time.perf_counter() - t0
+        all_s = time.perf_counter() - t0
+    sides = [sc.width for sc in scenes]
+    line = {
+        "metric": METRIC, "value": sub_all / all_s, "unit": "particle-substeps/s (aggregate over all scenes)",
+        "workload": "batched", "n_gpus": 1, "steps": args.steps, "higher_is_better": True,
+        "config": {"workload": f"{len(scenes)} independent dam-break scenes, side log-uniform in [64, 512] "
+                               f"(rounded to x8, seed 3), fluid share U[0.2, 0.6], 4 ppc, dt=1/240, "
+                               f"mixed-precision PCG to true rel. residual 1e-6",
+                   "particles": n_tot, "sides_min_median_max": [min(sides), int(np.median(sides)), max(sides)],
+                   "batching": "apic_update_batch: every scene's update graph enqueued on its own stream, "
+                               "then all completed",
+                   "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8 (default)"),
+                   "dsm_vcycle": not args.no_dsm},
+        "batched_vs_plain": {"updates_compared": cmp_steps, "batched": sub_cmp / cmp_s, "plain": sub_plain / plain_s,
+                             "ratio": (sub_cmp / cmp_s) / (sub_plain / plain_s),
+                             "plain_is": "the same scenes' updates one after another through apic_update"},
+        "round_ms_p50": float(np.percentile(round_ms, 50)), "round_ms_p99": float(np.percentile(round_ms, 99)),
+        "true_residual_rel_max": res_max, "clocks": clocks.summary(), "data": "synthetic",
+    }
+    print(json.dumps(line), flush=True)
+    for g in sims:
+        g.close()
+
+
+def served_stream(A, rate, seconds, seed=4, lo=64, hi=1024):
+    """Config 5: Poisson arrivals; side log-uniform in [lo, hi] (even, x8),
+    steps U[20, 200], dam break or disk drop 50/50, 4 ppc."""
+    rng = np.random.default_rng(seed)
+    t, out, i = 0.0, [], 0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        side = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi))) / 8.0)) * 8
+        steps = int(rng.integers(20, 201))
+        if rng.uniform() < 0.5:
+            f = float(np.sqrt(rng.uniform(0.2, 0.6)))
+            sc = A.scene_params(A.SCENE_DAM_BREAK, side, cell_size=1.0 / side, sub=2, seed=seed * 100000 + i,
+                                fluid_x=f, fluid_y=f)
+        else:
+            sc = A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=1.0 / side, sub=2, seed=seed * 100000 + i,
+                                fluid_x=0.4, fluid_y=0.3, disk=(0.7, 0.75, 0.08), disk_v=(0.0, -2.0))
+        out.append((t, sc, steps))
+        i += 1
+    return out
+
+
+def serve_stream(A, stream, budget, max_active, dt, time_limit):
+    sv = A.Server(budget, max_active)
+    t0 = time.perf_counter()
+    nxt = 0
+    while True:
+        now = time.perf_counter() - t0
+        while nxt < len(stream) and stream[nxt][0] <= now:
+            sv.submit(stream[nxt][1], props(A), stream[nxt][2], dt)
+            nxt += 1
+        rd = sv.step()
+        if rd.active == 0 and rd.queued == 0:
+            if nxt >= len(stream):
+                break
+            time.sleep(max(0.0, min(stream[nxt][0] - (time.perf_counter() - t0), 0.01)))
+        if time.perf_counter() - t0 > time_limit:
+            break
+    st = sv.stats()
+    sv.close()
+    return st, nxt
+
+
+def run_served(args):
+    """Config 5: the continuous-batching server on a Poisson request stream,
+    against the plain path (one scene at a time: max_active = 1)."""
+    import apic_gb300 as A
+    from apic_gb300 import build as gpu_build
+    gpu_build.build()
+    import torch
+    torch.cuda.set_device(0)
+    stream = served_stream(A, args.rate, args.seconds)
+    budget = int(args.budget_gb * (1 << 30))
+    dt = 1.0 / 240.0
+    res = {}
+    for name, active in (("served", args.max_active), ("plain", 1)):
+        st, n_sub = serve_stream(A, stream, budget, active, dt, args.time_limit)
+        res[name] = {"particle_substeps_per_s": st.particle_substeps / (st.elapsed_ms / 1e3),
+                     "requests_submitted": n_sub, "requests_completed": st.completed, "failed": st.failed,
+                     "step_p50_ms": st.step_p50_ms, "step_p99_ms": st.step_p99_ms,
+                     "request_p50_ms": st.request_p50_ms, "request_p99_ms": st.request_p99_ms,
+                     "memory_peak_gb": st.memory_peak / (1 << 30), "elapsed_s": st.elapsed_ms / 1e3,
+                     "max_active": active}
+    line = {
+        "metric": METRIC, "value": res["served"]["particle_substeps_per_s"],
+        "unit": "particle-substeps/s (aggregate)", "workload": "served", "n_gpus": 1, "higher_is_better": True,
+        "config": {"workload": f"Poisson arrivals at {args.rate}/s for {args.seconds} s (seed 4), side log-uniform "
+                               f"in [64, 1024] (x8), steps U[20, 200], dam break or disk drop 50/50, 4 ppc, "
+                               f"dt=1/240, mixed-precision PCG to 1e-6, budget {args.budget_gb} GB",
+                   "time_limit_s": args.time_limit},
+        "served": res["served"], "plain": res["plain"],
+        "ratio": res["served"]["particle_substeps_per_s"] / max(res["plain"]["particle_substeps_per_s"], 1e-9),
+        "data": "synthetic",
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
+    # Scenes run on one stream each; the driver maps streams onto this many
+    # hardware work queues (default 8), and kernels of streams that share a
+    # queue run one after another.  Read when CUDA initialises, so set here.
+    if any(w in sys.argv for w in ("batched", "served")):
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -431,6 +611,15 @@ def main():
                     help="keep the middle multigrid levels in global memory instead of a cluster's shared memory")
     ap.add_argument("--no-pdl", action="store_true",
                     help="launch the PCG loop's kernels in plain stream order")
+    ap.add_argument("--workload", default="single", choices=["single", "batched", "served"],
+                    help="single: the 1024^2 scene (default); batched: config 4; served: config 5")
+    ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")
+    ap.add_argument("--compare-steps", type=int, default=5, help="batched: updates compared with the plain path")
+    ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
+    ap.add_argument("--seconds", type=float, default=2.0, help="served: length of the arrival stream")
+    ap.add_argument("--budget-gb", type=float, default=120.0, help="served: device-memory budget")
+    ap.add_argument("--max-active", type=int, default=256, help="served: active scenes at most")
+    ap.add_argument("--time-limit", type=float, default=60.0, help="served: stop each run after this many seconds")
     ap.add_argument("--cpu-steps", type=int, default=0, help="CPU sample updates (default: --steps)")
     ap.add_argument("--cpu-budget", type=float, default=30.0)
     args = ap.parse_args()
@@ -439,6 +628,10 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference_arm(args, world, rank)
+    elif args.workload == "batched":
+        run_batched(args)
+    elif args.workload == "served":
+        run_served(args)
     else:
         run_gpu_arm(args, world, rank, local)
     if world > 1:
