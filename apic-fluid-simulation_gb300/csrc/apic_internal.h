@@ -177,6 +177,8 @@ struct Scene {
     int persist_grid = 0;                     // CTAs of the persistent solver (0: unavailable)
     size_t persist_smem = 0;
     bool use_persistent = false;              // persistent kernel vs graph of per-phase kernels
+    uint32_t cluster_solve_cells = 65536;     // scenes up to this many cells solve in one cluster (0: never)
+    int cluster_solve_ctas = 0;               // CTAs of that cluster (0: not used for this scene)
     bool fused_vcycle = false;                // one kernel per level and direction in the V-cycle
     // middle levels [cluster_first, tail_first) of the V-cycle run in one
     // thread-block cluster (cluster_first == tail_first: none)
@@ -239,6 +241,8 @@ cudaError_t launch_level_lists(Scene& s, int level);
 // pcg_persistent.cu
 void plan_persistent_solve(Scene& s);
 cudaError_t enqueue_persistent_solve(Scene& s);
+void plan_cluster_solve(Scene& s);     // small scenes: the whole solve in one cluster
+cudaError_t enqueue_cluster_solve(Scene& s);
 // solver.cu: the same solve launched kernel by kernel with host loop control
 // (profiling runs, so every kernel is a separate launch)
 cudaError_t run_solve_eager(Scene& s);

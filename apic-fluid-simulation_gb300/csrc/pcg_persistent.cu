@@ -21,6 +21,7 @@
 // * Cells are always visited by the same warp in every base-level phase
 //   (warp w owns segments w, w + nwarps, ...), so phases that read only their
 //   own cells need no barrier in between.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "apic_device.cuh"
@@ -124,14 +125,27 @@ struct Ctx {
     const uint32_t* nseg;
     uint32_t warp, nwarps, last_fluid, pad_count;
     int slot;
+    bool cluster;  // the grid is one thread-block cluster: hardware barrier
 };
+
+// Barrier over every CTA of the solve.  A single cluster uses the hardware
+// cluster barrier (all its CTAs are co-scheduled, no polling; its release /
+// acquire order covers global memory too); a cooperative grid uses the
+// bounded software barrier.
+__device__ __forceinline__ bool sync_all(Ctx& c) {
+    if (c.cluster) {
+        cooperative_groups::this_cluster().sync();
+        return true;
+    }
+    return grid_barrier(c.a.gs, c.a.ctl);
+}
 
 // Deterministic grid-wide sum (includes one barrier).
 __device__ __forceinline__ bool grid_sum(Ctx& c, double v, double& out) {
     double b = block_sum_bcast(v);
     double* part = c.a.partials + size_t(c.slot) * gridDim.x;
     if (threadIdx.x == 0) part[blockIdx.x] = b;
-    if (!grid_barrier(c.a.gs, c.a.ctl)) return false;
+    if (!sync_all(c)) return false;
     double t = threadIdx.x < gridDim.x ? __ldcg(part + threadIdx.x) : 0.0;
     out = block_sum_bcast(t);
     c.slot ^= 1;
@@ -144,7 +158,7 @@ __device__ __forceinline__ bool grid_max(Ctx& c, float v, float& out) {
     float b = block_max_bcast(v);
     double* part = c.a.partials + size_t(c.slot) * gridDim.x;
     if (threadIdx.x == 0) part[blockIdx.x] = double(b);
-    if (!grid_barrier(c.a.gs, c.a.ctl)) return false;
+    if (!sync_all(c)) return false;
     float t = threadIdx.x < gridDim.x ? float(__ldcg(part + threadIdx.x)) : 0.0f;
     out = block_max_bcast(t);
     c.slot ^= 1;
@@ -152,7 +166,7 @@ __device__ __forceinline__ bool grid_max(Ctx& c, float v, float& out) {
 }
 
 #define SYNC_OR_FAIL() \
-    if (!grid_barrier(c.a.gs, c.a.ctl)) return false
+    if (!sync_all(c)) return false
 
 // One V-cycle (apply_preconditioner, src/apic.rs:1788-1821); z in lv[0].err.
 // The last phase writes only base cells that the caller's own-cell phases read.
@@ -347,7 +361,7 @@ __device__ bool solve(Ctx& c) {
 
 #undef SYNC_OR_FAIL
 
-__global__ void __launch_bounds__(kPThreads, 1) k_solve_persistent(SolveArgs a) {
+__global__ void __launch_bounds__(kPThreads, 1) k_solve_persistent(SolveArgs a, int cluster) {
     extern __shared__ uint32_t sm[];
     __shared__ uint32_t nseg[kMaxLevels];
     __shared__ uint32_t s_last, s_pad;
@@ -358,7 +372,8 @@ __global__ void __launch_bounds__(kPThreads, 1) k_solve_persistent(SolveArgs a) 
     }
     if (blockIdx.x == 0 && a.tail_first < a.nlevels) cta_tail_load_coeffs(a.tp, sm);
     __syncthreads();
-    Ctx c{a, sm, nseg, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5, s_last, s_pad, 0};
+    Ctx c{a, sm, nseg, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5, s_last, s_pad, 0,
+          cluster != 0};
     solve(c);
     if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl->pcg_done = 1;
 }
@@ -375,7 +390,9 @@ void plan_persistent_solve(Scene& s) {
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop || sms <= 0) return;
     size_t smem = s.tail_first < s.nlevels ? s.tail_smem : 0;
-    if (smem) cudaFuncSetAttribute(k_solve_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    // a per-function limit shared by every scene of the process: the largest
+    // tail any scene may use, not this scene's
+    cudaFuncSetAttribute(k_solve_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTailSmemBudget));
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_persistent, kPThreads, smem) != cudaSuccess ||
         per_sm < 1) {
         cudaGetLastError();
@@ -385,6 +402,75 @@ void plan_persistent_solve(Scene& s) {
     if (grid > kPThreads || grid > kMaxRedBlocks) grid = kPThreads < kMaxRedBlocks ? kPThreads : kMaxRedBlocks;
     s.persist_grid = grid;
     s.persist_smem = smem;
+}
+
+// The whole solve in one thread-block cluster, for scenes small enough that
+// 1..16 CTAs cover a base-level phase in about one pass: CTAs = base cells /
+// 4096 rounded up to a power of two.  0 when the scene is larger than
+// cluster_solve_cells or the GPU cannot hold such a cluster.
+void plan_cluster_solve(Scene& s) {
+    s.cluster_solve_ctas = 0;
+    if (s.cluster_solve_cells == 0 || s.cells > s.cluster_solve_cells || s.nlevels < 2) return;
+    int ctas = 1;
+    while (ctas < 16 && uint64_t(ctas) * 4096 < s.cells) ctas *= 2;
+    size_t smem = s.tail_first < s.nlevels ? s.tail_smem : 0;
+    cudaFuncSetAttribute(k_solve_persistent, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(k_solve_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTailSmemBudget));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(kPThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = unsigned(ctas);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    const bool ok = cudaOccupancyMaxActiveClusters(&clusters, k_solve_persistent, &cfg) == cudaSuccess && clusters > 0;
+    cudaGetLastError();
+    if (ok) s.cluster_solve_ctas = ctas;
+}
+
+static SolveArgs solve_args(Scene& s, uint32_t* words) {
+    SolveArgs a;
+    for (int l = 0; l < kMaxLevels; ++l) a.lv[l] = s.lv[l];
+    a.nlevels = s.nlevels;
+    a.tail_first = s.tail_first;
+    *words = 0;
+    if (s.tail_first < s.nlevels) a.tp = make_tail_params(s, s.tail_first, words);
+    else a.tp.n = 0;
+    a.pressure = s.pressure; a.search = s.search; a.ap = s.ap; a.corr = s.corr;
+    a.cg_s = s.cg_s; a.cg_ap = s.cg_ap; a.cg_r = s.cg_r;
+    a.b64 = s.b64; a.p64 = s.p64; a.partials = s.partials;
+    a.ctl = s.ctl;
+    a.gs = s.gsync;
+    a.mode = s.solver_mode;
+    a.solve_error = s.props.solve_error;
+    a.tol = double(s.rel_tol);
+    a.max_iter = s.max_iter;
+    return a;
+}
+
+// Enqueue the whole solve on s.stream as one cluster launch.
+cudaError_t enqueue_cluster_solve(Scene& s) {
+    uint32_t words = 0;
+    SolveArgs a = solve_args(s, &words);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(s.cluster_solve_ctas);
+    cfg.blockDim = dim3(kPThreads);
+    cfg.dynamicSmemBytes = size_t(words) * 4;
+    cfg.stream = s.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = unsigned(s.cluster_solve_ctas);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    s.p64_valid = s.solver_mode == APIC_SOLVER_REL_MIXED;
+    return cudaLaunchKernelEx(&cfg, k_solve_persistent, a, 1);
 }
 
 // Enqueue the whole solve on s.stream: reset the barrier, launch cooperatively.
@@ -418,7 +504,7 @@ cudaError_t enqueue_persistent_solve(Scene& s) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     s.p64_valid = s.solver_mode == APIC_SOLVER_REL_MIXED;
-    return cudaLaunchKernelEx(&cfg, k_solve_persistent, a);
+    return cudaLaunchKernelEx(&cfg, k_solve_persistent, a, 0);
 }
 
 }  // namespace apic

@@ -549,6 +549,7 @@ int apic::create_scene(uint32_t width, uint32_t height, float cell_size, const a
     plan_vcycle(s);
     AL(s.gsync, 1);
     plan_persistent_solve(s);
+    plan_cluster_solve(s);
     AL(s.ctl, 1);
     AL(s.partials, 2 * kMaxRedBlocks);
     s.scan_tmp_len = 3 * (div_up(max_words, 1024) + 1);
@@ -989,6 +990,12 @@ int apic_set_option(apic_handle* h, int option, int value) {
             s.use_dsm = value != 0;
             invalidate_graphs(s);
             return APIC_OK;
+        case APIC_OPT_CLUSTER_SOLVE:
+            if (value < 0) return fail(APIC_ERR_INVALID_ARG, "cluster solve size must be >= 0");
+            s.cluster_solve_cells = uint32_t(value);
+            plan_cluster_solve(s);
+            invalidate_graphs(s);
+            return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }
@@ -1005,6 +1012,7 @@ int apic_get_option(apic_handle* h, int option, int* value) {
         case APIC_OPT_DSM_VCYCLE:
             *value = (h->s.use_dsm && h->s.dsm_first < h->s.dsm_tail) ? 1 : 0;
             return APIC_OK;
+        case APIC_OPT_CLUSTER_SOLVE: *value = h->s.cluster_solve_ctas; return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }

@@ -269,6 +269,8 @@ cudaError_t build_solve(Scene& s, GraphCursor& c) {
     s.kn_pcg = s.kn_refine = 0;
     if (s.use_persistent && s.persist_grid > 0)
         return capture_into(s, c, [&]() { return enqueue_persistent_solve(s); });
+    if (s.cluster_solve_ctas > 0)  // a small scene: the whole solve is one cluster launch
+        return capture_into(s, c, [&]() { return enqueue_cluster_solve(s); });
     const Level& B = s.lv[0];
     uint32_t g = seg_grid(B.words);
     int mode = s.solver_mode;

@@ -483,8 +483,17 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 }
 
 // Start copying every tail level's mask and coefficients into shared memory
-// (complete after cp_async_wait_all).
+// (complete after cp_async_wait_all).  The whole tail region is zeroed first:
+// cells outside the fluid mask are never written, and with the stale shared
+// memory of earlier kernels left in place the cluster-launched solve reached
+// NaN (after other scenes had run in the process; the read that carried it
+// was not located), while zeroed memory gives the same results as before.
 __device__ __forceinline__ void cta_tail_issue_coeffs(const TailParams& tp, uint32_t* sm) {
+    if (tp.n > 0) {
+        const uint32_t words = tp.o_cr + tp.lv[tp.n - 1].padded;
+        for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) sm[i] = 0u;
+        __syncthreads();  // zeroes land before any copy into the same words
+    }
     for (int l = 0; l < tp.n; ++l) {
         const TailLevel& t = tp.lv[l];
         SmemLevel L = smem_level(sm, t);

@@ -510,3 +510,41 @@ def test_read_vec2x8_layout(gpu_lib):
         chunks = out.reshape(-1, 16)
         eq(chunks[:, :8].ravel(), x, f"Vec2x8 x lanes ({fx})")
         eq(chunks[:, 8:].ravel(), y, f"Vec2x8 y lanes ({fy})")
+
+
+@pytest.mark.parametrize("mode", [A.SOLVER_REFERENCE, A.SOLVER_REL_FP32, A.SOLVER_REL_MIXED])
+@pytest.mark.parametrize("side", [64, 176, 256])
+def test_cluster_solve_matches_graph_solver(gpu_lib, mode, side):
+    """A small scene's whole solve in one cluster launch runs the same iterations as the graph of per-phase kernels."""
+    props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+    cs = 1 / side
+    scene = A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=cs, sub=2, seed=3, fluid_x=0.5, fluid_y=0.5,
+                           disk=(0.7, 0.8, 0.08), disk_v=(0.0, -2.0))
+    px, py, vx, vy = A.generate_scene(scene)
+    sims = []
+    for cells in (1 << 20, 0):
+        g = A.Apic(side, side, cs, props)
+        g.set_particles(px, py, vx, vy)
+        g.set_solver(mode, 1e-6, 500)
+        g.set_option(A.OPT_CLUSTER_SOLVE, cells)
+        sims.append(g)
+    if sims[0].get_option(A.OPT_CLUSTER_SOLVE) == 0:
+        pytest.skip("cluster launch unavailable")
+    assert sims[1].get_option(A.OPT_CLUSTER_SOLVE) == 0
+    opts = A.DebugOptions(disable_particle_sort=True)
+    for k in range(6):
+        for g in sims:
+            g.update(opts, 1 / 480)
+        a, b = sims[0].stats(), sims[1].stats()
+        # FP32 Krylov loops whose reductions are grouped differently cross a
+        # relative threshold a few iterations apart
+        slack = max(3, int(0.15 * b.pcg_iterations_total))
+        assert abs(int(a.pcg_iterations_total) - int(b.pcg_iterations_total)) <= slack, (
+            k, a.pcg_iterations_total, b.pcg_iterations_total)
+        if mode == A.SOLVER_REL_MIXED:
+            assert a.true_residual_rel <= 1e-6 and b.true_residual_rel <= 1e-6
+    pa, pb = sims[0].read_field("pressure"), sims[1].read_field("pressure")
+    scale = float(np.max(np.abs(pa))) or 1.0
+    assert float(np.max(np.abs(pa - pb))) <= 1e-3 * scale
+    for f in ("pos_x", "pos_y"):
+        assert float(np.max(np.abs(sims[0].read_field(f) - sims[1].read_field(f)))) < 1e-3 * cs
