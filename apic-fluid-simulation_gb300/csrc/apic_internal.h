@@ -177,7 +177,7 @@ struct Scene {
     int persist_grid = 0;                     // CTAs of the persistent solver (0: unavailable)
     size_t persist_smem = 0;
     bool use_persistent = false;              // persistent kernel vs graph of per-phase kernels
-    uint32_t cluster_solve_cells = 65536;     // scenes up to this many cells solve in one cluster (0: never)
+    uint32_t cluster_solve_cells = 0;         // scenes up to this many cells solve in one cluster (0: never)
     int cluster_solve_ctas = 0;               // CTAs of that cluster (0: not used for this scene)
     bool fused_vcycle = false;                // one kernel per level and direction in the V-cycle
     // middle levels [cluster_first, tail_first) of the V-cycle run in one

@@ -241,13 +241,15 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
  * apic_get_option reports 0 where no level qualifies.  Same results bit for
  * bit. */
 #define APIC_OPT_DSM_VCYCLE 5
-/* Scenes of at most this many cells (default 65536) run their whole pressure
- * solve (every PCG iteration and refinement) as one launch of a single
- * thread-block cluster of 1..16 CTAs, phases separated by the cluster's
- * hardware barrier; larger scenes use the graph of per-phase kernels.  0:
- * never.  apic_get_option returns the CTAs the scene's cluster uses (0: not
- * used).  Same per-cell arithmetic; reductions are grouped differently.
- * Profiling runs (apic_set_profiling) keep the per-phase kernels. */
+/* Scenes of at most this many cells run their whole pressure solve (every
+ * PCG iteration and refinement) as one launch of a single thread-block
+ * cluster of 1..16 CTAs, phases separated by the cluster's hardware barrier;
+ * larger scenes use the graph of per-phase kernels.  0 (default): never --
+ * on GB300 the graph is faster per iteration even at 64^2; the cluster form
+ * only saves launches.  apic_get_option returns the CTAs the scene's cluster
+ * uses (0: not used).  Same per-cell arithmetic; reductions are grouped
+ * differently.  Profiling runs (apic_set_profiling) keep the per-phase
+ * kernels. */
 #define APIC_OPT_CLUSTER_SOLVE 6
 int apic_set_option(apic_handle* h, int option, int value);
 int apic_get_option(apic_handle* h, int option, int* value);
