@@ -293,7 +293,7 @@ __device__ __forceinline__ void dsm_load_first(const DsmParams& p, uint8_t* sm, 
 }
 
 __global__ void __launch_bounds__(kTailThreads, 1) k_vcycle_dsm(DsmParams p, TailParams tp, uint32_t dsm_off,
-                                                               const Ctl* ctl) {
+                                                               uint32_t dsm_bytes, const Ctl* ctl) {
     extern __shared__ __align__(16) uint8_t smem[];
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t rank = cl.block_rank();
@@ -302,6 +302,13 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_vcycle_dsm(DsmParams p, Tai
     // the first tail level's residual and error live in CTA 0's shared memory
     float* tail_res = cl.map_shared_rank(reinterpret_cast<float*>(tail_sm) + tp.lv[0].o_res, 0);
     const float* tail_err = cl.map_shared_rank(reinterpret_cast<float*>(tail_sm) + tp.lv[0].o_err, 0);
+    // Zero the distributed levels first (error and residual of cells outside
+    // the fluid mask are never written): with stale shared memory from
+    // earlier kernels in place the V-cycle reached NaN on scenes with fluid in
+    // every band (noise masks, 512^2), like the coarse tail did; the read
+    // that carried the stale value was not located.
+    for (uint32_t i = threadIdx.x; i < dsm_bytes / 4; i += blockDim.x) reinterpret_cast<uint32_t*>(dsm)[i] = 0u;
+    __syncthreads();
     // masks and coefficients were written by the multigrid setup, before the
     // solve: their copies start while the previous kernel drains
     if (rank == 0) cta_tail_issue_coeffs(tp, tail_sm);
@@ -474,7 +481,8 @@ void launch_vcycle_dsm(Scene& s, cudaStream_t st) {
     p.terr = T.err;
     cudaLaunchAttribute attr[2];
     cudaLaunchConfig_t cfg = dsm_config(s.dsm_smem, st, attr, s.use_pdl);
-    cudaLaunchKernelEx(&cfg, k_vcycle_dsm, p, tp, s.dsm_off, static_cast<const Ctl*>(s.ctl));
+    cudaLaunchKernelEx(&cfg, k_vcycle_dsm, p, tp, s.dsm_off, uint32_t(s.dsm_smem - s.dsm_off),
+                       static_cast<const Ctl*>(s.ctl));
 }
 
 }  // namespace apic

@@ -448,13 +448,18 @@ def test_cluster_option_rejected_without_middle_levels(gpu_lib):
     g.set_option(A.OPT_CLUSTER_VCYCLE, 0)
 
 
-@pytest.mark.parametrize("side", [256, 1024, 2048])
-def test_dsm_vcycle_equals_global(gpu_lib, side):
-    """Levels held in a cluster's distributed shared memory give the same z = M^-1 r, bit for bit."""
+@pytest.mark.parametrize("side,kind", [(256, "dam"), (1024, "dam"), (2048, "dam"), (512, "noise"), (1024, "noise")])
+def test_dsm_vcycle_equals_global(gpu_lib, side, kind):
+    """Levels held in a cluster's distributed shared memory give the same z = M^-1 r, bit for bit.
+    Noise masks put fluid in every row band and against every border."""
     props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
     cs = 1 / side
-    scene = A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=cs, sub=2, seed=1, fluid_x=0.5, fluid_y=0.5,
-                           disk=(0.7, 0.8, 0.08), disk_v=(0.0, -2.0))
+    if kind == "noise":
+        scene = A.scene_params(A.SCENE_NOISE, side, cell_size=cs, sub=2, seed=2, noise_period=1 / 64,
+                               noise_threshold=0.5, vel_sigma=0.5)
+    else:
+        scene = A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=cs, sub=2, seed=1, fluid_x=0.5,
+                               fluid_y=0.5, disk=(0.7, 0.8, 0.08), disk_v=(0.0, -2.0))
     g = A.Apic(side, side, cs, props)
     if g.get_option(A.OPT_DSM_VCYCLE) == 0:
         pytest.skip("no level qualifies for the distributed form on this GPU")
