@@ -38,13 +38,28 @@ sys.path.insert(0, os.path.join(ROOT, "apic-fluid-simulation_gb300"))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s"
+UNIT_NOTE = ("1 particle-step = 1 particle through one CFL substep of the update pipeline; an update of dt "
+             "splits into substeps by the CFL condition (updates_per_s is reported beside)")
 SIDE = 1024
 FRAME_DT = 1.0 / 480.0
+STRESS = False  # --workload stress: config 3 instead of the 1024^2 scene
+NOISE_PERIOD = 1.0 / 64.0  # value-noise lattice period of config 3 (domain units)
 
 
 def scene_params(A, side=SIDE):
+    if STRESS:
+        # config 3: value-noise mask > 0.5 (seed 2), 4 ppc, v ~ N(0, 0.5^2) per component
+        return A.scene_params(A.SCENE_NOISE, side, cell_size=1.0 / side, sub=2, seed=2,
+                              noise_period=NOISE_PERIOD, noise_threshold=0.5, vel_sigma=0.5)
     return A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=1.0 / side, sub=2, seed=1, fluid_x=0.5,
                           fluid_y=0.5, disk=(0.7, 0.8, 0.08), disk_v=(0.0, -2.0))
+
+
+def workload_name(side):
+    if STRESS:
+        return (f"stress: value-noise fluid mask > 0.5 (period {NOISE_PERIOD:g}, seed 2), {side}x{side} MAC grid, "
+                f"dx=1/{side}, 4 ppc, v ~ N(0, 0.5^2), dt=1/1000 per step, Morton sort every step")
+    return f"dam break + disk, {side}x{side} MAC grid, dx=1/{side}, 4 ppc, seed 1, dt=1/480 per step"
 
 
 def props(A):
@@ -137,9 +152,10 @@ def dist_barrier(world: int) -> None:
 
 
 # ---------------------------------------------------------------- CPU arm --
-def cpu_restatement_rate(n_steps: int, warmup: int, budget_s: float, side: int = SIDE, threads: int = 0):
+def cpu_restatement_rate(n_steps: int, warmup: int, budget_s: float, side: int = 0, threads: int = 0):
     """Particle-steps/s of the C++ restatement of the reference step (OpenMP)."""
     import apic_gb300 as A
+    side = side or SIDE  # SIDE is read at call time: --workload stress changes it
     from oracle.oracle import OracleSim
     threads = threads or os.cpu_count() or 1
     px, py, vx, vy = A.generate_scene(scene_params(A, side))
@@ -149,17 +165,19 @@ def cpu_restatement_rate(n_steps: int, warmup: int, budget_s: float, side: int =
     opts = A.DebugOptions()
     for _ in range(warmup):
         o.update(opts, FRAME_DT)
-    times = []
+    times, substeps = [], 0
     t_start = time.perf_counter()
     for _ in range(n_steps):
         t0 = time.perf_counter()
         o.update(opts, FRAME_DT)
         times.append(time.perf_counter() - t0)
+        substeps += o.stats().substeps
         if time.perf_counter() - t_start > budget_s:
             break
     n = len(px)
     total = sum(times)
-    return {"value": n * len(times) / total, "steps": len(times), "seconds": total, "threads": threads,
+    return {"value": n * substeps / total, "steps": len(times), "substeps": substeps,
+            "updates_per_s": len(times) / total, "seconds": total, "threads": threads,
             "particles": n, "ms_per_step": 1e3 * total / len(times),
             "p50_ms": 1e3 * float(np.percentile(times, 50)), "p99_ms": 1e3 * float(np.percentile(times, 99))}
 
@@ -172,8 +190,9 @@ def run_reference_arm(args, world, rank):
         "impl": "reference", "metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": args.gpus,
         "steps": r["steps"], "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"dam break + disk, {SIDE}x{SIDE} MAC grid, 4 ppc, seed 1, dt=1/480",
-                   "particles": r["particles"], "solver": "FP32 MG-PCG + FP64 refinement to 1e-6"},
+        "config": {"workload": workload_name(SIDE), "particles": r["particles"], "substeps": r["substeps"],
+                   "unit": UNIT_NOTE, "solver": "FP32 MG-PCG + FP64 refinement to 1e-6"},
+        "updates_per_s": r["updates_per_s"],
         "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"],
         "cpu_baseline": {"value": r["value"], "unit": METRIC, "cores": r["threads"], "kind": "port",
                          "sample": f"{r['steps']} updates after {args.warmup} warm-up updates from t=0"},
@@ -257,7 +276,7 @@ def run_gpu_arm(args, world, rank, local):
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     dev_s = sum(step_ms) / 1e3
     dev_s_max = dist_max(dev_s, world)
-    value = world * n * args.steps / dev_s_max
+    value = world * n * substeps / dev_s_max  # substeps: summed over the timed updates (same on every replica)
 
     # ---- e2e through the C-ABI with host buffers (pinned), copies inside the
     # timed region: a second scene from the same start, over the same updates
@@ -282,14 +301,16 @@ def run_gpu_arm(args, world, rank, local):
     torch.cuda.synchronize()
     dist_barrier(world)
     te = time.perf_counter()
+    e2e_sub = 0
     for _ in range(e2e_steps):
         lib.apic_write_field(sim2._h, A.FIELDS["ext_force_u"], fu.data_ptr(), fu.numel() * 4)
         lib.apic_write_field(sim2._h, A.FIELDS["ext_force_v"], fv.data_ptr(), fv.numel() * 4)
         sim2.update(opts, FRAME_DT)
+        e2e_sub += sim2.stats().substeps
         lib.apic_read_vec2x8(sim2._h, 0, A.ctypes.cast(pos_h.data_ptr(), A._FP), nc * 16)
         lib.apic_read_vec2x8(sim2._h, 1, A.ctypes.cast(vel_h.data_ptr(), A._FP), nc * 16)
     e2e_s = dist_max(time.perf_counter() - te, world)
-    e2e_value = world * n * e2e_steps / e2e_s
+    e2e_value = world * n * e2e_sub / e2e_s
     h2d = (fu.numel() + fv.numel()) * 4
     d2h = 2 * nc * 16 * 4
     sim2.close()
@@ -325,12 +346,11 @@ def run_gpu_arm(args, world, rank, local):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dev_s_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"dam break + disk, {args.side}x{args.side} MAC grid, dx=1/{args.side}, 4 ppc, "
-                                   f"seed 1, dt=1/480 per step", "particles": n,
+            "config": {"workload": workload_name(args.side), "particles": n,
                        "solver": {"mixed": "FP32 MG-PCG + FP64 refinement, true rel. residual <= 1e-6",
                                   "fp32": "FP32 MG-PCG to recursive rel. residual 1e-6",
                                   "reference": "reference exits (max|r| < 1e-5, 100 iterations)"}[args.solver],
-                       "substeps": substeps, "pcg_iterations": iters,
+                       "unit": UNIT_NOTE, "substeps": substeps, "pcg_iterations": iters,
                        "true_residual_rel_max": max(true_res) if true_res else None,
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
                        "solve_form": "persistent kernel" if args.persistent else "graph of per-phase kernels",
@@ -341,6 +361,7 @@ def run_gpu_arm(args, world, rank, local):
                            if cluster_cells else ""),
                        "launch": ("stage by stage" if args.eager else "one CUDA graph per update")
                        + ("" if args.no_pdl else "; programmatic dependent launch in the PCG loop")},
+            "updates_per_s": world * args.steps / dev_s_max,
             "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
             "wall_s": wall,
             "clocks": clocks.summary(),
@@ -585,6 +606,16 @@ def run_served(args):
     print(json.dumps(line), flush=True)
 
 
+def set_stress(args):
+    """Switch the module to config 3 (scene, frame dt, default side)."""
+    global STRESS, FRAME_DT, SIDE
+    STRESS = True
+    FRAME_DT = 1.0 / 1000.0
+    SIDE = 4096
+    if args.side == 1024:
+        args.side = SIDE
+
+
 def main():
     # Scenes run on one stream each; the driver maps streams onto this many
     # hardware work queues (default 8), and kernels of streams that share a
@@ -611,8 +642,9 @@ def main():
                     help="keep the middle multigrid levels in global memory instead of a cluster's shared memory")
     ap.add_argument("--no-pdl", action="store_true",
                     help="launch the PCG loop's kernels in plain stream order")
-    ap.add_argument("--workload", default="single", choices=["single", "batched", "served"],
-                    help="single: the 1024^2 scene (default); batched: config 4; served: config 5")
+    ap.add_argument("--workload", default="single", choices=["single", "stress", "batched", "served"],
+                    help="single: the 1024^2 scene (default); stress: config 3 (4096^2 noise scene); "
+                         "batched: config 4; served: config 5")
     ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")
     ap.add_argument("--compare-steps", type=int, default=5, help="batched: updates compared with the plain path")
     ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
@@ -625,6 +657,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "stress":
+        set_stress(args)
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference_arm(args, world, rank)
