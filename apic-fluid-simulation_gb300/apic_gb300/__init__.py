@@ -107,6 +107,33 @@ class ServerStatsC(ctypes.Structure):
                 ("memory_used", ctypes.c_uint64), ("memory_peak", ctypes.c_uint64)]
 
 
+class RenderParamsC(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("scale", ctypes.c_float),
+                ("draw_radius", ctypes.c_float), ("margin", ctypes.c_float), ("pick_x", ctypes.c_float),
+                ("pick_y", ctypes.c_float), ("pick_radius", ctypes.c_float), ("background", ctypes.c_uint32)]
+
+
+class RenderStatsC(ctypes.Structure):
+    _fields_ = [("valid", ctypes.c_uint32), ("nan", ctypes.c_uint32), ("out_of_bounds", ctypes.c_uint32),
+                ("fluid_cells", ctypes.c_uint32), ("picked", ctypes.c_int64), ("volume", ctypes.c_float),
+                ("kernels", ctypes.c_uint32)]
+
+
+def render_params(width: int = 1920, height: int = 1080, scale: float | None = None, grid_width: int = 256,
+                  cell_size: float = 0.075, draw_radius: float = 3.0, margin: float = 50.0, pick=None,
+                  pick_radius: float = 12.0, background=(0, 0, 0)) -> RenderParamsC:
+    """Parameters of the GUI's particle view (src/main.rs:26-36): a 1920 x 1080
+    frame, SIM_SCALE = WIDTH / (GRID_WIDTH * CELL_SIZE) pixels per unit unless
+    `scale` is given, 3-pixel discs, a 50-pixel out-of-bounds margin; `pick`:
+    (x, y) in pixels to pick the nearest particle within `pick_radius`."""
+    if scale is None:
+        scale = float(np.float32(width) / (np.float32(grid_width) * np.float32(cell_size)))
+    px, py, pr = (0.0, 0.0, -1.0) if pick is None else (float(pick[0]), float(pick[1]), float(pick_radius))
+    r, g, b = background
+    return RenderParamsC(width, height, scale, draw_radius, margin, px, py, pr,
+                         (int(r) & 255) | ((int(g) & 255) << 8) | ((int(b) & 255) << 16) | (255 << 24))
+
+
 # Every symbol that include/apic_gpu.h declares, with its ctypes signature.
 _VP = ctypes.c_void_p
 _FP = ctypes.POINTER(ctypes.c_float)
@@ -157,6 +184,13 @@ SIGNATURES = {
     "apic_server_request": (ctypes.c_int, [_VP, ctypes.c_uint64, ctypes.POINTER(RequestInfoC)]),
     "apic_server_result_positions": (ctypes.c_int, [_VP, ctypes.c_uint64, _FP, ctypes.c_uint64]),
     "apic_server_get_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ServerStatsC)]),
+    "apic_snapshot_bytes": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_uint64)]),
+    "apic_snapshot": (ctypes.c_int, [_VP, _VP, ctypes.c_uint64]),
+    "apic_restore": (ctypes.c_int, [_VP, _VP, ctypes.c_uint64]),
+    "apic_render": (ctypes.c_int, [_VP, ctypes.POINTER(RenderParamsC), ctypes.POINTER(RenderStatsC)]),
+    "apic_read_frame": (ctypes.c_int, [_VP, _VP, ctypes.c_uint64]),
+    "apic_frame_device_ptr": (ctypes.c_int, [_VP, ctypes.POINTER(_VP), ctypes.POINTER(ctypes.c_uint32),
+                                             ctypes.POINTER(ctypes.c_uint32)]),
 }
 
 _lib = None
@@ -398,6 +432,37 @@ class Apic:
         v = ctypes.c_int(0)
         _check(self._lib.apic_get_option(self._h, option, ctypes.byref(v)), "apic_get_option")
         return v.value
+
+    # -- snapshot / restore (the state a later update reads)
+    def snapshot(self) -> bytes:
+        n = ctypes.c_uint64()
+        _check(self._lib.apic_snapshot_bytes(self._h, ctypes.byref(n)), "apic_snapshot_bytes")
+        buf = ctypes.create_string_buffer(n.value)
+        _check(self._lib.apic_snapshot(self._h, ctypes.cast(buf, _VP), n.value), "apic_snapshot")
+        return buf.raw
+
+    def restore(self, blob: bytes) -> None:
+        buf = ctypes.create_string_buffer(bytes(blob), len(blob))
+        _check(self._lib.apic_restore(self._h, ctypes.cast(buf, _VP), len(blob)), "apic_restore")
+
+    # -- headless particle view (src/main.rs:207-277)
+    def render(self, params: RenderParamsC | None = None, read: bool = True):
+        """Splat the particles into the scene's device frame; returns (frame as
+        a height x width x 4 uint8 array, or None when read is False; stats)."""
+        p = params if params is not None else render_params()
+        st = RenderStatsC()
+        _check(self._lib.apic_render(self._h, ctypes.byref(p), ctypes.byref(st)), "apic_render")
+        if not read:
+            return None, st
+        frame = np.empty((p.height, p.width, 4), dtype=np.uint8)
+        _check(self._lib.apic_read_frame(self._h, frame.ctypes.data_as(_VP), frame.nbytes), "apic_read_frame")
+        return frame, st
+
+    def frame_device_ptr(self):
+        ptr, w, h = _VP(), ctypes.c_uint32(), ctypes.c_uint32()
+        _check(self._lib.apic_frame_device_ptr(self._h, ctypes.byref(ptr), ctypes.byref(w), ctypes.byref(h)),
+               "apic_frame_device_ptr")
+        return ptr.value, w.value, h.value
 
     # -- measurement and testing hooks
     def set_profiling(self, on: bool) -> None:

@@ -124,6 +124,24 @@ struct PartPtrs {
     float* alt[NPF];
 };
 
+struct RenderBuffers;  // render.cu
+
+// Splatting parameters as the kernels use them (render.cu).
+struct RenderParamsDev {
+    uint32_t width, height;     // frame in pixels
+    uint32_t ntx, nty, ntiles;  // 16 x 16 pixel tiles
+    float fw, fh;               // width, height as floats
+    float scale, margin, radius, size;  // pixels per unit, out-of-bounds margin, disc radius, 2 * radius
+    float pick_x, pick_y, pick_r2;      // pick centre and squared radius (< 0: no pick)
+    uint32_t bg;                // clear colour, RGBA8 little-endian
+};
+
+struct RenderResult {
+    uint32_t valid, nan, oob;
+    int64_t picked;
+    uint32_t kernels;
+};
+
 struct Scene {
     uint32_t W = 0, H = 0, cells = 0;
     float dx = 0;
@@ -208,6 +226,7 @@ struct Scene {
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
 
     apic_step_stats stats{};
+    RenderBuffers* render = nullptr;          // splatting buffers (allocated on the first frame)
 };
 
 // ---- launchers (each enqueues on s.stream) --------------------------------
@@ -215,6 +234,10 @@ struct Scene {
 cudaError_t launch_sort(Scene& s);
 // Exclusive scan of data[0..n) in place; tmp holds div_up(n, 1024) words.
 cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t n, uint32_t* tmp, cudaStream_t st);
+// render.cu: splat the particles into the scene's frame and wait for it
+cudaError_t render_frame(Scene& s, const RenderParamsDev& p, RenderResult* out);
+const uint32_t* render_frame_ptr(const Scene& s, uint32_t* width, uint32_t* height);
+void free_render(Scene& s);
 cudaError_t radix_sort_pairs_in(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* hist,
                                 uint32_t* scan_tmp, uint32_t n, int bits, cudaStream_t st);
 int morton_key_bits(uint32_t width, uint32_t height);

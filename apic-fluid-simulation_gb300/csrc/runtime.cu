@@ -201,6 +201,7 @@ void free_scene(Scene& s) {
         dfree(L.fluid); dfree(L.seg); dfree(L.diag); dfree(L.inv_diag); dfree(L.px); dfree(L.py);
         dfree(L.res); dfree(L.err); dfree(L.err2);
     }
+    free_render(s);
     dfree(s.vec_stage);
     s.vec_stage = nullptr;
     s.vec_stage_floats = 0;
@@ -957,6 +958,209 @@ int apic_read_vec2x8(apic_handle* h, int which, float* dst, uint64_t floats) {
     CK(launch_pack_vec2x8(s, which, s.vec_stage));
     CK(cudaMemcpyAsync(dst, s.vec_stage, floats * sizeof(float), cudaMemcpyDeviceToHost, s.stream));
     CK(cudaStreamSynchronize(s.stream));
+    return APIC_OK;
+}
+
+// ---- snapshot / restore -----------------------------------------------------
+// The state a later update reads: the nine particle arrays (all padded lanes),
+// the obstacle mask, pending external / post forces, the substep bookkeeping
+// (timestamp, prev_deltatime) and the solver settings.  Everything else is
+// rebuilt from the particles inside every substep.
+
+namespace {
+
+constexpr uint32_t kSnapMagic = 0x4E535041u;  // "APSN"
+constexpr uint32_t kSnapVersion = 1;
+
+struct SnapHeader {
+    uint32_t magic, version;
+    uint32_t width, height;
+    float cell_size;
+    apic_world_props props;
+    uint32_t num_particles, lanes;
+    uint32_t timestamp;
+    float prev_deltatime;
+    int32_t solver_mode;
+    float rel_tol;
+    uint32_t max_iterations;
+    uint32_t has_ext, has_post;
+    uint32_t obstacle_words;  // u64 words
+    uint32_t u_faces, v_faces;
+    uint64_t bytes;           // whole snapshot
+};
+
+uint64_t snap_bytes(uint32_t lanes, uint32_t obstacle_words, uint32_t uf, uint32_t vf, bool ext, bool post) {
+    return sizeof(SnapHeader) + uint64_t(NPF) * lanes * 4 + uint64_t(obstacle_words) * 8 +
+           (ext ? uint64_t(uf + vf) * 4 : 0) + (post ? uint64_t(uf + vf) * 4 : 0);
+}
+
+}  // namespace
+
+int apic_snapshot_bytes(apic_handle* h, uint64_t* bytes) {
+    if (valid_handle(h) || !bytes) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    const Scene& s = h->s;
+    *bytes = snap_bytes(s.npad, even_words(s.cells) / 2, s.uf, s.vf, s.has_ext, s.has_post);
+    return APIC_OK;
+}
+
+int apic_snapshot(apic_handle* h, void* dst, uint64_t bytes) {
+    uint64_t need = 0;
+    int rc = apic_snapshot_bytes(h, &need);
+    if (rc) return rc;
+    if (bytes != need) return fail(APIC_ERR_INVALID_ARG, "size mismatch (apic_snapshot_bytes)");
+    if (!dst) return fail(APIC_ERR_INVALID_ARG, "null destination");
+    Scene& s = h->s;
+    if ((rc = sync_ctl(s))) return rc;
+    SnapHeader hd{};
+    hd.magic = kSnapMagic;
+    hd.version = kSnapVersion;
+    hd.width = s.W;
+    hd.height = s.H;
+    hd.cell_size = s.dx;
+    hd.props = s.props;
+    hd.num_particles = s.n;
+    hd.lanes = s.npad;
+    hd.timestamp = s.ctl_host->timestamp;
+    hd.prev_deltatime = s.ctl_host->prev_dt;
+    hd.solver_mode = s.solver_mode;
+    hd.rel_tol = s.rel_tol;
+    hd.max_iterations = s.max_iter;
+    hd.has_ext = s.has_ext;
+    hd.has_post = s.has_post;
+    hd.obstacle_words = even_words(s.cells) / 2;
+    hd.u_faces = s.uf;
+    hd.v_faces = s.vf;
+    hd.bytes = need;
+    uint8_t* out = static_cast<uint8_t*>(dst);
+    std::memcpy(out, &hd, sizeof(hd));
+    uint64_t off = sizeof(hd);
+    auto take = [&](int field, uint64_t n) {
+        int r = n ? apic_read_field(h, field, out + off, n) : APIC_OK;
+        off += n;
+        return r;
+    };
+    for (int f = APIC_F_POS_X; f <= APIC_F_TRES; ++f)
+        if ((rc = take(f, uint64_t(s.npad) * 4))) return rc;
+    if ((rc = take(APIC_F_OBSTACLE_BITS, uint64_t(hd.obstacle_words) * 8))) return rc;
+    if (s.has_ext && ((rc = take(APIC_F_EXT_FORCE_U, uint64_t(s.uf) * 4)) ||
+                      (rc = take(APIC_F_EXT_FORCE_V, uint64_t(s.vf) * 4))))
+        return rc;
+    if (s.has_post && ((rc = take(APIC_F_POST_FORCE_U, uint64_t(s.uf) * 4)) ||
+                       (rc = take(APIC_F_POST_FORCE_V, uint64_t(s.vf) * 4))))
+        return rc;
+    return APIC_OK;
+}
+
+int apic_restore(apic_handle* h, const void* src, uint64_t bytes) {
+    if (valid_handle(h) || !src) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    if (bytes < sizeof(SnapHeader)) return fail(APIC_ERR_INVALID_ARG, "not a snapshot");
+    Scene& s = h->s;
+    SnapHeader hd;
+    std::memcpy(&hd, src, sizeof(hd));
+    if (hd.magic != kSnapMagic || hd.version != kSnapVersion) return fail(APIC_ERR_INVALID_ARG, "not a snapshot");
+    if (hd.bytes != bytes || hd.lanes < hd.num_particles || hd.lanes % 8 != 0 ||
+        bytes != snap_bytes(hd.lanes, hd.obstacle_words, hd.u_faces, hd.v_faces, hd.has_ext, hd.has_post))
+        return fail(APIC_ERR_INVALID_ARG, "snapshot size mismatch");
+    if (hd.width != s.W || hd.height != s.H || std::memcmp(&hd.cell_size, &s.dx, 4) != 0 ||
+        std::memcmp(&hd.props, &s.props, sizeof(apic_world_props)) != 0 || hd.u_faces != s.uf ||
+        hd.v_faces != s.vf || hd.obstacle_words != even_words(s.cells) / 2)
+        return fail(APIC_ERR_INVALID_ARG, "snapshot of a scene with another grid or world properties");
+    const uint8_t* in = static_cast<const uint8_t*>(src) + sizeof(hd);
+    const float* f[NPF];
+    for (int k = 0; k < NPF; ++k) f[k] = reinterpret_cast<const float*>(in + uint64_t(k) * hd.lanes * 4);
+    // particle count and padding first, then every lane exactly as saved
+    int rc = apic_set_particles(h, hd.num_particles, f[PX], f[PY], f[VX], f[VY]);
+    if (rc) return rc;
+    if (s.npad != hd.lanes) return fail(APIC_ERR_INVALID_ARG, "snapshot lane count differs");
+    for (int k = 0; k < NPF; ++k)
+        if (hd.lanes && (rc = apic_write_field(h, APIC_F_POS_X + k, f[k], uint64_t(hd.lanes) * 4))) return rc;
+    uint64_t off = uint64_t(NPF) * hd.lanes * 4;
+    if ((rc = apic_write_field(h, APIC_F_OBSTACLE_BITS, in + off, uint64_t(hd.obstacle_words) * 8))) return rc;
+    off += uint64_t(hd.obstacle_words) * 8;
+    s.has_ext = s.has_post = false;
+    if (hd.has_ext) {
+        if ((rc = apic_write_field(h, APIC_F_EXT_FORCE_U, in + off, uint64_t(s.uf) * 4))) return rc;
+        if ((rc = apic_write_field(h, APIC_F_EXT_FORCE_V, in + off + uint64_t(s.uf) * 4, uint64_t(s.vf) * 4)))
+            return rc;
+        off += uint64_t(s.uf + s.vf) * 4;
+    }
+    if (hd.has_post) {
+        if ((rc = apic_write_field(h, APIC_F_POST_FORCE_U, in + off, uint64_t(s.uf) * 4))) return rc;
+        if ((rc = apic_write_field(h, APIC_F_POST_FORCE_V, in + off + uint64_t(s.uf) * 4, uint64_t(s.vf) * 4)))
+            return rc;
+    }
+    if ((rc = apic_set_solver(h, hd.solver_mode, hd.rel_tol, hd.max_iterations))) return rc;
+    CK(cudaMemcpy(&s.ctl->timestamp, &hd.timestamp, sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(&s.ctl->prev_dt, &hd.prev_deltatime, sizeof(float), cudaMemcpyHostToDevice));
+    s.vmax_valid = false;
+    return APIC_OK;
+}
+
+int apic_render(apic_handle* h, const apic_render_params* rp, apic_render_stats* out) {
+    if (valid_handle(h) || !rp) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    Scene& s = h->s;
+    const apic_render_params& q = *rp;
+    if (q.width == 0 || q.height == 0 || q.width > 16384 || q.height > 16384)
+        return fail(APIC_ERR_INVALID_ARG, "frame size must be 1..16384 pixels per side");
+    if (!(q.scale > 0.0f) || !std::isfinite(q.scale)) return fail(APIC_ERR_INVALID_ARG, "scale must be > 0");
+    if (!(q.draw_radius > 0.0f) || q.draw_radius > 7.0f)
+        return fail(APIC_ERR_INVALID_ARG, "draw_radius must be in (0, 7]");
+    if (!(q.margin >= 0.0f) || q.margin > 65536.0f) return fail(APIC_ERR_INVALID_ARG, "margin must be in [0, 65536]");
+    if (!std::isfinite(q.pick_x) || !std::isfinite(q.pick_y) || std::isnan(q.pick_radius))
+        return fail(APIC_ERR_INVALID_ARG, "pick centre and radius must be finite");
+    if (uint64_t(s.n) * 4 > 0x7FFFFFFFull) return fail(APIC_ERR_INVALID_ARG, "too many particles to render");
+    RenderParamsDev p{};
+    p.width = q.width;
+    p.height = q.height;
+    p.ntx = div_up(q.width, 16);
+    p.nty = div_up(q.height, 16);
+    p.ntiles = p.ntx * p.nty;
+    p.fw = float(q.width);
+    p.fh = float(q.height);
+    p.scale = q.scale;
+    p.margin = q.margin;
+    p.radius = q.draw_radius;
+    p.size = q.draw_radius * 2.0f;
+    p.pick_x = q.pick_x;
+    p.pick_y = q.pick_y;
+    p.pick_r2 = q.pick_radius < 0.0f ? -1.0f : q.pick_radius * q.pick_radius;
+    p.bg = q.background;
+    RenderResult r{};
+    cudaError_t e = render_frame(s, p, &r);
+    if (e == cudaErrorMemoryAllocation) return fail(APIC_ERR_OOM, "out of device memory (render buffers)");
+    if (e != cudaSuccess) return fail(APIC_ERR_CUDA, std::string("render: ") + cudaGetErrorString(e));
+    if (out) {
+        out->valid = r.valid;
+        out->nan = r.nan;
+        out->out_of_bounds = r.oob;
+        out->fluid_cells = s.ctl_host ? s.ctl_host->fluid_cells : 0u;
+        out->picked = r.picked;
+        out->volume = float(out->fluid_cells) * (s.dx * s.dx);
+        out->kernels = r.kernels;
+    }
+    return APIC_OK;
+}
+
+int apic_read_frame(apic_handle* h, uint8_t* dst, uint64_t bytes) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    uint32_t w = 0, ht = 0;
+    const uint32_t* f = render_frame_ptr(h->s, &w, &ht);
+    if (!f) return fail(APIC_ERR_INVALID_ARG, "no frame rendered yet");
+    if (bytes != uint64_t(w) * ht * 4) return fail(APIC_ERR_INVALID_ARG, "size mismatch");
+    if (!dst) return fail(APIC_ERR_INVALID_ARG, "null destination");
+    CK(cudaMemcpyAsync(dst, f, bytes, cudaMemcpyDeviceToHost, h->s.stream));
+    CK(cudaStreamSynchronize(h->s.stream));
+    return APIC_OK;
+}
+
+int apic_frame_device_ptr(apic_handle* h, void** ptr, uint32_t* width, uint32_t* height) {
+    if (valid_handle(h) || !ptr || !width || !height) return fail(APIC_ERR_INVALID_ARG, "null argument");
+    uint32_t w = 0, ht = 0;
+    const uint32_t* f = render_frame_ptr(h->s, &w, &ht);
+    if (!f) return fail(APIC_ERR_INVALID_ARG, "no frame rendered yet");
+    *ptr = const_cast<uint32_t*>(f);
+    *width = w;
+    *height = ht;
     return APIC_OK;
 }
 

@@ -606,6 +606,148 @@ def run_served(args):
     print(json.dumps(line), flush=True)
 
 
+def run_criterion(args):
+    """The reference's own benchmark shape (benches/fluid_benchmark.rs:5-41):
+    Apic::new(size, size, 1.0) with its default particle block for sizes
+    64..1024, 15 warm-up update(0.016) calls, then timed update(0.016) calls,
+    through the C-ABI (apic_update returns after the update, as Apic::update
+    does); the CPU restatement runs the same sequence per size."""
+    import apic_gb300 as A
+    from apic_gb300 import build as gpu_build
+    from oracle.oracle import OracleSim
+    gpu_build.build()
+    import torch
+    torch.cuda.set_device(0)
+    dt, warm = 0.016, 15
+    solver = {"reference": A.SOLVER_REFERENCE, "fp32": A.SOLVER_REL_FP32, "mixed": A.SOLVER_REL_MIXED}[
+        args.criterion_solver]
+    threads = os.cpu_count() or 1
+    rows = []
+    with ClockSampler(0) as clocks:
+        for size in (64, 128, 256, 512, 1024):
+            g = A.Apic(size, size, 1.0, props(A))
+            g.set_solver(solver, 1e-6, 500 if solver != A.SOLVER_REFERENCE else 100)
+            n = g.num_particles
+            for _ in range(warm):
+                g.update(A.DebugOptions(), dt)
+            g.synchronize()
+            wall, sub = [], 0
+            for _ in range(args.steps):
+                t0 = time.perf_counter()
+                g.update(A.DebugOptions(), dt)
+                wall.append(time.perf_counter() - t0)
+                sub += g.stats().substeps
+            g.close()
+            row = {"size": f"{size}x{size}", "particles": n, "gpu_ms_mean": 1e3 * float(np.mean(wall)),
+                   "gpu_ms_p50": 1e3 * float(np.percentile(wall, 50)),
+                   "gpu_particle_steps_per_s": n * sub / sum(wall), "substeps": sub}
+            if not args.no_cpu_baseline:
+                px, py, vx, vy = A.generate_scene(A.scene_params(A.SCENE_REFERENCE_DEFAULT, size, size,
+                                                                 cell_size=1.0))
+                o = OracleSim(size, size, 1.0, props(A), threads=threads)
+                o.set_particles(px, py, vx, vy)
+                o.set_solver(solver, 1e-6, 500 if solver != A.SOLVER_REFERENCE else 100)
+                for _ in range(warm):
+                    o.update(A.DebugOptions(), dt)
+                ct, csub, t_start = [], 0, time.perf_counter()
+                for _ in range(args.steps):
+                    t0 = time.perf_counter()
+                    o.update(A.DebugOptions(), dt)
+                    ct.append(time.perf_counter() - t0)
+                    csub += o.stats().substeps
+                    if time.perf_counter() - t_start > args.cpu_budget / 5:
+                        break
+                o.close()
+                row.update({"cpu_ms_mean": 1e3 * float(np.mean(ct)), "cpu_updates": len(ct),
+                            "cpu_particle_steps_per_s": n * csub / sum(ct),
+                            "gpu_vs_cpu": (n * sub / sum(wall)) / (n * csub / sum(ct))})
+            rows.append(row)
+    last = rows[-1]
+    line = {
+        "metric": METRIC, "value": last["gpu_particle_steps_per_s"], "unit": METRIC, "workload": "criterion",
+        "n_gpus": 1, "steps": args.steps, "warmup": warm, "higher_is_better": True, "data": "synthetic",
+        "config": {"workload": "benches/fluid_benchmark.rs shape: Apic::new(size, size, 1.0) default particle "
+                               "block, gravity -9.81, damping 0.1, cfl 5, 15 warm-up update(0.016), timed "
+                               "update(0.016); value = the 1024x1024 case",
+                   "solver": args.criterion_solver, "unit": UNIT_NOTE,
+                   "cpu": f"C++ restatement, OpenMP {threads} threads" if not args.no_cpu_baseline else None,
+                   "timing": "wall clock per apic_update call (returns when the update is done)"},
+        "sizes": rows, "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_render(args):
+    """The headless particle view (render_particles, src/main.rs:207-277) of the
+    1024^2 bench scene after its warm-up updates: 1.13 M particles splatted
+    into a 1920 x 1080 RGBA8 frame (the domain fills the frame's height)."""
+    import apic_gb300 as A
+    from apic_gb300 import build as gpu_build
+    from oracle import oracle as O
+    gpu_build.build()
+    import torch
+    torch.cuda.set_device(0)
+    side = args.side
+    sim = A.Apic(side, side, 1.0 / side, props(A))
+    px, py, vx, vy = A.generate_scene(scene_params(A, side))
+    sim.set_particles(px, py, vx, vy)
+    sim.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+    for _ in range(args.warmup):
+        sim.update(A.DebugOptions(), FRAME_DT)
+    n = sim.num_particles
+    rp = A.render_params(width=1920, height=1080, scale=1080.0)
+    ext = torch.cuda.ExternalStream(ctypes_stream(sim))
+    for _ in range(3):
+        sim.render(rp, read=False)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    kernels = 0
+    with ClockSampler(0) as clocks:
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ev[k][0].record(ext)
+            _, st = sim.render(rp, read=False)
+            ev[k][1].record(ext)
+            kernels += st.kernels
+        torch.cuda.synchronize()
+    dev_ms = [a.elapsed_time(b) for a, b in ev]
+    # end to end: render + frame to host memory, wall clock
+    frame_h = torch.empty((1080, 1920, 4), dtype=torch.uint8).pin_memory()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.render(rp, read=False)
+        A._check(A.load_library().apic_read_frame(sim._h, A.ctypes.c_void_p(frame_h.data_ptr()), frame_h.numel()),
+                 "apic_read_frame")
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    frame, st = sim.render(rp)
+    cpu = None
+    if not args.no_cpu_baseline:
+        q = [sim.read_field(f)[:n] for f in ("pos_x", "pos_y", "vel_x", "vel_y")]
+        t0 = time.perf_counter()
+        ref, _ = O.render(*q, rp)
+        cpu_s = time.perf_counter() - t0
+        cpu = {"value": n / cpu_s, "unit": "particles splatted/s", "cores": 1, "kind": "port",
+               "sample": "one frame of the same particles (oracle draw loop, 1 thread)",
+               "frame_identical": bool(np.array_equal(ref, frame))}
+    mean_ms = float(np.mean(dev_ms))
+    line = {
+        "metric": "particles splatted/s", "value": n / (mean_ms / 1e3), "unit": "particles/s", "workload": "render",
+        "n_gpus": 1, "steps": args.steps, "warmup": 3, "higher_is_better": True, "data": "synthetic",
+        "ms_per_frame": mean_ms, "frame_ms_p50": float(np.percentile(dev_ms, 50)),
+        "config": {"workload": f"{workload_name(side)}, after {args.warmup} updates; 1920x1080 RGBA8 frame, "
+                               f"1080 px per unit, 3 px discs", "particles": n,
+                   "l2": "flushed (256 MB write) before each frame"},
+        "stats": {"valid": st.valid, "nan": st.nan, "out_of_bounds": st.out_of_bounds, "kernels": st.kernels},
+        "e2e": {"value": n / e2e_s, "unit": "particles/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(frame_h.numel()),
+                "what": "apic_render + apic_read_frame to pinned host memory, wall clock"},
+        "gpu_launches": kernels, "clocks": clocks.summary(), "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    sim.close()
+
+
 def set_stress(args):
     """Switch the module to config 3 (scene, frame dt, default side)."""
     global STRESS, FRAME_DT, SIDE
@@ -642,9 +784,13 @@ def main():
                     help="keep the middle multigrid levels in global memory instead of a cluster's shared memory")
     ap.add_argument("--no-pdl", action="store_true",
                     help="launch the PCG loop's kernels in plain stream order")
-    ap.add_argument("--workload", default="single", choices=["single", "stress", "batched", "served"],
+    ap.add_argument("--workload", default="single", choices=["single", "stress", "batched", "served", "criterion",
+                                                             "render"],
                     help="single: the 1024^2 scene (default); stress: config 3 (4096^2 noise scene); "
-                         "batched: config 4; served: config 5")
+                         "batched: config 4; served: config 5; criterion: the reference's own bench shape "
+                         "(sizes 64..1024, cell 1.0, update(0.016)); render: the headless particle view")
+    ap.add_argument("--criterion-solver", default="reference", choices=["reference", "fp32", "mixed"],
+                    help="criterion: pressure solver (reference: the reference's exit rule)")
     ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")
     ap.add_argument("--compare-steps", type=int, default=5, help="batched: updates compared with the plain path")
     ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
@@ -666,6 +812,10 @@ def main():
         run_batched(args)
     elif args.workload == "served":
         run_served(args)
+    elif args.workload == "criterion":
+        run_criterion(args)
+    elif args.workload == "render":
+        run_render(args)
     else:
         run_gpu_arm(args, world, rank, local)
     if world > 1:

@@ -339,6 +339,57 @@ int apic_server_request(apic_server* sv, uint64_t id, apic_request_info* out);
 int apic_server_result_positions(apic_server* sv, uint64_t id, float* dst, uint64_t floats);
 int apic_server_get_stats(apic_server* sv, apic_server_stats* out);
 
+/* ---- snapshot / restore ------------------------------------------------ */
+/* No counterpart in the reference (its state lives in the Apic struct's pub
+ * fields, src/apic.rs:716-775).  A snapshot is a host byte blob of the state
+ * that a later apic_update reads: the nine particle arrays with their padding
+ * lanes, the obstacle mask, pending external and post forces, timestamp and
+ * prev_deltatime, and the solver settings.  apic_restore loads it into a handle
+ * created with the same width, height, cell size and world properties; the
+ * next updates of both handles then compute the same thing. */
+int apic_snapshot_bytes(apic_handle* h, uint64_t* bytes);
+int apic_snapshot(apic_handle* h, void* dst, uint64_t bytes);
+int apic_restore(apic_handle* h, const void* src, uint64_t bytes);
+
+/* ---- headless particle view -------------------------------------------- */
+/* Replaces the GUI's particle drawing (render_particles, src/main.rs:207-277,
+ * with make_circle_texture, :73-101) by a frame in device memory: each
+ * particle with finite coordinates inside the frame plus `margin` is splatted,
+ * in particle order, as a 2*draw_radius pixel quad textured with the 32 x 32
+ * anti-aliased disc, tinted r = min(0.01 |v|^2, 1), g = 0.5, b = 1 - r/2, and
+ * alpha blended into an RGBA8 frame cleared to `background`.  Pixel (px, py)
+ * has its centre at (px + 0.5, py + 0.5); row 0 is the top of the view:
+ * draw_x = x * scale, draw_y = height - y * scale (the GUI's default camera,
+ * :222-235).  The GL window, its camera zoom/pan and the text HUD are not
+ * rendered (no graphics stack is used). */
+typedef struct apic_render_params {
+    uint32_t width, height;  /* frame in pixels (1920 x 1080 in the GUI, src/main.rs:26-27); 1..16384 */
+    float scale;             /* pixels per world unit (SIM_SCALE, :34) */
+    float draw_radius;       /* disc radius in pixels (DRAW_RADIUS = 3, :35); (0, 7] */
+    float margin;            /* out-of-bounds margin in pixels (50, :237-240); [0, 65536] */
+    float pick_x, pick_y;    /* pick centre in pixels (:247-256) */
+    float pick_radius;       /* pick radius in pixels; < 0: no pick */
+    uint32_t background;     /* clear colour, RGBA8 little-endian (0xFF000000: clear_background(BLACK)) */
+} apic_render_params;
+
+typedef struct apic_render_stats {
+    uint32_t valid, nan, out_of_bounds;  /* RenderStats (:39-43) */
+    uint32_t fluid_cells;                /* base fluid cells of the last substep */
+    int64_t picked;                      /* nearest particle within pick_radius (first on ties); -1: none */
+    float volume;                        /* fluid_cells * cell_size^2 (:461-468) */
+    uint32_t kernels;                    /* kernels launched for the frame */
+} apic_render_stats;
+
+/* Render the particles into the scene's frame (device memory, allocated on
+ * first use and kept until the handle is destroyed) and wait for it. */
+int apic_render(apic_handle* h, const apic_render_params* params, apic_render_stats* stats);
+/* Copy the last frame to host memory: width * height * 4 bytes, rows top to
+ * bottom, bytes R, G, B, A per pixel. */
+int apic_read_frame(apic_handle* h, uint8_t* dst, uint64_t bytes);
+/* Device address and size of the last frame (valid until the next apic_render
+ * or apic_destroy), for consumers that keep it on the GPU. */
+int apic_frame_device_ptr(apic_handle* h, void** ptr, uint32_t* width, uint32_t* height);
+
 /* ---- testing hook ------------------------------------------------------ */
 /* Run one stage of the substep on the current device state with substep dt.
  * Derived device structures (fluid lists, segment lists) are rebuilt from the

@@ -1522,6 +1522,113 @@ int oracle_write_field(oracle_sim* o, int field, const void* src, uint64_t bytes
     });
 }
 
+// ---- headless particle view ----------------------------------------------
+// render_particles (src/main.rs:207-277) as a sequential loop over the
+// particles in index order, each drawn as a textured quad into an RGBA8
+// frame: texture of make_circle_texture (:73-101), bilinear clamp-to-edge
+// sampling with texel centres at (i + 0.5) / 32, a pixel covered when its
+// centre lies in [x0, x0 + 2R), blend src*a + dst*(1 - a) rounded to 8 bits
+// after every particle.
+static uint8_t circle_alpha(int x, int y) {
+    const float radius = 32.0f / 2.0f;
+    const float dx = float(x) - radius + 0.5f;
+    const float dy = float(y) - radius + 0.5f;
+    const float dist = std::sqrt(dx * dx + dy * dy);
+    if (dist < radius - 1.0f) return 255;
+    if (dist < radius) {
+        const float a = (radius - dist) * 255.0f;  // Rust `as u8` saturates
+        return a >= 255.0f ? 255 : (a > 0.0f ? uint8_t(a) : 0);
+    }
+    return 0;
+}
+
+static uint8_t blend8(float c, float a, uint8_t dst) {
+    const float d = float(dst) / 255.0f;
+    const float o = c * a + d * (1.0f - a);
+    const float q = o * 255.0f + 0.5f;
+    return q >= 255.0f ? 255 : (q > 0.0f ? uint8_t(q) : 0);
+}
+
+int oracle_render(uint32_t n, const float* px, const float* py, const float* vx, const float* vy,
+                  const apic_render_params* rp, uint32_t fluid_cells, float cell_size, uint8_t* rgba,
+                  apic_render_stats* st) {
+    if (!rp || !rgba || !st || (n && (!px || !py || !vx || !vy))) return APIC_ERR_INVALID_ARG;
+    const apic_render_params& p = *rp;
+    const uint32_t W = p.width, H = p.height;
+    float tex[32 * 32];
+    for (int y = 0; y < 32; ++y)
+        for (int x = 0; x < 32; ++x) tex[y * 32 + x] = float(circle_alpha(x, y)) / 255.0f;
+    for (uint64_t i = 0; i < uint64_t(W) * H; ++i) {
+        rgba[i * 4 + 0] = uint8_t(p.background & 0xFFu);
+        rgba[i * 4 + 1] = uint8_t((p.background >> 8) & 0xFFu);
+        rgba[i * 4 + 2] = uint8_t((p.background >> 16) & 0xFFu);
+        rgba[i * 4 + 3] = 255;
+    }
+    const float fw = float(W), fh = float(H);
+    const float R = p.draw_radius, S = p.draw_radius * 2.0f;
+    const float pick_r2 = p.pick_radius < 0.0f ? -1.0f : p.pick_radius * p.pick_radius;
+    float best = INFINITY;
+    int64_t picked = -1;
+    uint32_t valid = 0, nan = 0, oob = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const float x = px[i], y = py[i];
+        if (!std::isfinite(x) || !std::isfinite(y)) {
+            ++nan;
+            continue;
+        }
+        const float draw_x = x * p.scale;
+        const float draw_y = fh - y * p.scale;
+        if (draw_x < -p.margin || draw_x > fw + p.margin || draw_y < -p.margin || draw_y > fh + p.margin) {
+            ++oob;
+            continue;
+        }
+        ++valid;
+        if (pick_r2 >= 0.0f) {
+            const float dx = draw_x - p.pick_x;
+            const float dy = draw_y - p.pick_y;
+            const float d2 = dx * dx + dy * dy;
+            if (d2 <= pick_r2 && d2 < best) {
+                best = d2;
+                picked = i;
+            }
+        }
+        const float speed_sq = vx[i] * vx[i] + vy[i] * vy[i];
+        const float r = std::fmin(speed_sq * 0.01f, 1.0f);  // f32::min ignores a NaN operand, as fmin does
+        const float g = 0.5f, b = 1.0f - r * 0.5f;
+        const float qx = draw_x - R, qy = draw_y - R;
+        // pixels whose centres can lie in [q, q + S): a window one pixel wider
+        const long x_lo = std::max(0L, long(std::floor(qx)) - 1), x_hi = std::min(long(W) - 1, long(std::floor(qx + S)) + 1);
+        const long y_lo = std::max(0L, long(std::floor(qy)) - 1), y_hi = std::min(long(H) - 1, long(std::floor(qy + S)) + 1);
+        for (long pyi = y_lo; pyi <= y_hi; ++pyi)
+            for (long pxi = x_lo; pxi <= x_hi; ++pxi) {
+                const float cx = float(pxi) + 0.5f, cy = float(pyi) + 0.5f;
+                if (!(qx <= cx && cx < qx + S && qy <= cy && cy < qy + S)) continue;
+                const float u = (cx - qx) / S * 32.0f - 0.5f;
+                const float v = (cy - qy) / S * 32.0f - 0.5f;
+                const float fu = std::floor(u), fv = std::floor(v);
+                const float wu = u - fu, wv = v - fv;
+                const int iu = int(fu), iv = int(fv);
+                const int u0 = std::min(std::max(iu, 0), 31), u1 = std::min(std::max(iu + 1, 0), 31);
+                const int v0 = std::min(std::max(iv, 0), 31), v1 = std::min(std::max(iv + 1, 0), 31);
+                const float top = tex[v0 * 32 + u0] * (1.0f - wu) + tex[v0 * 32 + u1] * wu;
+                const float bot = tex[v1 * 32 + u0] * (1.0f - wu) + tex[v1 * 32 + u1] * wu;
+                const float a = top * (1.0f - wv) + bot * wv;
+                uint8_t* d = rgba + (uint64_t(pyi) * W + uint64_t(pxi)) * 4;
+                d[0] = blend8(r, a, d[0]);
+                d[1] = blend8(g, a, d[1]);
+                d[2] = blend8(b, a, d[2]);
+            }
+    }
+    st->valid = valid;
+    st->nan = nan;
+    st->out_of_bounds = oob;
+    st->fluid_cells = fluid_cells;
+    st->picked = picked;
+    st->volume = float(fluid_cells) * (cell_size * cell_size);
+    st->kernels = 0;
+    return APIC_OK;
+}
+
 uint32_t oracle_morton(uint32_t x, uint32_t y) { return morton(x, y); }
 float oracle_random_lane(uint32_t slot, uint32_t seed) { return random_lane(slot, seed); }
 float oracle_temporal_weight(float tau) { return temporal_w(tau); }

@@ -43,6 +43,11 @@ int  oracle_get_stats(oracle_sim* o, apic_step_stats* out);
 int  oracle_field_shape(oracle_sim* o, int field, uint64_t* count, uint32_t* elem_bytes);
 int  oracle_read_field(oracle_sim* o, int field, void* dst, uint64_t bytes);
 int  oracle_write_field(oracle_sim* o, int field, const void* src, uint64_t bytes);
+/* Headless particle view (src/main.rs:73-101, :207-277): RGBA8 frame of
+ * width * height * 4 bytes into rgba, stats as apic_render returns them. */
+int  oracle_render(uint32_t n, const float* px, const float* py, const float* vx, const float* vy,
+                   const apic_render_params* params, uint32_t fluid_cells, float cell_size, uint8_t* rgba,
+                   apic_render_stats* stats);
 /* Stand-alone helpers for known-answer tests. */
 uint32_t oracle_morton(uint32_t x, uint32_t y);
 float    oracle_random_lane(uint32_t slot, uint32_t seed);

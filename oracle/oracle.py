@@ -13,7 +13,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "apic-fluid-simulation_gb300"))
-from apic_gb300 import FIELDS, STAGES, InfoC, StatsC, WorldPropsC, WorldProperties  # noqa: E402
+from apic_gb300 import (FIELDS, STAGES, InfoC, RenderParamsC, RenderStatsC, StatsC, WorldPropsC,  # noqa: E402
+                        WorldProperties)
 
 from . import build as _build  # noqa: E402
 
@@ -47,6 +48,8 @@ def load(rebuild: bool = True) -> ctypes.CDLL:
                                               ctypes.POINTER(ctypes.c_uint32)]),
         "oracle_read_field": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_uint64]),
         "oracle_write_field": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_uint64]),
+        "oracle_render": (ctypes.c_int, [ctypes.c_uint32, _FP, _FP, _FP, _FP, ctypes.POINTER(RenderParamsC),
+                                         ctypes.c_uint32, ctypes.c_float, _VP, ctypes.POINTER(RenderStatsC)]),
         "oracle_morton": (ctypes.c_uint32, [ctypes.c_uint32, ctypes.c_uint32]),
         "oracle_random_lane": (ctypes.c_float, [ctypes.c_uint32, ctypes.c_uint32]),
         "oracle_temporal_weight": (ctypes.c_float, [ctypes.c_float]),
@@ -168,3 +171,17 @@ def random_lane(slot: int, seed: int) -> float:
 
 def temporal_weight(tau: float) -> float:
     return float(load().oracle_temporal_weight(tau))
+
+
+def render(px, py, vx, vy, params: RenderParamsC, fluid_cells: int = 0, cell_size: float = 0.0):
+    """The oracle's frame (height x width x 4 uint8) and RenderStatsC for the
+    particles given as float32 arrays, drawn in index order."""
+    lib = load()
+    arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (px, py, vx, vy)]
+    n = len(arrs[0])
+    frame = np.empty((params.height, params.width, 4), dtype=np.uint8)
+    st = RenderStatsC()
+    ptr = [a.ctypes.data_as(_FP) for a in arrs]
+    _ck(lib.oracle_render(n, *ptr, ctypes.byref(params), fluid_cells, cell_size, frame.ctypes.data_as(_VP),
+                          ctypes.byref(st)), "oracle_render")
+    return frame, st
