@@ -31,6 +31,7 @@ OPT_CLUSTER_VCYCLE = 3
 OPT_PDL = 4
 OPT_DSM_VCYCLE = 5
 OPT_CLUSTER_SOLVE = 6
+OPT_WARM_START = 7
 
 FIELDS = {
     "pos_x": 0, "pos_y": 1, "vel_x": 2, "vel_y": 3, "cu_x": 4, "cu_y": 5, "cv_x": 6, "cv_y": 7, "tres": 8,

@@ -175,6 +175,7 @@ struct Scene {
     double* p64 = nullptr;                    // FP64 pressure of the refinement loop (padded)
     double* b64 = nullptr;                    // FP64 right-hand side (padded)
     bool p64_valid = false;                   // p64 holds the refined pressure (mixed mode)
+    bool warm_start = true;                   // mixed mode: start from the previous solve's FP64 pressure
 
     int nlevels = 0;                          // including the base (levels[0])
     int tail_first = 0;                       // first level of the shared-memory tail (nlevels: none)
@@ -234,6 +235,9 @@ struct Scene {
 cudaError_t launch_sort(Scene& s);
 // Exclusive scan of data[0..n) in place; tmp holds div_up(n, 1024) words.
 cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t n, uint32_t* tmp, cudaStream_t st);
+// The mixed-precision solve starts from the FP64 pressure that the previous
+// solve left in p64 (zeroed whenever the particle set is replaced).
+inline int warm_start(const Scene& s) { return s.warm_start && s.solver_mode == APIC_SOLVER_REL_MIXED ? 1 : 0; }
 // render.cu: splat the particles into the scene's frame and wait for it
 cudaError_t render_frame(Scene& s, const RenderParamsDev& p, RenderResult* out);
 const uint32_t* render_frame_ptr(const Scene& s, uint32_t* width, uint32_t* height);

@@ -220,14 +220,16 @@ __device__ __forceinline__ void ph_search(const Level& B, uint32_t nseg, uint32_
 // ---- FP64 refinement (APIC_SOLVER_REL_MIXED) ---------------------------------
 
 // b64 = res, p64 = 0; returns ||b||^2.
+// warm: keep p64 as the previous solve left it (the initial guess of the
+// refinement), else start from zero.
 __device__ __forceinline__ double ph_mixed_init(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
-                                                double* b64, double* p64) {
+                                                double* b64, double* p64, int warm) {
     double bb = 0;
     APIC_BASE_LOOP(B, nseg, warp, nwarps) {
         uint32_t c = word_ * 32 + lane_ + B.w;
         double b = double(B.res[c]);
         b64[c] = b;
-        p64[c] = 0.0;
+        if (!warm) p64[c] = 0.0;
         bb += b * b;
     }
     return bb;

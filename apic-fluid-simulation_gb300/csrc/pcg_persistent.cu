@@ -48,6 +48,7 @@ struct SolveArgs {
     Ctl* ctl;
     GridSync* gs;
     int mode;
+    int warm;  // mixed mode starts from the previous solve's FP64 pressure
     float solve_error;
     double tol;
     uint32_t max_iter;
@@ -306,7 +307,7 @@ __device__ bool solve(Ctx& c) {
         return true;
     }
     double bnorm2;
-    if (!grid_sum(c, pcg::ph_mixed_init(B, n0, c.warp, c.nwarps, a.b64, a.p64), bnorm2)) return false;
+    if (!grid_sum(c, pcg::ph_mixed_init(B, n0, c.warp, c.nwarps, a.b64, a.p64, a.warm), bnorm2)) return false;
     pcg::ph_clear_pressure(B, n0, c.warp, c.nwarps, a.pressure);
     if (a.mode == APIC_SOLVER_REL_FP32) {
         LoopOut o;
@@ -447,6 +448,7 @@ static SolveArgs solve_args(Scene& s, uint32_t* words) {
     a.ctl = s.ctl;
     a.gs = s.gsync;
     a.mode = s.solver_mode;
+    a.warm = warm_start(s);
     a.solve_error = s.props.solve_error;
     a.tol = double(s.rel_tol);
     a.max_iter = s.max_iter;
@@ -488,6 +490,7 @@ cudaError_t enqueue_persistent_solve(Scene& s) {
     a.ctl = s.ctl;
     a.gs = s.gsync;
     a.mode = s.solver_mode;
+    a.warm = warm_start(s);
     a.solve_error = s.props.solve_error;
     a.tol = double(s.rel_tol);
     a.max_iter = s.max_iter;

@@ -286,6 +286,8 @@ int load_particles(apic_handle* h, uint32_t n, const float* px, const float* py,
         CK(dalloc(&s.sort_hist, size_t(256) * nb));
         CK(dalloc(&s.sort_scan_tmp, div_up(uint64_t(256) * nb, 1024) + 1));
     }
+    // a new particle set: the next mixed solve starts from zero pressure
+    if (s.p64) CK(cudaMemset(s.p64, 0, sizeof(double) * (uint64_t(s.cells) + 2ull * s.W)));
     std::vector<float> buf(std::max<uint32_t>(npad, 1), 0.0f);
     auto put = [&](int f, const float* src, bool pad_last) -> int {
         std::fill(buf.begin(), buf.end(), 0.0f);
@@ -986,20 +988,26 @@ struct SnapHeader {
     uint32_t has_ext, has_post;
     uint32_t obstacle_words;  // u64 words
     uint32_t u_faces, v_faces;
+    uint32_t p64_words;       // FP64 pressure kept for the next mixed solve's start (0: none)
+    uint32_t pad;
     uint64_t bytes;           // whole snapshot
 };
 
-uint64_t snap_bytes(uint32_t lanes, uint32_t obstacle_words, uint32_t uf, uint32_t vf, bool ext, bool post) {
+uint64_t snap_bytes(uint32_t lanes, uint32_t obstacle_words, uint32_t uf, uint32_t vf, bool ext, bool post,
+                    uint32_t p64_words) {
     return sizeof(SnapHeader) + uint64_t(NPF) * lanes * 4 + uint64_t(obstacle_words) * 8 +
-           (ext ? uint64_t(uf + vf) * 4 : 0) + (post ? uint64_t(uf + vf) * 4 : 0);
+           (ext ? uint64_t(uf + vf) * 4 : 0) + (post ? uint64_t(uf + vf) * 4 : 0) + uint64_t(p64_words) * 8;
 }
+
+// The warm start of the mixed solve reads the last solve's FP64 pressure.
+uint32_t snap_p64_words(const Scene& s) { return warm_start(s) ? s.cells + 2 * s.W : 0u; }
 
 }  // namespace
 
 int apic_snapshot_bytes(apic_handle* h, uint64_t* bytes) {
     if (valid_handle(h) || !bytes) return fail(APIC_ERR_INVALID_ARG, "null argument");
     const Scene& s = h->s;
-    *bytes = snap_bytes(s.npad, even_words(s.cells) / 2, s.uf, s.vf, s.has_ext, s.has_post);
+    *bytes = snap_bytes(s.npad, even_words(s.cells) / 2, s.uf, s.vf, s.has_ext, s.has_post, snap_p64_words(s));
     return APIC_OK;
 }
 
@@ -1030,6 +1038,7 @@ int apic_snapshot(apic_handle* h, void* dst, uint64_t bytes) {
     hd.obstacle_words = even_words(s.cells) / 2;
     hd.u_faces = s.uf;
     hd.v_faces = s.vf;
+    hd.p64_words = snap_p64_words(s);
     hd.bytes = need;
     uint8_t* out = static_cast<uint8_t*>(dst);
     std::memcpy(out, &hd, sizeof(hd));
@@ -1048,6 +1057,7 @@ int apic_snapshot(apic_handle* h, void* dst, uint64_t bytes) {
     if (s.has_post && ((rc = take(APIC_F_POST_FORCE_U, uint64_t(s.uf) * 4)) ||
                        (rc = take(APIC_F_POST_FORCE_V, uint64_t(s.vf) * 4))))
         return rc;
+    if (hd.p64_words) CK(cudaMemcpy(out + off, s.p64, uint64_t(hd.p64_words) * 8, cudaMemcpyDeviceToHost));
     return APIC_OK;
 }
 
@@ -1059,11 +1069,13 @@ int apic_restore(apic_handle* h, const void* src, uint64_t bytes) {
     std::memcpy(&hd, src, sizeof(hd));
     if (hd.magic != kSnapMagic || hd.version != kSnapVersion) return fail(APIC_ERR_INVALID_ARG, "not a snapshot");
     if (hd.bytes != bytes || hd.lanes < hd.num_particles || hd.lanes % 8 != 0 ||
-        bytes != snap_bytes(hd.lanes, hd.obstacle_words, hd.u_faces, hd.v_faces, hd.has_ext, hd.has_post))
+        bytes != snap_bytes(hd.lanes, hd.obstacle_words, hd.u_faces, hd.v_faces, hd.has_ext, hd.has_post,
+                            hd.p64_words))
         return fail(APIC_ERR_INVALID_ARG, "snapshot size mismatch");
     if (hd.width != s.W || hd.height != s.H || std::memcmp(&hd.cell_size, &s.dx, 4) != 0 ||
         std::memcmp(&hd.props, &s.props, sizeof(apic_world_props)) != 0 || hd.u_faces != s.uf ||
-        hd.v_faces != s.vf || hd.obstacle_words != even_words(s.cells) / 2)
+        hd.v_faces != s.vf || hd.obstacle_words != even_words(s.cells) / 2 ||
+        (hd.p64_words != 0 && hd.p64_words != s.cells + 2 * s.W))
         return fail(APIC_ERR_INVALID_ARG, "snapshot of a scene with another grid or world properties");
     const uint8_t* in = static_cast<const uint8_t*>(src) + sizeof(hd);
     const float* f[NPF];
@@ -1088,7 +1100,9 @@ int apic_restore(apic_handle* h, const void* src, uint64_t bytes) {
         if ((rc = apic_write_field(h, APIC_F_POST_FORCE_U, in + off, uint64_t(s.uf) * 4))) return rc;
         if ((rc = apic_write_field(h, APIC_F_POST_FORCE_V, in + off + uint64_t(s.uf) * 4, uint64_t(s.vf) * 4)))
             return rc;
+        off += uint64_t(s.uf + s.vf) * 4;
     }
+    if (hd.p64_words) CK(cudaMemcpy(s.p64, in + off, uint64_t(hd.p64_words) * 8, cudaMemcpyHostToDevice));
     if ((rc = apic_set_solver(h, hd.solver_mode, hd.rel_tol, hd.max_iterations))) return rc;
     CK(cudaMemcpy(&s.ctl->timestamp, &hd.timestamp, sizeof(uint32_t), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(&s.ctl->prev_dt, &hd.prev_deltatime, sizeof(float), cudaMemcpyHostToDevice));
@@ -1200,6 +1214,10 @@ int apic_set_option(apic_handle* h, int option, int value) {
             plan_cluster_solve(s);
             invalidate_graphs(s);
             return APIC_OK;
+        case APIC_OPT_WARM_START:
+            s.warm_start = value != 0;
+            invalidate_graphs(s);
+            return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }
@@ -1217,6 +1235,7 @@ int apic_get_option(apic_handle* h, int option, int* value) {
             *value = (h->s.use_dsm && h->s.dsm_first < h->s.dsm_tail) ? 1 : 0;
             return APIC_OK;
         case APIC_OPT_CLUSTER_SOLVE: *value = h->s.cluster_solve_ctas; return APIC_OK;
+        case APIC_OPT_WARM_START: *value = h->s.warm_start ? 1 : 0; return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }

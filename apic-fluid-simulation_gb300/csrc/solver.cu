@@ -133,11 +133,11 @@ __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, double*
 
 // ---- FP64 refinement helpers (APIC_SOLVER_REL_MIXED) ----------------------
 
-// b64 = res, p64 = 0 and ||b||^2.
+// b64 = res, p64 = 0 (unless warm) and ||b||^2.
 __global__ void __launch_bounds__(kSegBlock) k_mixed_init(Level B, double* b64, double* p64, Ctl* ctl,
-                                                          double* partials) {
+                                                          double* partials, int warm) {
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->solve_t0 = global_ns();  // the relative-mode solve starts here
-    double bb = pcg::ph_mixed_init(B, ctl->seg_count[0], gwarp(), gnwarps(), b64, p64);
+    double bb = pcg::ph_mixed_init(B, ctl->seg_count[0], gwarp(), gnwarps(), b64, p64, warm);
     double tot;
     if (block_sum_last<kSegBlock>(bb, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) ctl->bnorm2 = tot;
 }
@@ -287,7 +287,7 @@ cudaError_t build_solve(Scene& s, GraphCursor& c) {
     const double tol = double(s.rel_tol);
     e = capture_into(s, c, [&]() {
         cudaStream_t st = s.stream;
-        k_mixed_init<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.ctl, s.partials);
+        k_mixed_init<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.ctl, s.partials, warm_start(s));
         k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
         k_rel_begin<<<1, 1, 0, st>>>(s.ctl, tol, s.max_iter);
         return cudaGetLastError();
@@ -381,7 +381,7 @@ cudaError_t run_solve_eager(Scene& s) {
         return cudaGetLastError();
     }
     const double tol = double(s.rel_tol);
-    k_mixed_init<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.ctl, s.partials);
+    k_mixed_init<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.ctl, s.partials, warm_start(s));
     k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
     k_rel_begin<<<1, 1, 0, st>>>(s.ctl, tol, s.max_iter);
     if (mode == APIC_SOLVER_REL_FP32) {

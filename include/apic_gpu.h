@@ -251,6 +251,13 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
  * differently.  Profiling runs (apic_set_profiling) keep the per-phase
  * kernels. */
 #define APIC_OPT_CLUSTER_SOLVE 6
+/* No counterpart in the reference (whose PCG starts from zero).  Value 1
+ * (default): in APIC_SOLVER_REL_MIXED each solve starts from the FP64
+ * pressure of the previous solve (zero after apic_set_particles or
+ * apic_restore) instead of zero; the exit test, true residual <= rel_tol of
+ * ||b||, is unchanged, so only the iteration count differs.  0: start from
+ * zero.  Other solver modes always start from zero. */
+#define APIC_OPT_WARM_START 7
 int apic_set_option(apic_handle* h, int option, int value);
 int apic_get_option(apic_handle* h, int option, int* value);
 
@@ -344,9 +351,11 @@ int apic_server_get_stats(apic_server* sv, apic_server_stats* out);
  * fields, src/apic.rs:716-775).  A snapshot is a host byte blob of the state
  * that a later apic_update reads: the nine particle arrays with their padding
  * lanes, the obstacle mask, pending external and post forces, timestamp and
- * prev_deltatime, and the solver settings.  apic_restore loads it into a handle
- * created with the same width, height, cell size and world properties; the
- * next updates of both handles then compute the same thing. */
+ * prev_deltatime, the solver settings, and (APIC_OPT_WARM_START in the mixed
+ * mode) the last solve's FP64 pressure that the next solve starts from.
+ * apic_restore loads it into a handle created with the same width, height,
+ * cell size and world properties; the next updates of both handles then
+ * compute the same thing. */
 int apic_snapshot_bytes(apic_handle* h, uint64_t* bytes);
 int apic_snapshot(apic_handle* h, void* dst, uint64_t bytes);
 int apic_restore(apic_handle* h, const void* src, uint64_t bytes);

@@ -312,6 +312,9 @@ template <class T> struct Sim : SimBase {
     apic_step_stats stats{};
     std::vector<double> p64;   // refined FP64 pressure of the mixed mode (padded layout)
     bool p64_valid = false;
+    // The mixed mode starts each solve from the previous solve's FP64
+    // pressure (the GPU library's APIC_OPT_WARM_START); empty p64: from zero.
+    bool warm_start = true;
 
     bool par() const { return threads > 1; }
     size_t npad() const { return size_t(num_chunks) * 8; }
@@ -973,6 +976,7 @@ template <class T> struct Sim : SimBase {
         stats.pcg_iterations = 0;
         stats.refinement_steps = 0;
         std::vector<double> b(n, 0.0), p64(n, 0.0), r64(n, 0.0);
+        if (mixed && warm_start && this->p64.size() == n) p64 = this->p64;
         for (size_t k = 0; k < fluid_cells; ++k) b[base.fluid[k]] = double(base.residual[base.fluid[k]]);
         std::vector<T> x(n, T(0));
         double rel = 0;
@@ -1418,6 +1422,8 @@ int oracle_set_particles(oracle_sim* o, uint32_t n, const float* px, const float
     return dispatch(o, [&](auto& s) {
         using T = typename std::remove_reference<decltype(s.cell_size)>::type;
         if (n > 0 && (!px || !py)) return APIC_ERR_INVALID_ARG;
+        s.p64.clear();  // a new particle set: the next mixed solve starts from zero
+        s.p64_valid = false;
         std::vector<T> ix(n), iy(n), ivx(n, T(0)), ivy(n, T(0));
         for (uint32_t i = 0; i < n; ++i) {
             ix[i] = T(px[i]); iy[i] = T(py[i]);
@@ -1433,6 +1439,13 @@ int oracle_set_particles(oracle_sim* o, uint32_t n, const float* px, const float
         if (s.levels.empty() && !s.build_levels()) return APIC_ERR_INVALID_ARG;
         s.load_positions(ix, iy, &ivx, &ivy);
         if (!s.world_ready) s.update_world();
+        return APIC_OK;
+    });
+}
+
+int oracle_set_warm_start(oracle_sim* o, int enabled) {
+    return dispatch(o, [&](auto& s) {
+        s.warm_start = enabled != 0;
         return APIC_OK;
     });
 }

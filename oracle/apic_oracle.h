@@ -32,6 +32,9 @@ int  oracle_set_threads(oracle_sim* o, int threads);
 int  oracle_set_particles(oracle_sim* o, uint32_t n, const float* px, const float* py,
                           const float* vx, const float* vy);
 int  oracle_set_solver(oracle_sim* o, int mode, float rel_tol, uint32_t max_iterations);
+/* Mixed mode: start each solve from the previous one's FP64 pressure (1, the
+ * default, as the GPU library's APIC_OPT_WARM_START) or from zero (0). */
+int  oracle_set_warm_start(oracle_sim* o, int enabled);
 int  oracle_update(oracle_sim* o, uint32_t flags, float frame_dt);
 int  oracle_run_stage(oracle_sim* o, int stage, float dt);
 /* End-of-substep bookkeeping (prev_deltatime, timestamp), src/apic.rs:2463-2467. */

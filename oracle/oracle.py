@@ -36,6 +36,7 @@ def load(rebuild: bool = True) -> ctypes.CDLL:
         "oracle_set_threads": (ctypes.c_int, [_VP, ctypes.c_int]),
         "oracle_set_particles": (ctypes.c_int, [_VP, ctypes.c_uint32, _FP, _FP, _FP, _FP]),
         "oracle_set_solver": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_float, ctypes.c_uint32]),
+        "oracle_set_warm_start": (ctypes.c_int, [_VP, ctypes.c_int]),
         "oracle_update": (ctypes.c_int, [_VP, ctypes.c_uint32, ctypes.c_float]),
         "oracle_run_stage": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_float]),
         "oracle_finish_substep": (ctypes.c_int, [_VP, ctypes.c_float]),
@@ -103,6 +104,9 @@ class OracleSim:
 
     def set_solver(self, mode: int, rel_tol: float = 1e-6, max_iterations: int = 500) -> None:
         _ck(self._lib.oracle_set_solver(self._h, mode, rel_tol, max_iterations), "oracle_set_solver")
+
+    def set_warm_start(self, enabled: bool) -> None:
+        _ck(self._lib.oracle_set_warm_start(self._h, 1 if enabled else 0), "oracle_set_warm_start")
 
     def update(self, debug_options=None, frame_deltatime: float = 1 / 60) -> None:
         flags = 1 if (debug_options is not None and debug_options.disable_particle_sort) else 0

@@ -561,3 +561,40 @@ def test_cluster_solve_matches_graph_solver(gpu_lib, mode, side):
     assert float(np.max(np.abs(pa - pb))) <= 1e-3 * scale
     for f in ("pos_x", "pos_y"):
         assert float(np.max(np.abs(sims[0].read_field(f) - sims[1].read_field(f)))) < 1e-3 * cs
+
+
+def test_warm_start_option(oracle_mod):
+    """APIC_OPT_WARM_START (default on): the mixed solve starts from the last
+    solve's FP64 pressure, meets the same true-residual bound in fewer
+    iterations than from zero, and follows the oracle's warm-started run."""
+    side = 256
+    props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+    sc = A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=1.0 / side, sub=2, seed=7, fluid_x=0.5,
+                        fluid_y=0.5, disk=(0.7, 0.8, 0.08), disk_v=(0.0, -2.0))
+    px, py, vx, vy = A.generate_scene(sc)
+    totals, pos = {}, {}
+    for warm in (0, 1):
+        g = A.Apic(side, side, 1.0 / side, props)
+        assert g.get_option(A.OPT_WARM_START) == 1
+        g.set_particles(px, py, vx, vy)
+        g.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+        g.set_option(A.OPT_WARM_START, warm)
+        assert g.get_option(A.OPT_WARM_START) == warm
+        its = 0
+        for _ in range(8):
+            g.update(A.DebugOptions(), 1 / 240)
+            st = g.stats()
+            assert st.true_residual_rel <= 1e-6 and st.not_converged == 0
+            its += st.pcg_iterations_total
+        totals[warm], pos[warm] = its, g.read_vec2x8(0)
+        g.close()
+    assert totals[1] < totals[0], totals
+    assert float(np.max(np.abs(pos[1] - pos[0]))) < 1e-3 / side
+    o = oracle_mod.OracleSim(side, side, 1.0 / side, props, threads=4)
+    o.set_particles(px, py, vx, vy)
+    o.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+    its = 0
+    for _ in range(8):
+        o.update(A.DebugOptions(), 1 / 240)
+        its += o.stats().pcg_iterations_total
+    assert iterations_close(its, totals[1]), (its, totals[1])

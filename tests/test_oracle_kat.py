@@ -144,3 +144,31 @@ def test_openmp_mode_matches_serial(oracle_mod):
         va, vb = a.read_field(f), b.read_field(f)
         scale = max(1e-6, float(np.max(np.abs(va))))
         assert np.max(np.abs(va - vb)) <= 1e-4 * scale, f
+
+
+def test_mixed_warm_start_same_tolerance_fewer_iterations(oracle_mod):
+    """The mixed solve started from the previous solve's FP64 pressure meets
+    the same true-residual bound in fewer iterations and gives the same flow
+    (the pressures differ only within that bound)."""
+    import apic_gb300 as A
+    side = 128
+    sc = A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=1.0 / side, sub=2, seed=7, fluid_x=0.5,
+                        fluid_y=0.5, disk=(0.7, 0.8, 0.08), disk_v=(0.0, -2.0))
+    px, py, vx, vy = A.generate_scene(sc)
+    runs = []
+    for warm in (False, True):
+        o = oracle_mod.OracleSim(side, side, 1.0 / side, A.WorldProperties(-9.81, 0.1, 5.0, 1e-5), threads=4)
+        o.set_particles(px, py, vx, vy)
+        o.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+        o.set_warm_start(warm)
+        its = 0
+        for _ in range(8):
+            o.update(A.DebugOptions(), 1 / 240)
+            st = o.stats()
+            assert st.true_residual_rel <= 1e-6 and st.not_converged == 0
+            its += st.pcg_iterations_total
+        runs.append((its, o.read_field("pos_x"), o.read_field("pos_y")))
+    (cold, cx, cy), (warm, wx, wy) = runs
+    assert warm < cold, (warm, cold)
+    assert float(np.max(np.abs(cx - wx))) < 1e-3 / side
+    assert float(np.max(np.abs(cy - wy))) < 1e-3 / side
