@@ -295,6 +295,114 @@ __device__ __forceinline__ bool block_sum_last(F2 v, double* partials, uint32_t*
     return true;
 }
 
+// ---- split grid reductions ---------------------------------------------------
+// The PCG loop's reductions stop at the block level: each block stores its
+// partial, and the kernel that needs the total sums the partials itself after
+// its dependency wait (the kernel boundary makes them visible), so no block
+// fences, counts or waits at the end of the producing kernel.  The sums run
+// in the order of block_sum_last's last block, so both forms give the same
+// total.
+
+// This block's F2 sum (and, with mx, its maximum) into slot blockIdx.x.
+template <int kThreads>
+__device__ __forceinline__ void block_store(F2 v, float2* part) {
+    __shared__ F2 s_bs[kThreads / 32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_bs[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        F2 b{0.0f, 0.0f};
+        for (int w = 0; w < kThreads / 32; ++w) b = f2_add(b, s_bs[w]);
+        part[blockIdx.x] = make_float2(b.hi, b.lo);
+    }
+}
+
+template <int kThreads>
+__device__ __forceinline__ void block_store(F2 v, float mx, float4* part) {
+    __shared__ F2 s_bs[kThreads / 32];
+    __shared__ float s_bm[kThreads / 32];
+    v = warp_sum(v);
+    mx = warp_maxf(mx);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_bs[warp] = v;
+        s_bm[warp] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        F2 b{0.0f, 0.0f};
+        float m = 0.0f;
+        for (int w = 0; w < kThreads / 32; ++w) {
+            b = f2_add(b, s_bs[w]);
+            m = fmaxf(m, s_bm[w]);
+        }
+        part[blockIdx.x] = make_float4(b.hi, b.lo, m, 0.0f);
+    }
+}
+
+// Total of n partials, returned to every thread of the block.
+template <int kThreads>
+__device__ __forceinline__ double sum_partials(const float2* part, uint32_t n) {
+    __shared__ F2 s_sp[kThreads / 32];
+    __shared__ double s_tot;
+    F2 t{0.0f, 0.0f};
+#pragma unroll 4
+    for (uint32_t b = threadIdx.x; b < n; b += kThreads) {
+        const float2 q = __ldcg(part + b);
+        t = f2_add(t, F2{q.x, q.y});
+    }
+    t = warp_sum(t);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_sp[warp] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        F2 a{0.0f, 0.0f};
+        for (int w = 0; w < kThreads / 32; ++w) a = f2_add(a, s_sp[w]);
+        s_tot = f2_value(a);
+    }
+    __syncthreads();
+    return s_tot;
+}
+
+// Sum and maximum of n float4 partials (x, y: F2 sum; z: maximum).
+template <int kThreads>
+__device__ __forceinline__ void sum_max_partials(const float4* part, uint32_t n, double* sum, float* mx) {
+    __shared__ F2 s_sp[kThreads / 32];
+    __shared__ float s_mp[kThreads / 32];
+    __shared__ double s_tot;
+    __shared__ float s_max;
+    F2 t{0.0f, 0.0f};
+    float m = 0.0f;
+#pragma unroll 4
+    for (uint32_t b = threadIdx.x; b < n; b += kThreads) {
+        const float4 q = __ldcg(part + b);
+        t = f2_add(t, F2{q.x, q.y});
+        m = fmaxf(m, q.z);
+    }
+    t = warp_sum(t);
+    m = warp_maxf(m);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_sp[warp] = t;
+        s_mp[warp] = m;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        F2 a{0.0f, 0.0f};
+        float b = 0.0f;
+        for (int w = 0; w < kThreads / 32; ++w) {
+            a = f2_add(a, s_sp[w]);
+            b = fmaxf(b, s_mp[w]);
+        }
+        s_tot = f2_value(a);
+        s_max = b;
+    }
+    __syncthreads();
+    *sum = s_tot;
+    *mx = s_max;
+}
+
 // Same pattern for a maximum of non-negative values (exact in any order).
 template <int kThreads>
 __device__ __forceinline__ bool block_max_last(float v, double* partials, uint32_t* counter, float* total) {

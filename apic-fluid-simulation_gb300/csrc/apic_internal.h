@@ -60,6 +60,7 @@ struct Ctl {
     float alpha;
     float beta;
     uint32_t beta_valid;    // beta belongs to this solve (the search direction is z + beta s)
+    uint32_t delta_stop;    // k_pcg_update found s.Ap unusable; the next kernel turns it into pcg_done
     unsigned long long solve_t0;  // %globaltimer at the start of the running solve (ns)
     unsigned long long solve_ns;  // summed solve time of this update (ns)
     uint32_t max_r_bits;    // max |r| (float bits)
@@ -185,7 +186,7 @@ struct Scene {
 
     Ctl* ctl = nullptr;                       // device
     Ctl* ctl_host = nullptr;                  // pinned mirror
-    double* partials = nullptr;               // kMaxRedBlocks doubles
+    double* partials = nullptr;               // kPartialDoubles doubles (block partials of reductions)
     uint32_t* scan_tmp = nullptr;             // compaction block counts
     uint32_t scan_tmp_len = 0;
 
@@ -235,6 +236,15 @@ struct Scene {
 cudaError_t launch_sort(Scene& s);
 // Exclusive scan of data[0..n) in place; tmp holds div_up(n, 1024) words.
 cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t n, uint32_t* tmp, cudaStream_t st);
+// Block partials of the PCG loop's split reductions, in Scene::partials after
+// the 2 * kMaxRedBlocks doubles of the single-kernel reductions: s.Ap (one
+// float2 per block), the residual's sum of squares and max (one float4) and
+// r.z (one float2).
+constexpr int kPartialDoubles = 6 * kMaxRedBlocks;
+inline float2* part_sap(const Scene& s) { return reinterpret_cast<float2*>(s.partials + 2 * kMaxRedBlocks); }
+inline float4* part_res(const Scene& s) { return reinterpret_cast<float4*>(s.partials + 3 * kMaxRedBlocks); }
+inline float2* part_rz(const Scene& s) { return reinterpret_cast<float2*>(s.partials + 5 * kMaxRedBlocks); }
+
 // The mixed-precision solve starts from the FP64 pressure that the previous
 // solve left in p64 (zeroed whenever the particle set is replaced).
 inline int warm_start(const Scene& s) { return s.warm_start && s.solver_mode == APIC_SOLVER_REL_MIXED ? 1 : 0; }
@@ -283,7 +293,9 @@ void launch_vcycle_dsm(Scene& s, cudaStream_t st);
 // was already written (by k_pcg_update); rz_mode >= 0: the last kernel also
 // reduces r.z and finishes the PCG iteration for that solver mode (returns
 // false when this V-cycle form cannot, and the caller must).
-bool enqueue_vcycle(Scene& s, bool base_red_done = false, int rz_mode = -1);
+// residual_exit: the first kernel also runs the PCG residual's exit test
+// (k_smooth_exit; with base_red_done, rz_mode = the solver mode).
+bool enqueue_vcycle(Scene& s, bool base_red_done = false, int rz_mode = -1, bool residual_exit = false);
 // runtime.cu
 cudaError_t launch_plan_first(Scene& s);
 cudaError_t launch_advance(Scene& s);

@@ -196,6 +196,30 @@ __device__ __forceinline__ void finish_rz(Ctl* ctl, double tot, int mode) {
     ctl->gamma = ng;
 }
 
+// The exits that k_pcg_update leaves to the next kernel: its delta stop, or
+// the residual test on its block parts, max|r| < solve_error (reference
+// mode, src/apic.rs:1929-1932) or ||r|| <= target * ||b||.  Run by one
+// block, after the caller's dependency wait.
+__device__ __forceinline__ void residual_exit(Ctl* ctl, const float4* part, uint32_t n, int mode, float solve_error) {
+    if (ctl->delta_stop) {  // s.Ap was unusable: no update, no residual parts
+        if (threadIdx.x == 0) ctl->pcg_done = 1;
+        return;
+    }
+    double tot;
+    float t;
+    sum_max_partials<kSegBlock>(part, n, &tot, &t);
+    if (threadIdx.x == 0) {
+        if (mode == APIC_SOLVER_REFERENCE) {
+            ctl->max_r_bits = __float_as_uint(t);
+            if (t < solve_error) ctl->pcg_done = 1;
+        } else {
+            ctl->rnorm2 = tot;
+            const double rel = ctl->bnorm2 > 0.0 ? sqrt(tot / ctl->bnorm2) : 0.0;
+            if (rel <= ctl->target_rel) ctl->pcg_done = 1;
+        }
+    }
+}
+
 // r.z after the preconditioner (:1936).
 __device__ __forceinline__ F2 ph_rz(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps) {
     F2 acc{0.0f, 0.0f};

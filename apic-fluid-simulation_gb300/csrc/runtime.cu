@@ -554,7 +554,7 @@ int apic::create_scene(uint32_t width, uint32_t height, float cell_size, const a
     plan_persistent_solve(s);
     plan_cluster_solve(s);
     AL(s.ctl, 1);
-    AL(s.partials, 2 * kMaxRedBlocks);
+    AL(s.partials, kPartialDoubles);
     s.scan_tmp_len = 3 * (div_up(max_words, 1024) + 1);
     AL(s.scan_tmp, s.scan_tmp_len);
 #undef AL

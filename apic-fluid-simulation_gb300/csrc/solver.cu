@@ -47,6 +47,7 @@ __global__ void k_pcg_begin(Ctl* ctl, int stamp) {
     ctl->alpha = 0.0f;
     ctl->beta = 0.0f;
     ctl->beta_valid = 0;
+    ctl->delta_stop = 0;
     ctl->rnorm2 = 0.0;
 }
 
@@ -69,9 +70,10 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl*
     }
 }
 
-// s' = z + beta s, Ap = A s' and delta = s'.Ap (apply_matrix_and_dot,
-// src/apic.rs:1823-1863; the search update :1945-1954 is folded in).
-__global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s, float* ap, Ctl* ctl, double* partials,
+// s' = z + beta s, Ap = A s' and this block's part of delta = s'.Ap
+// (apply_matrix_and_dot, src/apic.rs:1823-1863; the search update
+// :1945-1954 is folded in).  k_pcg_update sums the parts.
+__global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s, float* ap, Ctl* ctl, float2* part,
                                                         int mode) {
     // the base segment list is written by the substep's setup: load this
     // warp's first word before waiting on the previous kernel
@@ -80,56 +82,57 @@ __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s,
     pdl_wait();
     if (ctl->pcg_done) return;
     F2 acc = pcg::ph_spmv_search(B, nseg, gwarp(), gnwarps(), s, ctl->beta, ctl->beta_valid != 0, ap, w0);
-    double tot;
-    if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
-        float delta = float(tot);
-        ctl->pcg_iters++;
-        bool stop = mode == APIC_SOLVER_REFERENCE ? fabsf(delta) < kSafety : (!(delta != 0.0f) || !isfinite(delta));
-        if (stop) ctl->pcg_done = 1;
-        else ctl->alpha = ctl->gamma / delta;
-    }
+    block_store<kSegBlock>(acc, part);
 }
 
-// p += alpha s', r = fma(-alpha, Ap, r), max|r| (src/apic.rs:1907-1932),
-// s = s', and the V-cycle's first red sweep on the base level; relative
-// modes reduce ||r||^2 instead of max|r|.
+// delta (the sum of k_spmv_dot's parts, formed by every block) gives alpha or
+// the exit (src/apic.rs:1899-1906, applied by the next kernel); then
+// p += alpha s', r = fma(-alpha, Ap, r)
+// (:1907-1932), s = s', the V-cycle's first red sweep on the base level, and
+// this block's part of ||r||^2 and max|r|, whose exit test runs in the next
+// kernel (k_smooth_conv).
 __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int p_padded, float* s,
-                                                          const float* ap, Ctl* ctl, double* partials, int mode,
-                                                          float solve_error) {
+                                                          const float* ap, Ctl* ctl, const float2* sap,
+                                                          uint32_t nsap, float4* part, int mode) {
     const uint32_t nseg = ctl->seg_count[0];
     const uint32_t w0 = gwarp() < nseg ? B.seg[gwarp()] : 0xFFFFFFFFu;
     pdl_wait();
     if (ctl->pcg_done) return;
+    const float delta = float(sum_partials<kSegBlock>(sap, nsap));
+    const bool stop = mode == APIC_SOLVER_REFERENCE ? fabsf(delta) < kSafety : (!(delta != 0.0f) || !isfinite(delta));
+    const float alpha = ctl->gamma / delta;
+    // every block reads pcg_done on entry, so the stop is recorded aside and
+    // the next kernel turns it into pcg_done
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctl->pcg_iters++;
+        ctl->delta_stop = stop ? 1u : 0u;
+        if (!stop) ctl->alpha = alpha;
+    }
+    if (stop) return;
     float mx;
     F2 acc;
-    pcg::ph_update_search(B, nseg, gwarp(), gnwarps(), ctl->alpha, ctl->beta, ctl->beta_valid != 0, p, p_padded, s,
-                          ap, &mx, &acc, w0);
-    if (mode == APIC_SOLVER_REFERENCE) {
-        float t;
-        if (block_max_last<kSegBlock>(mx, partials, &ctl->red_counter, &t) && threadIdx.x == 0) {
-            ctl->max_r_bits = __float_as_uint(t);
-            if (t < solve_error) ctl->pcg_done = 1;
-        }
-    } else {
-        double tot;
-        if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
-            ctl->rnorm2 = tot;
-            double rel = ctl->bnorm2 > 0.0 ? sqrt(tot / ctl->bnorm2) : 0.0;
-            if (rel <= ctl->target_rel) ctl->pcg_done = 1;
-        }
-    }
+    pcg::ph_update_search(B, nseg, gwarp(), gnwarps(), alpha, ctl->beta, ctl->beta_valid != 0, p, p_padded, s, ap,
+                          &mx, &acc, w0);
+    block_store<kSegBlock>(acc, mx, part);
 }
 
-// gamma' = r.z, beta (src/apic.rs:1934-1943).
-__global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, double* partials, int mode) {
+// Stand-alone exit test (paths whose V-cycle does not start with the base
+// level's black sweep).
+__global__ void __launch_bounds__(kSegBlock) k_residual_exit(Ctl* ctl, const float4* part, uint32_t n, int mode,
+                                                             float solve_error) {
+    pdl_wait();
+    if (ctl->pcg_done) return;
+    pcg::residual_exit(ctl, part, n, mode, solve_error);
+}
+
+// This block's part of gamma' = r.z (src/apic.rs:1934-1943); k_pcg_cond
+// finishes it.
+__global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, float2* part) {
     pdl_wait();
     if (ctl->pcg_done) return;
     F2 acc = pcg::ph_rz(B, ctl->seg_count[0], gwarp(), gnwarps());
-    double tot;
-    if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0)
-        pcg::finish_rz(ctl, tot, mode);
+    block_store<kSegBlock>(acc, part);
 }
-
 
 // ---- FP64 refinement helpers (APIC_SOLVER_REL_MIXED) ----------------------
 
@@ -163,10 +166,21 @@ __global__ void __launch_bounds__(kSegBlock) k_pressure_to64(Level B, const floa
 
 // ---- loop control (device side; each sets a graph conditional) ------------
 
-// Continue the PCG loop while not converged and under the iteration cap
-// (src/apic.rs:1894-1899); dyn_cap reads the remaining budget of a refinement.
-__global__ void k_pcg_cond(const Ctl* __restrict__ ctl, cudaGraphConditionalHandle h, uint32_t cap, int dyn_cap) {
+// End of an iteration: gamma' = r.z from the parts of the V-cycle's last
+// kernel (flags & 1; pcg::finish_rz sets beta or the exit), then the loop
+// condition (flags & 2): go on while not converged and under the iteration
+// cap (src/apic.rs:1894-1899); dyn_cap reads the remaining budget of a
+// refinement.  One block.
+__global__ void __launch_bounds__(kSegBlock) k_pcg_cond(Ctl* __restrict__ ctl, cudaGraphConditionalHandle h,
+                                                        uint32_t cap, int dyn_cap, const float2* rz, uint32_t nrz,
+                                                        int mode, int flags) {
     pdl_wait();
+    if ((flags & 1) && !ctl->pcg_done) {
+        const double tot = sum_partials<kSegBlock>(rz, nrz);
+        if (threadIdx.x == 0) pcg::finish_rz(ctl, tot, mode);
+        __syncthreads();
+    }
+    if (threadIdx.x != 0 || !(flags & 2)) return;
     uint32_t c = dyn_cap ? ctl->inner_cap : cap;
     cudaGraphSetConditional(h, (!ctl->pcg_done && ctl->pcg_iters < c) ? 1u : 0u);
 }
@@ -226,11 +240,23 @@ static void pcg_iteration(Scene& s, int mode, float* x, int p_padded) {
     uint32_t g = seg_grid(B.words);
     cudaStream_t st = s.stream;
     const bool pdl = s.use_pdl;
-    k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, s.partials, mode);
-    launch(pdl, k_pcg_update, g, kSegBlock, 0, st, B, x, p_padded, s.search, s.ap, s.ctl, s.partials, mode,
-           s.props.solve_error);
-    // the V-cycle's last kernel also reduces r.z and sets beta (k_dot_rz's work)
-    if (!enqueue_vcycle(s, true, mode)) launch(pdl, k_dot_rz, g, kSegBlock, 0, st, B, s.ctl, s.partials, mode);
+    k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, part_sap(s), mode);
+    launch(pdl, k_pcg_update, g, kSegBlock, 0, st, B, x, p_padded, s.search, s.ap, s.ctl,
+           static_cast<const float2*>(part_sap(s)), g, part_res(s), mode);
+    // the residual's exit test runs inside the V-cycle's first kernel when
+    // that is the base level's black sweep, else on its own
+    const bool exit_in_vcycle = !s.fused_vcycle && s.nlevels >= 2;
+    if (!exit_in_vcycle)
+        launch(pdl, k_residual_exit, 1, kSegBlock, 0, st, s.ctl, static_cast<const float4*>(part_res(s)), g, mode,
+               s.props.solve_error);
+    // the V-cycle's last kernel also stores the parts of r.z (k_dot_rz's work)
+    if (!enqueue_vcycle(s, true, mode, exit_in_vcycle)) launch(pdl, k_dot_rz, g, kSegBlock, 0, st, B, s.ctl, part_rz(s));
+}
+
+// Finish an iteration (r.z) and, in a graph, set the loop condition.
+static void pcg_finish(Scene& s, cudaGraphConditionalHandle h, uint32_t cap, int dyn_cap, int mode, int flags) {
+    launch(s.use_pdl, k_pcg_cond, 1, kSegBlock, 0, s.stream, s.ctl, h, cap, dyn_cap,
+           static_cast<const float2*>(part_rz(s)), seg_grid(s.lv[0].words), mode, flags);
 }
 
 // PCG setup (src/apic.rs:1885-1892) followed by a device-controlled WHILE
@@ -249,7 +275,7 @@ static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p
         if (clear_pressure) k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
         enqueue_vcycle(s);
         launch(s.use_pdl, k_pcg_start, g, kSegBlock, 0, st, B, s.search, s.ctl, s.partials, mode);
-        launch(s.use_pdl, k_pcg_cond, 1, 1, 0, st, s.ctl, h, cap, dyn_cap);
+        pcg_finish(s, h, cap, dyn_cap, mode, 2);
         return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
@@ -258,7 +284,7 @@ static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p
     if (e != cudaSuccess) return e;
     e = capture_into(s, body, [&]() {
         pcg_iteration(s, mode, x, p_padded);
-        launch(s.use_pdl, k_pcg_cond, 1, 1, 0, s.stream, s.ctl, h, cap, dyn_cap);
+        pcg_finish(s, h, cap, dyn_cap, mode, 3);
         return cudaGetLastError();
     });
     s.kn_pcg = count_kernel_nodes(body.g);
@@ -363,6 +389,7 @@ static cudaError_t eager_pcg(Scene& s, int mode, float* x, int p_padded, uint32_
         if (e != cudaSuccess) return e;
         if (s.ctl_host->pcg_done || s.ctl_host->pcg_iters >= cap) break;
         pcg_iteration(s, mode, x, p_padded);
+        pcg_finish(s, 0, cap, 0, mode, 1);
     }
     return cudaGetLastError();
 }

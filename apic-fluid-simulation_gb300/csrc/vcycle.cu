@@ -52,6 +52,25 @@ __device__ __forceinline__ uint32_t early_word(const uint32_t* seg, uint32_t nse
     return s < nseg ? seg[s] : kNoWord;
 }
 
+// The base level's black sweep after k_pcg_update (which ran the red one),
+// with the exit test of k_pcg_update's residual in an extra block 0 that
+// runs beside the sweep; later kernels see its verdict.
+__global__ void __launch_bounds__(kSegBlock) k_smooth_exit(Level L, Ctl* ctl, const float4* part, uint32_t nparts,
+                                                           int mode, float solve_error) {
+    const uint32_t nseg = ctl->seg_count[0];
+    if (blockIdx.x == 0) {
+        pdl_wait();
+        if (ctl->pcg_done) return;
+        pcg::residual_exit(ctl, part, nparts, mode, solve_error);
+        return;
+    }
+    const uint32_t warp = gwarp() - kSegWarps, nwarps = gnwarps() - kSegWarps;
+    const uint32_t w0 = warp < nseg ? L.seg[warp] : kNoWord;
+    pdl_wait();
+    if (ctl->pcg_done) return;
+    ph_smooth(L, nseg, warp, nwarps, 1, 1, w0);
+}
+
 __global__ void __launch_bounds__(kSegBlock) k_smooth(Level L, int li, const Ctl* ctl, int color, int init) {
     const uint32_t nseg = ctl->seg_count[li];
     const uint32_t w0 = early_word(L.seg, nseg);
@@ -88,20 +107,17 @@ __global__ void __launch_bounds__(kSegBlock) k_prolong_black(Level c, Level f, i
     ph_prolong(c, f, nseg, gwarp(), gnwarps(), 1, last, extra, w0);
 }
 
-// Base-level prolongation fused with the final red sweep, which also reduces
-// r.z over every fluid cell (red cells' new z, black cells' final z) and
-// finishes the PCG iteration (k_dot_rz's work).
-__global__ void __launch_bounds__(kSegBlock) k_prolong_red_rz(Level c, Level B, Ctl* ctl, double* partials,
-                                                              int mode) {
+// Base-level prolongation fused with the final red sweep, which also stores
+// this block's part of r.z over every fluid cell (red cells' new z, black
+// cells' final z): k_dot_rz's work; k_pcg_cond finishes the sum.
+__global__ void __launch_bounds__(kSegBlock) k_prolong_red_rz(Level c, Level B, const Ctl* ctl, float2* part) {
     const uint32_t nseg = ctl->seg_count[0];
     const uint32_t w0 = early_word(B.seg, nseg);
     const uint32_t last = ctl->last_fluid, extra = ctl->pad_count;
     pdl_wait();
     if (ctl->pcg_done) return;
     const F2 acc = ph_prolong_red_rz(c, B, nseg, gwarp(), gnwarps(), last, extra, w0);
-    double tot;
-    if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0)
-        pcg::finish_rz(ctl, tot, mode);
+    block_store<kSegBlock>(acc, part);
 }
 
 // Prolongation fused with the final red sweep (black neighbours are final).
@@ -276,13 +292,13 @@ void plan_vcycle_cluster(Scene& s) {
     }
 }
 
-static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode);
+static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode, bool residual_exit);
 
 // One V-cycle on s.stream: z = M^-1 r in lv[0].err.  Fused form: one kernel
 // per level down (k_down) and up (k_up) around the coarse tail.
-bool enqueue_vcycle(Scene& s, bool base_red_done, int rz_mode) {
+bool enqueue_vcycle(Scene& s, bool base_red_done, int rz_mode, bool residual_exit) {
     if (!s.fused_vcycle || s.nlevels < 2) {
-        enqueue_vcycle_unfused(s, base_red_done, rz_mode);
+        enqueue_vcycle_unfused(s, base_red_done, rz_mode, residual_exit);
         return rz_mode < 0 || s.nlevels >= 2;
     }
     // the fused descent recomputes the base level's red sweep from the
@@ -313,14 +329,18 @@ bool enqueue_vcycle(Scene& s, bool base_red_done, int rz_mode) {
 }
 
 // Two kernels per sweep and per transfer (the reference's sequence launch by launch).
-static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode) {
+static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode, bool residual_exit) {
     cudaStream_t st = s.stream;
     Level* L = s.lv;
     auto grid = [&](int l) { return seg_grid(L[l].words); };
     const int last = s.nlevels - 1;
     const bool pdl = s.use_pdl;
     if (!base_red_done) launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 0, 1);
-    launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 1, 1);
+    if (residual_exit && base_red_done)
+        launch(pdl, k_smooth_exit, grid(0) + 1, kSegBlock, 0, st, L[0], s.ctl,
+               static_cast<const float4*>(part_res(s)), grid(0), rz_mode, s.props.solve_error);
+    else
+        launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 1, 1);
     if (last < 1) {
         launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 1, 0);
         launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 0, 0);
@@ -362,7 +382,8 @@ static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode) {
     }
     launch(pdl, k_prolong_black, grid(0), kSegBlock, 0, st, L[1], L[0], 0, s.ctl, 1);
     if (rz_mode >= 0)
-        launch(pdl, k_prolong_red_rz, grid(0), kSegBlock, 0, st, L[1], L[0], s.ctl, s.partials, rz_mode);
+        launch(pdl, k_prolong_red_rz, grid(0), kSegBlock, 0, st, L[1], L[0], static_cast<const Ctl*>(s.ctl),
+               part_rz(s));
     else
         launch(pdl, k_prolong_red, grid(0), kSegBlock, 0, st, L[1], L[0], 0, s.ctl, 1);
 }
