@@ -95,6 +95,7 @@ __device__ __forceinline__ uint32_t load_clean_word(uint32_t* fluid, const uint3
 
 __global__ void __launch_bounds__(256) k_compact_count(uint32_t* __restrict__ fluid, const uint32_t* __restrict__ obstacle,
                                                        uint32_t words, uint32_t* __restrict__ cnt) {
+    pdl_wait();
     uint32_t nz = 0, cells = 0, last = 0;
     for (int k = 0; k < 4; ++k) {
         uint32_t w = blockIdx.x * kCompactWords + threadIdx.x * 4 + k;
@@ -146,65 +147,63 @@ __device__ __forceinline__ uint32_t scan_1024(uint32_t v, uint32_t* total) {
     return pre + x - v;
 }
 
-// Single block: exclusive scan of the per-block word counts, totals into Ctl.
-__global__ void __launch_bounds__(1024) k_compact_scan(uint32_t* __restrict__ cnt, uint32_t nb,
-                                                       const uint32_t* __restrict__ fluid, uint32_t W, int level,
-                                                       Ctl* __restrict__ ctl) {
-    uint32_t carry = 0, cells = 0, last = 0;
-    for (uint32_t c = 0; c < nb; c += 1024) {
-        uint32_t i = c + threadIdx.x;
-        uint32_t v = i < nb ? cnt[3 * i] : 0u;
-        uint32_t tot;
-        uint32_t ex = scan_1024(v, &tot);
-        if (i < nb) {
-            cnt[3 * i] = carry + ex;
-            cells += cnt[3 * i + 1];
-            last = max(last, cnt[3 * i + 2]);
-        }
-        carry += tot;
+// Segment list of one level (ascending non-zero mask words): block b writes
+// its words after those of blocks [0, b), whose counts (k_compact_count) it
+// sums itself; the last block also records the level's totals in Ctl (and,
+// on the base level, the fluid-cell count, the last fluid cell and the
+// padding of the reference's fluid list to a multiple of 8).
+__global__ void __launch_bounds__(256) k_compact_write(const uint32_t* __restrict__ fluid, uint32_t words,
+                                                       const uint32_t* __restrict__ cnt, uint32_t* __restrict__ seg,
+                                                       uint32_t W, int level, Ctl* __restrict__ ctl) {
+    pdl_wait();
+    const uint32_t nb = gridDim.x, b0 = blockIdx.x;
+    const bool last_block = b0 + 1 == nb;
+    uint32_t before = 0, total = 0, cells = 0, lastw = 0;
+    for (uint32_t b = threadIdx.x; b < (last_block ? nb : b0); b += 256) {
+        const uint32_t c = cnt[3 * b];
+        before += b < b0 ? c : 0u;
+        total += c;
+        cells += cnt[3 * b + 1];
+        lastw = max(lastw, cnt[3 * b + 2]);
     }
-    // reduce cells and last over the block
-    __shared__ uint32_t sc[1024], sl[1024];
-    sc[threadIdx.x] = cells;
-    sl[threadIdx.x] = last;
+    __shared__ uint32_t red[4][256];
+    red[0][threadIdx.x] = before;
+    red[1][threadIdx.x] = total;
+    red[2][threadIdx.x] = cells;
+    red[3][threadIdx.x] = lastw;
     __syncthreads();
-    for (int o = 512; o > 0; o >>= 1) {
+    for (int o = 128; o > 0; o >>= 1) {
         if (threadIdx.x < o) {
-            sc[threadIdx.x] += sc[threadIdx.x + o];
-            sl[threadIdx.x] = max(sl[threadIdx.x], sl[threadIdx.x + o]);
+            red[0][threadIdx.x] += red[0][threadIdx.x + o];
+            red[1][threadIdx.x] += red[1][threadIdx.x + o];
+            red[2][threadIdx.x] += red[2][threadIdx.x + o];
+            red[3][threadIdx.x] = max(red[3][threadIdx.x], red[3][threadIdx.x + o]);
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        ctl->seg_count[level] = carry;
-        if (level == 0) {
-            uint32_t f = sc[0];
-            ctl->fluid_cells = f;
-            uint32_t lw = sl[0];
-            if (f > 0 && lw > 0) {
-                uint32_t m = fluid[lw - 1];
-                uint32_t raw = (lw - 1) * 32u + (31u - uint32_t(__clz(m)));
-                ctl->last_fluid = raw + W;
-            } else {
-                ctl->last_fluid = 0;
-            }
-            ctl->pad_count = (8u - f % 8u) % 8u;
-        }
-    }
-}
-
-__global__ void __launch_bounds__(256) k_compact_write(const uint32_t* __restrict__ fluid, uint32_t words,
-                                                       const uint32_t* __restrict__ cnt, uint32_t* __restrict__ seg) {
     uint32_t m[4], nz = 0;
     for (int k = 0; k < 4; ++k) {
-        uint32_t w = blockIdx.x * kCompactWords + threadIdx.x * 4 + k;
+        uint32_t w = b0 * kCompactWords + threadIdx.x * 4 + k;
         m[k] = w < words ? fluid[w] : 0u;
         nz += m[k] ? 1u : 0u;
     }
     uint32_t tot;
-    uint32_t off = cnt[3 * blockIdx.x] + scan_1024(nz, &tot);
+    uint32_t off = red[0][0] + scan_1024(nz, &tot);
     for (int k = 0; k < 4; ++k)
-        if (m[k]) seg[off++] = blockIdx.x * kCompactWords + threadIdx.x * 4 + k;
+        if (m[k]) seg[off++] = b0 * kCompactWords + threadIdx.x * 4 + k;
+    if (!last_block || threadIdx.x != 0) return;
+    ctl->seg_count[level] = red[1][0];
+    if (level == 0) {
+        const uint32_t f = red[2][0], lw = red[3][0];
+        ctl->fluid_cells = f;
+        if (f > 0 && lw > 0) {
+            const uint32_t mw = fluid[lw - 1];
+            ctl->last_fluid = (lw - 1) * 32u + (31u - uint32_t(__clz(mw))) + W;
+        } else {
+            ctl->last_fluid = 0;
+        }
+        ctl->pad_count = (8u - f % 8u) % 8u;
+    }
 }
 
 // Smoothed density as the consumers see it: the three-pass result at fluid
@@ -308,6 +307,7 @@ __global__ void __launch_bounds__(kSegBlock) k_laplacian(const uint32_t* __restr
 // One coarse level from its finer level: thread per coarse cell, one warp per
 // coarse mask word.
 __global__ void __launch_bounds__(256) k_coarsen(Level f, Level c) {
+    pdl_wait();
     uint32_t raw = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t word = raw >> 5;
     if (word >= c.words) return;  // whole warps exit together
@@ -490,9 +490,10 @@ cudaError_t launch_external_forces(Scene& s) {
 static cudaError_t compact_level(Scene& s, int level, const uint32_t* obstacle) {
     Level& L = s.lv[level];
     uint32_t nb = div_up(L.words, kCompactWords);
-    k_compact_count<<<nb, 256, 0, s.stream>>>(L.fluid, obstacle, L.words, s.scan_tmp);
-    k_compact_scan<<<1, 1024, 0, s.stream>>>(s.scan_tmp, nb, L.fluid, L.w, level, s.ctl);
-    k_compact_write<<<nb, 256, 0, s.stream>>>(L.fluid, L.words, s.scan_tmp, L.seg);
+    if (nb == 0) nb = 1;  // the last block records the (empty) level's totals
+    launch(s.use_pdl, k_compact_count, nb, 256, 0, s.stream, L.fluid, obstacle, L.words, s.scan_tmp);
+    launch(s.use_pdl, k_compact_write, nb, 256, 0, s.stream, static_cast<const uint32_t*>(L.fluid), L.words,
+           static_cast<const uint32_t*>(s.scan_tmp), L.seg, L.w, level, s.ctl);
     return cudaGetLastError();
 }
 
@@ -513,7 +514,7 @@ cudaError_t launch_build_pressure(Scene& s) {
 cudaError_t launch_multilevel(Scene& s) {
     for (int l = 1; l < s.nlevels; ++l) {
         Level& c = s.lv[l];
-        k_coarsen<<<div_up(uint64_t(c.words) * 32, 256), 256, 0, s.stream>>>(s.lv[l - 1], c);
+        launch(s.use_pdl, k_coarsen, div_up(uint64_t(c.words) * 32, 256), 256, 0, s.stream, s.lv[l - 1], c);
         cudaError_t e = compact_level(s, l, nullptr);
         if (e != cudaSuccess) return e;
     }
