@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(256) k_faces(uint32_t uf, uint32_t vf, int W, 
                                                const float* __restrict__ ext_v, const uint32_t* __restrict__ fluid,
                                                const uint32_t* __restrict__ obstacle, const Ctl* __restrict__ ctl,
                                                float gravity, int normalize, int forces, int apply_gravity) {
+    pdl_wait();
     uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= uf + vf) return;
     const float dt = ctl->dt;
@@ -222,6 +223,7 @@ __global__ void __launch_bounds__(kSegBlock) k_smooth_density(const uint32_t* __
                                                                const uint32_t* __restrict__ seg,
                                                                const Ctl* __restrict__ ctl, uint32_t W, uint32_t cells,
                                                                const float* __restrict__ src, float* __restrict__ dst) {
+    pdl_wait();
     const uint32_t nseg = ctl->seg_count[0];
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -252,6 +254,7 @@ __global__ void __launch_bounds__(kSegBlock) k_laplacian(const uint32_t* __restr
                                                           float* __restrict__ res, float* __restrict__ diag_o,
                                                           float* __restrict__ inv_o, float* __restrict__ px_o,
                                                           float* __restrict__ py_o) {
+    pdl_wait();
     const uint32_t nseg = ctl->seg_count[0];
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -356,6 +359,7 @@ __global__ void __launch_bounds__(256) k_gradient(uint32_t uf, uint32_t vf, int 
                                                   const float* __restrict__ dens, const float* __restrict__ post_u,
                                                   const float* __restrict__ post_v, const Ctl* __restrict__ ctl,
                                                   const double* __restrict__ p64, int do_gradient, int do_post) {
+    pdl_wait();
     uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= uf + vf) return;
     const float target = 9.0f;
@@ -427,6 +431,7 @@ __global__ void __launch_bounds__(256) k_extrapolate(uint32_t uf, uint32_t vf, i
                                                      float* __restrict__ nu, uint8_t* __restrict__ nvu,
                                                      const float* __restrict__ ov, const uint8_t* __restrict__ ovv,
                                                      float* __restrict__ nv, uint8_t* __restrict__ nvv) {
+    pdl_wait();
     uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= uf + vf) return;
     if (f < uf) {
@@ -472,7 +477,7 @@ uint32_t seg_grid(uint32_t words) {
 
 cudaError_t launch_finalize_faces(Scene& s, bool forces, bool gravity) {
     uint32_t nf = s.uf + s.vf;
-    k_faces<<<div_up(nf, 256), 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), s.acc_u, s.acc_uw, s.acc_v,
+    launch(s.use_pdl, k_faces, div_up(nf, 256), 256, 0, s.stream, s.uf, s.vf, int(s.W), int(s.H), s.acc_u, s.acc_uw, s.acc_v,
                                                     s.acc_vw, s.u, s.v, s.valid_u, s.valid_v, s.ext_u, s.ext_v,
                                                     s.lv[0].fluid, s.obstacle, s.ctl, s.props.gravity, 1,
                                                     forces ? 1 : 0, gravity ? 1 : 0);
@@ -481,7 +486,7 @@ cudaError_t launch_finalize_faces(Scene& s, bool forces, bool gravity) {
 
 cudaError_t launch_external_forces(Scene& s) {
     uint32_t nf = s.uf + s.vf;
-    k_faces<<<div_up(nf, 256), 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), s.acc_u, s.acc_uw, s.acc_v,
+    launch(s.use_pdl, k_faces, div_up(nf, 256), 256, 0, s.stream, s.uf, s.vf, int(s.W), int(s.H), s.acc_u, s.acc_uw, s.acc_v,
                                                     s.acc_vw, s.u, s.v, s.valid_u, s.valid_v, s.ext_u, s.ext_v,
                                                     s.lv[0].fluid, s.obstacle, s.ctl, s.props.gravity, 0, 1, 1);
     return cudaGetLastError();
@@ -503,10 +508,10 @@ cudaError_t launch_level_lists(Scene& s, int level) { return compact_level(s, le
 cudaError_t launch_build_pressure(Scene& s) {
     const Level& B = s.lv[0];
     uint32_t g = seg_grid(B.words);
-    k_smooth_density<<<g, kSegBlock, 0, s.stream>>>(B.fluid, B.seg, s.ctl, s.W, s.cells, s.density, s.sm_a);
-    k_smooth_density<<<g, kSegBlock, 0, s.stream>>>(B.fluid, B.seg, s.ctl, s.W, s.cells, s.sm_a, s.sm_b);
-    k_smooth_density<<<g, kSegBlock, 0, s.stream>>>(B.fluid, B.seg, s.ctl, s.W, s.cells, s.sm_b, s.sm_a);
-    k_laplacian<<<g, kSegBlock, 0, s.stream>>>(B.fluid, s.obstacle, B.seg, s.ctl, s.W, s.cells, s.dx, s.u, s.v,
+    launch(s.use_pdl, k_smooth_density, g, kSegBlock, 0, s.stream, B.fluid, B.seg, s.ctl, s.W, s.cells, s.density, s.sm_a);
+    launch(s.use_pdl, k_smooth_density, g, kSegBlock, 0, s.stream, B.fluid, B.seg, s.ctl, s.W, s.cells, s.sm_a, s.sm_b);
+    launch(s.use_pdl, k_smooth_density, g, kSegBlock, 0, s.stream, B.fluid, B.seg, s.ctl, s.W, s.cells, s.sm_b, s.sm_a);
+    launch(s.use_pdl, k_laplacian, g, kSegBlock, 0, s.stream, B.fluid, s.obstacle, B.seg, s.ctl, s.W, s.cells, s.dx, s.u, s.v,
                                                s.sm_a, s.density, B.res, B.diag, B.inv_diag, B.px, B.py);
     return cudaGetLastError();
 }
@@ -523,7 +528,7 @@ cudaError_t launch_multilevel(Scene& s) {
 
 cudaError_t launch_gradient(Scene& s, bool post) {
     uint32_t nf = s.uf + s.vf;
-    k_gradient<<<div_up(nf, 256), 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), 1.0f / s.dx, s.u, s.v,
+    launch(s.use_pdl, k_gradient, div_up(nf, 256), 256, 0, s.stream, s.uf, s.vf, int(s.W), int(s.H), 1.0f / s.dx, s.u, s.v,
                                                        s.valid_u, s.valid_v, s.lv[0].fluid, s.obstacle, s.pressure,
                                                        s.sm_a, s.density, s.post_u, s.post_v, s.ctl,
                                                        s.p64_valid ? s.p64 : nullptr, 1, post ? 1 : 0);
@@ -532,7 +537,7 @@ cudaError_t launch_gradient(Scene& s, bool post) {
 
 cudaError_t launch_post_forces(Scene& s) {
     uint32_t nf = s.uf + s.vf;
-    k_gradient<<<div_up(nf, 256), 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), 1.0f / s.dx, s.u, s.v,
+    launch(s.use_pdl, k_gradient, div_up(nf, 256), 256, 0, s.stream, s.uf, s.vf, int(s.W), int(s.H), 1.0f / s.dx, s.u, s.v,
                                                        s.valid_u, s.valid_v, s.lv[0].fluid, s.obstacle, s.pressure,
                                                        s.sm_a, s.density, s.post_u, s.post_v, s.ctl, nullptr,
                                                        0, 1);
@@ -543,9 +548,9 @@ cudaError_t launch_extrapolate(Scene& s) {
     uint32_t nf = s.uf + s.vf;
     uint32_t g = div_up(nf, 256);
     for (int k = 0; k < 2; ++k) {
-        k_extrapolate<<<g, 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), s.u, s.valid_u, s.u_alt,
+        launch(s.use_pdl, k_extrapolate, g, 256, 0, s.stream, s.uf, s.vf, int(s.W), int(s.H), s.u, s.valid_u, s.u_alt,
                                                s.valid_u_alt, s.v, s.valid_v, s.v_alt, s.valid_v_alt);
-        k_extrapolate<<<g, 256, 0, s.stream>>>(s.uf, s.vf, int(s.W), int(s.H), s.u_alt, s.valid_u_alt, s.u,
+        launch(s.use_pdl, k_extrapolate, g, 256, 0, s.stream, s.uf, s.vf, int(s.W), int(s.H), s.u_alt, s.valid_u_alt, s.u,
                                                s.valid_u, s.v_alt, s.valid_v_alt, s.v, s.valid_v);
     }
     return cudaGetLastError();

@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(256) k_p2g(const PartPtrs* __restrict__ pp, ui
                                              float* __restrict__ acc_uw, float* __restrict__ acc_v,
                                              float* __restrict__ acc_vw, float* __restrict__ dens,
                                              uint32_t* __restrict__ fluid) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float prev_dt = ctl->prev_dt;
@@ -123,6 +124,7 @@ __global__ void __launch_bounds__(256) k_g2p(const PartPtrs* __restrict__ pp, ui
                                              const float* __restrict__ gu, const float* __restrict__ gv,
                                              const uint32_t* __restrict__ u_open,
                                              const uint32_t* __restrict__ v_open) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float speed_out = 0.0f;
     uint32_t bad = 0;
@@ -203,6 +205,7 @@ __global__ void __launch_bounds__(256) k_g2p(const PartPtrs* __restrict__ pp, ui
 }
 
 __global__ void __launch_bounds__(256) k_vmax(const PartPtrs* __restrict__ pp, uint32_t npad, Ctl* __restrict__ ctl) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float m = 0.0f;
     if (i < npad) {
@@ -213,10 +216,12 @@ __global__ void __launch_bounds__(256) k_vmax(const PartPtrs* __restrict__ pp, u
     block_max_count(m, 0u, ctl);
 }
 
-__global__ void k_zero_vmax(Ctl* ctl) { ctl->vmax_bits = 0; ctl->nonfinite = 0; }
+__global__ void k_zero_vmax(Ctl* ctl) {
+    pdl_wait(); ctl->vmax_bits = 0; ctl->nonfinite = 0; }
 
 __global__ void __launch_bounds__(256) k_permute(PartPtrs* __restrict__ pp, const uint32_t* __restrict__ vals,
                                                  uint32_t n, uint32_t npad) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npad) return;
     if (i < n) {
@@ -230,6 +235,7 @@ __global__ void __launch_bounds__(256) k_permute(PartPtrs* __restrict__ pp, cons
 }
 
 __global__ void k_swap_tables(PartPtrs* pp) {
+    pdl_wait();
     int f = threadIdx.x;
     if (f < NPF) {
         float* t = pp->f[f];
@@ -242,22 +248,22 @@ __global__ void k_swap_tables(PartPtrs* pp) {
 
 cudaError_t launch_p2g(Scene& s) {
     if (s.n == 0) return cudaSuccess;
-    k_p2g<<<div_up(s.n, 256), 256, 0, s.stream>>>(s.pp, s.n, int(s.W), int(s.H), s.dx, s.ctl, s.acc_u, s.acc_uw,
+    launch(s.use_pdl, k_p2g, div_up(s.n, 256), 256, 0, s.stream, s.pp, s.n, int(s.W), int(s.H), s.dx, s.ctl, s.acc_u, s.acc_uw,
                                                     s.acc_v, s.acc_vw, s.density, s.lv[0].fluid);
     return cudaGetLastError();
 }
 
 cudaError_t launch_g2p(Scene& s) {
     if (s.npad == 0) return cudaSuccess;
-    k_g2p<<<div_up(s.npad, 256), 256, 0, s.stream>>>(s.pp, s.npad, int(s.W), int(s.H), s.dx, s.props.border_damping,
+    launch(s.use_pdl, k_g2p, div_up(s.npad, 256), 256, 0, s.stream, s.pp, s.npad, int(s.W), int(s.H), s.dx, s.props.border_damping,
                                                       s.ctl, s.u, s.v, s.u_open, s.v_open);
     return cudaGetLastError();
 }
 
 // Zero the running maximum, then reduce over the current velocities.
 cudaError_t launch_vmax(Scene& s) {
-    k_zero_vmax<<<1, 1, 0, s.stream>>>(s.ctl);
-    if (s.npad) k_vmax<<<div_up(s.npad, 256), 256, 0, s.stream>>>(s.pp, s.npad, s.ctl);
+    launch(s.use_pdl, k_zero_vmax, 1, 1, 0, s.stream, s.ctl);
+    if (s.npad) launch(s.use_pdl, k_vmax, div_up(s.npad, 256), 256, 0, s.stream, s.pp, s.npad, s.ctl);
     return cudaGetLastError();
 }
 
@@ -280,8 +286,8 @@ cudaError_t launch_pack_vec2x8(Scene& s, int which, float* out) {
 
 cudaError_t launch_permute(Scene& s) {
     if (s.npad == 0) return cudaSuccess;
-    k_permute<<<div_up(s.npad, 256), 256, 0, s.stream>>>(s.pp, s.vals, s.n, s.npad);
-    k_swap_tables<<<1, 32, 0, s.stream>>>(s.pp);
+    launch(s.use_pdl, k_permute, div_up(s.npad, 256), 256, 0, s.stream, s.pp, s.vals, s.n, s.npad);
+    launch(s.use_pdl, k_swap_tables, 1, 32, 0, s.stream, s.pp);
     return cudaGetLastError();
 }
 

@@ -28,6 +28,7 @@ constexpr int kScanBlock = 1024;                  // elements per scan block
 
 __global__ void k_morton_keys(const PartPtrs* __restrict__ pp, uint32_t n, float dx, float max_x, float max_y,
                               uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float gx = pp->f[PX][i] / dx, gy = pp->f[PY][i] / dx;  // Vec2x8 / f32x8: per-component division
@@ -40,6 +41,7 @@ __global__ void k_morton_keys(const PartPtrs* __restrict__ pp, uint32_t n, float
 // Per-tile digit histogram, written digit-major: hist[d * nblocks + b].
 __global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n,
                                                              int shift, uint32_t* __restrict__ hist) {
+    pdl_wait();
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -61,6 +63,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* _
                                                                 int shift, const uint32_t* __restrict__ offs,
                                                                 uint32_t* __restrict__ okeys,
                                                                 uint32_t* __restrict__ ovals) {
+    pdl_wait();
     __shared__ uint32_t wh[kSortThreads / 32][256];
     __shared__ uint32_t boff[256];
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -133,6 +136,7 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
 
 __global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t* __restrict__ in, uint32_t n,
                                                      uint32_t* __restrict__ bsum) {
+    pdl_wait();
     uint32_t b0 = blockIdx.x * kScanBlock;
     uint32_t s = 0;
     for (int k = 0; k < kScanBlock / 256; ++k) {
@@ -150,6 +154,7 @@ __global__ void __launch_bounds__(256) k_scan_reduce(const uint32_t* __restrict_
 }
 
 __global__ void __launch_bounds__(1024) k_scan_blocksums(uint32_t* __restrict__ bsum, uint32_t nb) {
+    pdl_wait();
     uint32_t carry = 0;
     for (uint32_t c = 0; c < nb; c += 1024) {
         uint32_t i = c + threadIdx.x;
@@ -163,6 +168,7 @@ __global__ void __launch_bounds__(1024) k_scan_blocksums(uint32_t* __restrict__ 
 
 __global__ void __launch_bounds__(256) k_scan_down(uint32_t* __restrict__ data, uint32_t n,
                                                    const uint32_t* __restrict__ bsum) {
+    pdl_wait();
     uint32_t b0 = blockIdx.x * kScanBlock;
     uint32_t carry = bsum[blockIdx.x];
     for (int k = 0; k < kScanBlock / 256; ++k) {
@@ -180,9 +186,9 @@ __global__ void __launch_bounds__(256) k_scan_down(uint32_t* __restrict__ data, 
 cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t n, uint32_t* tmp, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     uint32_t nb = div_up(n, kScanBlock);
-    k_scan_reduce<<<nb, 256, 0, st>>>(data, n, tmp);
-    k_scan_blocksums<<<1, 1024, 0, st>>>(tmp, nb);
-    k_scan_down<<<nb, 256, 0, st>>>(data, n, tmp);
+    launch(st != nullptr, k_scan_reduce, nb, 256, 0, st, data, n, tmp);
+    launch(st != nullptr, k_scan_blocksums, 1, 1024, 0, st, tmp, nb);
+    launch(st != nullptr, k_scan_down, nb, 256, 0, st, data, n, tmp);
     return cudaGetLastError();
 }
 
@@ -206,7 +212,7 @@ static int key_bits(const Scene& s) {
 cudaError_t launch_sort(Scene& s) {
     if (s.n == 0) return cudaSuccess;
     float max_x = float(s.W > 0 ? s.W - 1 : 0), max_y = float(s.H > 0 ? s.H - 1 : 0);
-    k_morton_keys<<<div_up(s.n, 256), 256, 0, s.stream>>>(s.pp, s.n, s.dx, max_x, max_y, s.keys, s.vals);
+    launch(s.use_pdl, k_morton_keys, div_up(s.n, 256), 256, 0, s.stream, s.pp, s.n, s.dx, max_x, max_y, s.keys, s.vals);
     uint32_t nb = div_up(s.n, kSortTile);
     int bits = key_bits(s);
     uint32_t* k_in = s.keys;
@@ -214,10 +220,10 @@ cudaError_t launch_sort(Scene& s) {
     uint32_t* k_out = s.keys_alt;
     uint32_t* v_out = s.vals_alt;
     for (int shift = 0; shift < bits; shift += 8) {
-        k_sort_hist<<<nb, kSortThreads, 0, s.stream>>>(k_in, s.n, shift, s.sort_hist);
+        launch(s.use_pdl, k_sort_hist, nb, kSortThreads, 0, s.stream, k_in, s.n, shift, s.sort_hist);
         cudaError_t e = exclusive_scan_u32(s.sort_hist, 256u * nb, s.sort_scan_tmp, s.stream);
         if (e != cudaSuccess) return e;
-        k_sort_scatter<<<nb, kSortThreads, 0, s.stream>>>(k_in, v_in, s.n, shift, s.sort_hist, k_out, v_out);
+        launch(s.use_pdl, k_sort_scatter, nb, kSortThreads, 0, s.stream, k_in, v_in, s.n, shift, s.sort_hist, k_out, v_out);
         std::swap(k_in, k_out);
         std::swap(v_in, v_out);
     }
@@ -241,10 +247,10 @@ cudaError_t radix_sort_pairs_in(uint32_t* keys, uint32_t* vals, uint32_t* keys_a
     uint32_t* k_out = keys_alt;
     uint32_t* v_out = vals_alt;
     for (int shift = 0; shift < bits; shift += 8) {
-        k_sort_hist<<<nb, kSortThreads, 0, st>>>(k_in, n, shift, hist);
+        launch(st != nullptr, k_sort_hist, nb, kSortThreads, 0, st, k_in, n, shift, hist);
         cudaError_t e = exclusive_scan_u32(hist, 256u * nb, scan_tmp, st);
         if (e != cudaSuccess) return e;
-        k_sort_scatter<<<nb, kSortThreads, 0, st>>>(k_in, v_in, n, shift, hist, k_out, v_out);
+        launch(st != nullptr, k_sort_scatter, nb, kSortThreads, 0, st, k_in, v_in, n, shift, hist, k_out, v_out);
         std::swap(k_in, k_out);
         std::swap(v_in, v_out);
     }
