@@ -295,6 +295,25 @@ __device__ __forceinline__ bool block_sum_last(F2 v, double* partials, uint32_t*
     return true;
 }
 
+// ---- segment walks -------------------------------------------------------------
+// A warp walks the segments s = warp, warp + nwarps, ... of a level (one
+// non-zero 32-cell mask word each); the word of its next segment is loaded
+// one step ahead, so a step's cell loads do not wait for their word (on
+// large levels a warp has many segments).  w0: the first word if the caller
+// loaded it already (else 0xFFFFFFFF).
+__device__ __forceinline__ uint32_t seg_first(const uint32_t* seg, uint32_t nseg, uint32_t warp, uint32_t w0) {
+    return w0 != 0xFFFFFFFFu ? w0 : (warp < nseg ? seg[warp] : 0u);
+}
+__device__ __forceinline__ uint32_t seg_next(const uint32_t* seg, uint32_t nseg, uint32_t s) {
+    return s < nseg ? seg[s] : 0u;
+}
+// Returns the current word and loads the one of segment s into `next`.
+__device__ __forceinline__ uint32_t seg_step(const uint32_t* seg, uint32_t nseg, uint32_t s, uint32_t& next) {
+    const uint32_t cur = next;
+    next = seg_next(seg, nseg, s);
+    return cur;
+}
+
 // ---- split grid reductions ---------------------------------------------------
 // The PCG loop's reductions stop at the block level: each block stores its
 // partial, and the kernel that needs the total sums the partials itself after

@@ -15,10 +15,11 @@
 namespace apic {
 namespace pcg {
 
-#define APIC_BASE_LOOP(B, nseg, warp, nwarps)                                                   \
-    const uint32_t lane_ = threadIdx.x & 31;                                                    \
-    for (uint32_t s_ = (warp); s_ < (nseg); s_ += (nwarps))                                     \
-        if (uint32_t word_ = (B).seg[s_]; ((B).fluid[word_] >> lane_) & 1u)
+#define APIC_BASE_LOOP(B, nseg, warp, nwarps)                                                          \
+    const uint32_t lane_ = threadIdx.x & 31;                                                           \
+    for (uint32_t s_ = (warp), nxt_ = seg_first((B).seg, (nseg), (warp), 0xFFFFFFFFu); s_ < (nseg);    \
+         s_ += (nwarps))                                                                               \
+        if (uint32_t word_ = seg_step((B).seg, (nseg), s_ + (nwarps), nxt_); ((B).fluid[word_] >> lane_) & 1u)
 
 // The same loop over every lane of a segment inside the grid: the body runs
 // without waiting for the mask word, so its loads issue at once, and tests
@@ -29,8 +30,9 @@ namespace pcg {
 // waiting on the previous kernel), else 0xFFFFFFFF.
 #define APIC_BASE_ALL_W0(B, nseg, warp, nwarps, w0)                                                  \
     const uint32_t lane_ = threadIdx.x & 31;                                                         \
-    for (uint32_t s_ = (warp); s_ < (nseg); s_ += (nwarps))                                          \
-        if (const uint32_t word_ = (s_ == (warp) && (w0) != 0xFFFFFFFFu) ? (w0) : (B).seg[s_],       \
+    for (uint32_t s_ = (warp), nxt_ = seg_first((B).seg, (nseg), (warp), (w0)); s_ < (nseg);        \
+         s_ += (nwarps))                                                                             \
+        if (const uint32_t word_ = seg_step((B).seg, (nseg), s_ + (nwarps), nxt_),                   \
             raw_ = word_ * 32 + lane_;                                                               \
             raw_ < (B).cells)                                                                        \
             if (const bool fluid_ = (((B).fluid[word_] >> lane_) & 1u) != 0u; true)

@@ -365,8 +365,9 @@ __device__ __forceinline__ void ph_smooth(const Level& L, uint32_t nseg, uint32_
                                           int init, uint32_t w0 = kNoWord) {
     const uint32_t lane = threadIdx.x & 31;
     const float* e = L.err;
-    for (uint32_t s = warp; s < nseg; s += nwarps) {
-        const uint32_t word = (s == warp && w0 != kNoWord) ? w0 : L.seg[s];
+    for (uint32_t s = warp, nxt = seg_first(L.seg, nseg, warp, w0); s < nseg; s += nwarps) {
+        const uint32_t word = nxt;
+        nxt = seg_next(L.seg, nseg, s + nwarps);
         const uint32_t raw = word * 32 + lane;
         if (raw >= L.cells || int(!is_red(raw, L.w)) != color) continue;
         const bool fluid = (L.fluid[word] >> lane) & 1u;
@@ -382,8 +383,9 @@ __device__ __forceinline__ void ph_smooth(const Level& L, uint32_t nseg, uint32_
 __device__ __forceinline__ void ph_restrict(const Level& f, const Level& c, uint32_t nseg_c, uint32_t warp,
                                             uint32_t nwarps, bool with_red, uint32_t w0 = kNoWord) {
     const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t s = warp; s < nseg_c; s += nwarps) {
-        const uint32_t word = (s == warp && w0 != kNoWord) ? w0 : c.seg[s];
+    for (uint32_t s = warp, nxt = seg_first(c.seg, nseg_c, warp, w0); s < nseg_c; s += nwarps) {
+        const uint32_t word = nxt;
+        nxt = seg_next(c.seg, nseg_c, s + nwarps);
         const uint32_t rc = word * 32 + lane;
         if (rc >= c.cells) continue;
         const bool fluid = (c.fluid[word] >> lane) & 1u;
@@ -414,8 +416,9 @@ __device__ __forceinline__ void ph_prolong(const Level& c, const Level& f, uint3
         const uint32_t r = uint32_t(rf < 0 ? 0 : (rf >= fcells ? fcells - 1 : rf));
         return ce[((r / fw) / 2) * cw + (r % fw) / 2 + cw];
     };
-    for (uint32_t s = warp; s < nseg_f; s += nwarps) {
-        const uint32_t word = (s == warp && w0 != kNoWord) ? w0 : f.seg[s];
+    for (uint32_t s = warp, nxt = seg_first(f.seg, nseg_f, warp, w0); s < nseg_f; s += nwarps) {
+        const uint32_t word = nxt;
+        nxt = seg_next(f.seg, nseg_f, s + nwarps);
         const uint32_t raw = word * 32 + lane;
         if (raw >= f.cells || int(!is_red(raw, fw)) != color) continue;
         const bool fluid = (f.fluid[word] >> lane) & 1u;
@@ -445,8 +448,9 @@ __device__ __forceinline__ F2 ph_prolong_red_rz(const Level& c, const Level& f, 
     const float* ce = c.err;
     const uint32_t fw = f.w, cw = c.w;
     F2 acc{0.0f, 0.0f};
-    for (uint32_t s = warp; s < nseg_f; s += nwarps) {
-        const uint32_t word = (s == warp && w0 != kNoWord) ? w0 : f.seg[s];
+    for (uint32_t s = warp, nxt = seg_first(f.seg, nseg_f, warp, w0); s < nseg_f; s += nwarps) {
+        const uint32_t word = nxt;
+        nxt = seg_next(f.seg, nseg_f, s + nwarps);
         const uint32_t raw = word * 32 + lane;
         if (raw >= f.cells) continue;
         const bool fluid = (f.fluid[word] >> lane) & 1u;
