@@ -133,6 +133,7 @@ struct RenderParamsDev {
     uint32_t ntx, nty, ntiles;  // 16 x 16 pixel tiles
     float fw, fh;               // width, height as floats
     float scale, margin, radius, size;  // pixels per unit, out-of-bounds margin, disc radius, 2 * radius
+    float tex_scale;                    // texels per pixel: 32 / size
     float pick_x, pick_y, pick_r2;      // pick centre and squared radius (< 0: no pick)
     uint32_t bg;                // clear colour, RGBA8 little-endian
 };

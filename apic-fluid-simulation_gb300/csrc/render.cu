@@ -16,8 +16,9 @@
 // a pixel is covered when its centre lies in [x0, x0 + 2R) x [y0, y0 + 2R)
 // (the top-left fill rule), the texture is sampled bilinearly with texel
 // centres at (i + 0.5) / 32 and clamp-to-edge addressing (macroquad's default
-// linear filter and clamp wrap), and the blend runs in float on 8-bit
-// framebuffer values.  Texture hardware quantises its filter weights, so a
+// linear filter and clamp wrap; the texel coordinate is
+// (pixel centre - quad corner) * (32 / 2R) - 0.5), and the blend runs in float
+// on 8-bit framebuffer values.  Texture hardware quantises its filter weights, so a
 // real GL frame may differ from this one by a unit in the last bit; the CPU
 // oracle states the same arithmetic and the GPU frame matches it exactly.
 //
@@ -137,8 +138,9 @@ __global__ void k_tile_ranges(const uint32_t* __restrict__ keys, uint32_t m, uin
     if (j + 1 == m || keys[j + 1] != k) end[k] = j + 1;
 }
 
-__device__ __forceinline__ uint32_t blend8(float c, float a, uint32_t dst) {
-    const float d = float(dst) / 255.0f;
+// d8: the 256 values k / 255 (an 8-bit channel as a float).
+__device__ __forceinline__ uint32_t blend8(float c, float a, uint32_t dst, const float* d8) {
+    const float d = d8[dst];
     const float o = c * a + d * (1.0f - a);
     const float q = o * 255.0f + 0.5f;
     return q >= 255.0f ? 255u : (q > 0.0f ? uint32_t(q) : 0u);
@@ -152,9 +154,11 @@ __global__ void __launch_bounds__(kTileThreads) k_splat_raster(const uint32_t* _
                                                               const float4* __restrict__ quad, RenderParamsDev p,
                                                               uint32_t* __restrict__ frame) {
     __shared__ float tex[kTex * kTex];
+    __shared__ float d8[256];
     __shared__ float4 ent[kTileThreads];
     for (int t = threadIdx.x; t < kTex * kTex; t += kTileThreads)
         tex[t] = float(circle_alpha(t % kTex, t / kTex)) / 255.0f;
+    d8[threadIdx.x] = float(threadIdx.x) / 255.0f;
     const uint32_t tile = blockIdx.x;
     const uint32_t px = (tile % p.ntx) * kTile + (threadIdx.x % kTile);
     const uint32_t py = (tile / p.ntx) * kTile + (threadIdx.x / kTile);
@@ -170,8 +174,8 @@ __global__ void __launch_bounds__(kTileThreads) k_splat_raster(const uint32_t* _
         for (uint32_t e = 0; e < cnt; ++e) {
             const float4 q = ent[e];
             if (!(q.x <= cx && cx < q.x + p.size && q.y <= cy && cy < q.y + p.size)) continue;
-            const float u = (cx - q.x) / p.size * float(kTex) - 0.5f;
-            const float v = (cy - q.y) / p.size * float(kTex) - 0.5f;
+            const float u = (cx - q.x) * p.tex_scale - 0.5f;
+            const float v = (cy - q.y) * p.tex_scale - 0.5f;
             const float fu = floorf(u), fv = floorf(v);
             const float wu = u - fu, wv = v - fv;
             const int iu = int(fu), iv = int(fv);
@@ -181,9 +185,9 @@ __global__ void __launch_bounds__(kTileThreads) k_splat_raster(const uint32_t* _
             const float bot = tex[v1 * kTex + u0] * (1.0f - wu) + tex[v1 * kTex + u1] * wu;
             const float a = top * (1.0f - wv) + bot * wv;
             const float r = q.z;
-            dr = blend8(r, a, dr);
-            dg = blend8(0.5f, a, dg);
-            db = blend8(1.0f - r * 0.5f, a, db);
+            dr = blend8(r, a, dr, d8);
+            dg = blend8(0.5f, a, dg, d8);
+            db = blend8(1.0f - r * 0.5f, a, db, d8);
         }
         __syncthreads();
     }

@@ -1135,6 +1135,7 @@ int apic_render(apic_handle* h, const apic_render_params* rp, apic_render_stats*
     p.margin = q.margin;
     p.radius = q.draw_radius;
     p.size = q.draw_radius * 2.0f;
+    p.tex_scale = 32.0f / p.size;
     p.pick_x = q.pick_x;
     p.pick_y = q.pick_y;
     p.pick_r2 = q.pick_radius < 0.0f ? -1.0f : q.pick_radius * q.pick_radius;

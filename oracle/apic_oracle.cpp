@@ -1539,7 +1539,8 @@ int oracle_write_field(oracle_sim* o, int field, const void* src, uint64_t bytes
 // render_particles (src/main.rs:207-277) as a sequential loop over the
 // particles in index order, each drawn as a textured quad into an RGBA8
 // frame: texture of make_circle_texture (:73-101), bilinear clamp-to-edge
-// sampling with texel centres at (i + 0.5) / 32, a pixel covered when its
+// sampling with texel centres at (i + 0.5) / 32 (texel coordinate
+// (pixel centre - quad corner) * (32 / 2R) - 0.5), a pixel covered when its
 // centre lies in [x0, x0 + 2R), blend src*a + dst*(1 - a) rounded to 8 bits
 // after every particle.
 static uint8_t circle_alpha(int x, int y) {
@@ -1579,6 +1580,7 @@ int oracle_render(uint32_t n, const float* px, const float* py, const float* vx,
     }
     const float fw = float(W), fh = float(H);
     const float R = p.draw_radius, S = p.draw_radius * 2.0f;
+    const float tex_scale = 32.0f / S;  // texels per pixel
     const float pick_r2 = p.pick_radius < 0.0f ? -1.0f : p.pick_radius * p.pick_radius;
     float best = INFINITY;
     int64_t picked = -1;
@@ -1616,8 +1618,8 @@ int oracle_render(uint32_t n, const float* px, const float* py, const float* vx,
             for (long pxi = x_lo; pxi <= x_hi; ++pxi) {
                 const float cx = float(pxi) + 0.5f, cy = float(pyi) + 0.5f;
                 if (!(qx <= cx && cx < qx + S && qy <= cy && cy < qy + S)) continue;
-                const float u = (cx - qx) / S * 32.0f - 0.5f;
-                const float v = (cy - qy) / S * 32.0f - 0.5f;
+                const float u = (cx - qx) * tex_scale - 0.5f;
+                const float v = (cy - qy) * tex_scale - 0.5f;
                 const float fu = std::floor(u), fv = std::floor(v);
                 const float wu = u - fu, wv = v - fv;
                 const int iu = int(fu), iv = int(fv);
