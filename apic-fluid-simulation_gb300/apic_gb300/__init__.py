@@ -24,6 +24,7 @@ OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_NONFINITE, ERR_NOT_CONV
 ERR_UNSUPPORTED = 8
 UPDATE_DISABLE_SORT = 0x1
 SOLVER_REFERENCE, SOLVER_REL_FP32, SOLVER_REL_MIXED = 0, 1, 2
+SERVER_ROUNDS, SERVER_CONTINUOUS = 0, 1
 SCENE_REFERENCE_DEFAULT, SCENE_DAM_BREAK, SCENE_DAM_BREAK_DISK, SCENE_NOISE = 0, 1, 2, 3
 OPT_PERSISTENT_SOLVE = 1
 OPT_FUSED_VCYCLE = 2
@@ -32,6 +33,7 @@ OPT_PDL = 4
 OPT_DSM_VCYCLE = 5
 OPT_CLUSTER_SOLVE = 6
 OPT_WARM_START = 7
+OPT_STREAM_PRIORITY = 8
 
 FIELDS = {
     "pos_x": 0, "pos_y": 1, "vel_x": 2, "vel_y": 3, "cu_x": 4, "cu_y": 5, "cv_x": 6, "cv_y": 7, "tres": 8,
@@ -105,7 +107,9 @@ class ServerStatsC(ctypes.Structure):
                 ("busy_ms", ctypes.c_double), ("elapsed_ms", ctypes.c_double),
                 ("step_p50_ms", ctypes.c_double), ("step_p99_ms", ctypes.c_double),
                 ("request_p50_ms", ctypes.c_double), ("request_p99_ms", ctypes.c_double),
-                ("memory_used", ctypes.c_uint64), ("memory_peak", ctypes.c_uint64)]
+                ("memory_used", ctypes.c_uint64), ("memory_peak", ctypes.c_uint64),
+                ("updates", ctypes.c_uint64), ("prepare_ms", ctypes.c_double), ("host_ms", ctypes.c_double),
+                ("mode", ctypes.c_int32), ("prepare_threads", ctypes.c_uint32)]
 
 
 class RenderParamsC(ctypes.Structure):
@@ -178,6 +182,8 @@ SIGNATURES = {
                                         ctypes.POINTER(ctypes.c_uint64)]),
     "apic_server_create": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_VP)]),
     "apic_server_destroy": (ctypes.c_int, [_VP]),
+    "apic_server_set_mode": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_uint32]),
+    "apic_server_scene_option": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64]),
     "apic_server_submit": (ctypes.c_int, [_VP, ctypes.POINTER(SceneParamsC), ctypes.POINTER(WorldPropsC),
                                           ctypes.c_uint32, ctypes.c_float, ctypes.c_int, ctypes.c_float,
                                           ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]),
@@ -511,12 +517,24 @@ def scene_bytes(width: int, height: int, particles: int) -> int:
 class Server:
     """Continuous-batching request loop over independent scenes (apic_server_*)."""
 
-    def __init__(self, memory_budget_bytes: int, max_active: int, keep_results: bool = False):
+    def __init__(self, memory_budget_bytes: int, max_active: int, keep_results: bool = False,
+                 mode: int = None, prepare_threads: int = 4):
         self._lib = load_library()
         h = _VP()
         _check(self._lib.apic_server_create(memory_budget_bytes, max_active, 1 if keep_results else 0,
                                             ctypes.byref(h)), "apic_server_create")
         self._h = h
+        if mode is not None:
+            self.set_mode(mode, prepare_threads)
+
+    def set_mode(self, mode: int, prepare_threads: int = 4) -> None:
+        """SERVER_CONTINUOUS (default) or SERVER_ROUNDS; only while no scene is admitted."""
+        _check(self._lib.apic_server_set_mode(self._h, mode, prepare_threads), "apic_server_set_mode")
+
+    def scene_option(self, option: int, value: int, min_cells: int = 0, max_cells: int = (1 << 64) - 1) -> None:
+        """Apic.set_option(option, value) on every scene with min_cells..max_cells cells."""
+        _check(self._lib.apic_server_scene_option(self._h, option, value, min_cells, max_cells),
+               "apic_server_scene_option")
 
     def submit(self, scene: SceneParamsC, props: WorldProperties, steps: int, frame_deltatime: float,
                solver: int = SOLVER_REL_MIXED, rel_tol: float = 1e-6, max_iterations: int = 500) -> int:

@@ -192,6 +192,7 @@ struct Scene {
     uint32_t scan_tmp_len = 0;
 
     cudaStream_t stream = nullptr;
+    int priority = 0;                         // stream priority: levels above the lowest
     cudaStream_t cap_stream = nullptr;        // stream used to record graphs
     cudaGraphExec_t update_exec = nullptr;    // whole Apic::update as one graph
     GridSync* gsync = nullptr;                // persistent solver barrier
@@ -307,6 +308,8 @@ int update_launch(apic_handle* h, uint32_t flags, float frame_dt);
 int create_scene(uint32_t width, uint32_t height, float cell_size, const apic_world_props* props,
                  bool default_particles, apic_handle** out);
 int update_finish(apic_handle* h);
+int update_prepare(apic_handle* h);       // build the update graph ahead of the first update
+cudaStream_t scene_stream(apic_handle* h);
 
 // helpers shared by the launchers
 inline uint32_t div_up(uint64_t a, uint64_t b) { return uint32_t((a + b - 1) / b); }

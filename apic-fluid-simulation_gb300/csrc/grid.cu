@@ -14,8 +14,8 @@
 //   k_coarsen        one multigrid level from its finer level (:1499-1602).
 //   k_gradient       pressure projection per face (:1958-2055), fused with the
 //                    post-force add (:2453-2458).
-//   k_extrapolate    one Jacobi sweep of velocity extrapolation for u and v
-//                    (:2266-2350).
+//   k_extrapolate2   two Jacobi sweeps of velocity extrapolation for u and v
+//                    in shared-memory tiles (:2266-2350).
 //
 // Cell stages run one warp per non-zero 32-bit mask word ("segment"): lane k
 // owns raw cell 32*word + k, so every field access of a warp is one 128-byte
@@ -426,37 +426,84 @@ __global__ void __launch_bounds__(256) k_gradient(uint32_t uf, uint32_t vf, int 
     }
 }
 
-__global__ void __launch_bounds__(256) k_extrapolate(uint32_t uf, uint32_t vf, int W, int H,
-                                                     const float* __restrict__ ou, const uint8_t* __restrict__ ovu,
-                                                     float* __restrict__ nu, uint8_t* __restrict__ nvu,
-                                                     const float* __restrict__ ov, const uint8_t* __restrict__ ovv,
-                                                     float* __restrict__ nv, uint8_t* __restrict__ nvv) {
+// Velocity extrapolation, two Jacobi sweeps per launch (src/apic.rs:2266-2350
+// runs four, swapping buffers after each).  A CTA owns a kExTX x kExTY tile
+// of one face field (u: (W+1) x H, v: W x (H+1)) and stages the tile plus a
+// two-face halo in shared memory; sweep 1 runs on the halo-shrunk region,
+// sweep 2 on the tile, which is written out.  A neighbour outside the field
+// reads as invalid, which is exactly the reference's x > 0 / x < width /
+// y > 0 / y < height guards, and every face adds its valid neighbours in the
+// reference's order (x-1, x+1, y-1, y+1) before the one division, so each
+// sweep's values and flags are bit-identical to a sweep over the whole grid.
+constexpr int kExTX = 128, kExTY = 24, kExHalo = 2;
+constexpr int kExRX = kExTX + 2 * kExHalo, kExRY = kExTY + 2 * kExHalo;
+
+struct ExField {
+    const float* in;
+    const uint8_t* in_ok;
+    float* out;
+    uint8_t* out_ok;
+    int w, h;          // faces per row, rows
+    int tiles_x;       // tiles per row of tiles
+};
+
+__device__ __forceinline__ void ex_face(const float* val, const uint8_t* ok, int i, float* nv, uint8_t* nok) {
+    if (ok[i]) { *nv = val[i]; *nok = 1; return; }
+    float sum = 0.0f;
+    uint32_t cnt = 0;
+    if (ok[i - 1]) { sum += val[i - 1]; cnt++; }
+    if (ok[i + 1]) { sum += val[i + 1]; cnt++; }
+    if (ok[i - kExRX]) { sum += val[i - kExRX]; cnt++; }
+    if (ok[i + kExRX]) { sum += val[i + kExRX]; cnt++; }
+    if (cnt > 0) { *nv = sum / float(cnt); *nok = 1; }
+    else { *nv = val[i]; *nok = 0; }
+}
+
+__global__ void __launch_bounds__(256) k_extrapolate2(ExField fu, ExField fv, int tiles_u) {
+    __shared__ float s_val[2][kExRX * kExRY];
+    __shared__ uint8_t s_ok[2][kExRX * kExRY];
+    const bool is_u = int(blockIdx.x) < tiles_u;
+    const ExField& F = is_u ? fu : fv;
+    const int t = is_u ? int(blockIdx.x) : int(blockIdx.x) - tiles_u;
+    const int x0 = (t % F.tiles_x) * kExTX - kExHalo, y0 = (t / F.tiles_x) * kExTY - kExHalo;
     pdl_wait();
-    uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= uf + vf) return;
-    if (f < uf) {
-        uint32_t x = f % uint32_t(W + 1), y = f / uint32_t(W + 1);
-        if (ovu[f]) { nu[f] = ou[f]; nvu[f] = 1; return; }
-        float sum = 0.0f;
-        uint32_t cnt = 0;
-        if (x > 0 && ovu[f - 1]) { sum += ou[f - 1]; cnt++; }
-        if (x < uint32_t(W) && ovu[f + 1]) { sum += ou[f + 1]; cnt++; }
-        if (y > 0 && ovu[f - (W + 1)]) { sum += ou[f - (W + 1)]; cnt++; }
-        if (y < uint32_t(H - 1) && ovu[f + W + 1]) { sum += ou[f + W + 1]; cnt++; }
-        if (cnt > 0) { nu[f] = sum / float(cnt); nvu[f] = 1; }
-        else { nu[f] = ou[f]; nvu[f] = 0; }
-    } else {
-        uint32_t g = f - uf;
-        uint32_t x = g % uint32_t(W), y = g / uint32_t(W);
-        if (ovv[g]) { nv[g] = ov[g]; nvv[g] = 1; return; }
-        float sum = 0.0f;
-        uint32_t cnt = 0;
-        if (x > 0 && ovv[g - 1]) { sum += ov[g - 1]; cnt++; }
-        if (x < uint32_t(W - 1) && ovv[g + 1]) { sum += ov[g + 1]; cnt++; }
-        if (y > 0 && ovv[g - W]) { sum += ov[g - W]; cnt++; }
-        if (y < uint32_t(H) && ovv[g + W]) { sum += ov[g + W]; cnt++; }
-        if (cnt > 0) { nv[g] = sum / float(cnt); nvv[g] = 1; }
-        else { nv[g] = ov[g]; nvv[g] = 0; }
+    for (int i = threadIdx.x; i < kExRX * kExRY; i += blockDim.x) {
+        const int gx = x0 + i % kExRX, gy = y0 + i / kExRX;
+        float v = 0.0f;
+        uint8_t k = 0;
+        if (gx >= 0 && gx < F.w && gy >= 0 && gy < F.h) {
+            const size_t g = size_t(gy) * F.w + gx;
+            v = F.in[g];
+            k = F.in_ok[g];
+        }
+        s_val[0][i] = v;
+        s_ok[0][i] = k;
+    }
+    __syncthreads();
+    // sweep 1 on the region one face inside the staged one (faces outside
+    // the field stay invalid)
+    for (int j = threadIdx.x; j < (kExRX - 2) * (kExRY - 2); j += blockDim.x) {
+        const int rx = 1 + j % (kExRX - 2), ry = 1 + j / (kExRX - 2);
+        const int i = ry * kExRX + rx;
+        const int gx = x0 + rx, gy = y0 + ry;
+        float v = 0.0f;
+        uint8_t k = 0;
+        if (gx >= 0 && gx < F.w && gy >= 0 && gy < F.h) ex_face(s_val[0], s_ok[0], i, &v, &k);
+        s_val[1][i] = v;
+        s_ok[1][i] = k;
+    }
+    __syncthreads();
+    // sweep 2 on the tile, written out
+    for (int j = threadIdx.x; j < kExTX * kExTY; j += blockDim.x) {
+        const int rx = kExHalo + j % kExTX, ry = kExHalo + j / kExTX;
+        const int gx = x0 + rx, gy = y0 + ry;
+        if (gx >= F.w || gy >= F.h) continue;
+        float v;
+        uint8_t k;
+        ex_face(s_val[1], s_ok[1], ry * kExRX + rx, &v, &k);
+        const size_t g = size_t(gy) * F.w + gx;
+        F.out[g] = v;
+        F.out_ok[g] = k;
     }
 }
 
@@ -544,15 +591,24 @@ cudaError_t launch_post_forces(Scene& s) {
     return cudaGetLastError();
 }
 
+// The reference's four sweeps as two launches of two sweeps each:
+// u, v -> u_alt, v_alt -> u, v (the result ends where the next stages read it).
 cudaError_t launch_extrapolate(Scene& s) {
-    uint32_t nf = s.uf + s.vf;
-    uint32_t g = div_up(nf, 256);
-    for (int k = 0; k < 2; ++k) {
-        launch(s.use_pdl, k_extrapolate, g, 256, 0, s.stream, s.uf, s.vf, int(s.W), int(s.H), s.u, s.valid_u, s.u_alt,
-                                               s.valid_u_alt, s.v, s.valid_v, s.v_alt, s.valid_v_alt);
-        launch(s.use_pdl, k_extrapolate, g, 256, 0, s.stream, s.uf, s.vf, int(s.W), int(s.H), s.u_alt, s.valid_u_alt, s.u,
-                                               s.valid_u, s.v_alt, s.valid_v_alt, s.v, s.valid_v);
-    }
+    auto field = [](const float* in, const uint8_t* in_ok, float* out, uint8_t* out_ok, int w, int h) {
+        ExField f;
+        f.in = in; f.in_ok = in_ok; f.out = out; f.out_ok = out_ok; f.w = w; f.h = h;
+        f.tiles_x = int(div_up(uint32_t(w), kExTX));
+        return f;
+    };
+    const int W = int(s.W), H = int(s.H);
+    const uint32_t tiles_u = div_up(uint32_t(W + 1), kExTX) * div_up(uint32_t(H), kExTY);
+    const uint32_t tiles_v = div_up(uint32_t(W), kExTX) * div_up(uint32_t(H + 1), kExTY);
+    launch(s.use_pdl, k_extrapolate2, tiles_u + tiles_v, 256, 0, s.stream,
+           field(s.u, s.valid_u, s.u_alt, s.valid_u_alt, W + 1, H), field(s.v, s.valid_v, s.v_alt, s.valid_v_alt, W, H + 1),
+           int(tiles_u));
+    launch(s.use_pdl, k_extrapolate2, tiles_u + tiles_v, 256, 0, s.stream,
+           field(s.u_alt, s.valid_u_alt, s.u, s.valid_u, W + 1, H), field(s.v_alt, s.valid_v_alt, s.v, s.valid_v, W, H + 1),
+           int(tiles_u));
     return cudaGetLastError();
 }
 

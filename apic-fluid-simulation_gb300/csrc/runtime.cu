@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -165,50 +166,114 @@ __global__ void k_force_box(float wx, float wy, float radius, float cs, int W, i
 
 // ---- host helpers ---------------------------------------------------------
 
-template <class T> cudaError_t dalloc(T** p, size_t count) {
+// Scene buffers come from a stream-ordered memory pool of the library's own
+// (one per device, kept for the life of the process), allocated and released
+// in order on the scene's stream.  Releasing them does not synchronise the
+// whole device the way cudaFree does, so a scene retired while others run
+// (the request server) never stalls the scenes still on the GPU; the pool
+// keeps released memory for the next scene (no release threshold).
+constexpr int kMaxPoolDevices = 64;
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pool[kMaxPoolDevices] = {};
+
+cudaError_t scene_pool(cudaMemPool_t* out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxPoolDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (!g_pool[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if ((e = cudaMemPoolCreate(&pool, &props)) != cudaSuccess) return e;
+        uint64_t keep = ~0ull;
+        if ((e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess) {
+            cudaMemPoolDestroy(pool);
+            return e;
+        }
+        g_pool[dev] = pool;
+    }
+    *out = g_pool[dev];
+    return cudaSuccess;
+}
+
+// Zeroed device buffer of `count` T, in stream order on st: use it from
+// another stream only after st has been synchronised.
+template <class T> cudaError_t dalloc(T** p, size_t count, cudaStream_t st) {
     *p = nullptr;
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = scene_pool(&pool);
     if (e != cudaSuccess) return e;
-    return cudaMemset(*p, 0, sizeof(T) * count);
+    e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(p), sizeof(T) * count, pool, st);
+    if (e != cudaSuccess) return e;
+    return cudaMemsetAsync(*p, 0, sizeof(T) * count, st);
 }
-template <class T> void dfree(T*& p) {
-    if (p) cudaFree(p);
+template <class T> void dfree(T*& p, cudaStream_t st) {
+    if (p) cudaFreeAsync(p, st);
     p = nullptr;
+}
+
+// Pinned host mirrors of the control blocks come from a process-wide free
+// list, for the same reason: cudaFreeHost synchronises the device.
+constexpr int kCtlPerSlab = 64;
+std::mutex g_ctl_mutex;
+std::vector<Ctl*> g_ctl_free;
+
+Ctl* ctl_mirror_get() {
+    std::lock_guard<std::mutex> lock(g_ctl_mutex);
+    if (g_ctl_free.empty()) {
+        Ctl* slab = nullptr;
+        if (cudaMallocHost(reinterpret_cast<void**>(&slab), sizeof(Ctl) * kCtlPerSlab) != cudaSuccess) return nullptr;
+        for (int i = kCtlPerSlab - 1; i >= 0; --i) g_ctl_free.push_back(slab + i);
+    }
+    Ctl* c = g_ctl_free.back();
+    g_ctl_free.pop_back();
+    return c;
+}
+void ctl_mirror_put(Ctl* c) {
+    if (!c) return;
+    std::lock_guard<std::mutex> lock(g_ctl_mutex);
+    g_ctl_free.push_back(c);
 }
 
 uint32_t even_words(uint64_t bits) { return uint32_t(((bits + 63) / 64) * 2); }
 
 void free_particles(Scene& s) {
-    for (int f = 0; f < NPF; ++f) { dfree(s.part[f]); dfree(s.part_alt[f]); }
-    dfree(s.keys); dfree(s.vals); dfree(s.keys_alt); dfree(s.vals_alt);
-    dfree(s.sort_hist); dfree(s.sort_scan_tmp);
+    const cudaStream_t st = s.stream;
+    for (int f = 0; f < NPF; ++f) { dfree(s.part[f], st); dfree(s.part_alt[f], st); }
+    dfree(s.keys, st); dfree(s.vals, st); dfree(s.keys_alt, st); dfree(s.vals_alt, st);
+    dfree(s.sort_hist, st); dfree(s.sort_scan_tmp, st);
     s.part_cap = 0;
 }
 
 void free_scene(Scene& s) {
+    const cudaStream_t st = s.stream;
     free_particles(s);
-    dfree(s.pp);
+    dfree(s.pp, st);
     float** fl[] = {&s.u, &s.v, &s.u_alt, &s.v_alt, &s.acc_u, &s.acc_uw, &s.acc_v, &s.acc_vw, &s.ext_u,
                     &s.ext_v, &s.post_u, &s.post_v, &s.density, &s.sm_a, &s.sm_b, &s.pressure, &s.search,
                     &s.ap, &s.corr, &s.cg_s, &s.cg_ap, &s.cg_r};
-    for (float** p : fl) dfree(*p);
-    dfree(s.valid_u); dfree(s.valid_v); dfree(s.valid_u_alt); dfree(s.valid_v_alt);
-    dfree(s.u_open); dfree(s.v_open); dfree(s.obstacle);
-    dfree(s.p64); dfree(s.b64);
+    for (float** p : fl) dfree(*p, st);
+    dfree(s.valid_u, st); dfree(s.valid_v, st); dfree(s.valid_u_alt, st); dfree(s.valid_v_alt, st);
+    dfree(s.u_open, st); dfree(s.v_open, st); dfree(s.obstacle, st);
+    dfree(s.p64, st); dfree(s.b64, st);
     for (int l = 0; l < s.nlevels; ++l) {
         Level& L = s.lv[l];
-        dfree(L.fluid); dfree(L.seg); dfree(L.diag); dfree(L.inv_diag); dfree(L.px); dfree(L.py);
-        dfree(L.res); dfree(L.err); dfree(L.err2);
+        dfree(L.fluid, st); dfree(L.seg, st); dfree(L.diag, st); dfree(L.inv_diag, st); dfree(L.px, st);
+        dfree(L.py, st); dfree(L.res, st); dfree(L.err, st); dfree(L.err2, st);
     }
     free_render(s);
-    dfree(s.vec_stage);
+    dfree(s.vec_stage, st);
     s.vec_stage = nullptr;
     s.vec_stage_floats = 0;
-    dfree(s.ctl);
-    if (s.ctl_host) cudaFreeHost(s.ctl_host);
+    dfree(s.ctl, st);
+    ctl_mirror_put(s.ctl_host);
     s.ctl_host = nullptr;
-    dfree(s.partials); dfree(s.scan_tmp); dfree(s.gsync);
+    dfree(s.partials, st); dfree(s.scan_tmp, st); dfree(s.gsync, st);
     if (s.ev_a) cudaEventDestroy(s.ev_a);
     if (s.ev_b) cudaEventDestroy(s.ev_b);
     if (s.update_exec) cudaGraphExecDestroy(s.update_exec);
@@ -249,10 +314,11 @@ int upload_world(apic_handle* h) {
     Scene& s = h->s;
     std::vector<uint32_t> uo, vo;
     open_masks(s, h->obstacle_host, uo, vo);
-    CK(cudaMemcpy(s.obstacle, h->obstacle_host.data(), sizeof(uint32_t) * h->obstacle_host.size(),
-                  cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s.u_open, uo.data(), sizeof(uint32_t) * uo.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s.v_open, vo.data(), sizeof(uint32_t) * vo.size(), cudaMemcpyHostToDevice));
+    // in order on the scene's stream (pageable sources are staged before each call returns)
+    CK(cudaMemcpyAsync(s.obstacle, h->obstacle_host.data(), sizeof(uint32_t) * h->obstacle_host.size(),
+                       cudaMemcpyHostToDevice, s.stream));
+    CK(cudaMemcpyAsync(s.u_open, uo.data(), sizeof(uint32_t) * uo.size(), cudaMemcpyHostToDevice, s.stream));
+    CK(cudaMemcpyAsync(s.v_open, vo.data(), sizeof(uint32_t) * vo.size(), cudaMemcpyHostToDevice, s.stream));
     s.world_ready = true;
     return APIC_OK;
 }
@@ -260,15 +326,16 @@ int upload_world(apic_handle* h) {
 int alloc_particles(Scene& s, uint32_t npad, uint32_t n) {
     if (npad <= s.part_cap && s.part_cap > 0) return APIC_OK;
     free_particles(s);
+    const cudaStream_t st = s.stream;
     for (int f = 0; f < NPF; ++f) {
-        CK(dalloc(&s.part[f], npad));
-        CK(dalloc(&s.part_alt[f], npad));
+        CK(dalloc(&s.part[f], npad, st));
+        CK(dalloc(&s.part_alt[f], npad, st));
     }
-    CK(dalloc(&s.keys, npad)); CK(dalloc(&s.vals, npad));
-    CK(dalloc(&s.keys_alt, npad)); CK(dalloc(&s.vals_alt, npad));
+    CK(dalloc(&s.keys, npad, st)); CK(dalloc(&s.vals, npad, st));
+    CK(dalloc(&s.keys_alt, npad, st)); CK(dalloc(&s.vals_alt, npad, st));
     uint32_t nb = div_up(std::max<uint32_t>(n, 1), kSortTile);
-    CK(dalloc(&s.sort_hist, size_t(256) * nb));
-    CK(dalloc(&s.sort_scan_tmp, div_up(uint64_t(256) * nb, 1024) + 1));
+    CK(dalloc(&s.sort_hist, size_t(256) * nb, st));
+    CK(dalloc(&s.sort_scan_tmp, div_up(uint64_t(256) * nb, 1024) + 1, st));
     s.part_cap = npad;
     return APIC_OK;
 }
@@ -282,20 +349,21 @@ int load_particles(apic_handle* h, uint32_t n, const float* px, const float* py,
     // sort scratch may need to grow when n grows within the same capacity
     {
         uint32_t nb = div_up(std::max<uint32_t>(n, 1), kSortTile);
-        dfree(s.sort_hist); dfree(s.sort_scan_tmp);
-        CK(dalloc(&s.sort_hist, size_t(256) * nb));
-        CK(dalloc(&s.sort_scan_tmp, div_up(uint64_t(256) * nb, 1024) + 1));
+        dfree(s.sort_hist, s.stream); dfree(s.sort_scan_tmp, s.stream);
+        CK(dalloc(&s.sort_hist, size_t(256) * nb, s.stream));
+        CK(dalloc(&s.sort_scan_tmp, div_up(uint64_t(256) * nb, 1024) + 1, s.stream));
     }
     // a new particle set: the next mixed solve starts from zero pressure
-    if (s.p64) CK(cudaMemset(s.p64, 0, sizeof(double) * (uint64_t(s.cells) + 2ull * s.W)));
+    if (s.p64) CK(cudaMemsetAsync(s.p64, 0, sizeof(double) * (uint64_t(s.cells) + 2ull * s.W), s.stream));
     std::vector<float> buf(std::max<uint32_t>(npad, 1), 0.0f);
     auto put = [&](int f, const float* src, bool pad_last) -> int {
         std::fill(buf.begin(), buf.end(), 0.0f);
         if (src) std::memcpy(buf.data(), src, sizeof(float) * n);
         if (pad_last && n > 0 && src)
             for (uint32_t l = n; l < npad; ++l) buf[l] = src[n - 1];
-        CK(cudaMemcpy(s.part[f], buf.data(), sizeof(float) * npad, cudaMemcpyHostToDevice));
-        CK(cudaMemset(s.part_alt[f], 0, sizeof(float) * npad));
+        // from pageable memory: staged before the call returns, so buf can be refilled
+        CK(cudaMemcpyAsync(s.part[f], buf.data(), sizeof(float) * npad, cudaMemcpyHostToDevice, s.stream));
+        CK(cudaMemsetAsync(s.part_alt[f], 0, sizeof(float) * npad, s.stream));
         return APIC_OK;
     };
     if (npad) {
@@ -306,7 +374,7 @@ int load_particles(apic_handle* h, uint32_t n, const float* px, const float* py,
     }
     PartPtrs t;
     for (int f = 0; f < NPF; ++f) { t.f[f] = s.part[f]; t.alt[f] = s.part_alt[f]; }
-    CK(cudaMemcpy(s.pp, &t, sizeof(PartPtrs), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(s.pp, &t, sizeof(PartPtrs), cudaMemcpyHostToDevice, s.stream));
     s.n = n;
     s.nchunks = nchunks;
     s.npad = npad;
@@ -517,7 +585,7 @@ int apic::create_scene(uint32_t width, uint32_t height, float cell_size, const a
 
     auto bail = [&](int rc) { free_scene(s); delete h; return rc; };
     cudaError_t e;
-#define AL(ptr, count) if ((e = dalloc(&(ptr), (count))) != cudaSuccess) return bail(fail(APIC_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e)))
+#define AL(ptr, count) if ((e = dalloc(&(ptr), (count), s.stream)) != cudaSuccess) return bail(fail(APIC_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e)))
     if ((e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking)) != cudaSuccess)
         return bail(fail(APIC_ERR_CUDA, cudaGetErrorString(e)));
     if ((e = cudaStreamCreateWithFlags(&s.cap_stream, cudaStreamNonBlocking)) != cudaSuccess)
@@ -558,7 +626,10 @@ int apic::create_scene(uint32_t width, uint32_t height, float cell_size, const a
     s.scan_tmp_len = 3 * (div_up(max_words, 1024) + 1);
     AL(s.scan_tmp, s.scan_tmp_len);
 #undef AL
-    if ((e = cudaMallocHost(&s.ctl_host, sizeof(Ctl))) != cudaSuccess) return bail(fail(APIC_ERR_OOM, "pinned alloc"));
+    // the buffers are ordered on the scene's stream; the copies below run on
+    // the legacy stream
+    if ((e = cudaStreamSynchronize(s.stream)) != cudaSuccess) return bail(fail(APIC_ERR_CUDA, cudaGetErrorString(e)));
+    if (!(s.ctl_host = ctl_mirror_get())) return bail(fail(APIC_ERR_OOM, "pinned alloc"));
     std::memset(s.ctl_host, 0, sizeof(Ctl));
     s.ctl_host->prev_dt = 1.0f / 60.0f;  // src/apic.rs:824
     s.ctl_host->cfl_cs = props->cfl * cell_size;
@@ -680,6 +751,17 @@ int update_finish(apic_handle* h) {
     if (c.status & kStatusBadStep) return fail(APIC_ERR_NONFINITE, "substep size is not positive (non-finite velocities)");
     return APIC_OK;
 }
+
+// Build the update graph before the first update, so that update can launch
+// at once (the request server does this on its preparation threads).
+int update_prepare(apic_handle* h) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    if (h->s.profiling) return APIC_OK;
+    return ensure_update_graph(h->s);
+}
+
+// The stream of a scene (the request server polls it for completion).
+cudaStream_t scene_stream(apic_handle* h) { return h ? h->s.stream : nullptr; }
 
 }  // namespace apic
 
@@ -950,10 +1032,10 @@ int apic_read_vec2x8(apic_handle* h, int which, float* dst, uint64_t floats) {
     // f32x8}), interleaved on the device, then one contiguous copy
     if (s.vec_stage_floats < floats) {
         CK(cudaStreamSynchronize(s.stream));
-        dfree(s.vec_stage);
+        dfree(s.vec_stage, s.stream);
         s.vec_stage = nullptr;
         s.vec_stage_floats = 0;
-        if (dalloc(&s.vec_stage, floats) != cudaSuccess)
+        if (dalloc(&s.vec_stage, floats, s.stream) != cudaSuccess)
             return fail(APIC_ERR_OOM, "out of device memory (Vec2x8 staging)");
         s.vec_stage_floats = uint32_t(floats);
     }
@@ -1219,6 +1301,20 @@ int apic_set_option(apic_handle* h, int option, int value) {
             s.warm_start = value != 0;
             invalidate_graphs(s);
             return APIC_OK;
+        case APIC_OPT_STREAM_PRIORITY: {
+            if (value < 0) return fail(APIC_ERR_INVALID_ARG, "stream priority must be >= 0");
+            // the scene's stream is idle (synchronised above): replace it by
+            // one of the asked priority; graphs launch into it unchanged
+            int least = 0, greatest = 0;
+            CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+            const int prio = std::max(greatest, least - value);
+            cudaStream_t ns = nullptr;
+            CK(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, prio));
+            if (s.stream) cudaStreamDestroy(s.stream);
+            s.stream = ns;
+            s.priority = least - prio;
+            return APIC_OK;
+        }
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }
@@ -1237,6 +1333,7 @@ int apic_get_option(apic_handle* h, int option, int* value) {
             return APIC_OK;
         case APIC_OPT_CLUSTER_SOLVE: *value = h->s.cluster_solve_ctas; return APIC_OK;
         case APIC_OPT_WARM_START: *value = h->s.warm_start ? 1 : 0; return APIC_OK;
+        case APIC_OPT_STREAM_PRIORITY: *value = h->s.priority; return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }

@@ -551,8 +551,24 @@ def served_stream(A, rate, seconds, seed=4, lo=64, hi=1024):
     return out
 
 
-def serve_stream(A, stream, budget, max_active, dt, time_limit):
-    sv = A.Server(budget, max_active)
+def parse_scene_options(A, specs):
+    """--scene-option NAME=VALUE[@[MIN_CELLS:]MAX_CELLS]: (option, value, min_cells, max_cells)."""
+    out = []
+    for spec in specs or []:
+        name, rest = spec.split("=", 1)
+        value, _, cells = rest.partition("@")
+        lo, hi = 0, (1 << 64) - 1
+        if cells:
+            a, sep, b = cells.partition(":")
+            lo, hi = (int(a), int(b)) if sep else (0, int(a))
+        out.append((getattr(A, "OPT_" + name.upper()), int(value), lo, hi))
+    return out
+
+
+def serve_stream(A, stream, budget, max_active, dt, time_limit, mode, threads, rules=()):
+    sv = A.Server(budget, max_active, mode=mode, prepare_threads=threads)
+    for opt, value, lo, hi in rules:
+        sv.scene_option(opt, value, lo, hi)
     t0 = time.perf_counter()
     nxt = 0
     while True:
@@ -584,23 +600,34 @@ def run_served(args):
     budget = int(args.budget_gb * (1 << 30))
     dt = 1.0 / 240.0
     res = {}
-    for name, active in (("served", args.max_active), ("plain", 1)):
-        st, n_sub = serve_stream(A, stream, budget, active, dt, args.time_limit)
+    rules = parse_scene_options(A, args.scene_option)
+    arms = [("served", args.max_active, A.SERVER_CONTINUOUS, args.prepare_threads, rules)]
+    if args.served_rounds:
+        arms.append(("served_rounds", args.max_active, A.SERVER_ROUNDS, 0, rules))
+    if not args.no_plain:
+        arms.append(("plain", 1, A.SERVER_ROUNDS, 0, ()))
+    for name, active, mode, threads, arm_rules in arms:
+        st, n_sub = serve_stream(A, stream, budget, active, dt, args.time_limit, mode, threads, arm_rules)
         res[name] = {"particle_substeps_per_s": st.particle_substeps / (st.elapsed_ms / 1e3),
                      "requests_submitted": n_sub, "requests_completed": st.completed, "failed": st.failed,
+                     "updates": st.updates,
                      "step_p50_ms": st.step_p50_ms, "step_p99_ms": st.step_p99_ms,
                      "request_p50_ms": st.request_p50_ms, "request_p99_ms": st.request_p99_ms,
                      "memory_peak_gb": st.memory_peak / (1 << 30), "elapsed_s": st.elapsed_ms / 1e3,
-                     "max_active": active}
+                     "busy_s": st.busy_ms / 1e3, "prepare_s": st.prepare_ms / 1e3, "host_s": st.host_ms / 1e3,
+                     "max_active": active, "mode": "continuous" if mode == A.SERVER_CONTINUOUS else "rounds",
+                     "prepare_threads": threads}
     line = {
         "metric": METRIC, "value": res["served"]["particle_substeps_per_s"],
         "unit": "particle-substeps/s (aggregate)", "workload": "served", "n_gpus": 1, "higher_is_better": True,
         "config": {"workload": f"Poisson arrivals at {args.rate}/s for {args.seconds} s (seed 4), side log-uniform "
                                f"in [64, 1024] (x8), steps U[20, 200], dam break or disk drop 50/50, 4 ppc, "
                                f"dt=1/240, mixed-precision PCG to 1e-6, budget {args.budget_gb} GB",
-                   "time_limit_s": args.time_limit},
-        "served": res["served"], "plain": res["plain"],
-        "ratio": res["served"]["particle_substeps_per_s"] / max(res["plain"]["particle_substeps_per_s"], 1e-9),
+                   "time_limit_s": args.time_limit, "scene_options": args.scene_option or [],
+                   "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8 (default)")},
+        **res,
+        "ratio": (res["served"]["particle_substeps_per_s"] / max(res["plain"]["particle_substeps_per_s"], 1e-9)
+                  if "plain" in res else None),
         "data": "synthetic",
     }
     print(json.dumps(line), flush=True)
@@ -797,6 +824,11 @@ def main():
     ap.add_argument("--seconds", type=float, default=2.0, help="served: length of the arrival stream")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="served: device-memory budget")
     ap.add_argument("--max-active", type=int, default=256, help="served: active scenes at most")
+    ap.add_argument("--prepare-threads", type=int, default=4, help="served: scene preparation threads")
+    ap.add_argument("--served-rounds", action="store_true", help="served: also run the lock-step rounds server")
+    ap.add_argument("--no-plain", action="store_true", help="served: skip the plain one-scene-at-a-time arm")
+    ap.add_argument("--scene-option", action="append",
+                    help="served: NAME=VALUE[@[MIN_CELLS:]MAX_CELLS], Apic.set_option on the served scenes of that size")
     ap.add_argument("--time-limit", type=float, default=60.0, help="served: stop each run after this many seconds")
     ap.add_argument("--cpu-steps", type=int, default=0, help="CPU sample updates (default: --steps)")
     ap.add_argument("--cpu-budget", type=float, default=30.0)

@@ -258,6 +258,12 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
  * ||b||, is unchanged, so only the iteration count differs.  0: start from
  * zero.  Other solver modes always start from zero. */
 #define APIC_OPT_WARM_START 7
+/* No counterpart in the reference.  Priority of the scene's stream, in
+ * levels above the lowest (0, the default); clamped to the device's range
+ * (apic_get_option reports the level used).  When several scenes share the
+ * GPU, the block scheduler starts the kernels of higher-priority streams
+ * first.  Results do not change. */
+#define APIC_OPT_STREAM_PRIORITY 8
 int apic_set_option(apic_handle* h, int option, int value);
 int apic_get_option(apic_handle* h, int option, int* value);
 
@@ -303,19 +309,31 @@ int apic_update_batch(apic_handle* const* handles, uint32_t count, uint32_t flag
 /* Estimated device bytes of a scene (upper bound used for admission). */
 int apic_scene_bytes(uint32_t width, uint32_t height, uint64_t particles, uint64_t* bytes_out);
 
-/* Continuous-batching request server: requests (scene, step count, dt) are
- * queued on submission; each apic_server_step admits queued requests in
- * arrival order while the active set is below max_active and their
- * estimated memory fits memory_budget_bytes, runs one update of every
- * active scene (as apic_update_batch), and retires scenes that reached their
- * step count.  State stays on the device between rounds.  keep_results: copy
- * each finished scene's positions (Vec2x8 layout) to the host before its
- * device memory is released. */
+/* Continuous-batching request server (no counterpart in the reference,
+ * which runs one scene per process): requests (scene, step count, dt) are
+ * queued on submission and admitted in arrival order while the scenes in the
+ * server are fewer than max_active and their estimated memory fits
+ * memory_budget_bytes; a scene's state stays on the device until it reached
+ * its step count.  keep_results: copy each finished scene's positions
+ * (Vec2x8 layout) to the host before its device memory is released.
+ *
+ * APIC_SERVER_CONTINUOUS (default): every scene is relaunched on its own
+ * stream as soon as its update completes; admitted scenes are prepared
+ * (particles generated, device state allocated and uploaded, update graph
+ * built) on `prepare_threads` host threads while the GPU runs the others.
+ * apic_server_step returns once at least one update has completed (or the
+ * server is empty).  APIC_SERVER_ROUNDS: apic_server_step admits on the
+ * calling thread, runs one update of every active scene (as
+ * apic_update_batch) and returns when all are done; max_active = 1 gives
+ * the plain path, one scene at a time.  Calls on one server must not
+ * overlap.  An update that does not complete within 120 s makes
+ * apic_server_step return APIC_ERR_TIMEOUT. */
+enum { APIC_SERVER_ROUNDS = 0, APIC_SERVER_CONTINUOUS = 1 };
 typedef struct apic_server apic_server;
 typedef struct apic_server_round {
-    uint32_t admitted, stepped, completed, active, queued;
-    double   round_ms;       /* wall time of this round's updates */
-    uint64_t memory_used;    /* estimated bytes of the active scenes */
+    uint32_t admitted, stepped, completed, active, queued;  /* active: running or being prepared */
+    double   round_ms;       /* wall time of this call's updates */
+    uint64_t memory_used;    /* estimated bytes of the admitted scenes */
 } apic_server_round;
 typedef struct apic_request_info {
     int      status;         /* APIC_OK, or why the request failed */
@@ -331,12 +349,24 @@ typedef struct apic_server_stats {
     uint64_t submitted, completed, failed, active, queued, rounds;
     uint64_t particle_substeps, particle_updates;
     double   busy_ms, elapsed_ms;
-    double   step_p50_ms, step_p99_ms;        /* per scene-step: its round's wall time */
+    double   step_p50_ms, step_p99_ms;        /* per update: launch to completion (rounds: the round) */
     double   request_p50_ms, request_p99_ms;  /* completion minus submission */
     uint64_t memory_used, memory_peak;
+    uint64_t updates;                         /* completed scene updates */
+    double   prepare_ms;                      /* host time spent preparing scenes (all threads) */
+    double   host_ms;                         /* step calls' time outside the update loop */
+    int32_t  mode;                            /* APIC_SERVER_* */
+    uint32_t prepare_threads;
 } apic_server_stats;
 int apic_server_create(uint64_t memory_budget_bytes, uint32_t max_active, uint32_t keep_results,
                        apic_server** out);
+/* Mode and preparation threads (0: prepare on the calling thread); only
+ * while no scene is admitted. */
+int apic_server_set_mode(apic_server* sv, int mode, uint32_t prepare_threads);
+/* apic_set_option(option, value) on every scene the server creates whose
+ * cell count lies in [min_cells, max_cells] (rules apply in the order given;
+ * only while no scene is admitted). */
+int apic_server_scene_option(apic_server* sv, int option, int value, uint64_t min_cells, uint64_t max_cells);
 int apic_server_destroy(apic_server* sv);
 int apic_server_submit(apic_server* sv, const apic_scene_params* scene, const apic_world_props* props,
                        uint32_t steps, float frame_deltatime, int solver_mode, float rel_tol,

@@ -72,3 +72,34 @@ def test_reference_default_scene_generator_matches_oracle(gpu_lib, oracle_mod):
     assert len(px) == n
     assert np.array_equal(o.read_field("pos_x")[:n], px)
     assert np.array_equal(o.read_field("pos_y")[:n], py)
+
+
+def test_server_host_logic_without_device(gpu_lib, has_gpu):
+    """Server bookkeeping on the host: modes, budget rejection, and a request
+    whose scene cannot be created (no device here) fails instead of hanging."""
+    import apic_gb300 as A
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    props = A.WorldProperties()
+    sc = A.scene_params(A.SCENE_DAM_BREAK, 64, cell_size=1 / 64, sub=2, seed=0, fluid_x=0.5, fluid_y=0.5)
+    with pytest.raises(A.ApicError) as ei:
+        A.Server(1 << 20, 2).submit(A.scene_params(A.SCENE_DAM_BREAK, 256, cell_size=1 / 256, sub=2, seed=0,
+                                                   fluid_x=0.7, fluid_y=0.7), props, 3, 1 / 240)
+    assert ei.value.code == A.ERR_OOM
+    for mode, threads in ((A.SERVER_CONTINUOUS, 2), (A.SERVER_CONTINUOUS, 0), (A.SERVER_ROUNDS, 0)):
+        sv = A.Server(1 << 30, 2, mode=mode, prepare_threads=threads)
+        with pytest.raises(A.ApicError):
+            sv.set_mode(7, 1)
+        ids = [sv.submit(sc, props, 2, 1 / 240) for _ in range(3)]
+        for _ in range(50):
+            rd = sv.step()
+            assert rd.memory_used <= 1 << 30
+            if rd.active == 0 and rd.queued == 0:
+                break
+        st = sv.stats()
+        assert st.submitted == 3 and st.failed == 3 and st.completed == 0 and st.memory_used == 0
+        assert st.mode == mode and st.prepare_threads == threads
+        for rid in ids:
+            info = sv.request(rid)
+            assert info.finished and info.status == A.ERR_NO_DEVICE
+        sv.close()

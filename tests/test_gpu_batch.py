@@ -71,13 +71,19 @@ def test_update_batch_rejects_bad_input(gpu_lib):
     assert ei.value.code == A.ERR_INVALID_ARG
 
 
-def test_server_results_same_alone_and_in_mix(gpu_lib):
+@pytest.mark.parametrize("mode,threads", [(A.SERVER_CONTINUOUS, 4), (A.SERVER_CONTINUOUS, 0), (A.SERVER_ROUNDS, 0)],
+                         ids=["continuous", "continuous-inline", "rounds"])
+def test_server_results_same_alone_and_in_mix(gpu_lib, mode, threads):
     reqs = [(dam_break(64, 21, 0.4), 5), (disk_drop(128, 22), 3), (dam_break(96, 23, 0.2), 7),
             (dam_break(128, 24, 0.5), 4), (disk_drop(64, 25), 6), (dam_break(192, 26, 0.3), 2)]
     dt = 1 / 240
     # room for about two of these scenes at a time: admission must queue the rest
     budget = 2 * max(A.scene_bytes(sc.width, sc.height, len(A.generate_scene(sc)[0])) for sc, _ in reqs)
-    sv = A.Server(budget, max_active=4, keep_results=True)
+    sv = A.Server(budget, max_active=4, keep_results=True, mode=mode, prepare_threads=threads)
+    if mode == A.SERVER_CONTINUOUS and threads:
+        # per-size rules change how a scene runs, never what it computes
+        sv.scene_option(A.OPT_STREAM_PRIORITY, 5, 0, 64 * 64)
+        sv.scene_option(A.OPT_DSM_VCYCLE, 0, 96 * 96, 128 * 128)
     ids = [sv.submit(sc, PROPS, steps, dt) for sc, steps in reqs]
     max_stepped, rounds, waited = 0, 0, False
     while True:
@@ -107,6 +113,27 @@ def test_server_results_same_alone_and_in_mix(gpu_lib):
         d = np.max(np.abs(sv.result_positions(rid) - ref.read_vec2x8(0)))
         assert float(d) < POS_TOL_CELLS * sc.cell_size, (rid, float(d))
     assert st.particle_substeps == total
+    assert st.updates == sum(steps for _, steps in reqs) and st.mode == mode
+    sv.close()
+
+
+def test_server_continuous_keeps_small_scenes_moving(gpu_lib):
+    """In continuous mode a small scene's updates do not wait for a large
+    scene's: the small request finishes while the large one still runs."""
+    sv = A.Server(1 << 40, max_active=4, mode=A.SERVER_CONTINUOUS)
+    big = sv.submit(dam_break(512, 31, 0.5), PROPS, 6, 1 / 240)
+    small = sv.submit(dam_break(64, 32, 0.3), PROPS, 6, 1 / 240)
+    small_done_first = False
+    for _ in range(200):
+        rd = sv.step()
+        ib, is_ = sv.request(big), sv.request(small)
+        if is_.finished and not ib.finished:
+            small_done_first = True
+        if rd.active == 0 and rd.queued == 0:
+            break
+    assert sv.request(big).finished and sv.request(small).finished
+    assert sv.request(big).status == A.OK and sv.request(small).status == A.OK
+    assert small_done_first
     sv.close()
 
 
@@ -137,3 +164,25 @@ def test_scene_bytes_bounds_server_scenes(gpu_lib):
         assert used <= est, (side, used, est)
         sv.step()  # last update: positions kept, device memory released
     sv.close()
+
+
+def test_stream_priority_option(gpu_lib):
+    """The scene's stream priority is clamped to the device's range and does
+    not change results beyond the spread of P2G's float atomics."""
+    sc = dam_break(64, 41, 0.4)
+    runs = []
+    for prio in (0, 3, 100):
+        g = A.Apic(sc.width, sc.height, sc.cell_size, PROPS)
+        g.set_particles(*A.generate_scene(sc))
+        g.set_option(A.OPT_STREAM_PRIORITY, prio)
+        got = g.get_option(A.OPT_STREAM_PRIORITY)
+        assert 0 <= got <= prio
+        if prio == 0:
+            assert got == 0
+        g.update(A.DebugOptions(disable_particle_sort=True), 1 / 240)
+        runs.append(g.read_field("pos_x"))
+        g.close()
+    with pytest.raises(A.ApicError):
+        A.Apic(64, 64, 1 / 64, PROPS).set_option(A.OPT_STREAM_PRIORITY, -1)
+    assert np.max(np.abs(runs[1] - runs[0])) < POS_TOL_CELLS / 64
+    assert np.max(np.abs(runs[2] - runs[0])) < POS_TOL_CELLS / 64
