@@ -109,7 +109,8 @@ class ServerStatsC(ctypes.Structure):
                 ("request_p50_ms", ctypes.c_double), ("request_p99_ms", ctypes.c_double),
                 ("memory_used", ctypes.c_uint64), ("memory_peak", ctypes.c_uint64),
                 ("updates", ctypes.c_uint64), ("prepare_ms", ctypes.c_double), ("host_ms", ctypes.c_double),
-                ("mode", ctypes.c_int32), ("prepare_threads", ctypes.c_uint32)]
+                ("mode", ctypes.c_int32), ("prepare_threads", ctypes.c_uint32),
+                ("kernel_launches", ctypes.c_uint64)]
 
 
 class RenderParamsC(ctypes.Structure):

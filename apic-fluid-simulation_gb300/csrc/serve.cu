@@ -103,6 +103,7 @@ struct apic_server {
     std::vector<SceneRule> rules;    // apic_set_option per scene size (read by the preparation threads)
     std::vector<double> step_ms, request_ms;
     uint64_t particle_substeps = 0, particle_updates = 0, rounds = 0, completed = 0, failed = 0, updates = 0;
+    uint64_t kernels = 0;            // kernel launches of the completed updates
     double busy_ms = 0.0, prepare_ms = 0.0, host_ms = 0.0;
 
     // preparation threads (continuous mode)
@@ -235,6 +236,7 @@ void account(apic_server* sv, Request* r) {
     sv->particle_substeps += r->particles * st.substeps;
     sv->particle_updates += r->particles;
     sv->updates++;
+    sv->kernels += st.kernel_launches;
 }
 
 // ---- rounds mode -----------------------------------------------------------
@@ -585,6 +587,7 @@ int apic_server_get_stats(apic_server* sv, apic_server_stats* out) {
     st.host_ms = sv->host_ms;
     st.mode = sv->mode;
     st.prepare_threads = sv->workers;
+    st.kernel_launches = sv->kernels;
     *out = st;
     return APIC_OK;
 }

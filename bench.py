@@ -489,7 +489,7 @@ def run_batched(args):
     sims = make_sims(A, scenes, not args.no_dsm)
     A.update_batch(sims, A.DebugOptions(), dt)
     torch.cuda.synchronize()
-    round_ms, sub_cmp, sub_all, res_max = [], 0, 0, 0.0
+    round_ms, sub_cmp, sub_all, res_max, kern_all = [], 0, 0, 0.0, 0
     with ClockSampler(0) as clocks:
         t0 = time.perf_counter()
         for k in range(args.steps):
@@ -499,6 +499,7 @@ def run_batched(args):
             stats = [g.stats() for g in sims]
             sub = sum(n * st.substeps for n, st in zip(counts, stats))
             res_max = max(res_max, max(float(st.true_residual_rel) for st in stats))
+            kern_all += sum(int(st.kernel_launches) for st in stats)
             sub_all += sub
             if k < cmp_steps:
                 sub_cmp += sub
@@ -521,6 +522,7 @@ def run_batched(args):
                              "ratio": (sub_cmp / cmp_s) / (sub_plain / plain_s),
                              "plain_is": "the same scenes' updates one after another through apic_update"},
         "round_ms_p50": float(np.percentile(round_ms, 50)), "round_ms_p99": float(np.percentile(round_ms, 99)),
+        "gpu_launches": kern_all, "kernels_per_s": kern_all / all_s,
         "true_residual_rel_max": res_max, "clocks": clocks.summary(), "data": "synthetic",
     }
     print(json.dumps(line), flush=True)
@@ -610,7 +612,8 @@ def run_served(args):
         st, n_sub = serve_stream(A, stream, budget, active, dt, args.time_limit, mode, threads, arm_rules)
         res[name] = {"particle_substeps_per_s": st.particle_substeps / (st.elapsed_ms / 1e3),
                      "requests_submitted": n_sub, "requests_completed": st.completed, "failed": st.failed,
-                     "updates": st.updates,
+                     "updates": st.updates, "kernel_launches": st.kernel_launches,
+                     "kernels_per_s": st.kernel_launches / (st.elapsed_ms / 1e3),
                      "step_p50_ms": st.step_p50_ms, "step_p99_ms": st.step_p99_ms,
                      "request_p50_ms": st.request_p50_ms, "request_p99_ms": st.request_p99_ms,
                      "memory_peak_gb": st.memory_peak / (1 << 30), "elapsed_s": st.elapsed_ms / 1e3,

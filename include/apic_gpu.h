@@ -357,6 +357,7 @@ typedef struct apic_server_stats {
     double   host_ms;                         /* step calls' time outside the update loop */
     int32_t  mode;                            /* APIC_SERVER_* */
     uint32_t prepare_threads;
+    uint64_t kernel_launches;                 /* kernels the completed updates launched */
 } apic_server_stats;
 int apic_server_create(uint64_t memory_budget_bytes, uint32_t max_active, uint32_t keep_results,
                        apic_server** out);
