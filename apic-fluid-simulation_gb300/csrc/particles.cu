@@ -12,11 +12,14 @@
 //   k_permute   gather of the nine fields by the sorted `val` (:1068-1110).
 //
 // The reference sums P2G contributions with float CAS loops, so its sums come
-// in thread-schedule order; here each contribution is one hardware float
-// atomic (red.global.add.f32), which is likewise order-dependent at the last
-// bit.  Every other result of these kernels is computed lane by lane with the
+// in thread-schedule order.  Here a CTA first sums its particles'
+// contributions in shared memory (hardware float atomics) over the window of
+// faces and cells they touch, then adds each touched entry to global memory
+// once; both levels are likewise order-dependent at the last bit.  Every other result of these kernels is computed lane by lane with the
 // reference's operation order.
 #include <cuda_runtime.h>
+
+#include <climits>
 
 #include "apic_device.cuh"
 #include "apic_internal.h"
@@ -24,71 +27,215 @@
 namespace apic {
 namespace {
 
-__global__ void __launch_bounds__(256) k_p2g(const PartPtrs* __restrict__ pp, uint32_t n, int W, int H, float dx,
-                                             const Ctl* __restrict__ ctl, float* __restrict__ acc_u,
-                                             float* __restrict__ acc_uw, float* __restrict__ acc_v,
-                                             float* __restrict__ acc_vw, float* __restrict__ dens,
-                                             uint32_t* __restrict__ fluid) {
+// P2G accumulation window of one CTA: the faces and cells that its 256
+// consecutive particles touch.  After the Morton sort consecutive slots are
+// neighbouring cells, so the window is small; a CTA whose window (per grid)
+// exceeds kP2gCap entries, e.g. across a jump of the Morton curve or with
+// unsorted particles, adds straight to global memory instead.
+constexpr int kP2gThreads = 256;
+constexpr int kP2gCap = 512;
+// Shared-memory float atomics are compare-and-swap loops, and consecutive
+// lanes hold particles of the same cell, so the window arrays are kept in
+// kP2gCopies interleaved copies (entry e, copy c at e * kP2gCopies + c, in
+// different banks) and lane l adds into copy l % kP2gCopies.
+constexpr int kP2gCopies = 4;
+
+struct Box {
+    int x0, y0, w, h;
+};
+
+__device__ __forceinline__ int warp_min_i(int v) { return __reduce_min_sync(0xffffffffu, v); }
+__device__ __forceinline__ int warp_max_i(int v) { return __reduce_max_sync(0xffffffffu, v); }
+
+__global__ void __launch_bounds__(kP2gThreads, 4) k_p2g(const PartPtrs* __restrict__ pp, uint32_t n, int W, int H,
+                                                     float dx, const Ctl* __restrict__ ctl, float* __restrict__ acc_u,
+                                                     float* __restrict__ acc_uw, float* __restrict__ acc_v,
+                                                     float* __restrict__ acc_vw, float* __restrict__ dens,
+                                                     uint32_t* __restrict__ fluid) {
+    __shared__ float s_um[kP2gCap * kP2gCopies], s_uw[kP2gCap * kP2gCopies], s_vm[kP2gCap * kP2gCopies],
+        s_vw[kP2gCap * kP2gCopies], s_d[kP2gCap * kP2gCopies];
+    __shared__ uint8_t s_fl[kP2gCap];  // fluid cells of the density window
+    __shared__ int s_red[kP2gThreads / 32][12];
+    __shared__ Box s_box[3];
+    __shared__ int s_tiled;
     pdl_wait();
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float prev_dt = ctl->prev_dt;
-    float px = pp->f[PX][i], py = pp->f[PY][i];
-    float vx = pp->f[VX][i], vy = pp->f[VY][i];
-    float cux = pp->f[CUX][i], cuy = pp->f[CUY][i];
-    float cvx = pp->f[CVX][i], cvy = pp->f[CVY][i];
-    float tr = pp->f[TR][i];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < n;
+    // bounds of the clamped node coordinates: u, v faces and density cells
+    int b[12];
+    float ua[4], wu[4], va[4], wv[4], cw[4];
+    int ux[2], uy[2], vx2[2], vy2[2], cx[2], cy[2];
+    int fx = 0, fy = 0;  // the particle's own cell (its fluid bit)
+    if (live) {
+        const float prev_dt = ctl->prev_dt;
+        float px = pp->f[PX][i], py = pp->f[PY][i];
+        float vx = pp->f[VX][i], vy = pp->f[VY][i];
+        float cux = pp->f[CUX][i], cuy = pp->f[CUY][i];
+        float cvx = pp->f[CVX][i], cvy = pp->f[CVY][i];
+        float tr = pp->f[TR][i];
 
-    float tau = (-tr) / prev_dt;
-    float wt = temporal_w(tau);
-    float gx = px / dx, gy = py / dx;
+        float tau = (-tr) / prev_dt;
+        float wt = temporal_w(tau);
+        float gx = px / dx, gy = py / dx;
 
-    // cell-centred density stencil
-    float cgx = gx - 0.5f, cgy = gy - 0.5f;
-    float cbx = floorf(cgx), cby = floorf(cgy);
-    float ctx = cgx - cbx, cty = cgy - cby;
-    float cw[4];
-    cw[0] = ((1.0f - ctx) * (1.0f - cty)) * wt;
-    cw[1] = (ctx * (1.0f - cty)) * wt;
-    cw[2] = ((1.0f - ctx) * cty) * wt;
-    cw[3] = (ctx * cty) * wt;
-    int mx = W - 1, my = H - 1;
-    int tbx = trunc_x86(cbx), tby = trunc_x86(cby);
-    int cx0 = max(min(tbx, mx), 0), cx1 = max(min(tbx + 1, mx), 0);
-    int cy0 = max(min(tby, my), 0), cy1 = max(min(tby + 1, my), 0);
-    uint32_t ci[4] = {uint32_t(cy0 * W + cx0), uint32_t(cy0 * W + cx1), uint32_t(cy1 * W + cx0),
-                      uint32_t(cy1 * W + cx1)};
+        // cell-centred density stencil
+        float cgx = gx - 0.5f, cgy = gy - 0.5f;
+        float cbx = floorf(cgx), cby = floorf(cgy);
+        float ctx = cgx - cbx, cty = cgy - cby;
+        cw[0] = ((1.0f - ctx) * (1.0f - cty)) * wt;
+        cw[1] = (ctx * (1.0f - cty)) * wt;
+        cw[2] = ((1.0f - ctx) * cty) * wt;
+        cw[3] = (ctx * cty) * wt;
+        int mx = W - 1, my = H - 1;
+        int tbx = trunc_x86(cbx), tby = trunc_x86(cby);
+        cx[0] = max(min(tbx, mx), 0); cx[1] = max(min(tbx + 1, mx), 0);
+        cy[0] = max(min(tby, my), 0); cy[1] = max(min(tby + 1, my), 0);
 
-    Stencil su, sv;
-    u_stencil(gx, gy, W, H, dx, su);
-    v_stencil(gx, gy, W, H, dx, sv);
+        Stencil su, sv;
+        u_stencil(gx, gy, W, H, dx, su);
+        v_stencil(gx, gy, W, H, dx, sv);
+        {
+            // the same clamps as u_index / v_index
+            int ix = trunc_x86(floorf(gx)), iy = trunc_x86(floorf(gy - 0.5f));
+            ux[0] = max(min(ix, W), 0); ux[1] = max(min(ix + 1, W), 0);
+            uy[0] = max(min(iy, H - 1), 0); uy[1] = max(min(iy + 1, H - 1), 0);
+            int jx = trunc_x86(floorf(gx - 0.5f)), jy = trunc_x86(floorf(gy));
+            vx2[0] = max(min(jx, W - 1), 0); vx2[1] = max(min(jx + 1, W - 1), 0);
+            vy2[0] = max(min(jy, H), 0); vy2[1] = max(min(jy + 1, H), 0);
+        }
 
-    float clx = fmax_x86(fmin_x86(gx, float(W) - 1.0f), 0.0f);
-    float cly = fmax_x86(fmin_x86(gy, float(H) - 1.0f), 0.0f);
-    uint32_t fi = uint32_t(trunc_x86(cly) * W + trunc_x86(clx));
-    atomicOr(fluid + (fi >> 5), 1u << (fi & 31u));
+        float clx = fmax_x86(fmin_x86(gx, float(W) - 1.0f), 0.0f);
+        float cly = fmax_x86(fmin_x86(gy, float(H) - 1.0f), 0.0f);
+        fx = trunc_x86(clx);
+        fy = trunc_x86(cly);
 
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        float wu = su.w[k] * wt;
-        float ua = (vx + cux * su.ox[k] + cuy * su.oy[k]) * wu;
-        if (ua != 0.0f || wu != 0.0f) {
-            atomicAdd(acc_u + su.idx[k], ua);
-            atomicAdd(acc_uw + su.idx[k], wu);
+        for (int k = 0; k < 4; ++k) {
+            wu[k] = su.w[k] * wt;
+            ua[k] = (vx + cux * su.ox[k] + cuy * su.oy[k]) * wu[k];
+            wv[k] = sv.w[k] * wt;
+            va[k] = (vy + cvx * sv.ox[k] + cvy * sv.oy[k]) * wv[k];
+        }
+        b[0] = ux[0]; b[1] = -ux[1]; b[2] = uy[0]; b[3] = -uy[1];
+        b[4] = vx2[0]; b[5] = -vx2[1]; b[6] = vy2[0]; b[7] = -vy2[1];
+        b[8] = min(cx[0], fx); b[9] = -max(cx[1], fx); b[10] = min(cy[0], fy); b[11] = -max(cy[1], fy);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) b[k] = INT_MAX;
+    }
+    // block minima of the lows and of the negated highs
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+        int m = warp_min_i(b[k]);
+        if (lane == 0) s_red[warp][k] = m;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        int lo_x = INT_MAX, hi_x = INT_MAX, lo_y = INT_MAX, hi_y = INT_MAX;
+        for (int w = 0; w < kP2gThreads / 32; ++w) {
+            lo_x = min(lo_x, s_red[w][4 * threadIdx.x + 0]);
+            hi_x = min(hi_x, s_red[w][4 * threadIdx.x + 1]);
+            lo_y = min(lo_y, s_red[w][4 * threadIdx.x + 2]);
+            hi_y = min(hi_y, s_red[w][4 * threadIdx.x + 3]);
+        }
+        Box bx;
+        bx.x0 = lo_x; bx.y0 = lo_y;
+        bx.w = -hi_x - lo_x + 1; bx.h = -hi_y - lo_y + 1;
+        s_box[threadIdx.x] = bx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        bool ok = true;
+        for (int g = 0; g < 3; ++g)
+            ok = ok && s_box[g].w > 0 && s_box[g].h > 0 && (long long)s_box[g].w * s_box[g].h <= kP2gCap;
+        s_tiled = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_tiled) {
+        if (!live) return;
+        const uint32_t fi = uint32_t(fy * W + fx);
+        atomicOr(fluid + (fi >> 5), 1u << (fi & 31u));
+        // node k = (x[k & 1], y[k >> 1]): the u_index / v_index of the stencils
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t iu = uint32_t(uy[k >> 1]) * uint32_t(W + 1) + uint32_t(ux[k & 1]);
+            if (ua[k] != 0.0f || wu[k] != 0.0f) { atomicAdd(acc_u + iu, ua[k]); atomicAdd(acc_uw + iu, wu[k]); }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t iv = uint32_t(vy2[k >> 1]) * uint32_t(W) + uint32_t(vx2[k & 1]);
+            if (va[k] != 0.0f || wv[k] != 0.0f) { atomicAdd(acc_v + iv, va[k]); atomicAdd(acc_vw + iv, wv[k]); }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t ic = uint32_t(cy[k >> 1]) * uint32_t(W) + uint32_t(cx[k & 1]);
+            if (cw[k] != 0.0f) atomicAdd(dens + ic, cw[k]);
+        }
+        return;
+    }
+    const Box bu = s_box[0], bv = s_box[1], bc = s_box[2];
+    for (int e = threadIdx.x; e < bu.w * bu.h * kP2gCopies; e += kP2gThreads) { s_um[e] = 0.0f; s_uw[e] = 0.0f; }
+    for (int e = threadIdx.x; e < bv.w * bv.h * kP2gCopies; e += kP2gThreads) { s_vm[e] = 0.0f; s_vw[e] = 0.0f; }
+    for (int e = threadIdx.x; e < bc.w * bc.h * kP2gCopies; e += kP2gThreads) s_d[e] = 0.0f;
+    for (int e = threadIdx.x; e < bc.w * bc.h; e += kP2gThreads) s_fl[e] = 0;
+    __syncthreads();
+    if (live) {
+        const int c = lane % kP2gCopies;
+        s_fl[(fy - bc.y0) * bc.w + (fx - bc.x0)] = 1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int lu = ((uy[k >> 1] - bu.y0) * bu.w + (ux[k & 1] - bu.x0)) * kP2gCopies + c;
+            if (ua[k] != 0.0f || wu[k] != 0.0f) { atomicAdd(s_um + lu, ua[k]); atomicAdd(s_uw + lu, wu[k]); }
+            const int lv = ((vy2[k >> 1] - bv.y0) * bv.w + (vx2[k & 1] - bv.x0)) * kP2gCopies + c;
+            if (va[k] != 0.0f || wv[k] != 0.0f) { atomicAdd(s_vm + lv, va[k]); atomicAdd(s_vw + lv, wv[k]); }
+            const int lc = ((cy[k >> 1] - bc.y0) * bc.w + (cx[k & 1] - bc.x0)) * kP2gCopies + c;
+            if (cw[k] != 0.0f) atomicAdd(s_d + lc, cw[k]);
         }
     }
+    __syncthreads();
+    // one global add per touched face and cell (the copies summed in order)
+    auto sum_copies = [](const float* a, int e) {
+        float t = a[e * kP2gCopies];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        float wv = sv.w[k] * wt;
-        float va = (vy + cvx * sv.ox[k] + cvy * sv.oy[k]) * wv;
-        if (va != 0.0f || wv != 0.0f) {
-            atomicAdd(acc_v + sv.idx[k], va);
-            atomicAdd(acc_vw + sv.idx[k], wv);
+        for (int c = 1; c < kP2gCopies; ++c) t += a[e * kP2gCopies + c];
+        return t;
+    };
+    for (int e = threadIdx.x; e < bu.w * bu.h; e += kP2gThreads) {
+        const float m = sum_copies(s_um, e), w = sum_copies(s_uw, e);
+        if (m != 0.0f || w != 0.0f) {
+            const uint32_t g = uint32_t(bu.y0 + e / bu.w) * uint32_t(W + 1) + uint32_t(bu.x0 + e % bu.w);
+            atomicAdd(acc_u + g, m);
+            atomicAdd(acc_uw + g, w);
         }
     }
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-        if (cw[k] != 0.0f) atomicAdd(dens + ci[k], cw[k]);
+    for (int e = threadIdx.x; e < bv.w * bv.h; e += kP2gThreads) {
+        const float m = sum_copies(s_vm, e), w = sum_copies(s_vw, e);
+        if (m != 0.0f || w != 0.0f) {
+            const uint32_t g = uint32_t(bv.y0 + e / bv.w) * uint32_t(W) + uint32_t(bv.x0 + e % bv.w);
+            atomicAdd(acc_v + g, m);
+            atomicAdd(acc_vw + g, w);
+        }
+    }
+    for (int e = threadIdx.x; e < bc.w * bc.h; e += kP2gThreads) {
+        const float d = sum_copies(s_d, e);
+        if (d != 0.0f) atomicAdd(dens + uint32_t(bc.y0 + e / bc.w) * uint32_t(W) + uint32_t(bc.x0 + e % bc.w), d);
+    }
+    // fluid bits: one OR per mask word that a window row overlaps (a row of
+    // bc.w raw cells spans at most bc.w / 32 + 2 words)
+    const int nw = bc.w / 32 + 2;
+    for (int e = threadIdx.x; e < bc.h * nw; e += kP2gThreads) {
+        const int r = e / nw, j = e % nw;
+        const uint32_t first = uint32_t(bc.y0 + r) * uint32_t(W) + uint32_t(bc.x0);
+        const uint32_t last = first + uint32_t(bc.w) - 1u;
+        const uint32_t word = (first >> 5) + uint32_t(j);
+        if (word > (last >> 5)) continue;
+        const uint32_t lo = max(first, word << 5), hi = min(last, (word << 5) + 31u);
+        uint32_t mask = 0;
+        for (uint32_t c = lo; c <= hi; ++c)
+            if (s_fl[r * bc.w + int(c - first)]) mask |= 1u << (c & 31u);
+        if (mask) atomicOr(fluid + word, mask);
+    }
 }
 
 // bilinear_interpolate, src/apic.rs:138-172.
@@ -248,7 +395,7 @@ __global__ void k_swap_tables(PartPtrs* pp) {
 
 cudaError_t launch_p2g(Scene& s) {
     if (s.n == 0) return cudaSuccess;
-    launch(s.use_pdl, k_p2g, div_up(s.n, 256), 256, 0, s.stream, s.pp, s.n, int(s.W), int(s.H), s.dx, s.ctl, s.acc_u, s.acc_uw,
+    launch(s.use_pdl, k_p2g, div_up(s.n, kP2gThreads), kP2gThreads, 0, s.stream, s.pp, s.n, int(s.W), int(s.H), s.dx, s.ctl, s.acc_u, s.acc_uw,
                                                     s.acc_v, s.acc_vw, s.density, s.lv[0].fluid);
     return cudaGetLastError();
 }
