@@ -598,7 +598,7 @@ def run_served(args):
     gpu_build.build()
     import torch
     torch.cuda.set_device(0)
-    stream = served_stream(A, args.rate, args.seconds)
+    stream = served_stream(A, args.rate, args.seconds, hi=args.served_max_side)
     budget = int(args.budget_gb * (1 << 30))
     dt = 1.0 / 240.0
     res = {}
@@ -624,7 +624,7 @@ def run_served(args):
         "metric": METRIC, "value": res["served"]["particle_substeps_per_s"],
         "unit": "particle-substeps/s (aggregate)", "workload": "served", "n_gpus": 1, "higher_is_better": True,
         "config": {"workload": f"Poisson arrivals at {args.rate}/s for {args.seconds} s (seed 4), side log-uniform "
-                               f"in [64, 1024] (x8), steps U[20, 200], dam break or disk drop 50/50, 4 ppc, "
+                               f"in [64, {args.served_max_side}] (x8), steps U[20, 200], dam break or disk drop 50/50, 4 ppc, "
                                f"dt=1/240, mixed-precision PCG to 1e-6, budget {args.budget_gb} GB",
                    "time_limit_s": args.time_limit, "scene_options": args.scene_option or [],
                    "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8 (default)")},
@@ -830,6 +830,7 @@ def main():
     ap.add_argument("--prepare-threads", type=int, default=4, help="served: scene preparation threads")
     ap.add_argument("--served-rounds", action="store_true", help="served: also run the lock-step rounds server")
     ap.add_argument("--no-plain", action="store_true", help="served: skip the plain one-scene-at-a-time arm")
+    ap.add_argument("--served-max-side", type=int, default=1024, help="served: largest grid side of the requests")
     ap.add_argument("--scene-option", action="append",
                     help="served: NAME=VALUE[@[MIN_CELLS:]MAX_CELLS], Apic.set_option on the served scenes of that size")
     ap.add_argument("--time-limit", type=float, default=60.0, help="served: stop each run after this many seconds")
