@@ -130,7 +130,8 @@ def dist_setup():
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return world, rank, local
 
@@ -140,7 +141,8 @@ def dist_max(x: float, world: int) -> float:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    # NCCL reduces device tensors; gloo (CPU-only runs) host tensors
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -826,8 +828,8 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
     ap.add_argument("--seconds", type=float, default=2.0, help="served: length of the arrival stream")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="served: device-memory budget")
-    ap.add_argument("--max-active", type=int, default=256, help="served: active scenes at most")
-    ap.add_argument("--prepare-threads", type=int, default=4, help="served: scene preparation threads")
+    ap.add_argument("--max-active", type=int, default=64, help="served: active scenes at most")
+    ap.add_argument("--prepare-threads", type=int, default=8, help="served: scene preparation threads")
     ap.add_argument("--served-rounds", action="store_true", help="served: also run the lock-step rounds server")
     ap.add_argument("--no-plain", action="store_true", help="served: skip the plain one-scene-at-a-time arm")
     ap.add_argument("--served-max-side", type=int, default=1024, help="served: largest grid side of the requests")
