@@ -185,6 +185,7 @@ SIGNATURES = {
     "apic_server_destroy": (ctypes.c_int, [_VP]),
     "apic_server_set_mode": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_uint32]),
     "apic_server_scene_option": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64]),
+    "apic_server_set_work_limit": (ctypes.c_int, [_VP, ctypes.c_uint64]),
     "apic_server_submit": (ctypes.c_int, [_VP, ctypes.POINTER(SceneParamsC), ctypes.POINTER(WorldPropsC),
                                           ctypes.c_uint32, ctypes.c_float, ctypes.c_int, ctypes.c_float,
                                           ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]),
@@ -531,6 +532,10 @@ class Server:
     def set_mode(self, mode: int, prepare_threads: int = 4) -> None:
         """SERVER_CONTINUOUS (default) or SERVER_ROUNDS; only while no scene is admitted."""
         _check(self._lib.apic_server_set_mode(self._h, mode, prepare_threads), "apic_server_set_mode")
+
+    def set_work_limit(self, max_active_cells: int) -> None:
+        """Admit while the admitted scenes' grid cells stay within max_active_cells (0: no limit)."""
+        _check(self._lib.apic_server_set_work_limit(self._h, max_active_cells), "apic_server_set_work_limit")
 
     def scene_option(self, option: int, value: int, min_cells: int = 0, max_cells: int = (1 << 64) - 1) -> None:
         """Apic.set_option(option, value) on every scene with min_cells..max_cells cells."""

@@ -5,7 +5,9 @@
 // and a frame dt.  Requests are admitted in arrival order while the scenes
 // in the server (running or being prepared) are fewer than max_active and
 // their estimated device memory fits the budget; the head of the queue waits
-// rather than being overtaken.  Two ways to run the admitted scenes:
+// rather than being overtaken.  An optional work limit also bounds the grid
+// cells of the admitted scenes, so a mix of small scenes runs many at once
+// and a mix of large ones few.  Two ways to run the admitted scenes:
 //
 //   continuous (default): every scene runs on its own stream and is
 //     relaunched the moment its update completes, so short updates of small
@@ -61,6 +63,7 @@ struct Request {
     double max_true_residual = 0.0;
     double prepare_ms = 0.0;                         // host time to build the scene
     uint64_t bytes = 0;
+    uint64_t cells = 0;                              // grid cells (admission work limit)
     apic_handle* h = nullptr;
     int status = APIC_OK;
     std::string error;
@@ -90,6 +93,8 @@ struct SceneRule {
 struct apic_server {
     uint64_t budget = 0, used = 0, peak = 0;
     uint32_t max_active = 0;
+    uint64_t max_cells = 0;          // grid cells of the admitted scenes at most (0: no limit)
+    uint64_t active_cells = 0;
     bool keep = false;
     int mode = APIC_SERVER_CONTINUOUS;
     uint32_t workers = 4;
@@ -203,6 +208,12 @@ void release(apic_server* sv, Request* r) {
     if (r->h) apic_destroy(r->h);
     r->h = nullptr;
     sv->used -= r->bytes;
+    sv->active_cells -= r->cells;
+}
+
+// The head of the queue fits the work limit (a lone request always does).
+bool fits_work(const apic_server* sv, const Request* r) {
+    return sv->max_cells == 0 || sv->active_cells == 0 || sv->active_cells + r->cells <= sv->max_cells;
 }
 
 void retire(apic_server* sv, Request* r, int status) {
@@ -244,7 +255,7 @@ void account(apic_server* sv, Request* r) {
 int step_rounds(apic_server* sv, apic_server_round& rd) {
     // 1. admission in arrival order, on the calling thread
     while (!sv->queue.empty() && sv->active.size() < sv->max_active &&
-           sv->used + sv->queue.front()->bytes <= sv->budget) {
+           sv->used + sv->queue.front()->bytes <= sv->budget && fits_work(sv, sv->queue.front())) {
         Request* r = sv->queue.front();
         sv->queue.pop_front();
         r->t_admit = sv->now_ms();
@@ -256,6 +267,7 @@ int step_rounds(apic_server* sv, apic_server_round& rd) {
             continue;
         }
         sv->used += r->bytes;
+        sv->active_cells += r->cells;
         sv->peak = std::max(sv->peak, sv->used);
         sv->active.push_back(r);
         rd.admitted++;
@@ -324,6 +336,7 @@ void take_ready(apic_server* sv, apic_server_round& rd) {
         sv->prepare_ms += r->prepare_ms;
         if (r->status != APIC_OK) {
             sv->used -= r->bytes;
+            sv->active_cells -= r->cells;
             r->t_done = sv->now_ms();
             sv->failed++;
             continue;
@@ -336,11 +349,12 @@ void take_ready(apic_server* sv, apic_server_round& rd) {
 void admit_continuous(apic_server* sv, apic_server_round& rd) {
     bool any = false;
     while (!sv->queue.empty() && sv->active.size() + sv->pending < sv->max_active &&
-           sv->used + sv->queue.front()->bytes <= sv->budget) {
+           sv->used + sv->queue.front()->bytes <= sv->budget && fits_work(sv, sv->queue.front())) {
         Request* r = sv->queue.front();
         sv->queue.pop_front();
         r->t_admit = sv->now_ms();
         sv->used += r->bytes;  // reserved from admission on
+        sv->active_cells += r->cells;
         sv->peak = std::max(sv->peak, sv->used);
         sv->pending++;
         rd.admitted++;
@@ -476,6 +490,12 @@ int apic_server_scene_option(apic_server* sv, int option, int value, uint64_t mi
     return APIC_OK;
 }
 
+int apic_server_set_work_limit(apic_server* sv, uint64_t max_active_cells) {
+    if (!sv) return bad(APIC_ERR_INVALID_ARG, "apic_server_set_work_limit: null server");
+    sv->max_cells = max_active_cells;
+    return APIC_OK;
+}
+
 int apic_server_destroy(apic_server* sv) {
     if (!sv) return APIC_OK;
     stop_workers(sv);
@@ -506,6 +526,7 @@ int apic_server_submit(apic_server* sv, const apic_scene_params* scene, const ap
     r->rel_tol = rel_tol;
     r->max_iter = max_iterations;
     r->t_submit = sv->now_ms();
+    r->cells = uint64_t(scene->width) * scene->height;
     apic_scene_bytes(scene->width, scene->height, n, &r->bytes);
     if (r->bytes > sv->budget) {
         delete r;

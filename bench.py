@@ -569,8 +569,9 @@ def parse_scene_options(A, specs):
     return out
 
 
-def serve_stream(A, stream, budget, max_active, dt, time_limit, mode, threads, rules=()):
+def serve_stream(A, stream, budget, max_active, dt, time_limit, mode, threads, rules=(), max_cells=0):
     sv = A.Server(budget, max_active, mode=mode, prepare_threads=threads)
+    sv.set_work_limit(max_cells)
     for opt, value, lo, hi in rules:
         sv.scene_option(opt, value, lo, hi)
     t0 = time.perf_counter()
@@ -605,13 +606,15 @@ def run_served(args):
     dt = 1.0 / 240.0
     res = {}
     rules = parse_scene_options(A, args.scene_option)
-    arms = [("served", args.max_active, A.SERVER_CONTINUOUS, args.prepare_threads, rules)]
+    cells = args.max_active_cells
+    arms = [("served", args.max_active, A.SERVER_CONTINUOUS, args.prepare_threads, rules, cells)]
     if args.served_rounds:
-        arms.append(("served_rounds", args.max_active, A.SERVER_ROUNDS, 0, rules))
+        arms.append(("served_rounds", args.max_active, A.SERVER_ROUNDS, 0, rules, cells))
     if not args.no_plain:
-        arms.append(("plain", 1, A.SERVER_ROUNDS, 0, ()))
-    for name, active, mode, threads, arm_rules in arms:
-        st, n_sub = serve_stream(A, stream, budget, active, dt, args.time_limit, mode, threads, arm_rules)
+        arms.append(("plain", 1, A.SERVER_ROUNDS, 0, (), 0))
+    for name, active, mode, threads, arm_rules, arm_cells in arms:
+        st, n_sub = serve_stream(A, stream, budget, active, dt, args.time_limit, mode, threads, arm_rules,
+                                 arm_cells)
         res[name] = {"particle_substeps_per_s": st.particle_substeps / (st.elapsed_ms / 1e3),
                      "requests_submitted": n_sub, "requests_completed": st.completed, "failed": st.failed,
                      "updates": st.updates, "kernel_launches": st.kernel_launches,
@@ -620,7 +623,8 @@ def run_served(args):
                      "request_p50_ms": st.request_p50_ms, "request_p99_ms": st.request_p99_ms,
                      "memory_peak_gb": st.memory_peak / (1 << 30), "elapsed_s": st.elapsed_ms / 1e3,
                      "busy_s": st.busy_ms / 1e3, "prepare_s": st.prepare_ms / 1e3, "host_s": st.host_ms / 1e3,
-                     "max_active": active, "mode": "continuous" if mode == A.SERVER_CONTINUOUS else "rounds",
+                     "max_active": active, "max_active_cells": arm_cells,
+                     "mode": "continuous" if mode == A.SERVER_CONTINUOUS else "rounds",
                      "prepare_threads": threads}
     line = {
         "metric": METRIC, "value": res["served"]["particle_substeps_per_s"],
@@ -828,7 +832,9 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
     ap.add_argument("--seconds", type=float, default=2.0, help="served: length of the arrival stream")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="served: device-memory budget")
-    ap.add_argument("--max-active", type=int, default=64, help="served: active scenes at most")
+    ap.add_argument("--max-active", type=int, default=256, help="served: active scenes at most")
+    ap.add_argument("--max-active-cells", type=int, default=16 << 20,
+                    help="served: grid cells of the admitted scenes at most (0: no limit)")
     ap.add_argument("--prepare-threads", type=int, default=8, help="served: scene preparation threads")
     ap.add_argument("--served-rounds", action="store_true", help="served: also run the lock-step rounds server")
     ap.add_argument("--no-plain", action="store_true", help="served: skip the plain one-scene-at-a-time arm")

@@ -368,6 +368,11 @@ int apic_server_set_mode(apic_server* sv, int mode, uint32_t prepare_threads);
  * cell count lies in [min_cells, max_cells] (rules apply in the order given;
  * only while no scene is admitted). */
 int apic_server_scene_option(apic_server* sv, int option, int value, uint64_t min_cells, uint64_t max_cells);
+/* Work limit: a queued request is admitted only while the grid cells of the
+ * admitted scenes plus its own stay within max_active_cells (a request that
+ * would be alone is always admitted); 0 (default) removes the limit.  Small
+ * scenes need many scenes in flight to fill the GPU, large ones few. */
+int apic_server_set_work_limit(apic_server* sv, uint64_t max_active_cells);
 int apic_server_destroy(apic_server* sv);
 int apic_server_submit(apic_server* sv, const apic_scene_params* scene, const apic_world_props* props,
                        uint32_t steps, float frame_deltatime, int solver_mode, float rel_tol,

@@ -186,3 +186,21 @@ def test_stream_priority_option(gpu_lib):
         A.Apic(64, 64, 1 / 64, PROPS).set_option(A.OPT_STREAM_PRIORITY, -1)
     assert np.max(np.abs(runs[1] - runs[0])) < POS_TOL_CELLS / 64
     assert np.max(np.abs(runs[2] - runs[0])) < POS_TOL_CELLS / 64
+
+
+def test_server_work_limit_bounds_admitted_cells(gpu_lib):
+    """With a work limit of one scene's cells, the server runs one scene at a
+    time (each still completes); without it, all are admitted at once."""
+    for limit, expect_max in ((96 * 96, 1), (0, 3)):
+        sv = A.Server(1 << 40, max_active=8, mode=A.SERVER_CONTINUOUS, prepare_threads=2)
+        sv.set_work_limit(limit)
+        ids = [sv.submit(dam_break(96, 51 + k, 0.3), PROPS, 2, 1 / 240) for k in range(3)]
+        most = 0
+        for _ in range(100):
+            rd = sv.step()
+            most = max(most, rd.active)
+            if rd.active == 0 and rd.queued == 0:
+                break
+        assert most == expect_max, (limit, most)
+        assert all(sv.request(i).status == A.OK and sv.request(i).finished for i in ids)
+        sv.close()
