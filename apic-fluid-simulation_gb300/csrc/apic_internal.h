@@ -259,6 +259,11 @@ cudaError_t radix_sort_pairs_in(uint32_t* keys, uint32_t* vals, uint32_t* keys_a
 int morton_key_bits(uint32_t width, uint32_t height);
 // runtime.cu: record the calling thread's last error text (apic_last_error)
 void set_last_error(const char* msg);
+// runtime.cu: unique id of the CUDA context current on the calling thread
+// (the runtime's primary context is made current first if none is).  Ids are
+// never reused within a process, so caches of device addresses keyed by it
+// cannot outlive their context (cudaDeviceReset, a caller's own context).
+cudaError_t current_context_key(unsigned long long* key);
 // particles.cu
 cudaError_t launch_p2g(Scene& s);
 cudaError_t launch_g2p(Scene& s);

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <vector>
 
 #include "apic_device.cuh"
 #include "apic_internal.h"
@@ -29,26 +30,35 @@ constexpr size_t kScratchWords = 2ull * kNoAllocMaxKeys + kHistWords + kScanWord
 
 static __device__ __align__(256) uint32_t g_sort_scratch[kScratchWords];
 
-constexpr int kMaxDevices = 64;
+// Device address of the scratch array in the current CUDA context.  In host
+// code the array's name only stands in for the symbol; kernels must receive
+// this address.  It is looked up with cudaGetSymbolAddress once per context
+// (normally once per device: the runtime's primary context) and cached under
+// the context's unique id, so a context created later (after
+// cudaDeviceReset, or a caller's own context) gets its own lookup instead of
+// a stale address.
+struct ScratchEntry {
+    unsigned long long ctx;
+    uint32_t* addr;
+};
 std::mutex g_setup_mutex;
-uint32_t* g_scratch_addr[kMaxDevices] = {};
+std::vector<ScratchEntry> g_scratch;
 
-// Device address of this device's scratch array, looked up once per device
-// with that device current.  In host code the array's name only stands in
-// for the symbol; kernels must receive this address.
-cudaError_t scratch_for_current_device(uint32_t** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+cudaError_t scratch_for_current_context(uint32_t** out) {
+    unsigned long long ctx = 0;
+    cudaError_t e = current_context_key(&ctx);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_sort_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_addr[dev] = static_cast<uint32_t*>(p);
-    }
-    *out = g_scratch_addr[dev];
+    for (const ScratchEntry& s : g_scratch)
+        if (s.ctx == ctx) {
+            *out = s.addr;
+            return cudaSuccess;
+        }
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_sort_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch.push_back({ctx, static_cast<uint32_t*>(p)});
+    *out = static_cast<uint32_t*>(p);
     return cudaSuccess;
 }
 
@@ -82,11 +92,13 @@ extern "C" int apic_morton_sort_noalloc(const float* pos_x, const float* pos_y, 
         return reject(APIC_ERR_INVALID_ARG, "apic_morton_sort_noalloc: more than 1048576 particles (scratch limit)");
     if (width == 0 || height == 0 || !(cell_size > 0.0f))
         return reject(APIC_ERR_INVALID_ARG, "apic_morton_sort_noalloc: width, height and cell_size must be positive");
+    if (width > 65536u || height > 65536u)
+        return reject(APIC_ERR_INVALID_ARG, "apic_morton_sort_noalloc: width and height are limited to 65536");
     if (n == 0) return APIC_OK;
     if (!pos_x || !pos_y || !keys_out || !vals_out)
         return reject(APIC_ERR_INVALID_ARG, "apic_morton_sort_noalloc: null buffer");
     uint32_t* scratch = nullptr;
-    cudaError_t e = scratch_for_current_device(&scratch);
+    cudaError_t e = scratch_for_current_context(&scratch);
     if (e != cudaSuccess) return reject(APIC_ERR_CUDA, cudaGetErrorString(e));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     uint32_t* keys_alt = scratch;

@@ -167,36 +167,46 @@ __global__ void k_force_box(float wx, float wy, float radius, float cs, int W, i
 // ---- host helpers ---------------------------------------------------------
 
 // Scene buffers come from a stream-ordered memory pool of the library's own
-// (one per device, kept for the life of the process), allocated and released
-// in order on the scene's stream.  Releasing them does not synchronise the
-// whole device the way cudaFree does, so a scene retired while others run
-// (the request server) never stalls the scenes still on the GPU; the pool
-// keeps released memory for the next scene (no release threshold).
-constexpr int kMaxPoolDevices = 64;
+// (one per CUDA context, kept for the life of that context), allocated and
+// released in order on the scene's stream.  Releasing them does not
+// synchronise the whole device the way cudaFree does, so a scene retired
+// while others run (the request server) never stalls the scenes still on the
+// GPU; the pool keeps released memory for the next scene (no release
+// threshold).  The pool is found by the current context's unique id, not by
+// the device number: after cudaDeviceReset, or under a caller's own context,
+// a pool made for an earlier context is never handed out.
+struct PoolEntry {
+    unsigned long long ctx;
+    cudaMemPool_t pool;
+};
 std::mutex g_pool_mutex;
-cudaMemPool_t g_pool[kMaxPoolDevices] = {};
+std::vector<PoolEntry> g_pools;
 
 cudaError_t scene_pool(cudaMemPool_t* out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    unsigned long long ctx = 0;
+    cudaError_t e = apic::current_context_key(&ctx);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxPoolDevices) return cudaErrorInvalidDevice;
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(g_pool_mutex);
-    if (!g_pool[dev]) {
-        cudaMemPoolProps props = {};
-        props.allocType = cudaMemAllocationTypePinned;
-        props.location.type = cudaMemLocationTypeDevice;
-        props.location.id = dev;
-        cudaMemPool_t pool = nullptr;
-        if ((e = cudaMemPoolCreate(&pool, &props)) != cudaSuccess) return e;
-        uint64_t keep = ~0ull;
-        if ((e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess) {
-            cudaMemPoolDestroy(pool);
-            return e;
+    for (const PoolEntry& p : g_pools)
+        if (p.ctx == ctx) {
+            *out = p.pool;
+            return cudaSuccess;
         }
-        g_pool[dev] = pool;
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if ((e = cudaMemPoolCreate(&pool, &props)) != cudaSuccess) return e;
+    uint64_t keep = ~0ull;
+    if ((e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess) {
+        cudaMemPoolDestroy(pool);
+        return e;
     }
-    *out = g_pool[dev];
+    g_pools.push_back({ctx, pool});
+    *out = pool;
     return cudaSuccess;
 }
 
@@ -513,6 +523,48 @@ int valid_handle(apic_handle* h) {
 
 void apic::set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
 
+// The driver's cuCtxGetCurrent / cuCtxGetId, found through the runtime so the
+// library needs no link-time dependency on libcuda.
+namespace {
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+std::once_flag g_ctx_fns_once;
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+cudaError_t context_id_now(unsigned long long* id) {
+    void* ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != 0) return cudaErrorUnknown;
+    if (!ctx) {
+        *id = 0;
+        return cudaSuccess;
+    }
+    return g_ctx_get_id(ctx, id) == 0 ? cudaSuccess : cudaErrorUnknown;
+}
+}  // namespace
+
+cudaError_t apic::current_context_key(unsigned long long* key) {
+    std::call_once(g_ctx_fns_once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void* f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f);
+    });
+    if (!g_ctx_get_current || !g_ctx_get_id) return cudaErrorNotSupported;
+    cudaError_t e = context_id_now(key);
+    if (e != cudaSuccess || *key != 0) return e;
+    // no context is current on this thread yet: let the runtime make its
+    // primary context current, as its first call on this thread would
+    if ((e = cudaFree(nullptr)) != cudaSuccess) return e;
+    if ((e = context_id_now(key)) != cudaSuccess) return e;
+    return *key != 0 ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
+
 extern "C" {
 
 const char* apic_last_error(void) { return g_last_error.c_str(); }
@@ -542,6 +594,8 @@ int apic::create_scene(uint32_t width, uint32_t height, float cell_size, const a
     if (width == 0 || height == 0 || !(cell_size > 0.0f) || !std::isfinite(cell_size))
         return fail(APIC_ERR_INVALID_ARG, "width, height and cell_size must be positive");
     if (uint64_t(width) * height > (1ull << 31)) return fail(APIC_ERR_INVALID_ARG, "grid too large");
+    // Morton keys interleave 16 bits per axis (src/apic.rs:185-203)
+    if (width > 65536u || height > 65536u) return fail(APIC_ERR_INVALID_ARG, "width and height are limited to 65536");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(APIC_ERR_NO_DEVICE, "no CUDA device");
 

@@ -288,9 +288,12 @@ int apic_get_stream(apic_handle* h, void** stream_out);
  * keys_out/vals_out: n device u32 (sorted keys; original slot of each).
  * Every intermediate buffer lives in one fixed device array inside the
  * library (about 8.5 MiB, held by every GPU that loads it until exit), so n is
- * limited to 1,048,576; larger n returns APIC_ERR_INVALID_ARG.  The first call
- * on a device looks up that array's device address (do it before any stream
- * capture).  Work is enqueued on `stream` (NULL: default stream); calls whose
+ * limited to 1,048,576; larger n, or a width or height above 65536 (the
+ * Morton code interleaves 16 bits per axis), returns APIC_ERR_INVALID_ARG.
+ * The first call in a CUDA context (normally: the first on a device) looks up
+ * that array's device address; make it before any stream capture.  A context
+ * created later (after cudaDeviceReset, or the caller's own) gets a fresh
+ * lookup.  Work is enqueued on `stream` (NULL: default stream); calls whose
  * work overlaps on the GPU share the array and race.  Nothing in the array has
  * to start at zero: every word is written before it is read. */
 int apic_morton_sort_noalloc(const float* pos_x, const float* pos_y, uint32_t n, uint32_t width, uint32_t height,

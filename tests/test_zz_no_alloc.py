@@ -57,8 +57,42 @@ def test_noalloc_sort_matches_handle_sort(gpu_lib):
         assert np.array_equal(vals.cpu().numpy().view(np.uint32), ref_vals)
 
 
+def test_noalloc_sort_at_the_scratch_limit_on_a_side_stream(gpu_lib):
+    """Exactly 1,048,576 particles (the largest count the fixed scratch array
+    holds, so its last word is used) on a non-default stream, twice in a row."""
+    if A.device_count() == 0:
+        pytest.skip("no CUDA device")
+    torch = pytest.importorskip("torch")
+    lib = A.load_library()
+    side, n = 1024, 1 << 20
+    rng = np.random.default_rng(7)
+    side_stream = torch.cuda.Stream()
+    for call in range(2):
+        px = rng.uniform(0.0, 1.0, n).astype(np.float32)
+        py = rng.uniform(0.0, 1.0, n).astype(np.float32)
+        if call == 1:  # ties and cells at the clamp
+            px[::3] = 0.5
+            py[::5] = 1.5
+        ref_keys, ref_vals = _handle_sort(side, px, py)
+        with torch.cuda.stream(side_stream):
+            dpx = torch.from_numpy(px).cuda()
+            dpy = torch.from_numpy(py).cuda()
+            keys = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+            vals = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+            rc = lib.apic_morton_sort_noalloc(dpx.data_ptr(), dpy.data_ptr(), n, side, side, 1.0 / side,
+                                              keys.data_ptr(), vals.data_ptr(),
+                                              ctypes.c_void_p(side_stream.cuda_stream))
+            assert rc == A.OK, lib.apic_last_error()
+        side_stream.synchronize()
+        assert np.array_equal(keys.cpu().numpy().view(np.uint32), ref_keys)
+        assert np.array_equal(vals.cpu().numpy().view(np.uint32), ref_vals)
+
+
 def test_noalloc_sort_rejects_oversize(gpu_lib):
     lib = A.load_library()
     rc = lib.apic_morton_sort_noalloc(None, None, (1 << 20) + 1, 64, 64, 1 / 64, None, None, None)
     assert rc == A.ERR_INVALID_ARG
     assert b"1048576" in lib.apic_last_error()
+    rc = lib.apic_morton_sort_noalloc(None, None, 16, 65537, 64, 1 / 64, None, None, None)
+    assert rc == A.ERR_INVALID_ARG
+    assert b"65536" in lib.apic_last_error()
