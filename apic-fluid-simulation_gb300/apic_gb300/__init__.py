@@ -26,12 +26,8 @@ UPDATE_DISABLE_SORT = 0x1
 SOLVER_REFERENCE, SOLVER_REL_FP32, SOLVER_REL_MIXED = 0, 1, 2
 SERVER_ROUNDS, SERVER_CONTINUOUS = 0, 1
 SCENE_REFERENCE_DEFAULT, SCENE_DAM_BREAK, SCENE_DAM_BREAK_DISK, SCENE_NOISE = 0, 1, 2, 3
-OPT_PERSISTENT_SOLVE = 1
-OPT_FUSED_VCYCLE = 2
-OPT_CLUSTER_VCYCLE = 3
 OPT_PDL = 4
 OPT_DSM_VCYCLE = 5
-OPT_CLUSTER_SOLVE = 6
 OPT_WARM_START = 7
 OPT_STREAM_PRIORITY = 8
 

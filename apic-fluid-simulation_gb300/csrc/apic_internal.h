@@ -36,6 +36,7 @@ constexpr int kSegWarps = kSegBlock / 32;
 constexpr int kMaxRedBlocks = 152 * (2048 / kSegBlock);  // one full wave on 152 SMs: grid of reduction kernels
 constexpr int kSortTile = 2048;       // keys per block in the radix sort
 constexpr int kSortThreads = 256;
+constexpr int kMaxDigitBits = 10;     // widest radix-sort digit (1024 buckets)
 
 // Device-resident control block of one scene.
 struct Ctl {
@@ -74,6 +75,7 @@ struct Ctl {
     uint32_t refinements_total;  // refinements summed over the substeps of an update
     uint32_t cond;          // last loop decision of a control kernel (eager runs read it)
     uint32_t sorted;        // the update ran the Morton sort
+    float rz_exact;         // reference mode: r.z in dot_product's order
     double dgamma;          // FP64 copies for the relative-tolerance modes
     double bnorm2;          // ||b||^2 of the running solve
     double rnorm2;          // ||r||^2 of the recursive residual
@@ -90,13 +92,7 @@ struct Ctl {
 enum : uint32_t {
     kStatusNonfinite = 1u,
     kStatusBadStep = 2u,
-    kStatusTimeout = 4u,
-};
-
-// Grid barrier state of the persistent solver (zeroed before each launch).
-struct GridSync {
-    unsigned int count;
-    unsigned int gen;
+    kStatusP2gLayout = 8u,  // a particle's staggered stencil left the bins P2G searches (never expected)
 };
 
 struct Level {
@@ -111,7 +107,6 @@ struct Level {
     float* py = nullptr;
     float* res = nullptr;
     float* err = nullptr;
-    float* err2 = nullptr;  // second error array of the fused V-cycle (never updated in place)
 };
 
 // Particle field order, matching apic_field ids 0..8.
@@ -159,8 +154,12 @@ struct Scene {
     uint32_t* vals = nullptr;
     uint32_t* keys_alt = nullptr;
     uint32_t* vals_alt = nullptr;
-    uint32_t* sort_hist = nullptr;         // 256 * sort blocks
+    uint32_t* sort_hist = nullptr;         // sort_hist_words(n)
     uint32_t* sort_scan_tmp = nullptr;
+    // P2G binning: (cell of the density stencil's base, slot) pairs sorted by
+    // cell, and each cell's run [bin_lo, bin_hi) in the sorted pairs
+    uint32_t *bin_keys = nullptr, *bin_vals = nullptr, *bin_keys_alt = nullptr, *bin_vals_alt = nullptr;
+    uint32_t *bin_lo = nullptr, *bin_hi = nullptr;
 
     uint32_t uf = 0, vf = 0;               // face counts
     float *u = nullptr, *v = nullptr, *u_alt = nullptr, *v_alt = nullptr;
@@ -188,6 +187,8 @@ struct Scene {
     Ctl* ctl = nullptr;                       // device
     Ctl* ctl_host = nullptr;                  // pinned mirror
     double* partials = nullptr;               // kPartialDoubles doubles (block partials of reductions)
+    float* exact_parts = nullptr;             // chunk sums of the reference-order s.Ap (cells / 8192 + 1)
+    uint32_t* seg_pre = nullptr;              // fluid cells before each base segment (words + 1)
     uint32_t* scan_tmp = nullptr;             // compaction block counts
     uint32_t scan_tmp_len = 0;
 
@@ -195,18 +196,6 @@ struct Scene {
     int priority = 0;                         // stream priority: levels above the lowest
     cudaStream_t cap_stream = nullptr;        // stream used to record graphs
     cudaGraphExec_t update_exec = nullptr;    // whole Apic::update as one graph
-    GridSync* gsync = nullptr;                // persistent solver barrier
-    int persist_grid = 0;                     // CTAs of the persistent solver (0: unavailable)
-    size_t persist_smem = 0;
-    bool use_persistent = false;              // persistent kernel vs graph of per-phase kernels
-    uint32_t cluster_solve_cells = 0;         // scenes up to this many cells solve in one cluster (0: never)
-    int cluster_solve_ctas = 0;               // CTAs of that cluster (0: not used for this scene)
-    bool fused_vcycle = false;                // one kernel per level and direction in the V-cycle
-    // middle levels [cluster_first, tail_first) of the V-cycle run in one
-    // thread-block cluster (cluster_first == tail_first: none)
-    uint32_t cluster_max_cells = 65536;       // largest level handed to the cluster (0: never)
-    int cluster_size = 0;                     // CTAs per cluster (0: clusters unavailable)
-    int cluster_first = 0;
     bool use_pdl = true;                      // programmatic dependent launch inside the PCG loop
     // levels [dsm_first, dsm_tail) of the V-cycle held in a cluster's
     // distributed shared memory, dsm_tail.. in CTA 0 (dsm_first == nlevels: none)
@@ -250,12 +239,27 @@ inline float2* part_rz(const Scene& s) { return reinterpret_cast<float2*>(s.part
 // The mixed-precision solve starts from the FP64 pressure that the previous
 // solve left in p64 (zeroed whenever the particle set is replaced).
 inline int warm_start(const Scene& s) { return s.warm_start && s.solver_mode == APIC_SOLVER_REL_MIXED ? 1 : 0; }
+// The reference solver mode reproduces the reference's FP32 reduction orders
+// (dot_product's eight lane sums, apply_matrix_and_dot's 8192-cell chunks,
+// the coarsest CG's serial sums), so its pressure is bit-identical to the
+// oracle's; the relative modes reduce in FP64 / double-float instead.
+inline bool coarse_cg_exact(const Scene& s) { return s.solver_mode == APIC_SOLVER_REFERENCE; }
 // render.cu: splat the particles into the scene's frame and wait for it
 cudaError_t render_frame(Scene& s, const RenderParamsDev& p, RenderResult* out);
 const uint32_t* render_frame_ptr(const Scene& s, uint32_t* width, uint32_t* height);
 void free_render(Scene& s);
 cudaError_t radix_sort_pairs_in(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* hist,
                                 uint32_t* scan_tmp, uint32_t n, int bits, cudaStream_t st);
+// Stable LSD sort with digits of up to kMaxDigitBits bits; the sorted pairs
+// stay where the last pass wrote them (*keys_out / *vals_out: keys/vals or
+// keys_alt/vals_alt).  hist: sort_hist_words(n), scan_tmp: sort_scan_words(n).
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* hist,
+                             uint32_t* scan_tmp, uint32_t n, int bits, cudaStream_t st, bool pdl,
+                             uint32_t** keys_out, uint32_t** vals_out);
+bool radix_sort_in_alt(int bits);     // radix_sort_pairs over `bits` bits ends in the alt buffers
+uint32_t sort_hist_words(uint32_t n);
+uint32_t sort_scan_words(uint32_t n);
+bool sort_result_in_alt(const Scene& s);  // where launch_sort leaves the Morton-sorted pairs
 int morton_key_bits(uint32_t width, uint32_t height);
 // runtime.cu: record the calling thread's last error text (apic_last_error)
 void set_last_error(const char* msg);
@@ -268,7 +272,7 @@ cudaError_t current_context_key(unsigned long long* key);
 cudaError_t launch_p2g(Scene& s);
 cudaError_t launch_g2p(Scene& s);
 cudaError_t launch_vmax(Scene& s);
-cudaError_t launch_permute(Scene& s);
+cudaError_t launch_permute(Scene& s, const uint32_t* sorted_vals);
 cudaError_t launch_pack_vec2x8(Scene& s, int which, float* out);  // which: 0 pos, 1 vel, 2 C_u, 3 C_v
 // grid.cu
 cudaError_t launch_finalize_faces(Scene& s, bool forces, bool gravity);
@@ -282,17 +286,11 @@ cudaError_t launch_extrapolate(Scene& s);
 cudaError_t launch_smoothed_view(Scene& s, float* out);
 cudaError_t launch_level_lists(Scene& s, int level);
 // solver.cu: the solve is recorded into graphs (apic_graph.h: build_solve)
-// pcg_persistent.cu
-void plan_persistent_solve(Scene& s);
-cudaError_t enqueue_persistent_solve(Scene& s);
-void plan_cluster_solve(Scene& s);     // small scenes: the whole solve in one cluster
-cudaError_t enqueue_cluster_solve(Scene& s);
 // solver.cu: the same solve launched kernel by kernel with host loop control
 // (profiling runs, so every kernel is a separate launch)
 cudaError_t run_solve_eager(Scene& s);
 // vcycle.cu
 void plan_vcycle(Scene& s);     // pick the coarse levels that run in one CTA / one cluster
-void plan_vcycle_cluster(Scene& s);  // re-pick the cluster's levels after cluster_max_cells changed
 // vcycle_dsm.cu
 void plan_vcycle_dsm(Scene& s);
 void launch_vcycle_dsm(Scene& s, cudaStream_t st);

@@ -27,214 +27,430 @@
 namespace apic {
 namespace {
 
-// P2G accumulation window of one CTA: the faces and cells that its 256
-// consecutive particles touch.  After the Morton sort consecutive slots are
-// neighbouring cells, so the window is small; a CTA whose window (per grid)
-// exceeds kP2gCap entries, e.g. across a jump of the Morton curve or with
-// unsorted particles, adds straight to global memory instead.
-constexpr int kP2gThreads = 256;
-constexpr int kP2gCap = 512;
-// Shared-memory float atomics are compare-and-swap loops, and consecutive
-// lanes hold particles of the same cell, so the window arrays are kept in
-// kP2gCopies interleaved copies (entry e, copy c at e * kP2gCopies + c, in
-// different banks) and lane l adds into copy l % kP2gCopies.
-constexpr int kP2gCopies = 4;
+// ---- P2G as an ordered gather ------------------------------------------------
+//
+// The reference adds every chunk's contributions to a face with a CAS loop
+// (add_to_mac :296-344, add_to_vec_f32 :347-369): per chunk of 8 slots and per
+// stencil corner k (bl, br, tl, tr), the lanes that hit the same face are
+// summed in lane order and that group sum is added to the face.  Run on one
+// thread, chunk after chunk, a face's sum is therefore the fold of its
+// (chunk, corner) group sums in that order, which is the order the oracle
+// defines.  Here every face is summed by one thread in exactly that order, so
+// the result is bit-identical to the oracle and the same on every run:
+//
+//   k_p2g_bin_keys  key = the cell of the density stencil's base (cx0, cy0)
+//                   for every particle; fluid bits (an OR: order-free)
+//   radix sort      stable, so each cell's particles stay in slot order
+//   k_p2g_bounds    each cell's run [lo, hi) in the sorted pairs
+//   k_p2g_gather    per 32 x 8 tile of cells: stage the particles of the
+//                   tile's cells and a two-cell halo below and to the left in
+//                   shared memory, compute their stencil contributions once
+//                   per grid, then let each face merge the runs of the (up to
+//                   six) cells whose particles can reach it by slot and fold
+//                   the contributions in (chunk, corner, lane) order.
+//
+// Which cells can reach a face follows from the clamped index arithmetic
+// (u_index / v_index, :1029-1041): the u stencil's rows equal the density
+// stencil's rows and its columns start at cx0 or cx0 + 1; the v stencil's
+// columns equal the density stencil's and its rows start at cy0 or cy0 + 1.
+// So u face (i, j) gathers from cells x in [i-2, i], y in [j-1, j], v face
+// (i, j) from x in [i-1, i], y in [j-2, j], and density cell (i, j) from
+// x in [i-1, i], y in [j-1, j].  A particle whose corners fall outside those
+// offsets (impossible by the arithmetic above, checked anyway) raises
+// kStatusP2gLayout.
+constexpr int kGatherTW = 32, kGatherTH = 8;           // tile of cells, one thread per cell
+constexpr int kGatherThreads = kGatherTW * kGatherTH;
+constexpr int kRegionW = kGatherTW + 2, kRegionH = kGatherTH + 2;
+constexpr int kRegionBins = kRegionW * kRegionH;       // 340 cells whose particles a tile reads
+constexpr int kGatherCap = 2048;                       // staged particles per tile (more: read from global)
+constexpr size_t kGatherSmem = size_t(kGatherCap) * (4 + 4 + 8 * 4) + size_t(kRegionBins) * 8 + 64;
 
-struct Box {
-    int x0, y0, w, h;
-};
+enum { kGridU = 0, kGridV = 1, kGridD = 2 };
 
-__device__ __forceinline__ int warp_min_i(int v) { return __reduce_min_sync(0xffffffffu, v); }
-__device__ __forceinline__ int warp_max_i(int v) { return __reduce_max_sync(0xffffffffu, v); }
+// Exclusive scan over the threads of a block (blockDim.x a multiple of 32).
+__device__ __forceinline__ uint32_t block_exclusive_scan_u32(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t sw[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sw[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t t = lane < int(blockDim.x / 32) ? sw[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        sw[lane] = t;
+    }
+    __syncthreads();
+    const uint32_t pre = warp > 0 ? sw[warp - 1] : 0u;
+    *total = sw[blockDim.x / 32 - 1];
+    __syncthreads();
+    return pre + x - v;
+}
 
-__global__ void __launch_bounds__(kP2gThreads, 4) k_p2g(const PartPtrs* __restrict__ pp, uint32_t n, int W, int H,
-                                                     float dx, const Ctl* __restrict__ ctl, float* __restrict__ acc_u,
-                                                     float* __restrict__ acc_uw, float* __restrict__ acc_v,
-                                                     float* __restrict__ acc_vw, float* __restrict__ dens,
-                                                     uint32_t* __restrict__ fluid) {
-    __shared__ float s_um[kP2gCap * kP2gCopies], s_uw[kP2gCap * kP2gCopies], s_vm[kP2gCap * kP2gCopies],
-        s_vw[kP2gCap * kP2gCopies], s_d[kP2gCap * kP2gCopies];
-    __shared__ uint8_t s_fl[kP2gCap];  // fluid cells of the density window
-    __shared__ int s_red[kP2gThreads / 32][12];
-    __shared__ Box s_box[3];
-    __shared__ int s_tiled;
+__global__ void __launch_bounds__(256) k_p2g_bin_keys(const PartPtrs* __restrict__ pp, uint32_t n, int W, int H,
+                                                      float dx, uint32_t* __restrict__ keys,
+                                                      uint32_t* __restrict__ vals, uint32_t* __restrict__ fluid) {
     pdl_wait();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
-    // bounds of the clamped node coordinates: u, v faces and density cells
-    int b[12];
-    float ua[4], wu[4], va[4], wv[4], cw[4];
-    int ux[2], uy[2], vx2[2], vy2[2], cx[2], cy[2];
-    int fx = 0, fy = 0;  // the particle's own cell (its fluid bit)
+    uint32_t word = 0xFFFFFFFFu, bit = 0;
     if (live) {
-        const float prev_dt = ctl->prev_dt;
-        float px = pp->f[PX][i], py = pp->f[PY][i];
-        float vx = pp->f[VX][i], vy = pp->f[VY][i];
-        float cux = pp->f[CUX][i], cuy = pp->f[CUY][i];
-        float cvx = pp->f[CVX][i], cvy = pp->f[CVY][i];
-        float tr = pp->f[TR][i];
-
-        float tau = (-tr) / prev_dt;
-        float wt = temporal_w(tau);
-        float gx = px / dx, gy = py / dx;
-
-        // cell-centred density stencil
-        float cgx = gx - 0.5f, cgy = gy - 0.5f;
-        float cbx = floorf(cgx), cby = floorf(cgy);
-        float ctx = cgx - cbx, cty = cgy - cby;
-        cw[0] = ((1.0f - ctx) * (1.0f - cty)) * wt;
-        cw[1] = (ctx * (1.0f - cty)) * wt;
-        cw[2] = ((1.0f - ctx) * cty) * wt;
-        cw[3] = (ctx * cty) * wt;
-        int mx = W - 1, my = H - 1;
-        int tbx = trunc_x86(cbx), tby = trunc_x86(cby);
-        cx[0] = max(min(tbx, mx), 0); cx[1] = max(min(tbx + 1, mx), 0);
-        cy[0] = max(min(tby, my), 0); cy[1] = max(min(tby + 1, my), 0);
-
-        Stencil su, sv;
-        u_stencil(gx, gy, W, H, dx, su);
-        v_stencil(gx, gy, W, H, dx, sv);
-        {
-            // the same clamps as u_index / v_index
-            int ix = trunc_x86(floorf(gx)), iy = trunc_x86(floorf(gy - 0.5f));
-            ux[0] = max(min(ix, W), 0); ux[1] = max(min(ix + 1, W), 0);
-            uy[0] = max(min(iy, H - 1), 0); uy[1] = max(min(iy + 1, H - 1), 0);
-            int jx = trunc_x86(floorf(gx - 0.5f)), jy = trunc_x86(floorf(gy));
-            vx2[0] = max(min(jx, W - 1), 0); vx2[1] = max(min(jx + 1, W - 1), 0);
-            vy2[0] = max(min(jy, H), 0); vy2[1] = max(min(jy + 1, H), 0);
-        }
-
-        float clx = fmax_x86(fmin_x86(gx, float(W) - 1.0f), 0.0f);
-        float cly = fmax_x86(fmin_x86(gy, float(H) - 1.0f), 0.0f);
-        fx = trunc_x86(clx);
-        fy = trunc_x86(cly);
-
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            wu[k] = su.w[k] * wt;
-            ua[k] = (vx + cux * su.ox[k] + cuy * su.oy[k]) * wu[k];
-            wv[k] = sv.w[k] * wt;
-            va[k] = (vy + cvx * sv.ox[k] + cvy * sv.oy[k]) * wv[k];
-        }
-        b[0] = ux[0]; b[1] = -ux[1]; b[2] = uy[0]; b[3] = -uy[1];
-        b[4] = vx2[0]; b[5] = -vx2[1]; b[6] = vy2[0]; b[7] = -vy2[1];
-        b[8] = min(cx[0], fx); b[9] = -max(cx[1], fx); b[10] = min(cy[0], fy); b[11] = -max(cy[1], fy);
-    } else {
-#pragma unroll
-        for (int k = 0; k < 12; ++k) b[k] = INT_MAX;
-    }
-    // block minima of the lows and of the negated highs
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 12; ++k) {
-        int m = warp_min_i(b[k]);
-        if (lane == 0) s_red[warp][k] = m;
-    }
-    __syncthreads();
-    if (threadIdx.x < 3) {
-        int lo_x = INT_MAX, hi_x = INT_MAX, lo_y = INT_MAX, hi_y = INT_MAX;
-        for (int w = 0; w < kP2gThreads / 32; ++w) {
-            lo_x = min(lo_x, s_red[w][4 * threadIdx.x + 0]);
-            hi_x = min(hi_x, s_red[w][4 * threadIdx.x + 1]);
-            lo_y = min(lo_y, s_red[w][4 * threadIdx.x + 2]);
-            hi_y = min(hi_y, s_red[w][4 * threadIdx.x + 3]);
-        }
-        Box bx;
-        bx.x0 = lo_x; bx.y0 = lo_y;
-        bx.w = -hi_x - lo_x + 1; bx.h = -hi_y - lo_y + 1;
-        s_box[threadIdx.x] = bx;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        bool ok = true;
-        for (int g = 0; g < 3; ++g)
-            ok = ok && s_box[g].w > 0 && s_box[g].h > 0 && (long long)s_box[g].w * s_box[g].h <= kP2gCap;
-        s_tiled = ok ? 1 : 0;
-    }
-    __syncthreads();
-    if (!s_tiled) {
-        if (!live) return;
+        const float gx = pp->f[PX][i] / dx, gy = pp->f[PY][i] / dx;
+        const int cx0 = max(min(trunc_x86(floorf(gx - 0.5f)), W - 1), 0);
+        const int cy0 = max(min(trunc_x86(floorf(gy - 0.5f)), H - 1), 0);
+        keys[i] = uint32_t(cy0) * uint32_t(W) + uint32_t(cx0);
+        vals[i] = i;
+        // the particle's own cell (:1358-1360)
+        const int fx = trunc_x86(fmax_x86(fmin_x86(gx, float(W) - 1.0f), 0.0f));
+        const int fy = trunc_x86(fmax_x86(fmin_x86(gy, float(H) - 1.0f), 0.0f));
         const uint32_t fi = uint32_t(fy * W + fx);
-        atomicOr(fluid + (fi >> 5), 1u << (fi & 31u));
-        // node k = (x[k & 1], y[k >> 1]): the u_index / v_index of the stencils
+        word = fi >> 5;
+        bit = 1u << (fi & 31u);
+    }
+    // one OR per mask word that the warp touches
+    const uint32_t peers = __match_any_sync(0xffffffffu, word);
+    const uint32_t m = __reduce_or_sync(peers, bit);
+    const int lane = threadIdx.x & 31;
+    if (live && (peers & ((1u << lane) - 1u)) == 0) atomicOr(fluid + word, m);
+}
+
+__global__ void __launch_bounds__(256) k_p2g_bounds(const uint32_t* __restrict__ keys, uint32_t n,
+                                                    uint32_t* __restrict__ lo, uint32_t* __restrict__ hi) {
+    pdl_wait();
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t k = keys[j];
+    if (j == 0 || keys[j - 1] != k) lo[k] = j;
+    if (j == n - 1 || keys[j + 1] != k) hi[k] = j + 1;
+}
+
+// One particle's contributions to one grid: per corner k the value and weight
+// (value unused for the density) and, per relative face position q of the
+// face that gathers it (q = ry * nx + rx, offsets from the particle's density
+// base cell), a 4-bit mask of the corners that land there.
+struct P2gRec {
+    uint32_t code;
+    float val[4], w[4];
+};
+
+__device__ __forceinline__ bool p2g_record(const PartPtrs* __restrict__ pp, uint32_t slot, int grid, int W, int H,
+                                           float dx, float prev_dt, P2gRec& r) {
+    const float px = pp->f[PX][slot], py = pp->f[PY][slot];
+    const float tr = pp->f[TR][slot];
+    const float tau = (-tr) / prev_dt;
+    const float wt = temporal_w(tau);
+    const float gx = px / dx, gy = py / dx;
+    const int cx0 = max(min(trunc_x86(floorf(gx - 0.5f)), W - 1), 0);
+    const int cy0 = max(min(trunc_x86(floorf(gy - 0.5f)), H - 1), 0);
+    int xs[2], ys[2], nx, ny;
+    if (grid == kGridD) {
+        // cell-centred density stencil (:1260-1284)
+        const float cgx = gx - 0.5f, cgy = gy - 0.5f;
+        const float cbx = floorf(cgx), cby = floorf(cgy);
+        const float ctx = cgx - cbx, cty = cgy - cby;
+        r.w[0] = ((1.0f - ctx) * (1.0f - cty)) * wt;
+        r.w[1] = (ctx * (1.0f - cty)) * wt;
+        r.w[2] = ((1.0f - ctx) * cty) * wt;
+        r.w[3] = (ctx * cty) * wt;
+        const int tbx = trunc_x86(cbx), tby = trunc_x86(cby);
+        xs[0] = max(min(tbx, W - 1), 0); xs[1] = max(min(tbx + 1, W - 1), 0);
+        ys[0] = max(min(tby, H - 1), 0); ys[1] = max(min(tby + 1, H - 1), 0);
+        nx = 2; ny = 2;
+    } else if (grid == kGridU) {
+        Stencil su;
+        u_stencil(gx, gy, W, H, dx, su);
+        const float vx = pp->f[VX][slot], cux = pp->f[CUX][slot], cuy = pp->f[CUY][slot];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const uint32_t iu = uint32_t(uy[k >> 1]) * uint32_t(W + 1) + uint32_t(ux[k & 1]);
-            if (ua[k] != 0.0f || wu[k] != 0.0f) { atomicAdd(acc_u + iu, ua[k]); atomicAdd(acc_uw + iu, wu[k]); }
+            r.w[k] = su.w[k] * wt;
+            r.val[k] = (vx + cux * su.ox[k] + cuy * su.oy[k]) * r.w[k];
         }
+        const int ix = trunc_x86(floorf(gx)), iy = trunc_x86(floorf(gy - 0.5f));
+        xs[0] = max(min(ix, W), 0); xs[1] = max(min(ix + 1, W), 0);
+        ys[0] = max(min(iy, H - 1), 0); ys[1] = max(min(iy + 1, H - 1), 0);
+        nx = 3; ny = 2;
+    } else {
+        Stencil sv;
+        v_stencil(gx, gy, W, H, dx, sv);
+        const float vy = pp->f[VY][slot], cvx = pp->f[CVX][slot], cvy = pp->f[CVY][slot];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const uint32_t iv = uint32_t(vy2[k >> 1]) * uint32_t(W) + uint32_t(vx2[k & 1]);
-            if (va[k] != 0.0f || wv[k] != 0.0f) { atomicAdd(acc_v + iv, va[k]); atomicAdd(acc_vw + iv, wv[k]); }
+            r.w[k] = sv.w[k] * wt;
+            r.val[k] = (vy + cvx * sv.ox[k] + cvy * sv.oy[k]) * r.w[k];
         }
+        const int jx = trunc_x86(floorf(gx - 0.5f)), jy = trunc_x86(floorf(gy));
+        xs[0] = max(min(jx, W - 1), 0); xs[1] = max(min(jx + 1, W - 1), 0);
+        ys[0] = max(min(jy, H), 0); ys[1] = max(min(jy + 1, H), 0);
+        nx = 2; ny = 3;
+    }
+    uint32_t code = 0;
+    bool ok = true;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t ic = uint32_t(cy[k >> 1]) * uint32_t(W) + uint32_t(cx[k & 1]);
-            if (cw[k] != 0.0f) atomicAdd(dens + ic, cw[k]);
+    for (int k = 0; k < 4; ++k) {
+        const int rx = xs[k & 1] - cx0, ry = ys[k >> 1] - cy0;
+        if (rx < 0 || rx >= nx || ry < 0 || ry >= ny) {
+            ok = false;
+            continue;
+        }
+        code |= (1u << k) << (4 * (ry * nx + rx));
+    }
+    r.code = code;
+    return ok;
+}
+
+// Records staged in shared memory (fast path) or computed from global memory
+// when they are needed (tiles with more than kGatherCap particles).
+struct StagedRecs {
+    const uint32_t* slot;
+    const uint32_t* code;
+    const float* val;  // [4][kGatherCap]
+    const float* w;    // [4][kGatherCap]
+    __device__ __forceinline__ uint32_t slot_at(int p) const { return slot[p]; }
+    __device__ __forceinline__ uint32_t code_at(int p) const { return code[p]; }
+    __device__ __forceinline__ void get(int p, int, float* v, float* wt) const {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { v[k] = val[k * kGatherCap + p]; wt[k] = w[k * kGatherCap + p]; }
+    }
+};
+struct GlobalRecs {
+    const uint32_t* vals;  // sorted slots
+    const PartPtrs* pp;
+    int grid, W, H;
+    float dx, prev_dt;
+    uint32_t* status;
+    __device__ __forceinline__ uint32_t slot_at(int p) const { return vals[p]; }
+    __device__ __forceinline__ uint32_t code_at(int p) const {
+        P2gRec r;
+        if (!p2g_record(pp, vals[p], grid, W, H, dx, prev_dt, r)) atomicOr(status, kStatusP2gLayout);
+        return r.code;
+    }
+    __device__ __forceinline__ void get(int p, int, float* v, float* wt) const {
+        P2gRec r;
+        p2g_record(pp, vals[p], grid, W, H, dx, prev_dt, r);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { v[k] = r.val[k]; wt[k] = r.w[k]; }
+    }
+};
+
+// Fold of one face: merge NR slot-ordered runs [b, e) by slot; run r's records
+// reach this face through the corners in bits sh[r] .. sh[r] + 3 of their
+// code.  Consecutive records of one chunk form the chunk's groups: per corner
+// k, the lanes' contributions summed in lane order; at the end of the chunk
+// the groups are added to the face in corner order.
+template <int NR, class Recs>
+__device__ __forceinline__ void fold_face(const Recs& R, int (&b)[NR], const int (&e)[NR], const int (&sh)[NR],
+                                          float& out_v, float& out_w) {
+    uint32_t hs[NR];
+#pragma unroll
+    for (int r = 0; r < NR; ++r) hs[r] = b[r] < e[r] ? R.slot_at(b[r]) : 0xFFFFFFFFu;
+    float acc_v = 0.0f, acc_w = 0.0f;
+    float gv[4] = {0.0f, 0.0f, 0.0f, 0.0f}, gw[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    uint32_t gm = 0, chunk = 0xFFFFFFFFu;
+    for (;;) {
+        uint32_t best = hs[0];
+        int m = 0;
+#pragma unroll
+        for (int r = 1; r < NR; ++r)
+            if (hs[r] < best) { best = hs[r]; m = r; }
+        if (best == 0xFFFFFFFFu) break;
+        int p = 0, s = 0;
+#pragma unroll
+        for (int r = 0; r < NR; ++r)
+            if (r == m) {
+                p = b[r];
+                s = sh[r];
+                b[r] = p + 1;
+                hs[r] = b[r] < e[r] ? R.slot_at(b[r]) : 0xFFFFFFFFu;
+            }
+        const uint32_t hit = (R.code_at(p) >> s) & 0xFu;
+        if (!hit) continue;
+        if ((best >> 3) != chunk) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (gm & (1u << k)) { acc_v = acc_v + gv[k]; acc_w = acc_w + gw[k]; }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) { gv[k] = 0.0f; gw[k] = 0.0f; }
+            gm = 0;
+            chunk = best >> 3;
+        }
+        float v[4], w[4];
+        R.get(p, s, v, w);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (hit & (1u << k)) { gv[k] = gv[k] + v[k]; gw[k] = gw[k] + w[k]; }
+        gm |= hit;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (gm & (1u << k)) { acc_v = acc_v + gv[k]; acc_w = acc_w + gw[k]; }
+    out_v = acc_v;
+    out_w = acc_w;
+}
+
+struct GatherOut {
+    float *acc_u, *acc_uw, *acc_v, *acc_vw, *dens;
+};
+
+// The faces and cells of this thread's cell (i, j) for one grid; bin(x, y)
+// gives a cell's run (empty outside the grid).
+template <class Recs, class Bin>
+__device__ __forceinline__ void fold_cell(const Recs& R, const Bin& bin, int grid, int i, int j, int W, int H,
+                                          const GatherOut& o) {
+    auto run = [&](int x, int y, int& b, int& e) {
+        if (x < 0 || x >= W || y < 0 || y >= H) { b = e = 0; return; }
+        bin(x, y, b, e);
+    };
+    if (grid == kGridU) {
+        // u face (fi, j), and (W, j) from the last column's thread
+        for (int fi = i; fi <= (i == W - 1 ? W : i); ++fi) {
+            int b[6], e[6], sh[6];
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                const int rx = r % 3, ry = r / 3;  // face offset from the cell
+                run(fi - rx, j - ry, b[r], e[r]);
+                sh[r] = 4 * (ry * 3 + rx);
+            }
+            float v, w;
+            fold_face<6>(R, b, e, sh, v, w);
+            const uint32_t f = uint32_t(j) * uint32_t(W + 1) + uint32_t(fi);
+            o.acc_u[f] = v;
+            o.acc_uw[f] = w;
+        }
+    } else if (grid == kGridV) {
+        for (int fj = j; fj <= (j == H - 1 ? H : j); ++fj) {
+            int b[6], e[6], sh[6];
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                const int rx = r % 2, ry = r / 2;
+                run(i - rx, fj - ry, b[r], e[r]);
+                sh[r] = 4 * (ry * 2 + rx);
+            }
+            float v, w;
+            fold_face<6>(R, b, e, sh, v, w);
+            const uint32_t f = uint32_t(fj) * uint32_t(W) + uint32_t(i);
+            o.acc_v[f] = v;
+            o.acc_vw[f] = w;
+        }
+    } else {
+        int b[4], e[4], sh[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int rx = r % 2, ry = r / 2;
+            run(i - rx, j - ry, b[r], e[r]);
+            sh[r] = 4 * (ry * 2 + rx);
+        }
+        float v, w;
+        fold_face<4>(R, b, e, sh, v, w);
+        o.dens[uint32_t(j) * uint32_t(W) + uint32_t(i)] = w;
+    }
+}
+
+__global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs* __restrict__ pp,
+                                                                  const uint32_t* __restrict__ vals,
+                                                                  const uint32_t* __restrict__ lo,
+                                                                  const uint32_t* __restrict__ hi, int W, int H,
+                                                                  float dx, Ctl* __restrict__ ctl, GatherOut o) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* s_slot = reinterpret_cast<uint32_t*>(smem);
+    uint32_t* s_code = s_slot + kGatherCap;
+    float* s_val = reinterpret_cast<float*>(s_code + kGatherCap);
+    float* s_w = s_val + 4 * kGatherCap;
+    uint32_t* s_off = reinterpret_cast<uint32_t*>(s_w + 4 * kGatherCap);  // kRegionBins + 1
+    uint32_t* s_glo = s_off + kRegionBins + 1;                            // kRegionBins
+    __shared__ uint32_t s_total;
+    __shared__ uint32_t s_rowg[kRegionH];
+
+    const int x0 = blockIdx.x * kGatherTW, y0 = blockIdx.y * kGatherTH;
+    const int rx0 = x0 - 2, ry0 = y0 - 2;
+    const int tx = threadIdx.x % kGatherTW, ty = threadIdx.x / kGatherTW;
+    const int i = x0 + tx, j = y0 + ty;
+    const bool cell = i < W && j < H;
+    pdl_wait();
+    const float prev_dt = ctl->prev_dt;
+
+    // the region's runs: counts, their exclusive scan, first global position per row
+    if (threadIdx.x < kRegionH) s_rowg[threadIdx.x] = 0xFFFFFFFFu;
+    uint32_t cnt[2] = {0u, 0u};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int rb = 2 * threadIdx.x + h;
+        if (rb < kRegionBins) {
+            const int x = rx0 + rb % kRegionW, y = ry0 + rb / kRegionW;
+            uint32_t gl = 0, gh = 0;
+            if (x >= 0 && x < W && y >= 0 && y < H) {
+                const uint32_t c = uint32_t(y) * uint32_t(W) + uint32_t(x);
+                gl = lo[c];
+                gh = hi[c];
+            }
+            cnt[h] = gh - gl;
+            s_glo[rb] = gl;
+        }
+    }
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan_u32(cnt[0] + cnt[1], &tot);
+    if (2 * threadIdx.x < kRegionBins) s_off[2 * threadIdx.x] = ex;
+    if (2 * threadIdx.x + 1 < kRegionBins) s_off[2 * threadIdx.x + 1] = ex + cnt[0];
+    if (threadIdx.x == 0) { s_off[kRegionBins] = tot; s_total = tot; }
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int rb = 2 * threadIdx.x + h;
+        if (rb < kRegionBins && cnt[h] > 0) atomicMin(&s_rowg[rb / kRegionW], s_glo[rb]);
+    }
+    __syncthreads();
+    const uint32_t P = s_total;
+
+    if (P > uint32_t(kGatherCap)) {
+        // more particles than the stage holds: every face reads its runs from
+        // global memory and computes the records it needs on the fly
+        for (int g = 0; g < 3; ++g) {
+            GlobalRecs R{vals, pp, g, W, H, dx, prev_dt, &ctl->status};
+            auto bin = [&](int x, int y, int& b, int& e) {
+                const uint32_t c = uint32_t(y) * uint32_t(W) + uint32_t(x);
+                b = int(lo[c]);
+                e = int(hi[c]);
+            };
+            if (cell) fold_cell(R, bin, g, i, j, W, H, o);
         }
         return;
     }
-    const Box bu = s_box[0], bv = s_box[1], bc = s_box[2];
-    for (int e = threadIdx.x; e < bu.w * bu.h * kP2gCopies; e += kP2gThreads) { s_um[e] = 0.0f; s_uw[e] = 0.0f; }
-    for (int e = threadIdx.x; e < bv.w * bv.h * kP2gCopies; e += kP2gThreads) { s_vm[e] = 0.0f; s_vw[e] = 0.0f; }
-    for (int e = threadIdx.x; e < bc.w * bc.h * kP2gCopies; e += kP2gThreads) s_d[e] = 0.0f;
-    for (int e = threadIdx.x; e < bc.w * bc.h; e += kP2gThreads) s_fl[e] = 0;
-    __syncthreads();
-    if (live) {
-        const int c = lane % kP2gCopies;
-        s_fl[(fy - bc.y0) * bc.w + (fx - bc.x0)] = 1;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int lu = ((uy[k >> 1] - bu.y0) * bu.w + (ux[k & 1] - bu.x0)) * kP2gCopies + c;
-            if (ua[k] != 0.0f || wu[k] != 0.0f) { atomicAdd(s_um + lu, ua[k]); atomicAdd(s_uw + lu, wu[k]); }
-            const int lv = ((vy2[k >> 1] - bv.y0) * bv.w + (vx2[k & 1] - bv.x0)) * kP2gCopies + c;
-            if (va[k] != 0.0f || wv[k] != 0.0f) { atomicAdd(s_vm + lv, va[k]); atomicAdd(s_vw + lv, wv[k]); }
-            const int lc = ((cy[k >> 1] - bc.y0) * bc.w + (cx[k & 1] - bc.x0)) * kP2gCopies + c;
-            if (cw[k] != 0.0f) atomicAdd(s_d + lc, cw[k]);
-        }
+    // stage the slots: each region row is one contiguous range of the sorted pairs
+    for (int r = 0; r < kRegionH; ++r) {
+        const uint32_t s0 = s_off[r * kRegionW], s1 = s_off[(r + 1) * kRegionW];
+        const uint32_t g0 = s_rowg[r];
+        for (uint32_t q = threadIdx.x; q < s1 - s0; q += kGatherThreads) s_slot[s0 + q] = vals[g0 + q];
     }
     __syncthreads();
-    // one global add per touched face and cell (the copies summed in order)
-    auto sum_copies = [](const float* a, int e) {
-        float t = a[e * kP2gCopies];
-#pragma unroll
-        for (int c = 1; c < kP2gCopies; ++c) t += a[e * kP2gCopies + c];
-        return t;
+    const StagedRecs R{s_slot, s_code, s_val, s_w};
+    auto bin = [&](int x, int y, int& b, int& e) {
+        const int rb = (y - ry0) * kRegionW + (x - rx0);
+        b = int(s_off[rb]);
+        e = int(s_off[rb + 1]);
     };
-    for (int e = threadIdx.x; e < bu.w * bu.h; e += kP2gThreads) {
-        const float m = sum_copies(s_um, e), w = sum_copies(s_uw, e);
-        if (m != 0.0f || w != 0.0f) {
-            const uint32_t g = uint32_t(bu.y0 + e / bu.w) * uint32_t(W + 1) + uint32_t(bu.x0 + e % bu.w);
-            atomicAdd(acc_u + g, m);
-            atomicAdd(acc_uw + g, w);
+    for (int g = 0; g < 3; ++g) {
+        bool bad = false;
+        for (uint32_t p = threadIdx.x; p < P; p += kGatherThreads) {
+            P2gRec rec;
+            if (!p2g_record(pp, s_slot[p], g, W, H, dx, prev_dt, rec)) bad = true;
+            s_code[p] = rec.code;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (g != kGridD) s_val[k * kGatherCap + p] = rec.val[k];
+                s_w[k * kGatherCap + p] = rec.w[k];
+            }
         }
-    }
-    for (int e = threadIdx.x; e < bv.w * bv.h; e += kP2gThreads) {
-        const float m = sum_copies(s_vm, e), w = sum_copies(s_vw, e);
-        if (m != 0.0f || w != 0.0f) {
-            const uint32_t g = uint32_t(bv.y0 + e / bv.w) * uint32_t(W) + uint32_t(bv.x0 + e % bv.w);
-            atomicAdd(acc_v + g, m);
-            atomicAdd(acc_vw + g, w);
-        }
-    }
-    for (int e = threadIdx.x; e < bc.w * bc.h; e += kP2gThreads) {
-        const float d = sum_copies(s_d, e);
-        if (d != 0.0f) atomicAdd(dens + uint32_t(bc.y0 + e / bc.w) * uint32_t(W) + uint32_t(bc.x0 + e % bc.w), d);
-    }
-    // fluid bits: one OR per mask word that a window row overlaps (a row of
-    // bc.w raw cells spans at most bc.w / 32 + 2 words)
-    const int nw = bc.w / 32 + 2;
-    for (int e = threadIdx.x; e < bc.h * nw; e += kP2gThreads) {
-        const int r = e / nw, j = e % nw;
-        const uint32_t first = uint32_t(bc.y0 + r) * uint32_t(W) + uint32_t(bc.x0);
-        const uint32_t last = first + uint32_t(bc.w) - 1u;
-        const uint32_t word = (first >> 5) + uint32_t(j);
-        if (word > (last >> 5)) continue;
-        const uint32_t lo = max(first, word << 5), hi = min(last, (word << 5) + 31u);
-        uint32_t mask = 0;
-        for (uint32_t c = lo; c <= hi; ++c)
-            if (s_fl[r * bc.w + int(c - first)]) mask |= 1u << (c & 31u);
-        if (mask) atomicOr(fluid + word, mask);
+        if (bad) atomicOr(&ctl->status, kStatusP2gLayout);
+        __syncthreads();
+        if (cell) fold_cell(R, bin, g, i, j, W, H, o);
+        __syncthreads();
     }
 }
 
@@ -393,10 +609,36 @@ __global__ void k_swap_tables(PartPtrs* pp) {
 
 }  // namespace
 
+// Bit length of the largest P2G bin key (row-major cell index).
+static int bin_key_bits(const Scene& s) {
+    uint32_t mx = s.cells > 0 ? s.cells - 1 : 0;
+    int b = 0;
+    while (b < 32 && (mx >> b)) ++b;
+    return b;
+}
+
+// P2G stage; bin_lo / bin_hi and the base fluid mask must be zero (the
+// caller clears them), every accumulator entry is written.
 cudaError_t launch_p2g(Scene& s) {
-    if (s.n == 0) return cudaSuccess;
-    launch(s.use_pdl, k_p2g, div_up(s.n, kP2gThreads), kP2gThreads, 0, s.stream, s.pp, s.n, int(s.W), int(s.H), s.dx, s.ctl, s.acc_u, s.acc_uw,
-                                                    s.acc_v, s.acc_vw, s.density, s.lv[0].fluid);
+    cudaError_t e = cudaFuncSetAttribute(k_p2g_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGatherSmem));
+    if (e != cudaSuccess) return e;
+    const uint32_t* svals = s.bin_vals;
+    if (s.n > 0) {
+        launch(s.use_pdl, k_p2g_bin_keys, div_up(s.n, 256), 256, 0, s.stream, static_cast<const PartPtrs*>(s.pp), s.n,
+               int(s.W), int(s.H), s.dx, s.bin_keys, s.bin_vals, s.lv[0].fluid);
+        uint32_t *kres, *vres;
+        e = radix_sort_pairs(s.bin_keys, s.bin_vals, s.bin_keys_alt, s.bin_vals_alt, s.sort_hist, s.sort_scan_tmp, s.n,
+                             bin_key_bits(s), s.stream, s.use_pdl, &kres, &vres);
+        if (e != cudaSuccess) return e;
+        launch(s.use_pdl, k_p2g_bounds, div_up(s.n, 256), 256, 0, s.stream, static_cast<const uint32_t*>(kres), s.n,
+               s.bin_lo, s.bin_hi);
+        svals = vres;
+    }
+    GatherOut o{s.acc_u, s.acc_uw, s.acc_v, s.acc_vw, s.density};
+    dim3 grid(div_up(s.W, kGatherTW), div_up(s.H, kGatherTH));
+    launch(s.use_pdl && s.n > 0, k_p2g_gather, grid, kGatherThreads, kGatherSmem, s.stream,
+           static_cast<const PartPtrs*>(s.pp), svals, static_cast<const uint32_t*>(s.bin_lo),
+           static_cast<const uint32_t*>(s.bin_hi), int(s.W), int(s.H), s.dx, s.ctl, o);
     return cudaGetLastError();
 }
 
@@ -431,9 +673,9 @@ cudaError_t launch_pack_vec2x8(Scene& s, int which, float* out) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_permute(Scene& s) {
+cudaError_t launch_permute(Scene& s, const uint32_t* sorted_vals) {
     if (s.npad == 0) return cudaSuccess;
-    launch(s.use_pdl, k_permute, div_up(s.npad, 256), 256, 0, s.stream, s.pp, s.vals, s.n, s.npad);
+    launch(s.use_pdl, k_permute, div_up(s.npad, 256), 256, 0, s.stream, s.pp, sorted_vals, s.n, s.npad);
     launch(s.use_pdl, k_swap_tables, 1, 32, 0, s.stream, s.pp);
     return cudaGetLastError();
 }

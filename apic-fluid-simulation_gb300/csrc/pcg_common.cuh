@@ -1,5 +1,5 @@
 // pcg_common.cuh — per-cell PCG phases on the base level, shared by the graph
-// kernels (solver.cu) and the persistent solver (pcg_persistent.cu).
+// kernels (solver.cu) and the V-cycle (vcycle.cu).
 //
 // Restates Apic::solve_pcg (src/apic.rs:1865-1956) and apply_matrix_and_dot
 // (:1823-1863).  Each phase visits the base fluid cells through the segment

@@ -256,6 +256,7 @@ void free_particles(Scene& s) {
     const cudaStream_t st = s.stream;
     for (int f = 0; f < NPF; ++f) { dfree(s.part[f], st); dfree(s.part_alt[f], st); }
     dfree(s.keys, st); dfree(s.vals, st); dfree(s.keys_alt, st); dfree(s.vals_alt, st);
+    dfree(s.bin_keys, st); dfree(s.bin_vals, st); dfree(s.bin_keys_alt, st); dfree(s.bin_vals_alt, st);
     dfree(s.sort_hist, st); dfree(s.sort_scan_tmp, st);
     s.part_cap = 0;
 }
@@ -270,11 +271,12 @@ void free_scene(Scene& s) {
     for (float** p : fl) dfree(*p, st);
     dfree(s.valid_u, st); dfree(s.valid_v, st); dfree(s.valid_u_alt, st); dfree(s.valid_v_alt, st);
     dfree(s.u_open, st); dfree(s.v_open, st); dfree(s.obstacle, st);
+    dfree(s.bin_lo, st); dfree(s.bin_hi, st);
     dfree(s.p64, st); dfree(s.b64, st);
     for (int l = 0; l < s.nlevels; ++l) {
         Level& L = s.lv[l];
         dfree(L.fluid, st); dfree(L.seg, st); dfree(L.diag, st); dfree(L.inv_diag, st); dfree(L.px, st);
-        dfree(L.py, st); dfree(L.res, st); dfree(L.err, st); dfree(L.err2, st);
+        dfree(L.py, st); dfree(L.res, st); dfree(L.err, st);
     }
     free_render(s);
     dfree(s.vec_stage, st);
@@ -283,7 +285,7 @@ void free_scene(Scene& s) {
     dfree(s.ctl, st);
     ctl_mirror_put(s.ctl_host);
     s.ctl_host = nullptr;
-    dfree(s.partials, st); dfree(s.scan_tmp, st); dfree(s.gsync, st);
+    dfree(s.partials, st); dfree(s.scan_tmp, st); dfree(s.exact_parts, st); dfree(s.seg_pre, st);
     if (s.ev_a) cudaEventDestroy(s.ev_a);
     if (s.ev_b) cudaEventDestroy(s.ev_b);
     if (s.update_exec) cudaGraphExecDestroy(s.update_exec);
@@ -343,9 +345,10 @@ int alloc_particles(Scene& s, uint32_t npad, uint32_t n) {
     }
     CK(dalloc(&s.keys, npad, st)); CK(dalloc(&s.vals, npad, st));
     CK(dalloc(&s.keys_alt, npad, st)); CK(dalloc(&s.vals_alt, npad, st));
-    uint32_t nb = div_up(std::max<uint32_t>(n, 1), kSortTile);
-    CK(dalloc(&s.sort_hist, size_t(256) * nb, st));
-    CK(dalloc(&s.sort_scan_tmp, div_up(uint64_t(256) * nb, 1024) + 1, st));
+    CK(dalloc(&s.bin_keys, npad, st)); CK(dalloc(&s.bin_vals, npad, st));
+    CK(dalloc(&s.bin_keys_alt, npad, st)); CK(dalloc(&s.bin_vals_alt, npad, st));
+    CK(dalloc(&s.sort_hist, sort_hist_words(n), st));
+    CK(dalloc(&s.sort_scan_tmp, sort_scan_words(n), st));
     s.part_cap = npad;
     return APIC_OK;
 }
@@ -358,10 +361,9 @@ int load_particles(apic_handle* h, uint32_t n, const float* px, const float* py,
     if (rc != APIC_OK) return rc;
     // sort scratch may need to grow when n grows within the same capacity
     {
-        uint32_t nb = div_up(std::max<uint32_t>(n, 1), kSortTile);
         dfree(s.sort_hist, s.stream); dfree(s.sort_scan_tmp, s.stream);
-        CK(dalloc(&s.sort_hist, size_t(256) * nb, s.stream));
-        CK(dalloc(&s.sort_scan_tmp, div_up(uint64_t(256) * nb, 1024) + 1, s.stream));
+        CK(dalloc(&s.sort_hist, sort_hist_words(n), s.stream));
+        CK(dalloc(&s.sort_scan_tmp, sort_scan_words(n), s.stream));
     }
     // a new particle set: the next mixed solve starts from zero pressure
     if (s.p64) CK(cudaMemsetAsync(s.p64, 0, sizeof(double) * (uint64_t(s.cells) + 2ull * s.W), s.stream));
@@ -423,13 +425,12 @@ struct StageTimer {
     }
 };
 
+// P2G writes every accumulator entry; it needs empty cell runs and a clear
+// fluid mask.
 cudaError_t clear_p2g_targets(Scene& s) {
     cudaStream_t st = s.stream;
-    cudaMemsetAsync(s.acc_u, 0, sizeof(float) * s.uf, st);
-    cudaMemsetAsync(s.acc_uw, 0, sizeof(float) * s.uf, st);
-    cudaMemsetAsync(s.acc_v, 0, sizeof(float) * s.vf, st);
-    cudaMemsetAsync(s.acc_vw, 0, sizeof(float) * s.vf, st);
-    cudaMemsetAsync(s.density, 0, sizeof(float) * s.cells, st);
+    cudaMemsetAsync(s.bin_lo, 0, sizeof(uint32_t) * s.cells, st);
+    cudaMemsetAsync(s.bin_hi, 0, sizeof(uint32_t) * s.cells, st);
     cudaMemsetAsync(s.lv[0].fluid, 0, sizeof(uint32_t) * s.lv[0].words, st);
     return cudaGetLastError();
 }
@@ -652,6 +653,7 @@ int apic::create_scene(uint32_t width, uint32_t height, float cell_size, const a
     AL(s.valid_u, s.uf); AL(s.valid_u_alt, s.uf); AL(s.valid_v, s.vf); AL(s.valid_v_alt, s.vf);
     AL(s.u_open, s.u_open_words); AL(s.v_open, s.v_open_words);
     AL(s.density, s.cells); AL(s.sm_a, s.cells); AL(s.sm_b, s.cells); AL(s.pressure, s.cells);
+    AL(s.bin_lo, s.cells); AL(s.bin_hi, s.cells);
     AL(s.obstacle, even_words(s.cells));
     size_t padded0 = (size_t(s.cells) + 2 * size_t(width) + 7) / 8 * 8;
     AL(s.search, padded0); AL(s.ap, padded0); AL(s.corr, padded0);
@@ -665,18 +667,17 @@ int apic::create_scene(uint32_t width, uint32_t height, float cell_size, const a
         max_words = std::max(max_words, L.words);
         AL(L.fluid, L.words); AL(L.seg, L.words);
         AL(L.diag, L.padded); AL(L.inv_diag, L.padded); AL(L.px, L.padded); AL(L.py, L.padded);
-        AL(L.res, L.padded); AL(L.err, L.padded); AL(L.err2, L.padded);
+        AL(L.res, L.padded); AL(L.err, L.padded);
     }
     {
         Level& C = s.lv[s.nlevels - 1];
         AL(s.cg_s, C.padded); AL(s.cg_ap, C.padded); AL(s.cg_r, C.padded);
     }
     plan_vcycle(s);
-    AL(s.gsync, 1);
-    plan_persistent_solve(s);
-    plan_cluster_solve(s);
     AL(s.ctl, 1);
     AL(s.partials, kPartialDoubles);
+    AL(s.exact_parts, s.cells / 8192 + 1);
+    AL(s.seg_pre, s.lv[0].words + 1);
     s.scan_tmp_len = 3 * (div_up(max_words, 1024) + 1);
     AL(s.scan_tmp, s.scan_tmp_len);
 #undef AL
@@ -801,7 +802,8 @@ int update_finish(apic_handle* h) {
     if (!s.profiling)
         s.stats.kernel_launches = uint64_t(s.kn_top) + (c.sorted ? s.kn_sort : 0u) + uint64_t(c.substeps) * s.kn_loop +
                                   uint64_t(c.pcg_iters_total) * s.kn_pcg + uint64_t(c.refinements_total) * s.kn_refine;
-    if (c.status & kStatusTimeout) return fail(APIC_ERR_TIMEOUT, "a bounded device wait gave up (persistent solver barrier)");
+    if (c.status & kStatusP2gLayout)
+        return fail(APIC_ERR_CUDA, "P2G: a particle's stencil left the cells its faces gather from (internal error)");
     if (c.status & kStatusBadStep) return fail(APIC_ERR_NONFINITE, "substep size is not positive (non-finite velocities)");
     return APIC_OK;
 }
@@ -960,8 +962,8 @@ FieldDesc describe(apic_handle* h, int id, const PartPtrs* pp) {
         case APIC_F_PLUS_X: F(s.lv[0].px, padded); return d;
         case APIC_F_PLUS_Y: F(s.lv[0].py, padded); return d;
         case APIC_F_ERROR: F(s.lv[0].err, padded); return d;
-        case APIC_F_SORT_KEYS: d = {s.keys, s.n, 4, kU32, true}; return d;
-        case APIC_F_SORT_VALS: d = {s.vals, s.n, 4, kU32, true}; return d;
+        case APIC_F_SORT_KEYS: d = {sort_result_in_alt(s) ? s.keys_alt : s.keys, s.n, 4, kU32, true}; return d;
+        case APIC_F_SORT_VALS: d = {sort_result_in_alt(s) ? s.vals_alt : s.vals, s.n, 4, kU32, true}; return d;
         case APIC_F_FLUID_LIST: d = {nullptr, 0, 4, kU32, true}; return d;  // derived on read
         case APIC_F_EXT_FORCE_U: F(s.ext_u, s.uf); return d;
         case APIC_F_EXT_FORCE_V: F(s.ext_v, s.vf); return d;
@@ -1320,35 +1322,12 @@ int apic_set_option(apic_handle* h, int option, int value) {
     Scene& s = h->s;
     if (s.stream) cudaStreamSynchronize(s.stream);
     switch (option) {
-        case APIC_OPT_PERSISTENT_SOLVE:
-            if (value && s.persist_grid == 0) return fail(APIC_ERR_UNSUPPORTED, "cooperative launch unavailable");
-            s.use_persistent = value != 0;
-            invalidate_graphs(s);
-            return APIC_OK;
-        case APIC_OPT_FUSED_VCYCLE:
-            s.fused_vcycle = value != 0;
-            invalidate_graphs(s);
-            return APIC_OK;
-        case APIC_OPT_CLUSTER_VCYCLE:
-            if (value < 0) return fail(APIC_ERR_INVALID_ARG, "cluster level size must be >= 0");
-            if (value > 0 && s.cluster_size == 0)
-                return fail(APIC_ERR_UNSUPPORTED, "thread-block clusters unavailable for this grid or GPU");
-            s.cluster_max_cells = uint32_t(value);
-            plan_vcycle_cluster(s);
-            invalidate_graphs(s);
-            return APIC_OK;
         case APIC_OPT_PDL:
             s.use_pdl = value != 0;
             invalidate_graphs(s);
             return APIC_OK;
         case APIC_OPT_DSM_VCYCLE:
             s.use_dsm = value != 0;
-            invalidate_graphs(s);
-            return APIC_OK;
-        case APIC_OPT_CLUSTER_SOLVE:
-            if (value < 0) return fail(APIC_ERR_INVALID_ARG, "cluster solve size must be >= 0");
-            s.cluster_solve_cells = uint32_t(value);
-            plan_cluster_solve(s);
             invalidate_graphs(s);
             return APIC_OK;
         case APIC_OPT_WARM_START:
@@ -1376,16 +1355,10 @@ int apic_set_option(apic_handle* h, int option, int value) {
 int apic_get_option(apic_handle* h, int option, int* value) {
     if (valid_handle(h) || !value) return fail(APIC_ERR_INVALID_ARG, "null argument");
     switch (option) {
-        case APIC_OPT_PERSISTENT_SOLVE: *value = (h->s.use_persistent && h->s.persist_grid > 0) ? 1 : 0; return APIC_OK;
-        case APIC_OPT_FUSED_VCYCLE: *value = h->s.fused_vcycle ? 1 : 0; return APIC_OK;
-        case APIC_OPT_CLUSTER_VCYCLE:
-            *value = h->s.cluster_size > 0 ? int(h->s.cluster_max_cells) : 0;
-            return APIC_OK;
         case APIC_OPT_PDL: *value = h->s.use_pdl ? 1 : 0; return APIC_OK;
         case APIC_OPT_DSM_VCYCLE:
             *value = (h->s.use_dsm && h->s.dsm_first < h->s.dsm_tail) ? 1 : 0;
             return APIC_OK;
-        case APIC_OPT_CLUSTER_SOLVE: *value = h->s.cluster_solve_ctas; return APIC_OK;
         case APIC_OPT_WARM_START: *value = h->s.warm_start ? 1 : 0; return APIC_OK;
         case APIC_OPT_STREAM_PRIORITY: *value = h->s.priority; return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");

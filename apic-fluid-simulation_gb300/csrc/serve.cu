@@ -444,13 +444,12 @@ int apic_scene_bytes(uint32_t width, uint32_t height, uint64_t particles, uint64
     const uint64_t cells = uint64_t(width) * height;
     const uint64_t faces = uint64_t(width + 1) * height + uint64_t(width) * (height + 1);
     const uint64_t lanes = (particles + 7) / 8 * 8;
-    // particles: two sets of 9 fields, sort keys and slots (two each), Vec2x8
-    // staging, sort scratch; faces: accumulators, velocities, forces, masks;
-    // cells: the base pressure system (padded, FP32 and FP64 vectors),
-    // smoothing and multigrid levels (a third of the base); plus control
-    // blocks and allocation granularity.  Measured footprints of scenes from
-    // 64^2 to 2048^2 (3 k to 6.7 M particles) stay below this bound.
-    *out = lanes * 128 + faces * 48 + cells * 160 + (24ull << 20);
+    // particles: two sets of 9 fields, Morton sort and P2G binning keys and
+    // slots (two each), Vec2x8 staging, sort scratch; faces: accumulators,
+    // velocities, forces, masks; cells: the base pressure system (padded,
+    // FP32 and FP64 vectors), smoothing, P2G bin bounds and multigrid levels
+    // (a third of the base); plus control blocks and allocation granularity.
+    *out = lanes * 148 + faces * 48 + cells * 168 + (24ull << 20);
     return APIC_OK;
 }
 
@@ -482,7 +481,8 @@ int apic_server_set_mode(apic_server* sv, int mode, uint32_t prepare_threads) {
 
 int apic_server_scene_option(apic_server* sv, int option, int value, uint64_t min_cells, uint64_t max_cells) {
     if (!sv || min_cells > max_cells) return bad(APIC_ERR_INVALID_ARG, "apic_server_scene_option: bad argument");
-    if (option < APIC_OPT_PERSISTENT_SOLVE || option > APIC_OPT_STREAM_PRIORITY)
+    if (option != APIC_OPT_PDL && option != APIC_OPT_DSM_VCYCLE && option != APIC_OPT_WARM_START &&
+        option != APIC_OPT_STREAM_PRIORITY)
         return bad(APIC_ERR_INVALID_ARG, "apic_server_scene_option: unknown option");
     if (!sv->active.empty() || sv->pending > 0)
         return bad(APIC_ERR_INVALID_ARG, "apic_server_scene_option: scenes are running");

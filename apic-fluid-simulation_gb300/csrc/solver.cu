@@ -35,6 +35,7 @@ namespace apic {
 namespace {
 
 constexpr float kSafety = 1e-5f;  // SAFTY, src/apic.rs:8
+constexpr uint32_t kDeltaChunk = 8192;  // apply_matrix_and_dot's par_chunks(8192), src/apic.rs:1857-1859
 
 __device__ __forceinline__ uint32_t gwarp() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
 __device__ __forceinline__ uint32_t gnwarps() { return (gridDim.x * blockDim.x) >> 5; }
@@ -58,9 +59,11 @@ __global__ void __launch_bounds__(kSegBlock) k_clear_pressure(Level B, float* p,
 }
 
 // s = z and gamma = r.z (src/apic.rs:1887-1892).
+// In the reference mode k_gamma_exact forms gamma and the exit instead.
 __global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl* ctl, double* partials, int mode) {
     pdl_wait();
     F2 acc = pcg::ph_start(B, ctl->seg_count[0], gwarp(), gnwarps(), s);
+    if (mode == APIC_SOLVER_REFERENCE) return;
     double tot;
     if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
         float gamma = float(tot);
@@ -93,12 +96,21 @@ __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s,
 // kernel (k_smooth_conv).
 __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int p_padded, float* s,
                                                           const float* ap, Ctl* ctl, const float2* sap,
-                                                          uint32_t nsap, float4* part, int mode) {
+                                                          uint32_t nsap, float4* part, int mode,
+                                                          const float* exact_parts, const uint32_t* seg_pre) {
     const uint32_t nseg = ctl->seg_count[0];
     const uint32_t w0 = gwarp() < nseg ? B.seg[gwarp()] : 0xFFFFFFFFu;
     pdl_wait();
     if (ctl->pcg_done) return;
-    const float delta = float(sum_partials<kSegBlock>(sap, nsap));
+    float delta;
+    if (mode == APIC_SOLVER_REFERENCE) {
+        // the chunk sums of k_delta_exact, added in chunk order from zero
+        const uint32_t nchunks = (seg_pre[ctl->seg_count[0]] + kDeltaChunk - 1) / kDeltaChunk;
+        delta = 0.0f;
+        for (uint32_t c = 0; c < nchunks; ++c) delta = delta + exact_parts[c];
+    } else {
+        delta = float(sum_partials<kSegBlock>(sap, nsap));
+    }
     const bool stop = mode == APIC_SOLVER_REFERENCE ? fabsf(delta) < kSafety : (!(delta != 0.0f) || !isfinite(delta));
     const float alpha = ctl->gamma / delta;
     // every block reads pcg_done on entry, so the stop is recorded aside and
@@ -132,6 +144,166 @@ __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, float2*
     if (ctl->pcg_done) return;
     F2 acc = pcg::ph_rz(B, ctl->seg_count[0], gwarp(), gnwarps());
     block_store<kSegBlock>(acc, part);
+}
+
+// ---- the reference's FP32 reduction orders (APIC_SOLVER_REFERENCE) --------
+//
+// Float addition is not associative, so the reference mode forms its two
+// Krylov reductions in exactly the reference's order; the solve is then
+// bit-identical to the oracle's.
+
+// gamma = dot_product(residual[W..W+cells], error[W..W+cells]) (:11-29): eight
+// lane sums, lane = raw index mod 8, each added in ascending order; then
+// wide's reduce_add pairing ((l0 + l2) + (l1 + l3)) + ((l4 + l6) + (l5 + l7));
+// then the cells beyond the last full chunk of 8, serially.  The error is
+// zero outside the fluid cells (apply_preconditioner zeroes it, :1790-1792,
+// and only fluid cells are smoothed or prolonged), and adding a zero product
+// leaves a lane sum unchanged (the sums start at +0 and never become -0), so
+// only the fluid cells' products count.  One block: all threads stage the
+// products of a batch of segments (32 raw cells each, zero where not fluid)
+// in shared memory, then threads 0..7 add their lane's products in order;
+// only those eight add chains are serial.
+// start: the solve's first gamma (sets gamma and the SAFTY exit,
+// :1887-1892), else the iteration's new gamma for k_pcg_cond.
+constexpr int kGammaThreads = 1024;
+constexpr uint32_t kGammaBatch = 512;  // segments staged per round (64 KB)
+constexpr size_t kGammaSmem = size_t(kGammaBatch) * 32 * sizeof(float);
+__global__ void __launch_bounds__(kGammaThreads) k_gamma_exact(Level B, Ctl* ctl, int start) {
+    extern __shared__ float stage[];
+    pdl_wait();
+    if (ctl->pcg_done) return;
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t nseg = ctl->seg_count[0];
+    const uint32_t full = (B.cells / 8u) * 8u;
+    float acc = 0.0f;
+    for (uint32_t k0 = 0; k0 < nseg; k0 += kGammaBatch) {
+        const uint32_t nb = min(kGammaBatch, nseg - k0);
+        for (uint32_t q = warp; q < nb; q += kGammaThreads / 32) {
+            const uint32_t w = B.seg[k0 + q];
+            const uint32_t raw = w * 32u + lane;
+            const bool on = ((B.fluid[w] >> lane) & 1u) && raw < full;
+            stage[q * 32u + lane] = on ? B.res[raw + B.w] * B.err[raw + B.w] : 0.0f;
+        }
+        __syncthreads();
+        if (t < 8)
+            for (uint32_t q = 0; q < nb; ++q) {
+                const float* p = stage + q * 32u + t;
+                acc = acc + p[0];
+                acc = acc + p[8];
+                acc = acc + p[16];
+                acc = acc + p[24];
+            }
+        __syncthreads();
+    }
+    __shared__ float lanes[8];
+    if (t < 8) lanes[t] = acc;
+    __syncthreads();
+    if (t != 0) return;
+    float g = ((lanes[0] + lanes[2]) + (lanes[1] + lanes[3])) + ((lanes[4] + lanes[6]) + (lanes[5] + lanes[7]));
+    for (uint32_t raw = full; raw < B.cells; ++raw)
+        if (bit_at(B.fluid, raw)) g = g + B.res[raw + B.w] * B.err[raw + B.w];
+    if (start) {
+        ctl->gamma = g;
+        ctl->dgamma = double(g);
+        if (g < kSafety) ctl->pcg_done = 1;
+    } else {
+        ctl->rz_exact = g;
+    }
+}
+
+// Fluid cells before each base segment (seg_pre[k], k <= nseg; seg_pre[nseg]
+// = all fluid cells): the position of a segment's cells in the reference's
+// ascending fluid list.  One block, once per solve.
+__global__ void __launch_bounds__(1024) k_seg_prefix(Level B, const Ctl* ctl, uint32_t* seg_pre) {
+    const uint32_t nseg = ctl->seg_count[0];
+    __shared__ uint32_t sw[32];
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint32_t carry = 0;
+    for (uint32_t k0 = 0; k0 < nseg; k0 += 1024) {
+        const uint32_t k = k0 + t;
+        const uint32_t v = k < nseg ? uint32_t(__popc(B.fluid[B.seg[k]])) : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= uint32_t(o)) x += y;
+        }
+        if (lane == 31) sw[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t u = sw[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, u, o);
+                if (lane >= uint32_t(o)) u += y;
+            }
+            sw[lane] = u;
+        }
+        __syncthreads();
+        if (k < nseg) seg_pre[k] = carry + (warp > 0 ? sw[warp - 1] : 0u) + x - v;
+        const uint32_t tot = sw[31];
+        __syncthreads();
+        carry += tot;
+    }
+    if (t == 0) seg_pre[nseg] = carry;
+}
+
+// delta = apply_matrix_and_dot's sum (:1823-1863): s'.Ap over the fluid cells
+// in ascending order, in chunks of 8192 cells each summed serially from zero
+// (rayon's par_chunks(8192)); k_pcg_update then adds the chunk sums in chunk
+// order.  s' is the iteration's search direction, z + beta s (k_spmv_dot
+// evaluates the same expression).  One block per chunk: its warps stage the
+// chunk's products in fluid order in shared memory (positions from
+// seg_pre), then one thread adds them in order.
+constexpr int kDeltaThreads = 256;
+__global__ void __launch_bounds__(kDeltaThreads) k_delta_exact(Level B, const float* __restrict__ s,
+                                                               const float* __restrict__ ap,
+                                                               const uint32_t* __restrict__ seg_pre, Ctl* ctl,
+                                                               float* __restrict__ parts) {
+    __shared__ float prod[kDeltaChunk];
+    __shared__ uint32_t s_k0, s_k1;
+    pdl_wait();
+    if (ctl->pcg_done) return;
+    const uint32_t nseg = ctl->seg_count[0];
+    const uint32_t nfluid = seg_pre[nseg];
+    const uint32_t c = blockIdx.x;
+    const uint32_t f0 = c * kDeltaChunk;
+    if (f0 >= nfluid) return;
+    const uint32_t f1 = min(f0 + kDeltaChunk, nfluid);
+    if (threadIdx.x == 0) {
+        // segments [k0, k1) hold fluid cells f0 .. f1-1 (every segment holds at least one)
+        uint32_t lo = 0, hi = nseg;  // last k with seg_pre[k] <= f0
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) / 2;
+            if (seg_pre[mid] <= f0) lo = mid; else hi = mid;
+        }
+        s_k0 = lo;
+        uint32_t lo2 = lo, hi2 = nseg;  // first k with seg_pre[k] >= f1
+        while (lo2 < hi2) {
+            const uint32_t mid = (lo2 + hi2) / 2;
+            if (seg_pre[mid] < f1) lo2 = mid + 1; else hi2 = mid;
+        }
+        s_k1 = lo2;
+    }
+    __syncthreads();
+    const float beta = ctl->beta;
+    const bool beta_valid = ctl->beta_valid != 0;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t k = s_k0 + warp; k < s_k1; k += kDeltaThreads / 32) {
+        const uint32_t w = B.seg[k];
+        const uint32_t m = B.fluid[w];
+        if (!((m >> lane) & 1u)) continue;
+        const uint32_t pos = seg_pre[k] + uint32_t(__popc(m & ((1u << lane) - 1u)));
+        if (pos < f0 || pos >= f1) continue;
+        const uint32_t cidx = w * 32u + lane + B.w;
+        prod[pos - f0] = ap[cidx] * pcg::search_at(B.err, s, beta, beta_valid, cidx);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float sum = 0.0f;
+        for (uint32_t i = 0; i < f1 - f0; ++i) sum = sum + prod[i];
+        parts[c] = sum;
+    }
 }
 
 // ---- FP64 refinement helpers (APIC_SOLVER_REL_MIXED) ----------------------
@@ -176,7 +348,8 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_cond(Ctl* __restrict__ ctl, c
                                                         int mode, int flags) {
     pdl_wait();
     if ((flags & 1) && !ctl->pcg_done) {
-        const double tot = sum_partials<kSegBlock>(rz, nrz);
+        // the reference mode's r.z comes from k_gamma_exact
+        const double tot = mode == APIC_SOLVER_REFERENCE ? double(ctl->rz_exact) : sum_partials<kSegBlock>(rz, nrz);
         if (threadIdx.x == 0) pcg::finish_rz(ctl, tot, mode);
         __syncthreads();
     }
@@ -241,16 +414,22 @@ static void pcg_iteration(Scene& s, int mode, float* x, int p_padded) {
     cudaStream_t st = s.stream;
     const bool pdl = s.use_pdl;
     k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, part_sap(s), mode);
+    if (mode == APIC_SOLVER_REFERENCE)
+        launch(pdl, k_delta_exact, div_up(B.cells, kDeltaChunk), kDeltaThreads, 0, st, B,
+               static_cast<const float*>(s.search), static_cast<const float*>(s.ap),
+               static_cast<const uint32_t*>(s.seg_pre), s.ctl, s.exact_parts);
     launch(pdl, k_pcg_update, g, kSegBlock, 0, st, B, x, p_padded, s.search, s.ap, s.ctl,
-           static_cast<const float2*>(part_sap(s)), g, part_res(s), mode);
+           static_cast<const float2*>(part_sap(s)), g, part_res(s), mode, static_cast<const float*>(s.exact_parts),
+           static_cast<const uint32_t*>(s.seg_pre));
     // the residual's exit test runs inside the V-cycle's first kernel when
     // that is the base level's black sweep, else on its own
-    const bool exit_in_vcycle = !s.fused_vcycle && s.nlevels >= 2;
+    const bool exit_in_vcycle = s.nlevels >= 2;
     if (!exit_in_vcycle)
         launch(pdl, k_residual_exit, 1, kSegBlock, 0, st, s.ctl, static_cast<const float4*>(part_res(s)), g, mode,
                s.props.solve_error);
     // the V-cycle's last kernel also stores the parts of r.z (k_dot_rz's work)
     if (!enqueue_vcycle(s, true, mode, exit_in_vcycle)) launch(pdl, k_dot_rz, g, kSegBlock, 0, st, B, s.ctl, part_rz(s));
+    if (mode == APIC_SOLVER_REFERENCE) launch(pdl, k_gamma_exact, 1, kGammaThreads, kGammaSmem, st, B, s.ctl, 0);
 }
 
 // Finish an iteration (r.z) and, in a graph, set the loop condition.
@@ -273,8 +452,11 @@ static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p
         // only the reference-mode solve clears the pressure, and it starts here
         k_pcg_begin<<<1, 1, 0, st>>>(s.ctl, clear_pressure ? 1 : 0);
         if (clear_pressure) k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
+        if (mode == APIC_SOLVER_REFERENCE) k_seg_prefix<<<1, 1024, 0, st>>>(B, s.ctl, s.seg_pre);
         enqueue_vcycle(s);
         launch(s.use_pdl, k_pcg_start, g, kSegBlock, 0, st, B, s.search, s.ctl, s.partials, mode);
+        if (mode == APIC_SOLVER_REFERENCE)
+            launch(s.use_pdl, k_gamma_exact, 1, kGammaThreads, kGammaSmem, st, B, s.ctl, 1);
         pcg_finish(s, h, cap, dyn_cap, mode, 2);
         return cudaGetLastError();
     });
@@ -293,10 +475,7 @@ static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p
 
 cudaError_t build_solve(Scene& s, GraphCursor& c) {
     s.kn_pcg = s.kn_refine = 0;
-    if (s.use_persistent && s.persist_grid > 0)
-        return capture_into(s, c, [&]() { return enqueue_persistent_solve(s); });
-    if (s.cluster_solve_ctas > 0)  // a small scene: the whole solve is one cluster launch
-        return capture_into(s, c, [&]() { return enqueue_cluster_solve(s); });
+    cudaFuncSetAttribute(k_gamma_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGammaSmem));
     const Level& B = s.lv[0];
     uint32_t g = seg_grid(B.words);
     int mode = s.solver_mode;
@@ -382,8 +561,10 @@ static cudaError_t eager_pcg(Scene& s, int mode, float* x, int p_padded, uint32_
     cudaStream_t st = s.stream;
     k_pcg_begin<<<1, 1, 0, st>>>(s.ctl, clear_pressure ? 1 : 0);
     if (clear_pressure) k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
+    if (mode == APIC_SOLVER_REFERENCE) k_seg_prefix<<<1, 1024, 0, st>>>(B, s.ctl, s.seg_pre);
     enqueue_vcycle(s);
     k_pcg_start<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl, s.partials, mode);
+    if (mode == APIC_SOLVER_REFERENCE) k_gamma_exact<<<1, kGammaThreads, kGammaSmem, st>>>(B, s.ctl, 1);
     for (;;) {
         cudaError_t e = read_ctl(s);
         if (e != cudaSuccess) return e;
@@ -395,7 +576,7 @@ static cudaError_t eager_pcg(Scene& s, int mode, float* x, int p_padded, uint32_
 }
 
 cudaError_t run_solve_eager(Scene& s) {
-    if (s.use_persistent && s.persist_grid > 0) return enqueue_persistent_solve(s);
+    cudaFuncSetAttribute(k_gamma_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGammaSmem));
     const Level& B = s.lv[0];
     uint32_t g = seg_grid(B.words);
     cudaStream_t st = s.stream;

@@ -8,12 +8,15 @@
 // to rdst; this sort is stable (equal keys keep ascending `val`), which is the
 // order the oracle defines.
 //
-// Per pass over one 8-bit digit: a histogram kernel (warp match + shared
-// counters), a device-wide exclusive scan of the digit-major histogram, and a
-// scatter kernel that ranks keys stably inside its tile with __match_any_sync
-// (per-warp running counters, then a per-digit prefix over warps).  Only the
-// digits below the bit length of the largest possible key are sorted: higher
-// digits are zero for every key, so their passes are identities.
+// Per pass over one digit of up to 10 bits: a histogram kernel (warp match +
+// shared counters), a device-wide exclusive scan of the digit-major
+// histogram, and a scatter kernel that ranks keys stably inside its tile with
+// __match_any_sync and writes them through a shared-memory stage.  Only the
+// bits below the bit length of the largest possible key are sorted: higher
+// bits are zero for every key, so their passes would be identities.  The
+// digit width is chosen per sort for the fewest passes (20-bit keys of a
+// 1024^2 grid: two 10-bit passes), and the sorted pairs stay in the buffer
+// the last pass wrote.
 #include <cuda_runtime.h>
 
 #include "apic_device.cuh"
@@ -24,6 +27,7 @@ namespace apic {
 namespace {
 
 constexpr int kItems = kSortTile / kSortThreads;  // 8 keys per thread
+constexpr uint32_t kMaxBuckets = 1u << kMaxDigitBits;
 constexpr int kScanBlock = 1024;                  // elements per scan block
 
 __global__ void k_morton_keys(const PartPtrs* __restrict__ pp, uint32_t n, float dx, float max_x, float max_y,
@@ -38,39 +42,54 @@ __global__ void k_morton_keys(const PartPtrs* __restrict__ pp, uint32_t n, float
     vals[i] = i;
 }
 
-// Per-tile digit histogram, written digit-major: hist[d * nblocks + b].
+// Per-tile digit histogram of a `dbits`-bit digit (dbits <= kMaxDigitBits),
+// written digit-major: hist[d * nblocks + b].
 __global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n,
-                                                             int shift, uint32_t* __restrict__ hist) {
+                                                             int shift, int dbits, uint32_t* __restrict__ hist) {
     pdl_wait();
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
+    __shared__ uint32_t h[kMaxBuckets];
+    const uint32_t nbk = 1u << dbits, mask = nbk - 1u;
+    for (uint32_t d = threadIdx.x; d < nbk; d += kSortThreads) h[d] = 0;
     __syncthreads();
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t base = blockIdx.x * kSortTile + warp * (kSortTile / kSortThreads * 32);
     for (int r = 0; r < kItems; ++r) {
         uint32_t i = base + r * 32 + lane;
-        uint32_t d = i < n ? (keys[i] >> shift) & 0xFFu : 256u;
+        uint32_t d = i < n ? (keys[i] >> shift) & mask : kMaxBuckets;
         uint32_t peers = __match_any_sync(0xffffffffu, d);
-        if (d < 256u && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&h[d], uint32_t(__popc(peers)));
+        if (d < kMaxBuckets && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&h[d], uint32_t(__popc(peers)));
     }
     __syncthreads();
-    hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+    for (uint32_t d = threadIdx.x; d < nbk; d += kSortThreads) hist[d * gridDim.x + blockIdx.x] = h[d];
 }
 
-// Stable scatter of one tile; offs = exclusive scan of hist.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total);
+
+// Stable scatter of one tile; offs = exclusive scan of hist.  Keys are ranked
+// inside the tile with __match_any_sync (per-warp running counters, then a
+// prefix over warps and over digits), staged in shared memory in the tile's
+// sorted order, and written out so that consecutive threads write the
+// consecutive positions of one digit's run.
 __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* __restrict__ keys,
                                                                 const uint32_t* __restrict__ vals, uint32_t n,
-                                                                int shift, const uint32_t* __restrict__ offs,
+                                                                int shift, int dbits,
+                                                                const uint32_t* __restrict__ offs,
                                                                 uint32_t* __restrict__ okeys,
                                                                 uint32_t* __restrict__ ovals) {
     pdl_wait();
-    __shared__ uint32_t wh[kSortThreads / 32][256];
-    __shared__ uint32_t boff[256];
+    __shared__ uint16_t wh[kSortThreads / 32][kMaxBuckets];  // per-warp counts, then offsets
+    __shared__ uint32_t boff[kMaxBuckets];                   // global start of this tile's digit d
+    __shared__ uint32_t lstart[kMaxBuckets];                 // tile-local start of digit d
+    __shared__ uint32_t sk[kSortTile], sv[kSortTile];
+    const uint32_t nbk = 1u << dbits, mask = nbk - 1u;
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int w = 0; w < kSortThreads / 32; ++w) wh[w][threadIdx.x] = 0;
-    boff[threadIdx.x] = offs[threadIdx.x * gridDim.x + blockIdx.x];
+    for (uint32_t d = threadIdx.x; d < nbk; d += kSortThreads) {
+        for (int w = 0; w < kSortThreads / 32; ++w) wh[w][d] = 0;
+        boff[d] = offs[d * gridDim.x + blockIdx.x];
+    }
     __syncthreads();
-    uint32_t base = blockIdx.x * kSortTile + warp * (kItems * 32);
+    const uint32_t tile0 = blockIdx.x * kSortTile;
+    uint32_t base = tile0 + warp * (kItems * 32);
     uint32_t k[kItems], v[kItems], rk[kItems];
     uint32_t lt = (1u << lane) - 1u;
     for (int r = 0; r < kItems; ++r) {
@@ -78,31 +97,54 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* _
         bool ok = i < n;
         k[r] = ok ? keys[i] : 0u;
         v[r] = ok ? vals[i] : 0u;
-        uint32_t d = ok ? (k[r] >> shift) & 0xFFu : 256u;
+        uint32_t d = ok ? (k[r] >> shift) & mask : kMaxBuckets;
         uint32_t peers = __match_any_sync(0xffffffffu, d);
         uint32_t before = ok ? wh[warp][d] : 0u;
         __syncwarp();
-        if (ok && (peers & lt) == 0) wh[warp][d] = before + uint32_t(__popc(peers));
+        if (ok && (peers & lt) == 0) wh[warp][d] = uint16_t(before + uint32_t(__popc(peers)));
         __syncwarp();
         rk[r] = before + uint32_t(__popc(peers & lt));
     }
     __syncthreads();
-    {
+    // per digit: warp offsets inside the digit, and the digit's tile count;
+    // then the tile-local start of each digit (digits split evenly over threads)
+    const uint32_t per = (nbk + kSortThreads - 1) / kSortThreads;
+    const uint32_t d0 = min(threadIdx.x * per, nbk), d1 = min(d0 + per, nbk);
+    uint32_t mine = 0;
+    for (uint32_t d = d0; d < d1; ++d) {
         uint32_t run = 0;
         for (int w = 0; w < kSortThreads / 32; ++w) {
-            uint32_t c = wh[w][threadIdx.x];
-            wh[w][threadIdx.x] = run;
+            uint32_t c = wh[w][d];
+            wh[w][d] = uint16_t(run);
             run += c;
         }
+        lstart[d] = run;
+        mine += run;
+    }
+    uint32_t tot;
+    uint32_t ex = block_exclusive_scan(mine, &tot);
+    for (uint32_t d = d0; d < d1; ++d) {
+        uint32_t c = lstart[d];
+        lstart[d] = ex;
+        ex += c;
     }
     __syncthreads();
     for (int r = 0; r < kItems; ++r) {
         uint32_t i = base + r * 32 + lane;
         if (i >= n) continue;
-        uint32_t d = (k[r] >> shift) & 0xFFu;
-        uint32_t pos = boff[d] + wh[warp][d] + rk[r];
-        okeys[pos] = k[r];
-        ovals[pos] = v[r];
+        uint32_t d = (k[r] >> shift) & mask;
+        uint32_t lp = lstart[d] + wh[warp][d] + rk[r];
+        sk[lp] = k[r];
+        sv[lp] = v[r];
+    }
+    __syncthreads();
+    const uint32_t cnt = n - tile0 < uint32_t(kSortTile) ? n - tile0 : uint32_t(kSortTile);
+    for (uint32_t q = threadIdx.x; q < cnt; q += kSortThreads) {
+        uint32_t key = sk[q];
+        uint32_t d = (key >> shift) & mask;
+        uint32_t pos = boff[d] + (q - lstart[d]);
+        okeys[pos] = key;
+        ovals[pos] = sv[q];
     }
 }
 
@@ -194,7 +236,8 @@ cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t n, uint32_t* tmp, cudaSt
 
 static int key_bits(const Scene& s) {
     uint32_t mx = s.W ? s.W - 1 : 0, my = s.H ? s.H - 1 : 0;
-    // Morton order is monotone in x and y, so the largest key is that of the far corner.
+    // Morton order is monotone in x and y, so the largest key is that of the
+    // far corner (sides are limited to 65536, so 16 bits per axis suffice).
     uint32_t ex = mx & 0xFFFFu, ey = my & 0xFFFFu;
     auto expand = [](uint32_t v) {
         v = (v | (v << 8)) & 0x00FF00FFu;
@@ -209,54 +252,85 @@ static int key_bits(const Scene& s) {
     return b;
 }
 
-cudaError_t launch_sort(Scene& s) {
-    if (s.n == 0) return cudaSuccess;
-    float max_x = float(s.W > 0 ? s.W - 1 : 0), max_y = float(s.H > 0 ? s.H - 1 : 0);
-    launch(s.use_pdl, k_morton_keys, div_up(s.n, 256), 256, 0, s.stream, s.pp, s.n, s.dx, max_x, max_y, s.keys, s.vals);
-    uint32_t nb = div_up(s.n, kSortTile);
-    int bits = key_bits(s);
-    uint32_t* k_in = s.keys;
-    uint32_t* v_in = s.vals;
-    uint32_t* k_out = s.keys_alt;
-    uint32_t* v_out = s.vals_alt;
-    for (int shift = 0; shift < bits; shift += 8) {
-        launch(s.use_pdl, k_sort_hist, nb, kSortThreads, 0, s.stream, k_in, s.n, shift, s.sort_hist);
-        cudaError_t e = exclusive_scan_u32(s.sort_hist, 256u * nb, s.sort_scan_tmp, s.stream);
-        if (e != cudaSuccess) return e;
-        launch(s.use_pdl, k_sort_scatter, nb, kSortThreads, 0, s.stream, k_in, v_in, s.n, shift, s.sort_hist, k_out, v_out);
-        std::swap(k_in, k_out);
-        std::swap(v_in, v_out);
-    }
-    if (k_in != s.keys) {  // keep the sorted pairs in keys/vals
-        cudaMemcpyAsync(s.keys, k_in, sizeof(uint32_t) * s.n, cudaMemcpyDeviceToDevice, s.stream);
-        cudaMemcpyAsync(s.vals, v_in, sizeof(uint32_t) * s.n, cudaMemcpyDeviceToDevice, s.stream);
-    }
-    return launch_permute(s);
+// Digit width of an LSD sort over `bits` key bits: the fewest passes of at
+// most kMaxDigitBits bits, split as evenly as possible.
+static int digit_bits(int bits) {
+    if (bits <= 0) return 0;
+    int passes = (bits + kMaxDigitBits - 1) / kMaxDigitBits;
+    return (bits + passes - 1) / passes;
 }
 
-// Stable LSD sort of (keys, vals)[0..n) over the low `bits` key bits, with all
-// intermediate storage supplied by the caller: keys_alt/vals_alt (n words
-// each), hist (256 * ceil(n / 2048) words) and scan_tmp (ceil(hist / 1024)
-// words).  The sorted pairs end in keys/vals.
-cudaError_t radix_sort_pairs_in(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* hist,
-                                uint32_t* scan_tmp, uint32_t n, int bits, cudaStream_t st) {
-    if (n == 0) return cudaSuccess;
+static cudaError_t lsd_passes(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt,
+                              uint32_t* hist, uint32_t* scan_tmp, uint32_t n, int bits, int dbits, cudaStream_t st,
+                              bool pdl, uint32_t** keys_out, uint32_t** vals_out) {
     uint32_t nb = div_up(n, kSortTile);
     uint32_t* k_in = keys;
     uint32_t* v_in = vals;
     uint32_t* k_out = keys_alt;
     uint32_t* v_out = vals_alt;
-    for (int shift = 0; shift < bits; shift += 8) {
-        launch(st != nullptr, k_sort_hist, nb, kSortThreads, 0, st, k_in, n, shift, hist);
-        cudaError_t e = exclusive_scan_u32(hist, 256u * nb, scan_tmp, st);
+    for (int shift = 0; dbits > 0 && shift < bits; shift += dbits) {
+        launch(pdl, k_sort_hist, nb, kSortThreads, 0, st, static_cast<const uint32_t*>(k_in), n, shift, dbits, hist);
+        cudaError_t e = exclusive_scan_u32(hist, (1u << dbits) * nb, scan_tmp, st);
         if (e != cudaSuccess) return e;
-        launch(st != nullptr, k_sort_scatter, nb, kSortThreads, 0, st, k_in, v_in, n, shift, hist, k_out, v_out);
+        launch(pdl, k_sort_scatter, nb, kSortThreads, 0, st, static_cast<const uint32_t*>(k_in),
+               static_cast<const uint32_t*>(v_in), n, shift, dbits, static_cast<const uint32_t*>(hist), k_out, v_out);
         std::swap(k_in, k_out);
         std::swap(v_in, v_out);
     }
-    if (k_in != keys) {
-        cudaMemcpyAsync(keys, k_in, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
-        cudaMemcpyAsync(vals, v_in, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+    *keys_out = k_in;
+    *vals_out = v_in;
+    return cudaGetLastError();
+}
+
+uint32_t sort_hist_words(uint32_t n) { return kMaxBuckets * div_up(n > 0 ? n : 1, kSortTile); }
+uint32_t sort_scan_words(uint32_t n) { return div_up(sort_hist_words(n), 1024) + 1; }
+
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* hist,
+                             uint32_t* scan_tmp, uint32_t n, int bits, cudaStream_t st, bool pdl,
+                             uint32_t** keys_out, uint32_t** vals_out) {
+    *keys_out = keys;
+    *vals_out = vals;
+    if (n == 0) return cudaSuccess;
+    return lsd_passes(keys, vals, keys_alt, vals_alt, hist, scan_tmp, n, bits, digit_bits(bits), st, pdl, keys_out,
+                      vals_out);
+}
+
+bool radix_sort_in_alt(int bits) {
+    int d = digit_bits(bits);
+    int passes = d > 0 ? (bits + d - 1) / d : 0;
+    return passes % 2 == 1;
+}
+
+cudaError_t launch_sort(Scene& s) {
+    if (s.n == 0) return cudaSuccess;
+    float max_x = float(s.W > 0 ? s.W - 1 : 0), max_y = float(s.H > 0 ? s.H - 1 : 0);
+    launch(s.use_pdl, k_morton_keys, div_up(s.n, 256), 256, 0, s.stream, s.pp, s.n, s.dx, max_x, max_y, s.keys, s.vals);
+    // the sorted pairs stay where the last pass wrote them (no copy back)
+    uint32_t *k_res, *v_res;
+    cudaError_t e = radix_sort_pairs(s.keys, s.vals, s.keys_alt, s.vals_alt, s.sort_hist, s.sort_scan_tmp, s.n,
+                                     key_bits(s), s.stream, s.use_pdl, &k_res, &v_res);
+    if (e != cudaSuccess) return e;
+    return launch_permute(s, v_res);
+}
+
+// Where launch_sort leaves the sorted pairs of a scene (the number of digit
+// passes is fixed by the grid size).
+bool sort_result_in_alt(const Scene& s) { return radix_sort_in_alt(key_bits(s)); }
+
+// Stable LSD sort of (keys, vals)[0..n) over the low `bits` key bits in 8-bit
+// digits, with all intermediate storage supplied by the caller:
+// keys_alt/vals_alt (n words each), hist (256 * ceil(n / 2048) words) and
+// scan_tmp (ceil(hist / 1024) words).  The sorted pairs end in keys/vals.
+cudaError_t radix_sort_pairs_in(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* hist,
+                                uint32_t* scan_tmp, uint32_t n, int bits, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    uint32_t *k_res, *v_res;
+    cudaError_t e = lsd_passes(keys, vals, keys_alt, vals_alt, hist, scan_tmp, n, bits, bits > 0 ? 8 : 0, st,
+                               st != nullptr, &k_res, &v_res);
+    if (e != cudaSuccess) return e;
+    if (k_res != keys) {
+        cudaMemcpyAsync(keys, k_res, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(vals, v_res, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
     }
     return cudaGetLastError();
 }

@@ -23,13 +23,12 @@
 //     (k_vcycle_tail);
 //   * the middle levels above the tail (a few thousand to some tens of
 //     thousands of fluid cells: too small to fill the GPU, so each of their
-//     launches costs mostly its latency) run in ONE thread-block cluster
-//     together with the tail (k_vcycle_mid): the same phases, separated by
-//     the cluster's hardware barrier instead of kernel boundaries.
+//     launches costs mostly its latency) live in the distributed shared
+//     memory of one thread-block cluster together with the tail
+//     (k_vcycle_dsm, vcycle_dsm.cu).
 // On the base level the last fluid cell receives the coarse correction once
 // more per duplicate that pads the reference's fluid list to a multiple of 8
 // (:1487-1494, iterated by prolongate :611-615).
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "apic_device.cuh"
@@ -130,27 +129,12 @@ __global__ void __launch_bounds__(kSegBlock) k_prolong_red(Level c, Level f, int
     ph_prolong(c, f, nseg, gwarp(), gnwarps(), 0, last, extra, w0);
 }
 
-// Fused descent: finish fine level's pre-smoothing, restrict, coarse red sweep.
-__global__ void __launch_bounds__(kSegBlock) k_down(Level f, Level c, int lc, const Ctl* ctl, int base, int with_red) {
-    if (ctl->pcg_done) return;
-    ph_down(f, c, ctl->seg_count[lc], gwarp(), gnwarps(), base != 0, with_red != 0);
-}
-
-// Fused ascent: prolongation with both post-smoothing sweeps.  c_fin: the
-// coarse level's final error; f_pre / f_fin: this level's pre-smoothed and
-// final error arrays.
-__global__ void __launch_bounds__(kSegBlock) k_up(const float* c_fin, uint32_t cw, Level f, const float* f_pre,
-                                                  float* f_fin, int lf, const Ctl* ctl, int base) {
-    if (ctl->pcg_done) return;
-    ph_up(c_fin, cw, f, f_pre, f_fin, ctl->seg_count[lf], gwarp(), gnwarps(), base ? ctl->last_fluid : 0xFFFFFFFFu,
-          base ? ctl->pad_count : 0u);
-}
-
 __global__ void __launch_bounds__(kTailThreads) k_coarse_solve(Level L, float* __restrict__ cs, float* __restrict__ cap,
-                                                               float* __restrict__ cr, const Ctl* __restrict__ ctl) {
+                                                               float* __restrict__ cr, const Ctl* __restrict__ ctl,
+                                                               int exact) {
     pdl_wait();
     if (ctl->pcg_done) return;
-    cta_coarse_cg(L.fluid, L.w, L.cells, L.diag, L.px, L.py, L.res, L.err, cs, cap, cr);
+    cta_coarse_cg(L.fluid, L.w, L.cells, L.diag, L.px, L.py, L.res, L.err, cs, cap, cr, exact != 0);
 }
 
 __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(TailParams tp, const Ctl* ctl) {
@@ -159,85 +143,6 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(TailParams tp, con
     extern __shared__ uint32_t sm[];
     cta_tail(tp, sm, true);
 }
-
-// Middle levels lv[0..n) (V-cycle levels first..first+n-1) and the coarse
-// tail, by one thread-block cluster.  On entry lv[0] holds its restricted
-// residual and its first red sweep (k_restrict_red); on exit its error is
-// final.  Every phase is the graph kernels' phase with the cluster's warps as
-// the grid; a cluster barrier (release/acquire at cluster scope, so global
-// writes before it are visible to every CTA after it) separates phases, and
-// CTA 0 runs the shared-memory tail while the others wait.  pcg_done is read
-// once and is the same for every CTA, so all of them reach every barrier.
-constexpr int kMaxMidLevels = 8;
-struct MidParams {
-    int first, n;
-    Level lv[kMaxMidLevels + 1];  // lv[n]: the first tail level
-};
-
-__global__ void __launch_bounds__(kTailThreads, 1) k_vcycle_mid(MidParams mp, TailParams tp, const Ctl* ctl) {
-    pdl_wait();
-    if (ctl->pcg_done) return;
-    extern __shared__ uint32_t sm[];
-    namespace cg = cooperative_groups;
-    cg::cluster_group cl = cg::this_cluster();
-    const uint32_t wpb = blockDim.x >> 5;
-    const uint32_t warp = cl.block_rank() * wpb + (threadIdx.x >> 5);
-    const uint32_t nwarps = cl.num_blocks() * wpb;
-    const int n = mp.n;
-    // CTA 0 starts copying the tail's coefficients now; they arrive while the
-    // middle levels run
-    if (cl.block_rank() == 0) cta_tail_issue_coeffs(tp, sm);
-    for (int k = 0; k < n; ++k) {
-        const int li = mp.first + k;
-        ph_smooth(mp.lv[k], ctl->seg_count[li], warp, nwarps, 1, 1);
-        cl.sync();
-        ph_restrict(mp.lv[k], mp.lv[k + 1], ctl->seg_count[li + 1], warp, nwarps, k + 1 < n);
-        cl.sync();
-    }
-    if (cl.block_rank() == 0) cta_tail(tp, sm, false);
-    cl.sync();
-    for (int k = n - 1; k >= 0; --k) {
-        const uint32_t nseg = ctl->seg_count[mp.first + k];
-        ph_prolong(mp.lv[k + 1], mp.lv[k], nseg, warp, nwarps, 1, 0xFFFFFFFFu, 0u);
-        cl.sync();
-        ph_prolong(mp.lv[k + 1], mp.lv[k], nseg, warp, nwarps, 0, 0xFFFFFFFFu, 0u);
-        if (k > 0) cl.sync();
-    }
-}
-
-cudaLaunchConfig_t mid_config(uint32_t ctas, size_t smem, cudaStream_t st, cudaLaunchAttribute* attr) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(ctas, 1, 1);
-    cfg.blockDim = dim3(kTailThreads, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = ctas;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cfg;
-}
-
-void launch_mid(Scene& s, cudaStream_t st) {
-    MidParams mp;
-    mp.first = s.cluster_first;
-    mp.n = s.tail_first - s.cluster_first;
-    for (int k = 0; k <= mp.n; ++k) mp.lv[k] = s.lv[s.cluster_first + k];
-    uint32_t off = 0;
-    TailParams tp = make_tail_params(s, s.tail_first, &off);
-    cudaLaunchAttribute attr[2];
-    cudaLaunchConfig_t cfg = mid_config(uint32_t(s.cluster_size), size_t(off) * 4, st, attr);
-    if (s.use_pdl) {
-        attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        attr[1].val.programmaticStreamSerializationAllowed = 1;
-        cfg.numAttrs = 2;
-    }
-    cudaLaunchKernelEx(&cfg, k_vcycle_mid, mp, tp, static_cast<const Ctl*>(s.ctl));
-}
-
-
 
 size_t tail_level_bytes(const Level& L) { return 4ull * (L.words + 6ull * L.padded); }
 
@@ -260,76 +165,14 @@ void plan_vcycle(Scene& s) {
         s.tail_smem = bytes;
         cudaFuncSetAttribute(k_vcycle_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTailSmemBudget));
     }
-    // largest cluster of 1024-thread CTAs with the tail's shared memory that
-    // the GPU can hold
-    s.cluster_size = 0;
-    if (s.tail_first >= 2 && s.tail_first < s.nlevels) {
-        cudaFuncSetAttribute(k_vcycle_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTailSmemBudget));
-        cudaFuncSetAttribute(k_vcycle_mid, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        for (uint32_t ctas : {16u, 8u, 4u}) {
-            cudaLaunchAttribute attr[1];
-            cudaLaunchConfig_t cfg = mid_config(ctas, s.tail_smem, nullptr, attr);
-            int clusters = 0;
-            if (cudaOccupancyMaxActiveClusters(&clusters, k_vcycle_mid, &cfg) == cudaSuccess && clusters > 0) {
-                s.cluster_size = int(ctas);
-                break;
-            }
-        }
-        cudaGetLastError();  // a refused size leaves an error behind
-    }
-    plan_vcycle_cluster(s);
     plan_vcycle_dsm(s);
 }
 
-// Middle levels for the cluster: the levels just above the tail with at most
-// cluster_max_cells cells each (never the base level).
-void plan_vcycle_cluster(Scene& s) {
-    s.cluster_first = s.tail_first;
-    if (s.cluster_size == 0 || s.cluster_max_cells == 0 || s.tail_first >= s.nlevels) return;
-    for (int l = s.tail_first - 1; l >= 1 && s.tail_first - l <= kMaxMidLevels; --l) {
-        if (s.lv[l].cells > s.cluster_max_cells) break;
-        s.cluster_first = l;
-    }
-}
-
-static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode, bool residual_exit);
-
-// One V-cycle on s.stream: z = M^-1 r in lv[0].err.  Fused form: one kernel
-// per level down (k_down) and up (k_up) around the coarse tail.
+// One V-cycle on s.stream: z = M^-1 r in lv[0].err.  Two kernels per sweep and
+// per transfer on the levels above the distributed-shared-memory cluster or
+// the tail (the reference's sequence launch by launch).  Returns false when
+// the caller must reduce r.z itself (a grid without multigrid levels).
 bool enqueue_vcycle(Scene& s, bool base_red_done, int rz_mode, bool residual_exit) {
-    if (!s.fused_vcycle || s.nlevels < 2) {
-        enqueue_vcycle_unfused(s, base_red_done, rz_mode, residual_exit);
-        return rz_mode < 0 || s.nlevels >= 2;
-    }
-    // the fused descent recomputes the base level's red sweep from the
-    // residual, so a sweep already written changes nothing
-    cudaStream_t st = s.stream;
-    Level* L = s.lv;
-    auto grid = [&](int l) { return seg_grid(L[l].words); };
-    const int last = s.nlevels - 1;
-    const int deepest = s.tail_first < s.nlevels ? s.tail_first : last;  // solved by the tail or the coarse CG
-    for (int l = 0; l < deepest; ++l)
-        k_down<<<grid(l + 1), kSegBlock, 0, st>>>(L[l], L[l + 1], l + 1, s.ctl, l == 0 ? 1 : 0,
-                                                   l + 1 < deepest ? 1 : 0);
-    if (s.tail_first < s.nlevels) {
-        uint32_t off = 0;
-        TailParams tp = make_tail_params(s, s.tail_first, &off);
-        k_vcycle_tail<<<1, kTailThreads, size_t(off) * 4, st>>>(tp, s.ctl);
-    } else {
-        k_coarse_solve<<<1, kTailThreads, 0, st>>>(L[last], s.cg_s, s.cg_ap, s.cg_r, s.ctl);
-    }
-    // pre-smoothed error: base in err2, other levels in err; final error:
-    // base in err (what PCG reads), mid levels in err2, the deepest level in
-    // err (written by the tail or the coarse CG)
-    auto pre = [&](int l) { return l == 0 ? L[0].err2 : L[l].err; };
-    auto fin = [&](int l) { return (l == 0 || l == deepest) ? L[l].err : L[l].err2; };
-    for (int l = deepest - 1; l >= 0; --l)
-        k_up<<<grid(l), kSegBlock, 0, st>>>(fin(l + 1), L[l + 1].w, L[l], pre(l), fin(l), l, s.ctl, l == 0 ? 1 : 0);
-    return rz_mode < 0;
-}
-
-// Two kernels per sweep and per transfer (the reference's sequence launch by launch).
-static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode, bool residual_exit) {
     cudaStream_t st = s.stream;
     Level* L = s.lv;
     auto grid = [&](int l) { return seg_grid(L[l].words); };
@@ -344,20 +187,14 @@ static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode, bo
     if (last < 1) {
         launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 1, 0);
         launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 0, 0);
-        return;
+        return rz_mode < 0;
     }
     const bool dsm = s.use_dsm && s.dsm_first < s.dsm_tail && s.dsm_tail < s.nlevels;
-    const bool cluster = !dsm && s.cluster_first < s.tail_first && s.tail_first < s.nlevels;
     int deepest_mid = 0;  // deepest level smoothed by the global kernels
     for (int l = 1; l <= last; ++l) {
         if (dsm && l == s.dsm_first) {
             launch(pdl, k_restrict_red, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
             launch_vcycle_dsm(s, st);
-            break;
-        }
-        if (cluster && l == s.cluster_first) {
-            launch(pdl, k_restrict_red, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
-            launch_mid(s, st);
             break;
         }
         if (l == s.tail_first) {
@@ -369,7 +206,8 @@ static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode, bo
         }
         if (l == last) {
             launch(pdl, k_restrict, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
-            launch(pdl, k_coarse_solve, 1, kTailThreads, 0, st, L[l], s.cg_s, s.cg_ap, s.cg_r, s.ctl);
+            launch(pdl, k_coarse_solve, 1, kTailThreads, 0, st, L[l], s.cg_s, s.cg_ap, s.cg_r, s.ctl,
+                   coarse_cg_exact(s) ? 1 : 0);
             break;
         }
         launch(pdl, k_restrict_red, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
@@ -386,6 +224,7 @@ static void enqueue_vcycle_unfused(Scene& s, bool base_red_done, int rz_mode, bo
                part_rz(s));
     else
         launch(pdl, k_prolong_red, grid(0), kSegBlock, 0, st, L[1], L[0], 0, s.ctl, 1);
+    return true;
 }
 
 }  // namespace apic

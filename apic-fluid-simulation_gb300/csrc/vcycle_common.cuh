@@ -1,5 +1,5 @@
 // vcycle_common.cuh — per-cell V-cycle arithmetic shared by the graph kernels
-// (vcycle.cu) and the persistent solver (pcg_persistent.cu).
+// (vcycle.cu) and the distributed-shared-memory V-cycle (vcycle_dsm.cu).
 //
 // Restates MultiGridLevel::smooth_level (src/apic.rs:471-535), restrict
 // (:537-594), prolongate (:596-616) and solve_coarse_exact (:618-704).
@@ -167,10 +167,35 @@ __device__ __forceinline__ float cta_max(float v, float* sh) {
     return t;
 }
 
+// solve_coarse_exact's FP32 sums (:627-629, :660, :681-687): a[c] * b[c]
+// added one fluid cell after another in ascending order, by one thread.
+__device__ __forceinline__ float serial_dot(const uint32_t* bits, uint32_t w, uint32_t cells, const float* a,
+                                            const float* b) {
+    float s = 0.0f;
+    for (uint32_t r = 0; r < cells; ++r)
+        if (bit_at(bits, r)) s = s + a[r + w] * b[r + w];
+    return s;
+}
+// Sum of a CTA: FP64 over the threads' parts (fast), or the serial FP32 sum
+// in the reference's order by thread 0 (exact; the vectors must be written
+// and visible to the CTA).
+__device__ __forceinline__ float cta_dot(bool exact, double part, const uint32_t* bits, uint32_t w, uint32_t cells,
+                                         const float* a, const float* b, double* shd) {
+    if (!exact) return float(cta_sum(part, shd));
+    __shared__ float s_dot;
+    __syncthreads();
+    if (threadIdx.x == 0) s_dot = serial_dot(bits, w, cells, a, b);
+    __syncthreads();
+    return s_dot;
+}
+
 // Plain CG on the coarsest level (solve_coarse_exact, :618-704) by one CTA.
-// Arrays may live in global or shared memory.
+// Arrays may live in global or shared memory.  exact: the dot products are
+// the reference's serial FP32 sums (reference solver mode); otherwise FP64
+// sums over the threads.
 static __device__ __noinline__ void cta_coarse_cg(const uint32_t* bits, uint32_t w, uint32_t cells, const float* diag, const float* px,
-                              const float* py, const float* res, float* err, float* cs, float* cap, float* cr) {
+                              const float* py, const float* res, float* err, float* cs, float* cap, float* cr,
+                              bool exact) {
     __shared__ double shd[32];
     __shared__ float shf[32];
     const long long W = w;
@@ -186,7 +211,7 @@ static __device__ __noinline__ void cta_coarse_cg(const uint32_t* bits, uint32_t
         g += double(rv * rv);
         nf++;
     }
-    float gamma = float(cta_sum(g, shd));
+    float gamma = cta_dot(exact, g, bits, w, cells, cr, cr, shd);
     uint32_t nfl = uint32_t(cta_sum(double(nf), shd));
     if (gamma < 1e-12f) return;
     uint32_t max_it = min(nfl, 100u);
@@ -204,7 +229,7 @@ static __device__ __noinline__ void cta_coarse_cg(const uint32_t* bits, uint32_t
             cap[c] = v;
             d += double(cs[c] * v);
         }
-        float delta = float(cta_sum(d, shd));
+        float delta = cta_dot(exact, d, bits, w, cells, cs, cap, shd);
         if (fabsf(delta) < 1e-5f) break;
         float alpha = gamma / delta;
         float me = 0.0f;
@@ -223,7 +248,7 @@ static __device__ __noinline__ void cta_coarse_cg(const uint32_t* bits, uint32_t
             uint32_t c = r + w;
             ng += double(cr[c] * cr[c]);
         }
-        float new_gamma = float(cta_sum(ng, shd));
+        float new_gamma = cta_dot(exact, ng, bits, w, cells, cr, cr, shd);
         float beta = new_gamma / gamma;
         gamma = new_gamma;
         for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
@@ -239,13 +264,21 @@ static __device__ __noinline__ void cta_coarse_cg(const uint32_t* bits, uint32_t
 // coarsest level of at most 32 * kWarpCgCells cells; the other warps wait.
 constexpr uint32_t kWarpCgCells = 8;
 static __device__ __noinline__ void warp_coarse_cg(const uint32_t* bits, uint32_t w, uint32_t cells, const float* diag, const float* px,
-                               const float* py, const float* res, float* err, float* cs, float* cap, float* cr) {
+                               const float* py, const float* res, float* err, float* cs, float* cap, float* cr,
+                               bool exact) {
     if (threadIdx.x < 32) {
         const long long W = w;
         const uint32_t lane = threadIdx.x;
         auto wsum = [](double v) {
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
             return v;
+        };
+        // FP64 over the lanes, or the reference's serial FP32 sum by lane 0
+        auto wdot = [&](double part, const float* a, const float* b) {
+            if (!exact) return float(wsum(part));
+            __syncwarp();
+            float v = lane == 0 ? serial_dot(bits, w, cells, a, b) : 0.0f;
+            return __shfl_sync(0xffffffffu, v, 0);
         };
         double g = 0, nf = 0;
         for (uint32_t r = lane; r < cells; r += 32) {
@@ -258,7 +291,7 @@ static __device__ __noinline__ void warp_coarse_cg(const uint32_t* bits, uint32_
             g += double(rv * rv);
             nf += 1.0;
         }
-        float gamma = float(wsum(g));
+        float gamma = wdot(g, cr, cr);
         uint32_t nfl = uint32_t(wsum(nf));
         if (!(gamma < 1e-12f)) {
             uint32_t max_it = min(nfl, 100u);
@@ -276,7 +309,7 @@ static __device__ __noinline__ void warp_coarse_cg(const uint32_t* bits, uint32_
                     cap[c] = v;
                     d += double(cs[c] * v);
                 }
-                float delta = float(wsum(d));
+                float delta = wdot(d, cs, cap);
                 if (fabsf(delta) < 1e-5f) break;
                 float alpha = gamma / delta;
                 float me = 0.0f;
@@ -295,7 +328,7 @@ static __device__ __noinline__ void warp_coarse_cg(const uint32_t* bits, uint32_
                     uint32_t c = r + w;
                     ng += double(cr[c] * cr[c]);
                 }
-                float new_gamma = float(wsum(ng));
+                float new_gamma = wdot(ng, cr, cr);
                 float beta = new_gamma / gamma;
                 gamma = new_gamma;
                 __syncwarp();
@@ -321,6 +354,7 @@ struct TailLevel {
 };
 struct TailParams {
     int n;                      // tail levels; lv[n - 1] is the coarsest
+    int exact;                  // coarsest CG with the reference's serial FP32 sums
     uint32_t o_cs, o_cap, o_cr;  // coarse CG vectors
     TailLevel lv[kMaxLevels];
 };
@@ -518,95 +552,6 @@ __device__ __forceinline__ void cta_tail_load_coeffs(const TailParams& tp, uint3
     __syncthreads();
 }
 
-// ---- fused sweeps: one kernel per level and direction ----------------------
-// The values a sweep would read from cells that another thread updates in
-// the same launch are recomputed locally from their own inputs, with the same
-// float operations, so the result equals the two-sweep sequence bit for bit.
-
-// First red sweep value of a cell whose error was zero-filled.
-__device__ __forceinline__ float red_init_value(const Level& L, uint32_t p) {
-    float inv = L.inv_diag[p];
-    return inv != 0.0f ? 0.0f + (kOmega * (L.res[p] * inv - 0.0f)) : 0.0f;
-}
-
-// Error of fine cell q after the two pre-smoothing sweeps (red then black,
-// from zero).  base: red values are computed on the fly from the residual;
-// otherwise they are already in L.err (written by the descent into L).
-__device__ __forceinline__ float pre_smoothed(const Level& L, uint32_t q, long long rq, bool base) {
-    if (is_red(uint32_t(rq), L.w)) return base ? red_init_value(L, q) : L.err[q];
-    const float* e = L.err;
-    if (base)
-        return sor_cell(L.fluid, L.w, L.cells, L.inv_diag, L.px, L.py, L.res, rq, q, 0.0f, true,
-                        [&L](uint32_t p, long long) { return red_init_value(L, p); });
-    return sor_cell(L.fluid, L.w, L.cells, L.inv_diag, L.px, L.py, L.res, rq, q, 0.0f, true,
-                    [e](uint32_t p, long long) { return e[p]; });
-}
-
-// Descent from fine level f to coarse level c, over coarse fluid cells:
-// store f's pre-smoothed error for the 2x2 children in f_pre (the base keeps
-// it apart in err2; other levels in err, whose red cells the previous
-// descent already set), restrict to c's residual and, with_red, run c's first
-// red sweep into c.err.  No value read in this launch is written in it.
-__device__ __forceinline__ void ph_down(const Level& f, const Level& c, uint32_t nseg_c, uint32_t warp,
-                                        uint32_t nwarps, bool base, bool with_red) {
-    const uint32_t lane = threadIdx.x & 31;
-    float* f_pre = base ? f.err2 : f.err;
-    for (uint32_t s = warp; s < nseg_c; s += nwarps) {
-        uint32_t word = c.seg[s];
-        if (!((c.fluid[word] >> lane) & 1u)) continue;
-        uint32_t rc = word * 32 + lane;
-        uint32_t cx = rc % c.w, cy = rc / c.w;
-        for (uint32_t dy = 0; dy < 2; ++dy)
-            for (uint32_t dx = 0; dx < 2; ++dx) {
-                long long rf = (long long)(cy * 2 + dy) * f.w + (cx * 2 + dx);
-                if (!fluid_raw(f.fluid, rf, f.cells)) continue;
-                uint32_t pf = uint32_t(rf) + f.w;
-                if (base || !is_red(uint32_t(rf), f.w)) f_pre[pf] = pre_smoothed(f, pf, rf, base);
-            }
-        float r = restrict_cell_fn(f.fluid, f.w, f.cells, f.diag, f.px, f.py, f.res,
-                                   [&f, base](uint32_t p, long long rp) { return pre_smoothed(f, p, rp, base); },
-                                   cx, cy);
-        uint32_t cp = rc + c.w;
-        c.res[cp] = r;
-        if (with_red && is_red(rc, c.w)) {
-            float inv = c.inv_diag[cp];
-            c.err[cp] = inv != 0.0f ? 0.0f + (kOmega * (r * inv - 0.0f)) : 0.0f;
-        }
-    }
-}
-
-// Ascent into fine level f from the coarse level's final error c_fin:
-// prolongation plus the black and red post-sweeps in one pass, reading the
-// pre-smoothed error f_pre and writing the final error f_fin (a different
-// array, so neighbours always read pre-sweep values).  Returns this thread's
-// r.z over its final values (used on the base level).
-__device__ __forceinline__ double ph_up(const float* c_fin, uint32_t cw, const Level& f, const float* f_pre,
-                                        float* f_fin, uint32_t nseg_f, uint32_t warp, uint32_t nwarps, uint32_t last,
-                                        uint32_t extra) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t fw = f.w;
-    auto pro = [=](uint32_t q, long long rq) {
-        uint32_t r = uint32_t(rq);
-        return prolonged(f_pre[q], c_fin[((r / fw) / 2) * cw + (r % fw) / 2 + cw], q == last ? extra : 0u);
-    };
-    auto black_new = [&](uint32_t q, long long rq) {
-        return sor_cell(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, rq, q, pro(q, rq), true, pro);
-    };
-    double rz = 0.0;
-    for (uint32_t s = warp; s < nseg_f; s += nwarps) {
-        uint32_t word = f.seg[s];
-        if (!((f.fluid[word] >> lane) & 1u)) continue;
-        uint32_t raw = word * 32 + lane;
-        uint32_t p = raw + fw;
-        float z;
-        if (!is_red(raw, fw)) z = black_new(p, raw);
-        else z = sor_cell(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, raw, p, pro(p, raw), true, black_new);
-        f_fin[p] = z;
-        rz += double(f.res[p] * z);
-    }
-    return rz;
-}
-
 // The coarse tail (levels held in shared memory) by one CTA.  load_coeffs:
 // copy masks and coefficients first (otherwise they are already resident);
 // the first level's residual is always copied in and its error copied out.
@@ -642,10 +587,10 @@ __device__ __forceinline__ void cta_tail(const TailParams& tp, uint32_t* sm, boo
         float* fs = reinterpret_cast<float*>(sm);
         if (L.cells <= 32 * kWarpCgCells)
             warp_coarse_cg(L.bits, L.w, L.cells, L.diag, L.px, L.py, L.res, L.err, fs + tp.o_cs, fs + tp.o_cap,
-                           fs + tp.o_cr);
+                           fs + tp.o_cr, tp.exact != 0);
         else
             cta_coarse_cg(L.bits, L.w, L.cells, L.diag, L.px, L.py, L.res, L.err, fs + tp.o_cs, fs + tp.o_cap,
-                          fs + tp.o_cr);
+                          fs + tp.o_cr, tp.exact != 0);
     }
     for (int l = tp.n - 2; l >= 0; --l) {
         SmemLevel f = smem_level(sm, tp.lv[l]);
@@ -673,6 +618,7 @@ __device__ __forceinline__ void cta_tail(const TailParams& tp, uint32_t* sm, boo
 inline TailParams make_tail_params(const Scene& s, int first, uint32_t* words_out) {
     TailParams tp;
     tp.n = s.nlevels - first;
+    tp.exact = coarse_cg_exact(s) ? 1 : 0;
     uint32_t off = 0;
     for (int k = 0; k < tp.n; ++k) {
         const Level& v = s.lv[first + k];

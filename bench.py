@@ -227,12 +227,6 @@ def run_gpu_arm(args, world, rank, local):
     sim.set_particles(px, py, vx, vy)
     mode = {"mixed": A.SOLVER_REL_MIXED, "fp32": A.SOLVER_REL_FP32, "reference": A.SOLVER_REFERENCE}[args.solver]
     sim.set_solver(mode, 1e-6, 500)
-    if args.persistent:
-        sim.set_option(A.OPT_PERSISTENT_SOLVE, 1)
-    sim.set_option(A.OPT_FUSED_VCYCLE, 1 if args.fused_vcycle else 0)
-    if args.cluster_cells is not None:
-        sim.set_option(A.OPT_CLUSTER_VCYCLE, args.cluster_cells)
-    cluster_cells = sim.get_option(A.OPT_CLUSTER_VCYCLE)
     if args.no_pdl:
         sim.set_option(A.OPT_PDL, 0)
     if args.no_dsm:
@@ -287,7 +281,7 @@ def run_gpu_arm(args, world, rank, local):
     sim2 = A.Apic(args.side, args.side, 1.0 / args.side, props(A))
     sim2.set_particles(px, py, vx, vy)
     sim2.set_solver(mode, 1e-6, 500)
-    for opt in (A.OPT_PERSISTENT_SOLVE, A.OPT_FUSED_VCYCLE, A.OPT_CLUSTER_VCYCLE, A.OPT_PDL, A.OPT_DSM_VCYCLE):
+    for opt in (A.OPT_PDL, A.OPT_DSM_VCYCLE):
         v = sim.get_option(opt)
         if sim2.get_option(opt) != v:
             sim2.set_option(opt, v)
@@ -355,12 +349,9 @@ def run_gpu_arm(args, world, rank, local):
                        "unit": UNIT_NOTE, "substeps": substeps, "pcg_iterations": iters,
                        "true_residual_rel_max": max(true_res) if true_res else None,
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
-                       "solve_form": "persistent kernel" if args.persistent else "graph of per-phase kernels",
-                       "vcycle": "one kernel per level per direction" if args.fused_vcycle
-                       else "one kernel per sweep and transfer" + (
-                           "; coarse levels in one cluster's distributed shared memory" if dsm else
-                           f"; levels of <= {cluster_cells} cells in one thread-block cluster"
-                           if cluster_cells else ""),
+                       "solve_form": "graph of per-phase kernels",
+                       "vcycle": "one kernel per sweep and transfer" + (
+                           "; coarse levels in one cluster's distributed shared memory" if dsm else ""),
                        "launch": ("stage by stage" if args.eager else "one CUDA graph per update")
                        + ("" if args.no_pdl else "; programmatic dependent launch in the PCG loop")},
             "updates_per_s": world * args.steps / dev_s_max,
@@ -810,12 +801,6 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--eager", action="store_true",
                     help="launch the stages one by one in the timed region (for ncu launch lists)")
-    ap.add_argument("--persistent", action="store_true",
-                    help="run the pressure solve as one persistent cooperative kernel")
-    ap.add_argument("--fused-vcycle", action="store_true",
-                    help="run the V-cycle as one kernel per level and direction")
-    ap.add_argument("--cluster-cells", type=int, default=None,
-                    help="largest multigrid level run inside the thread-block cluster (0: none)")
     ap.add_argument("--no-dsm", action="store_true",
                     help="keep the middle multigrid levels in global memory instead of a cluster's shared memory")
     ap.add_argument("--no-pdl", action="store_true",

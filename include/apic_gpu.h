@@ -212,24 +212,10 @@ int apic_set_particles(apic_handle* h, uint32_t n, const float* pos_x, const flo
 int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterations);
 
 /* ---- execution options --------------------------------------------------- */
-/* 1: the whole pressure solve runs as one persistent cooperative kernel (one
- * CTA per SM, grid barriers between phases; needs cooperative launch).
- * 0 (default): a CUDA graph of per-phase kernels with device-side WHILE
- * loops.  Both compute the same iterations. */
-#define APIC_OPT_PERSISTENT_SOLVE 1
-/* 1: the V-cycle runs one kernel per level going down and one going up
- * (values another thread updates in the same kernel are recomputed locally).
- * 0 (default, faster on GB300: the recomputation costs more than the launches
- * it saves): one kernel per sweep and per transfer.  Same results bit for
- * bit. */
-#define APIC_OPT_FUSED_VCYCLE 2
-/* Largest multigrid level (in cells) whose sweeps and transfers run inside
- * one thread-block cluster together with the shared-memory coarse levels,
- * instead of one kernel each; 0 turns the cluster off.  Default 65536.
- * Setting a non-zero value fails with APIC_ERR_UNSUPPORTED when the GPU
- * cannot hold a cluster of 1024-thread CTAs; apic_get_option reports 0 then.
- * Same results bit for bit.  Applies when APIC_OPT_FUSED_VCYCLE is 0. */
-#define APIC_OPT_CLUSTER_VCYCLE 3
+/* Options 1-3 and 6 (a persistent cooperative solve, a fused V-cycle, a
+ * cluster of middle levels reading global memory, a one-cluster solve for
+ * small scenes) were measured slower than the defaults on GB300 and are no
+ * longer offered; their ids are rejected as unknown options. */
 /* 1 (default): kernels inside the PCG loop use programmatic dependent launch
  * (each is scheduled while its predecessor drains and waits on the device
  * for its results); 0: plain stream order.  Same results bit for bit. */
@@ -237,20 +223,11 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
 /* 1 (default where the level sizes allow): the multigrid levels from the
  * largest that fits down to 32 rows live in the distributed shared memory of
  * one 16-CTA thread-block cluster (each CTA owns a band of rows) and the
- * coarser ones in its first CTA; overrides APIC_OPT_CLUSTER_VCYCLE.  0: off.
+ * coarser ones in its first CTA.  0: every level above the shared-memory
+ * tail runs as separate sweep and transfer kernels.
  * apic_get_option reports 0 where no level qualifies.  Same results bit for
  * bit. */
 #define APIC_OPT_DSM_VCYCLE 5
-/* Scenes of at most this many cells run their whole pressure solve (every
- * PCG iteration and refinement) as one launch of a single thread-block
- * cluster of 1..16 CTAs, phases separated by the cluster's hardware barrier;
- * larger scenes use the graph of per-phase kernels.  0 (default): never --
- * on GB300 the graph is faster per iteration even at 64^2; the cluster form
- * only saves launches.  apic_get_option returns the CTAs the scene's cluster
- * uses (0: not used).  Same per-cell arithmetic; reductions are grouped
- * differently.  Profiling runs (apic_set_profiling) keep the per-phase
- * kernels. */
-#define APIC_OPT_CLUSTER_SOLVE 6
 /* No counterpart in the reference (whose PCG starts from zero).  Value 1
  * (default): in APIC_SOLVER_REL_MIXED each solve starts from the FP64
  * pressure of the previous solve (zero after apic_set_particles or

@@ -11,7 +11,8 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "apic-fluid-simulation_gb300")
-for p in (ROOT, PKG):
+TESTS = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, PKG, TESTS):
     if p not in sys.path:
         sys.path.insert(0, p)
 

@@ -1,9 +1,8 @@
 """Snapshot / restore through the C-ABI (needs a GB300).
 
 A restored handle holds exactly the saved state (compared field by field and
-by re-snapshotting), and its next updates compute what the original's do: the
-only difference between two runs is the order of P2G's float atomics, so
-positions agree within the bound the drift test uses.
+by re-snapshotting), and its next updates compute what the original's do, bit
+for bit (every kernel's result is independent of scheduling).
 """
 import numpy as np
 import pytest
@@ -13,7 +12,6 @@ import apic_gb300 as A
 pytestmark = pytest.mark.gpu
 
 PROPS = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
-POS_TOL_CELLS = 1e-3
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -50,8 +48,9 @@ def test_restore_then_continue():
         a.update(A.DebugOptions(), 1 / 240)
         b.update(A.DebugOptions(), 1 / 240)
         assert a.stats().substeps == b.stats().substeps
-    d = np.max(np.abs(a.read_vec2x8(0) - b.read_vec2x8(0)))
-    assert float(d) < POS_TOL_CELLS / side, float(d)
+    # (the pressure outside the current fluid cells is stale history, src/apic.rs:1872-1883, and not compared)
+    for f in A.PARTICLE_FIELDS + ["u", "v"]:
+        assert np.array_equal(a.read_field(f), b.read_field(f), equal_nan=True), f
     assert a.info().timestamp == b.info().timestamp
     a.close()
     b.close()
