@@ -175,6 +175,9 @@ SIGNATURES = {
     "apic_debug_finish_substep": (ctypes.c_int, [_VP, ctypes.c_float]),
     "apic_update_batch": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
                                          ctypes.POINTER(ctypes.c_int)]),
+    "apic_place_scenes": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                                         ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
+                                         ctypes.POINTER(ctypes.c_int32)]),
     "apic_scene_bytes": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
                                         ctypes.POINTER(ctypes.c_uint64)]),
     "apic_server_create": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_VP)]),
@@ -247,6 +250,13 @@ def scene_params(kind: int, width: int, height: int | None = None, cell_size: fl
     height = width if height is None else height
     return SceneParamsC(kind, width, height, cell_size, sub, seed, fluid_x, fluid_y, disk[0], disk[1], disk[2],
                         disk_v[0], disk_v[1], noise_period, noise_threshold, vel_sigma)
+
+
+def scene_count(p: SceneParamsC) -> int:
+    """Number of particles the scene holds (apic_scene_count; host code only)."""
+    n = ctypes.c_uint64(0)
+    _check(load_library().apic_scene_count(ctypes.byref(p), ctypes.byref(n)), "apic_scene_count")
+    return n.value
 
 
 def generate_scene(p: SceneParamsC):
@@ -510,6 +520,19 @@ def scene_bytes(width: int, height: int, particles: int) -> int:
     out = ctypes.c_uint64(0)
     _check(load_library().apic_scene_bytes(width, height, particles, ctypes.byref(out)), "apic_scene_bytes")
     return out.value
+
+
+def place_scenes(bytes_per_scene, work_per_scene, budgets):
+    """Device of each independent scene on len(budgets) GPUs (apic_place_scenes):
+    largest scenes first, each to the least-loaded device whose memory budget
+    still holds it; -1 where none does.  The same on every rank."""
+    n, d = len(bytes_per_scene), len(budgets)
+    b = (ctypes.c_uint64 * max(n, 1))(*[int(x) for x in bytes_per_scene])
+    w = (ctypes.c_uint64 * max(n, 1))(*[int(x) for x in work_per_scene])
+    bud = (ctypes.c_uint64 * max(d, 1))(*[int(x) for x in budgets])
+    out = (ctypes.c_int32 * max(n, 1))()
+    _check(load_library().apic_place_scenes(b, w, n, bud, d, out), "apic_place_scenes")
+    return [int(out[i]) for i in range(n)]
 
 
 class Server:

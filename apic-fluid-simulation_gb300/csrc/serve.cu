@@ -453,6 +453,30 @@ int apic_scene_bytes(uint32_t width, uint32_t height, uint64_t particles, uint64
     return APIC_OK;
 }
 
+int apic_place_scenes(const uint64_t* bytes, const uint64_t* work, uint32_t count, const uint64_t* budgets,
+                      uint32_t devices, int32_t* device_out) {
+    if (count == 0) return APIC_OK;
+    if (!bytes || !work || !budgets || !device_out || devices == 0)
+        return bad(APIC_ERR_INVALID_ARG, "apic_place_scenes: bad argument");
+    std::vector<uint32_t> order(count);
+    for (uint32_t i = 0; i < count; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return bytes[a] > bytes[b]; });
+    std::vector<uint64_t> used(devices, 0), load(devices, 0);
+    for (uint32_t i : order) {
+        int32_t best = -1;
+        for (uint32_t d = 0; d < devices; ++d) {
+            if (budgets[d] < used[d] || bytes[i] > budgets[d] - used[d]) continue;
+            if (best < 0 || load[d] < load[uint32_t(best)]) best = int32_t(d);
+        }
+        device_out[i] = best;
+        if (best >= 0) {
+            used[uint32_t(best)] += bytes[i];
+            load[uint32_t(best)] += work[i];
+        }
+    }
+    return APIC_OK;
+}
+
 int apic_server_create(uint64_t memory_budget_bytes, uint32_t max_active, uint32_t keep_results, apic_server** out) {
     if (!out || max_active == 0) return bad(APIC_ERR_INVALID_ARG, "apic_server_create: bad argument");
     apic_server* sv = new apic_server();

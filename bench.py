@@ -147,6 +147,25 @@ def dist_max(x: float, world: int) -> float:
     return float(t.item())
 
 
+def dist_sum(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def place_on_ranks(A, scenes, world, budget_bytes):
+    """Device (rank) of each independent scene: apic_place_scenes with each
+    GPU's memory budget; every rank computes the same placement, so no
+    exchange is needed before the run."""
+    counts = [A.scene_count(sc) for sc in scenes]
+    sizes = [A.scene_bytes(sc.width, sc.height, n) for sc, n in zip(scenes, counts)]
+    return A.place_scenes(sizes, counts, [budget_bytes] * world)
+
+
 def dist_barrier(world: int) -> None:
     if world > 1:
         import torch.distributed as dist
@@ -155,12 +174,15 @@ def dist_barrier(world: int) -> None:
 
 # ---------------------------------------------------------------- CPU arm --
 def cpu_restatement_rate(n_steps: int, warmup: int, budget_s: float, side: int = 0, threads: int = 0):
-    """Particle-steps/s of the C++ restatement of the reference step (OpenMP)."""
+    """Particle-steps/s of the C++ restatement of the reference step (OpenMP).
+
+    Only the oracle's library is loaded (it carries the benchmark scenes'
+    particle generator too); apic_gb300 supplies plain Python parameter types."""
     import apic_gb300 as A
     side = side or SIDE  # SIDE is read at call time: --workload stress changes it
-    from oracle.oracle import OracleSim
+    from oracle.oracle import OracleSim, generate_scene
     threads = threads or os.cpu_count() or 1
-    px, py, vx, vy = A.generate_scene(scene_params(A, side))
+    px, py, vx, vy = generate_scene(scene_params(A, side))
     o = OracleSim(side, side, 1.0 / side, props(A), threads=threads)
     o.set_particles(px, py, vx, vy)
     o.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
@@ -326,6 +348,15 @@ def run_gpu_arm(args, world, rank, local):
     counts = level_fluid_counts(A, sim)
     peak, peak_kind = peaks()
     roof = roofline(iters, solve_ms, args.steps, counts, peak, peak_kind) if solve_ms > 0 and not args.eager else None
+    if roof is not None:
+        l2 = l2_copy_gbs(torch)
+        roof["l2"] = {"copy_gbs_measured": l2, "frac": roof["achieved"] / l2,
+                      "how": "the same algorithmic bytes per second against a device copy of a 32 MiB buffer "
+                             "into another (64 MiB working set, resident in the 129 MB L2; read + write bytes, "
+                             "best of 20 repetitions, CUDA events)"}
+    compare = None
+    if args.solver == "mixed" and not args.no_solver_compare and not args.eager:
+        compare = solver_compare(A, torch, args, px, py, vx, vy, mode)
 
     result = None
     if rank == 0:
@@ -365,7 +396,13 @@ def run_gpu_arm(args, world, rank, local):
                             "scene over the same updates as the timed region"},
             "gpu_launches": launches if not args.eager else None,
             "roofline": roof,
-            "stage_ms_per_step": {k: v[0] / prof_steps for k, v in stages.items() if v[1]},
+            "solver_compare": compare,
+            "stage_ms_profiling": {
+                "note": "profiling mode, not additive to ms_per_step: each stage of each substep launched on "
+                        "its own between CUDA events and the solve's loops driven from the host (every PCG "
+                        "iteration pays host round trips the update graph does not); for the split between "
+                        "stages, not their sum",
+                "ms_per_step": {k: v[0] / prof_steps for k, v in stages.items() if v[1]}},
             "cpu_baseline": cpu,
         }
         print(json.dumps(result), flush=True)
@@ -381,13 +418,75 @@ def ctypes_stream(sim) -> int:
 
 
 # Algorithmic bytes of one PCG iteration per fluid cell (each array read or
-# written once per pass; neighbour reads hit cached lines):
-#   base level: SpMV with the search update 24 B, update + first red sweep
-#   38 B, black sweep 22 B, restriction 20 B, prolongation + black sweep 23 B,
-#   prolongation + red sweep 23 B, r.z 8 B = 158 B;
-#   coarser levels: sweeps, restriction, prolongations = 88 B.
-SOLVE_BYTES_BASE = 158
-SOLVE_BYTES_COARSE = 88
+# written once per pass; neighbour reads hit cached lines): 132 B per base
+# fluid cell for the SpMV with its dot product, the pressure/residual update,
+# the SOR pre- and post-smoothing, restriction, prolongation, r.z and the
+# search update; 76 B per coarse fluid cell (pre-smoothing 24, restriction
+# 20, prolongation 8, post-smoothing 24).  The coarse tail and the coarsest
+# CG run in shared memory and are not counted.
+SOLVE_BYTES_BASE = 132
+SOLVE_BYTES_COARSE = 76
+
+
+def l2_copy_gbs(torch) -> float:
+    """Device copy bandwidth with an L2-resident working set (GB/s, read + write)."""
+    n = 32 * 1024 * 1024 // 4
+    a = torch.ones(n, dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(5):
+        b.copy_(a)
+    best = None
+    for _ in range(20):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            b.copy_(a)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / 10
+        best = t if best is None else min(best, t)
+    return 2 * n * 4 / best / 1e9
+
+
+def solver_compare(A, torch, args, px, py, vx, vy, mixed_mode):
+    """The plain FP32 solve (PCG on the recursive residual, tolerance 1e-6)
+    beside the mixed-precision one on the same scene and updates: device ms
+    per update, PCG iterations and the true relative residual (FP64) each
+    reaches."""
+    out = {}
+    for name, mode in (("plain_fp32", A.SOLVER_REL_FP32), ("mixed", mixed_mode)):
+        g = A.Apic(args.side, args.side, 1.0 / args.side, props(A))
+        g.set_particles(px, py, vx, vy)
+        g.set_solver(mode, 1e-6, 500)
+        opts = A.DebugOptions()
+        for _ in range(args.warmup):
+            g.update(opts, FRAME_DT)
+        g.synchronize()
+        st_ptr = torch.cuda.ExternalStream(ctypes_stream(g))
+        steps = min(args.steps, 10)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        iters, res, notc, sub, solve = 0, [], 0, 0, 0.0
+        e0.record(st_ptr)
+        for _ in range(steps):
+            g.update(opts, FRAME_DT)
+            st = g.stats()
+            iters += st.pcg_iterations_total
+            res.append(float(st.true_residual_rel))
+            notc += st.not_converged
+            sub += st.substeps
+            solve += st.solve_ms
+        e1.record(st_ptr)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[name] = {"ms_per_update": ms, "solve_ms_per_update": solve / steps, "pcg_iterations": iters,
+                     "substeps": sub, "true_residual_rel_max": max(res), "true_residual_rel_min": min(res),
+                     "substeps_not_converged": notc, "updates": steps}
+        g.close()
+    out["note"] = ("both asked for relative residual 1e-6 with at most 500 iterations; the plain FP32 PCG stops on "
+                   "its recursive residual, whose true value (FP64, reported) stays far above 1e-6 because FP32 "
+                   "rounding of the pressure limits it; the mixed solve refines in FP64 until the true residual "
+                   "is below 1e-6 (updates after the same warm-up, L2 not flushed)")
+    return out
 
 
 def solve_traffic():
@@ -416,8 +515,9 @@ def roofline(iters, solve_ms, steps, counts, peak, peak_kind):
     sec = solve_ms / 1e3
     achieved = per_iter * iters / sec / 1e9
     traffic = solve_traffic()
-    return {"bound": "hbm", "kernel": "pressure solve: MG-preconditioned CG (k_spmv_dot, k_pcg_update, "
-                                      "V-cycle kernels, k_dot_rz per iteration)",
+    return {"bound": "hbm", "kernel": "pressure solve: MG-preconditioned CG (per iteration k_spmv_dot, "
+                                      "k_pcg_update, k_smooth_exit, the V-cycle's sweep and transfer kernels, "
+                                      "k_vcycle_dsm, k_prolong_red_rz, k_pcg_cond)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
             "traffic": traffic, "traffic_unit": "DRAM bytes per PCG iteration" if traffic else None,
             "algorithmic_bytes_per_iteration": per_iter, "iterations": iters,
@@ -451,15 +551,26 @@ def make_sims(A, scenes, dsm=True):
     return sims
 
 
-def run_batched(args):
+def run_batched(args, world=1, rank=0, local=0):
     """Config 4: many uneven scenes, one batched update per round, against the
-    plain path (one scene's update after another) over the same updates."""
+    plain path (one scene's update after another) over the same updates.
+    Under torchrun the scenes are placed on the ranks' GPUs by
+    apic_place_scenes (memory budget per GPU, least-loaded first); each rank
+    runs its own scenes, with no collective on the data path, and rank 0
+    reports the summed particle-substeps over the slowest rank's time."""
     import apic_gb300 as A
     from apic_gb300 import build as gpu_build
     gpu_build.build()
     import torch
-    torch.cuda.set_device(0)
+    torch.cuda.set_device(local)
     scenes = batched_scenes(A, args.scenes)
+    placement = None
+    if world > 1:
+        where = place_on_ranks(A, scenes, world, int(args.budget_gb * (1 << 30)))
+        if any(d < 0 for d in where):
+            raise SystemExit("a scene fits no GPU's budget")
+        placement = [where.count(r) for r in range(world)]
+        scenes = [sc for sc, d in zip(scenes, where) if d == rank]
     dt = 1.0 / 240.0
     # plain: fresh scenes, the first `cmp` updates one scene at a time
     cmp_steps = args.compare_steps
@@ -499,10 +610,23 @@ def run_batched(args):
                 if k == cmp_steps - 1:
                     cmp_s = time.perf_counter() - t0
         all_s = time.perf_counter() - t0
-    sides = [sc.width for sc in scenes]
+    # every rank ran its own scenes: totals summed, times of the slowest rank
+    sub_all, sub_cmp, sub_plain = dist_sum(sub_all, world), dist_sum(sub_cmp, world), dist_sum(sub_plain, world)
+    all_s, cmp_s, plain_s = dist_max(all_s, world), dist_max(cmp_s, world), dist_max(plain_s, world)
+    kern_all, n_tot = int(dist_sum(kern_all, world)), int(dist_sum(n_tot, world))
+    res_max = dist_max(res_max, world)
+    if rank != 0:
+        for g in sims:
+            g.close()
+        return
+    sides = [sc.width for sc in batched_scenes(A, args.scenes)]
     line = {
         "metric": METRIC, "value": sub_all / all_s, "unit": "particle-substeps/s (aggregate over all scenes)",
-        "workload": "batched", "n_gpus": 1, "steps": args.steps, "higher_is_better": True,
+        "workload": "batched", "n_gpus": world, "steps": args.steps, "higher_is_better": True,
+        "scaling": "strong" if world > 1 else None,
+        "placement": None if placement is None else {
+            "scenes_per_gpu": placement, "how": "apic_place_scenes: largest first, least-loaded GPU whose "
+                                               "memory budget holds the scene; no collective on the data path"},
         "config": {"workload": f"{len(scenes)} independent dam-break scenes, side log-uniform in [64, 512] "
                                f"(rounded to x8, seed 3), fluid share U[0.2, 0.6], 4 ppc, dt=1/240, "
                                f"mixed-precision PCG to true rel. residual 1e-6",
@@ -799,6 +923,8 @@ def main():
     ap.add_argument("--solver", default="mixed", choices=["mixed", "fp32", "reference"])
     ap.add_argument("--side", type=int, default=SIDE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-solver-compare", action="store_true",
+                    help="skip the plain-FP32-vs-mixed solve comparison of the default workload")
     ap.add_argument("--eager", action="store_true",
                     help="launch the stages one by one in the timed region (for ncu launch lists)")
     ap.add_argument("--no-dsm", action="store_true",
@@ -838,7 +964,7 @@ def main():
     if args.impl == "reference":
         run_reference_arm(args, world, rank)
     elif args.workload == "batched":
-        run_batched(args)
+        run_batched(args, world, rank, local)
     elif args.workload == "served":
         run_served(args)
     elif args.workload == "criterion":

@@ -289,6 +289,19 @@ int apic_update_batch(apic_handle* const* handles, uint32_t count, uint32_t flag
 /* Estimated device bytes of a scene (upper bound used for admission). */
 int apic_scene_bytes(uint32_t width, uint32_t height, uint64_t particles, uint64_t* bytes_out);
 
+/* Placement of independent scenes on several GPUs (no counterpart in the
+ * reference, which runs one scene in one process).  Scenes share nothing, so
+ * a multi-GPU batch needs no collective: each GPU runs the scenes placed on it
+ * and the results are gathered on the host.  Scenes are taken largest first
+ * (by bytes, ties by index) and each goes to the device with the least work
+ * placed so far among those whose remaining budget holds it (ties: lowest
+ * device).  bytes / work: per scene (work e.g. particles x steps); budgets:
+ * per device.  device_out[i] = the device of scene i, or -1 when no device
+ * can hold it.  Deterministic: the same inputs give the same placement on
+ * every rank. */
+int apic_place_scenes(const uint64_t* bytes, const uint64_t* work, uint32_t count, const uint64_t* budgets,
+                      uint32_t devices, int32_t* device_out);
+
 /* Continuous-batching request server (no counterpart in the reference,
  * which runs one scene per process): requests (scene, step count, dt) are
  * queued on submission and admitted in arrival order while the scenes in the

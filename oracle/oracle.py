@@ -13,8 +13,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "apic-fluid-simulation_gb300"))
-from apic_gb300 import (FIELDS, STAGES, InfoC, RenderParamsC, RenderStatsC, StatsC, WorldPropsC,  # noqa: E402
-                        WorldProperties)
+from apic_gb300 import (FIELDS, STAGES, InfoC, RenderParamsC, RenderStatsC, SceneParamsC, StatsC,  # noqa: E402
+                        WorldPropsC, WorldProperties)
 
 from . import build as _build  # noqa: E402
 
@@ -52,6 +52,8 @@ def load(rebuild: bool = True) -> ctypes.CDLL:
         "oracle_render": (ctypes.c_int, [ctypes.c_uint32, _FP, _FP, _FP, _FP, ctypes.POINTER(RenderParamsC),
                                          ctypes.c_uint32, ctypes.c_float, _VP, ctypes.POINTER(RenderStatsC)]),
         "oracle_morton": (ctypes.c_uint32, [ctypes.c_uint32, ctypes.c_uint32]),
+        "oracle_scene_count": (ctypes.c_int, [ctypes.POINTER(SceneParamsC), ctypes.POINTER(ctypes.c_uint64)]),
+        "oracle_scene_fill": (ctypes.c_int, [ctypes.POINTER(SceneParamsC), ctypes.c_uint64, _FP, _FP, _FP, _FP]),
         "oracle_random_lane": (ctypes.c_float, [ctypes.c_uint32, ctypes.c_uint32]),
         "oracle_temporal_weight": (ctypes.c_float, [ctypes.c_float]),
     }
@@ -163,6 +165,17 @@ class OracleSim:
         n, e = self.field_shape(fid)
         data = np.ascontiguousarray(data, self._dtype(fid, e))
         _ck(self._lib.oracle_write_field(self._h, fid, data.ctypes.data, data.nbytes), "oracle_write_field")
+
+
+def generate_scene(p: SceneParamsC):
+    """The scene's particles (pos_x, pos_y, vel_x, vel_y as float32), from the
+    same generator as apic_gb300.generate_scene, without the GPU library."""
+    lib = load()
+    n = ctypes.c_uint64(0)
+    _ck(lib.oracle_scene_count(ctypes.byref(p), ctypes.byref(n)), "oracle_scene_count")
+    arrs = [np.zeros(n.value, np.float32) for _ in range(4)]
+    _ck(lib.oracle_scene_fill(ctypes.byref(p), n.value, *[a.ctypes.data_as(_FP) for a in arrs]), "oracle_scene_fill")
+    return tuple(arrs)
 
 
 def morton(x: int, y: int) -> int:
