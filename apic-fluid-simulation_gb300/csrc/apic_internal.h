@@ -75,7 +75,6 @@ struct Ctl {
     uint32_t refinements_total;  // refinements summed over the substeps of an update
     uint32_t cond;          // last loop decision of a control kernel (eager runs read it)
     uint32_t sorted;        // the update ran the Morton sort
-    float rz_exact;         // reference mode: r.z in dot_product's order
     double dgamma;          // FP64 copies for the relative-tolerance modes
     double bnorm2;          // ||b||^2 of the running solve
     double rnorm2;          // ||r||^2 of the recursive residual
@@ -206,6 +205,13 @@ struct Scene {
     // kernel nodes per execution of each graph body (launch accounting)
     uint32_t kn_top = 0, kn_sort = 0, kn_loop = 0, kn_pcg = 0, kn_refine = 0;
     int solver_mode = APIC_SOLVER_REFERENCE;
+    // WHILE node of the PCG loop being recorded: the kernel that runs the
+    // residual's exit test also sets the loop condition (pcg_set_cond false:
+    // host-driven loops of profiling runs)
+    cudaGraphConditionalHandle pcg_h = 0;
+    uint32_t pcg_cap = 0;
+    int pcg_dyn_cap = 0;
+    bool pcg_set_cond = false;
     float rel_tol = 1e-6f;
     uint32_t max_iter = 500;
     bool vmax_valid = false;

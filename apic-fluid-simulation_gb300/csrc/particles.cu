@@ -63,7 +63,9 @@ constexpr int kGatherThreads = kGatherTW * kGatherTH;
 constexpr int kRegionW = kGatherTW + 2, kRegionH = kGatherTH + 2;
 constexpr int kRegionBins = kRegionW * kRegionH;       // 340 cells whose particles a tile reads
 constexpr int kGatherCap = 2048;                       // staged particles per tile (more: read from global)
-constexpr size_t kGatherSmem = size_t(kGatherCap) * (4 + 4 + 8 * 4) + size_t(kRegionBins) * 8 + 64;
+// slot, corner code, 4 values, 4 weights, and the grid position and temporal
+// weight that every grid's contributions share
+constexpr size_t kGatherSmem = size_t(kGatherCap) * (4 + 4 + 8 * 4 + 3 * 4) + size_t(kRegionBins) * 8 + 64;
 
 enum { kGridU = 0, kGridV = 1, kGridD = 2 };
 
@@ -141,13 +143,24 @@ struct P2gRec {
     float val[4], w[4];
 };
 
-__device__ __forceinline__ bool p2g_record(const PartPtrs* __restrict__ pp, uint32_t slot, int grid, int W, int H,
-                                           float dx, float prev_dt, P2gRec& r) {
-    const float px = pp->f[PX][slot], py = pp->f[PY][slot];
+// The quantities of one particle that every grid's contributions share:
+// grid position and temporal weight (:1246-1256).
+struct P2gBase {
+    float gx, gy, wt;
+};
+__device__ __forceinline__ P2gBase p2g_base(const PartPtrs* __restrict__ pp, uint32_t slot, float dx, float prev_dt) {
     const float tr = pp->f[TR][slot];
     const float tau = (-tr) / prev_dt;
-    const float wt = temporal_w(tau);
-    const float gx = px / dx, gy = py / dx;
+    P2gBase b;
+    b.wt = temporal_w(tau);
+    b.gx = pp->f[PX][slot] / dx;
+    b.gy = pp->f[PY][slot] / dx;
+    return b;
+}
+
+__device__ __forceinline__ bool p2g_record(const PartPtrs* __restrict__ pp, uint32_t slot, const P2gBase& b, int grid,
+                                           int W, int H, float dx, P2gRec& r) {
+    const float gx = b.gx, gy = b.gy, wt = b.wt;
     const int cx0 = max(min(trunc_x86(floorf(gx - 0.5f)), W - 1), 0);
     const int cy0 = max(min(trunc_x86(floorf(gy - 0.5f)), H - 1), 0);
     int xs[2], ys[2], nx, ny;
@@ -215,10 +228,8 @@ struct StagedRecs {
     const float* w;    // [4][kGatherCap]
     __device__ __forceinline__ uint32_t slot_at(int p) const { return slot[p]; }
     __device__ __forceinline__ uint32_t code_at(int p) const { return code[p]; }
-    __device__ __forceinline__ void get(int p, int, float* v, float* wt) const {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) { v[k] = val[k * kGatherCap + p]; wt[k] = w[k * kGatherCap + p]; }
-    }
+    __device__ __forceinline__ float val_at(int k, int p) const { return val[k * kGatherCap + p]; }
+    __device__ __forceinline__ float w_at(int k, int p) const { return w[k * kGatherCap + p]; }
 };
 struct GlobalRecs {
     const uint32_t* vals;  // sorted slots
@@ -227,17 +238,15 @@ struct GlobalRecs {
     float dx, prev_dt;
     uint32_t* status;
     __device__ __forceinline__ uint32_t slot_at(int p) const { return vals[p]; }
-    __device__ __forceinline__ uint32_t code_at(int p) const {
+    __device__ __forceinline__ P2gRec rec(int p) const {
         P2gRec r;
-        if (!p2g_record(pp, vals[p], grid, W, H, dx, prev_dt, r)) atomicOr(status, kStatusP2gLayout);
-        return r.code;
+        const uint32_t sl = vals[p];
+        if (!p2g_record(pp, sl, p2g_base(pp, sl, dx, prev_dt), grid, W, H, dx, r)) atomicOr(status, kStatusP2gLayout);
+        return r;
     }
-    __device__ __forceinline__ void get(int p, int, float* v, float* wt) const {
-        P2gRec r;
-        p2g_record(pp, vals[p], grid, W, H, dx, prev_dt, r);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) { v[k] = r.val[k]; wt[k] = r.w[k]; }
-    }
+    __device__ __forceinline__ uint32_t code_at(int p) const { return rec(p).code; }
+    __device__ __forceinline__ float val_at(int k, int p) const { return rec(p).val[k]; }
+    __device__ __forceinline__ float w_at(int k, int p) const { return rec(p).w[k]; }
 };
 
 // Fold of one face: merge NR slot-ordered runs [b, e) by slot; run r's records
@@ -245,7 +254,7 @@ struct GlobalRecs {
 // code.  Consecutive records of one chunk form the chunk's groups: per corner
 // k, the lanes' contributions summed in lane order; at the end of the chunk
 // the groups are added to the face in corner order.
-template <int NR, class Recs>
+template <int NR, bool kVal, class Recs>
 __device__ __forceinline__ void fold_face(const Recs& R, int (&b)[NR], const int (&e)[NR], const int (&sh)[NR],
                                           float& out_v, float& out_w) {
     uint32_t hs[NR];
@@ -275,22 +284,30 @@ __device__ __forceinline__ void fold_face(const Recs& R, int (&b)[NR], const int
         if ((best >> 3) != chunk) {
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                if (gm & (1u << k)) { acc_v = acc_v + gv[k]; acc_w = acc_w + gw[k]; }
+                if (gm & (1u << k)) {
+                    if (kVal) acc_v = acc_v + gv[k];
+                    acc_w = acc_w + gw[k];
+                }
 #pragma unroll
             for (int k = 0; k < 4; ++k) { gv[k] = 0.0f; gw[k] = 0.0f; }
             gm = 0;
             chunk = best >> 3;
         }
-        float v[4], w[4];
-        R.get(p, s, v, w);
+        // only the corners that land here are read (usually one)
 #pragma unroll
         for (int k = 0; k < 4; ++k)
-            if (hit & (1u << k)) { gv[k] = gv[k] + v[k]; gw[k] = gw[k] + w[k]; }
+            if (hit & (1u << k)) {
+                if (kVal) gv[k] = gv[k] + R.val_at(k, p);
+                gw[k] = gw[k] + R.w_at(k, p);
+            }
         gm |= hit;
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-        if (gm & (1u << k)) { acc_v = acc_v + gv[k]; acc_w = acc_w + gw[k]; }
+        if (gm & (1u << k)) {
+            if (kVal) acc_v = acc_v + gv[k];
+            acc_w = acc_w + gw[k];
+        }
     out_v = acc_v;
     out_w = acc_w;
 }
@@ -319,7 +336,7 @@ __device__ __forceinline__ void fold_cell(const Recs& R, const Bin& bin, int gri
                 sh[r] = 4 * (ry * 3 + rx);
             }
             float v, w;
-            fold_face<6>(R, b, e, sh, v, w);
+            fold_face<6, true>(R, b, e, sh, v, w);
             const uint32_t f = uint32_t(j) * uint32_t(W + 1) + uint32_t(fi);
             o.acc_u[f] = v;
             o.acc_uw[f] = w;
@@ -334,7 +351,7 @@ __device__ __forceinline__ void fold_cell(const Recs& R, const Bin& bin, int gri
                 sh[r] = 4 * (ry * 2 + rx);
             }
             float v, w;
-            fold_face<6>(R, b, e, sh, v, w);
+            fold_face<6, true>(R, b, e, sh, v, w);
             const uint32_t f = uint32_t(fj) * uint32_t(W) + uint32_t(i);
             o.acc_v[f] = v;
             o.acc_vw[f] = w;
@@ -348,7 +365,7 @@ __device__ __forceinline__ void fold_cell(const Recs& R, const Bin& bin, int gri
             sh[r] = 4 * (ry * 2 + rx);
         }
         float v, w;
-        fold_face<4>(R, b, e, sh, v, w);
+        fold_face<4, false>(R, b, e, sh, v, w);
         o.dens[uint32_t(j) * uint32_t(W) + uint32_t(i)] = w;
     }
 }
@@ -363,7 +380,10 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
     uint32_t* s_code = s_slot + kGatherCap;
     float* s_val = reinterpret_cast<float*>(s_code + kGatherCap);
     float* s_w = s_val + 4 * kGatherCap;
-    uint32_t* s_off = reinterpret_cast<uint32_t*>(s_w + 4 * kGatherCap);  // kRegionBins + 1
+    float* s_gx = s_w + 4 * kGatherCap;
+    float* s_gy = s_gx + kGatherCap;
+    float* s_wt = s_gy + kGatherCap;
+    uint32_t* s_off = reinterpret_cast<uint32_t*>(s_wt + kGatherCap);  // kRegionBins + 1
     uint32_t* s_glo = s_off + kRegionBins + 1;                            // kRegionBins
     __shared__ uint32_t s_total;
     __shared__ uint32_t s_rowg[kRegionH];
@@ -429,6 +449,12 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
         for (uint32_t q = threadIdx.x; q < s1 - s0; q += kGatherThreads) s_slot[s0 + q] = vals[g0 + q];
     }
     __syncthreads();
+    for (uint32_t p = threadIdx.x; p < P; p += kGatherThreads) {
+        const P2gBase bs = p2g_base(pp, s_slot[p], dx, prev_dt);
+        s_gx[p] = bs.gx;
+        s_gy[p] = bs.gy;
+        s_wt[p] = bs.wt;
+    }
     const StagedRecs R{s_slot, s_code, s_val, s_w};
     auto bin = [&](int x, int y, int& b, int& e) {
         const int rb = (y - ry0) * kRegionW + (x - rx0);
@@ -439,7 +465,8 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
         bool bad = false;
         for (uint32_t p = threadIdx.x; p < P; p += kGatherThreads) {
             P2gRec rec;
-            if (!p2g_record(pp, s_slot[p], g, W, H, dx, prev_dt, rec)) bad = true;
+            const P2gBase bs{s_gx[p], s_gy[p], s_wt[p]};
+            if (!p2g_record(pp, s_slot[p], bs, g, W, H, dx, rec)) bad = true;
             s_code[p] = rec.code;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -582,18 +609,36 @@ __global__ void __launch_bounds__(256) k_vmax(const PartPtrs* __restrict__ pp, u
 __global__ void k_zero_vmax(Ctl* ctl) {
     pdl_wait(); ctl->vmax_bits = 0; ctl->nonfinite = 0; }
 
+// Four consecutive slots per thread: 128-bit loads of the sorted slots and
+// 128-bit stores of each field (the gathered reads are one float each).
 __global__ void __launch_bounds__(256) k_permute(PartPtrs* __restrict__ pp, const uint32_t* __restrict__ vals,
                                                  uint32_t n, uint32_t npad) {
     pdl_wait();
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= npad) return;
-    if (i < n) {
-        uint32_t src = vals[i];
+    const uint32_t i0 = 4u * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (i0 >= npad) return;  // npad is a multiple of 8
+    uint32_t src[4];
+    bool ok[4];
+    if (i0 + 4u <= n) {
+        const uint4 v = *reinterpret_cast<const uint4*>(vals + i0);
+        src[0] = v.x; src[1] = v.y; src[2] = v.z; src[3] = v.w;
 #pragma unroll
-        for (int f = 0; f < NPF; ++f) pp->alt[f][i] = pp->f[f][src];
+        for (int k = 0; k < 4; ++k) ok[k] = true;
     } else {
 #pragma unroll
-        for (int f = 0; f < NPF; ++f) pp->alt[f][i] = 0.0f;
+        for (int k = 0; k < 4; ++k) {
+            ok[k] = i0 + uint32_t(k) < n;
+            src[k] = ok[k] ? vals[i0 + k] : 0u;
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < NPF; ++f) {
+        const float* a = pp->f[f];
+        float4 o;
+        o.x = ok[0] ? a[src[0]] : 0.0f;
+        o.y = ok[1] ? a[src[1]] : 0.0f;
+        o.z = ok[2] ? a[src[2]] : 0.0f;
+        o.w = ok[3] ? a[src[3]] : 0.0f;
+        *reinterpret_cast<float4*>(pp->alt[f] + i0) = o;
     }
 }
 
@@ -675,7 +720,7 @@ cudaError_t launch_pack_vec2x8(Scene& s, int which, float* out) {
 
 cudaError_t launch_permute(Scene& s, const uint32_t* sorted_vals) {
     if (s.npad == 0) return cudaSuccess;
-    launch(s.use_pdl, k_permute, div_up(s.npad, 256), 256, 0, s.stream, s.pp, sorted_vals, s.n, s.npad);
+    launch(s.use_pdl, k_permute, div_up(s.npad / 4, 256), 256, 0, s.stream, s.pp, sorted_vals, s.n, s.npad);
     launch(s.use_pdl, k_swap_tables, 1, 32, 0, s.stream, s.pp);
     return cudaGetLastError();
 }

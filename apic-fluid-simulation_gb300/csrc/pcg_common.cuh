@@ -184,18 +184,33 @@ __device__ __forceinline__ void ph_update_search(const Level& B, uint32_t nseg, 
     *r2 = acc;
 }
 
-// gamma' = r.z ends the iteration (:1934-1943): beta, or the exit when r.z
-// is below SAFTY (reference mode) or zero.  Run by one thread with the total.
-__device__ __forceinline__ void finish_rz(Ctl* ctl, double tot, int mode) {
+// gamma' = r.z ends the reference mode's iteration (:1934-1943): beta, or
+// the exit when r.z is below SAFTY.  Run by one thread.  (The relative modes
+// form beta at the start of the next iteration, where a zero r.z ends the
+// solve.)
+__device__ __forceinline__ void finish_rz_reference(Ctl* ctl, float ng) {
     constexpr float kSafetyRz = 1e-5f;  // SAFTY, src/apic.rs:8
-    const float ng = float(tot);
-    if (mode == APIC_SOLVER_REFERENCE ? (ng < kSafetyRz) : !(ng != 0.0f)) {
+    if (ng < kSafetyRz) {
         ctl->pcg_done = 1;
         return;
     }
     ctl->beta = ng / ctl->gamma;
     ctl->beta_valid = 1;
     ctl->gamma = ng;
+}
+
+// After the residual's exit test: whether the PCG loop goes on (not
+// converged, under the iteration cap; dyn_cap reads the remaining budget of a
+// refinement).  In the relative modes a continuing loop's next iteration
+// forms beta from the r.z parts that this iteration's V-cycle stores
+// (beta_valid); the reference mode's k_gamma_exact does that itself.  Run by
+// thread 0 of one block; sets the graph's loop condition when set_cond.
+__device__ __forceinline__ void loop_decision(Ctl* ctl, int mode, cudaGraphConditionalHandle h, uint32_t cap,
+                                              int dyn_cap, int set_cond) {
+    const uint32_t c = dyn_cap ? ctl->inner_cap : cap;
+    const bool cont = !ctl->pcg_done && ctl->pcg_iters < c;
+    if (cont && mode != APIC_SOLVER_REFERENCE) ctl->beta_valid = 1;
+    if (set_cond) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 
 // The exits that k_pcg_update leaves to the next kernel: its delta stop, or

@@ -76,15 +76,27 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl*
 // s' = z + beta s, Ap = A s' and this block's part of delta = s'.Ap
 // (apply_matrix_and_dot, src/apic.rs:1823-1863; the search update
 // :1945-1954 is folded in).  k_pcg_update sums the parts.
+// In the relative modes the previous iteration's r.z arrives as the parts
+// its V-cycle stored (rz): every block sums them into gamma' and forms
+// beta = gamma' / gamma (:1934-1943); a zero r.z ends the solve (k_pcg_update
+// records it).  Block 0 keeps beta for k_pcg_update.
 __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s, float* ap, Ctl* ctl, float2* part,
-                                                        int mode) {
+                                                        int mode, const float2* rz, uint32_t nrz) {
     // the base segment list is written by the substep's setup: load this
     // warp's first word before waiting on the previous kernel
     const uint32_t nseg = ctl->seg_count[0];
     const uint32_t w0 = gwarp() < nseg ? B.seg[gwarp()] : 0xFFFFFFFFu;
     pdl_wait();
     if (ctl->pcg_done) return;
-    F2 acc = pcg::ph_spmv_search(B, nseg, gwarp(), gnwarps(), s, ctl->beta, ctl->beta_valid != 0, ap, w0);
+    float beta = ctl->beta;
+    const bool bv = ctl->beta_valid != 0;
+    if (mode != APIC_SOLVER_REFERENCE && bv) {
+        const float ng = float(sum_partials<kSegBlock>(rz, nrz));
+        if (!(ng != 0.0f)) return;
+        beta = ng / ctl->gamma;
+        if (blockIdx.x == 0 && threadIdx.x == 0) ctl->beta = beta;
+    }
+    F2 acc = pcg::ph_spmv_search(B, nseg, gwarp(), gnwarps(), s, beta, bv, ap, w0);
     block_store<kSegBlock>(acc, part);
 }
 
@@ -97,11 +109,22 @@ __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s,
 __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int p_padded, float* s,
                                                           const float* ap, Ctl* ctl, const float2* sap,
                                                           uint32_t nsap, float4* part, int mode,
-                                                          const float* exact_parts, const uint32_t* seg_pre) {
+                                                          const float* exact_parts, const uint32_t* seg_pre,
+                                                          const float2* rz, uint32_t nrz) {
     const uint32_t nseg = ctl->seg_count[0];
     const uint32_t w0 = gwarp() < nseg ? B.seg[gwarp()] : 0xFFFFFFFFu;
     pdl_wait();
     if (ctl->pcg_done) return;
+    // this iteration's gamma: from the solve's start, or (relative modes) the
+    // previous iteration's r.z parts, which k_spmv_dot summed the same way
+    float gamma = ctl->gamma;
+    if (mode != APIC_SOLVER_REFERENCE && ctl->beta_valid) {
+        gamma = float(sum_partials<kSegBlock>(rz, nrz));
+        if (!(gamma != 0.0f)) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pcg_done = 1;
+            return;
+        }
+    }
     float delta;
     if (mode == APIC_SOLVER_REFERENCE) {
         // the chunk sums of k_delta_exact, added in chunk order from zero
@@ -112,10 +135,11 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int
         delta = float(sum_partials<kSegBlock>(sap, nsap));
     }
     const bool stop = mode == APIC_SOLVER_REFERENCE ? fabsf(delta) < kSafety : (!(delta != 0.0f) || !isfinite(delta));
-    const float alpha = ctl->gamma / delta;
+    const float alpha = gamma / delta;
     // every block reads pcg_done on entry, so the stop is recorded aside and
     // the next kernel turns it into pcg_done
     if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctl->gamma = gamma;
         ctl->pcg_iters++;
         ctl->delta_stop = stop ? 1u : 0u;
         if (!stop) ctl->alpha = alpha;
@@ -131,14 +155,15 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int
 // Stand-alone exit test (paths whose V-cycle does not start with the base
 // level's black sweep).
 __global__ void __launch_bounds__(kSegBlock) k_residual_exit(Ctl* ctl, const float4* part, uint32_t n, int mode,
-                                                             float solve_error) {
+                                                             float solve_error, cudaGraphConditionalHandle h,
+                                                             uint32_t cap, int dyn_cap, int set_cond) {
     pdl_wait();
-    if (ctl->pcg_done) return;
-    pcg::residual_exit(ctl, part, n, mode, solve_error);
+    if (!ctl->pcg_done) pcg::residual_exit(ctl, part, n, mode, solve_error);
+    if (threadIdx.x == 0) pcg::loop_decision(ctl, mode, h, cap, dyn_cap, set_cond);
 }
 
-// This block's part of gamma' = r.z (src/apic.rs:1934-1943); k_pcg_cond
-// finishes it.
+// This block's part of gamma' = r.z (src/apic.rs:1934-1943); the next
+// iteration's k_spmv_dot and k_pcg_update sum the parts.
 __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, float2* part) {
     pdl_wait();
     if (ctl->pcg_done) return;
@@ -164,11 +189,15 @@ __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, float2*
 // in shared memory, then threads 0..7 add their lane's products in order;
 // only those eight add chains are serial.
 // start: the solve's first gamma (sets gamma and the SAFTY exit,
-// :1887-1892), else the iteration's new gamma for k_pcg_cond.
+// :1887-1892), else the iteration's new gamma.
 constexpr int kGammaThreads = 1024;
 constexpr uint32_t kGammaBatch = 512;  // segments staged per round (64 KB)
 constexpr size_t kGammaSmem = size_t(kGammaBatch) * 32 * sizeof(float);
-__global__ void __launch_bounds__(kGammaThreads) k_gamma_exact(Level B, Ctl* ctl, int start) {
+// The iteration's form (start 0) also finishes the iteration (beta, or the
+// SAFTY exit) and, when set_cond, sets the loop condition.
+__global__ void __launch_bounds__(kGammaThreads) k_gamma_exact(Level B, Ctl* ctl, int start,
+                                                               cudaGraphConditionalHandle h, uint32_t cap,
+                                                               int dyn_cap, int set_cond) {
     extern __shared__ float stage[];
     pdl_wait();
     if (ctl->pcg_done) return;
@@ -207,7 +236,11 @@ __global__ void __launch_bounds__(kGammaThreads) k_gamma_exact(Level B, Ctl* ctl
         ctl->dgamma = double(g);
         if (g < kSafety) ctl->pcg_done = 1;
     } else {
-        ctl->rz_exact = g;
+        pcg::finish_rz_reference(ctl, g);
+        if (set_cond) {
+            const uint32_t c = dyn_cap ? ctl->inner_cap : cap;
+            cudaGraphSetConditional(h, (!ctl->pcg_done && ctl->pcg_iters < c) ? 1u : 0u);
+        }
     }
 }
 
@@ -338,23 +371,14 @@ __global__ void __launch_bounds__(kSegBlock) k_pressure_to64(Level B, const floa
 
 // ---- loop control (device side; each sets a graph conditional) ------------
 
-// End of an iteration: gamma' = r.z from the parts of the V-cycle's last
-// kernel (flags & 1; pcg::finish_rz sets beta or the exit), then the loop
-// condition (flags & 2): go on while not converged and under the iteration
+// Entry of the PCG loop: go on while not converged and under the iteration
 // cap (src/apic.rs:1894-1899); dyn_cap reads the remaining budget of a
-// refinement.  One block.
-__global__ void __launch_bounds__(kSegBlock) k_pcg_cond(Ctl* __restrict__ ctl, cudaGraphConditionalHandle h,
-                                                        uint32_t cap, int dyn_cap, const float2* rz, uint32_t nrz,
-                                                        int mode, int flags) {
+// refinement.  Inside the loop the same decision is taken by the kernel that
+// runs the residual's exit test (pcg::loop_decision) or, in the reference
+// mode, by k_gamma_exact.
+__global__ void k_pcg_cond(const Ctl* __restrict__ ctl, cudaGraphConditionalHandle h, uint32_t cap, int dyn_cap) {
     pdl_wait();
-    if ((flags & 1) && !ctl->pcg_done) {
-        // the reference mode's r.z comes from k_gamma_exact
-        const double tot = mode == APIC_SOLVER_REFERENCE ? double(ctl->rz_exact) : sum_partials<kSegBlock>(rz, nrz);
-        if (threadIdx.x == 0) pcg::finish_rz(ctl, tot, mode);
-        __syncthreads();
-    }
-    if (threadIdx.x != 0 || !(flags & 2)) return;
-    uint32_t c = dyn_cap ? ctl->inner_cap : cap;
+    const uint32_t c = dyn_cap ? ctl->inner_cap : cap;
     cudaGraphSetConditional(h, (!ctl->pcg_done && ctl->pcg_iters < c) ? 1u : 0u);
 }
 
@@ -413,29 +437,26 @@ static void pcg_iteration(Scene& s, int mode, float* x, int p_padded) {
     uint32_t g = seg_grid(B.words);
     cudaStream_t st = s.stream;
     const bool pdl = s.use_pdl;
-    k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, part_sap(s), mode);
+    k_spmv_dot<<<g, kSegBlock, 0, st>>>(B, s.search, s.ap, s.ctl, part_sap(s), mode,
+                                         static_cast<const float2*>(part_rz(s)), g);
     if (mode == APIC_SOLVER_REFERENCE)
         launch(pdl, k_delta_exact, div_up(B.cells, kDeltaChunk), kDeltaThreads, 0, st, B,
                static_cast<const float*>(s.search), static_cast<const float*>(s.ap),
                static_cast<const uint32_t*>(s.seg_pre), s.ctl, s.exact_parts);
     launch(pdl, k_pcg_update, g, kSegBlock, 0, st, B, x, p_padded, s.search, s.ap, s.ctl,
            static_cast<const float2*>(part_sap(s)), g, part_res(s), mode, static_cast<const float*>(s.exact_parts),
-           static_cast<const uint32_t*>(s.seg_pre));
+           static_cast<const uint32_t*>(s.seg_pre), static_cast<const float2*>(part_rz(s)), g);
     // the residual's exit test runs inside the V-cycle's first kernel when
     // that is the base level's black sweep, else on its own
     const bool exit_in_vcycle = s.nlevels >= 2;
     if (!exit_in_vcycle)
         launch(pdl, k_residual_exit, 1, kSegBlock, 0, st, s.ctl, static_cast<const float4*>(part_res(s)), g, mode,
-               s.props.solve_error);
+               s.props.solve_error, s.pcg_h, s.pcg_cap, s.pcg_dyn_cap, s.pcg_set_cond ? 1 : 0);
     // the V-cycle's last kernel also stores the parts of r.z (k_dot_rz's work)
     if (!enqueue_vcycle(s, true, mode, exit_in_vcycle)) launch(pdl, k_dot_rz, g, kSegBlock, 0, st, B, s.ctl, part_rz(s));
-    if (mode == APIC_SOLVER_REFERENCE) launch(pdl, k_gamma_exact, 1, kGammaThreads, kGammaSmem, st, B, s.ctl, 0);
-}
-
-// Finish an iteration (r.z) and, in a graph, set the loop condition.
-static void pcg_finish(Scene& s, cudaGraphConditionalHandle h, uint32_t cap, int dyn_cap, int mode, int flags) {
-    launch(s.use_pdl, k_pcg_cond, 1, kSegBlock, 0, s.stream, s.ctl, h, cap, dyn_cap,
-           static_cast<const float2*>(part_rz(s)), seg_grid(s.lv[0].words), mode, flags);
+    if (mode == APIC_SOLVER_REFERENCE)
+        launch(pdl, k_gamma_exact, 1, kGammaThreads, kGammaSmem, st, B, s.ctl, 0, s.pcg_h, s.pcg_cap, s.pcg_dyn_cap,
+               s.pcg_set_cond ? 1 : 0);
 }
 
 // PCG setup (src/apic.rs:1885-1892) followed by a device-controlled WHILE
@@ -456,19 +477,26 @@ static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p
         enqueue_vcycle(s);
         launch(s.use_pdl, k_pcg_start, g, kSegBlock, 0, st, B, s.search, s.ctl, s.partials, mode);
         if (mode == APIC_SOLVER_REFERENCE)
-            launch(s.use_pdl, k_gamma_exact, 1, kGammaThreads, kGammaSmem, st, B, s.ctl, 1);
-        pcg_finish(s, h, cap, dyn_cap, mode, 2);
+            launch(s.use_pdl, k_gamma_exact, 1, kGammaThreads, kGammaSmem, st, B, s.ctl, 1,
+                   cudaGraphConditionalHandle(0), 0u, 0, 0);
+        launch(s.use_pdl, k_pcg_cond, 1, 1, 0, st, static_cast<const Ctl*>(s.ctl), h, cap, dyn_cap);
         return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
     GraphCursor body;
     e = add_conditional_with(c, cudaGraphCondTypeWhile, h, &body);
     if (e != cudaSuccess) return e;
+    // the loop condition is set inside the iteration (the residual's exit test,
+    // or k_gamma_exact in the reference mode): no kernel of its own
+    s.pcg_h = h;
+    s.pcg_cap = cap;
+    s.pcg_dyn_cap = dyn_cap;
+    s.pcg_set_cond = true;
     e = capture_into(s, body, [&]() {
         pcg_iteration(s, mode, x, p_padded);
-        pcg_finish(s, h, cap, dyn_cap, mode, 3);
         return cudaGetLastError();
     });
+    s.pcg_set_cond = false;
     s.kn_pcg = count_kernel_nodes(body.g);
     return e;
 }
@@ -564,13 +592,16 @@ static cudaError_t eager_pcg(Scene& s, int mode, float* x, int p_padded, uint32_
     if (mode == APIC_SOLVER_REFERENCE) k_seg_prefix<<<1, 1024, 0, st>>>(B, s.ctl, s.seg_pre);
     enqueue_vcycle(s);
     k_pcg_start<<<g, kSegBlock, 0, st>>>(B, s.search, s.ctl, s.partials, mode);
-    if (mode == APIC_SOLVER_REFERENCE) k_gamma_exact<<<1, kGammaThreads, kGammaSmem, st>>>(B, s.ctl, 1);
+    if (mode == APIC_SOLVER_REFERENCE)
+        k_gamma_exact<<<1, kGammaThreads, kGammaSmem, st>>>(B, s.ctl, 1, cudaGraphConditionalHandle(0), 0u, 0, 0);
+    s.pcg_set_cond = false;
+    s.pcg_cap = cap;
+    s.pcg_dyn_cap = 0;
     for (;;) {
         cudaError_t e = read_ctl(s);
         if (e != cudaSuccess) return e;
         if (s.ctl_host->pcg_done || s.ctl_host->pcg_iters >= cap) break;
         pcg_iteration(s, mode, x, p_padded);
-        pcg_finish(s, 0, cap, 0, mode, 1);
     }
     return cudaGetLastError();
 }

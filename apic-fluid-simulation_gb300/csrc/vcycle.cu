@@ -52,15 +52,17 @@ __device__ __forceinline__ uint32_t early_word(const uint32_t* seg, uint32_t nse
 }
 
 // The base level's black sweep after k_pcg_update (which ran the red one),
-// with the exit test of k_pcg_update's residual in an extra block 0 that
-// runs beside the sweep; later kernels see its verdict.
+// with the exit test of k_pcg_update's residual and the PCG loop's decision
+// in an extra block 0 that runs beside the sweep; later kernels see its
+// verdict.
 __global__ void __launch_bounds__(kSegBlock) k_smooth_exit(Level L, Ctl* ctl, const float4* part, uint32_t nparts,
-                                                           int mode, float solve_error) {
+                                                           int mode, float solve_error, cudaGraphConditionalHandle h,
+                                                           uint32_t cap, int dyn_cap, int set_cond) {
     const uint32_t nseg = ctl->seg_count[0];
     if (blockIdx.x == 0) {
         pdl_wait();
-        if (ctl->pcg_done) return;
-        pcg::residual_exit(ctl, part, nparts, mode, solve_error);
+        if (!ctl->pcg_done) pcg::residual_exit(ctl, part, nparts, mode, solve_error);
+        if (threadIdx.x == 0) pcg::loop_decision(ctl, mode, h, cap, dyn_cap, set_cond);
         return;
     }
     const uint32_t warp = gwarp() - kSegWarps, nwarps = gnwarps() - kSegWarps;
@@ -108,7 +110,7 @@ __global__ void __launch_bounds__(kSegBlock) k_prolong_black(Level c, Level f, i
 
 // Base-level prolongation fused with the final red sweep, which also stores
 // this block's part of r.z over every fluid cell (red cells' new z, black
-// cells' final z): k_dot_rz's work; k_pcg_cond finishes the sum.
+// cells' final z): k_dot_rz's work; the next iteration sums the parts.
 __global__ void __launch_bounds__(kSegBlock) k_prolong_red_rz(Level c, Level B, const Ctl* ctl, float2* part) {
     const uint32_t nseg = ctl->seg_count[0];
     const uint32_t w0 = early_word(B.seg, nseg);
@@ -181,7 +183,8 @@ bool enqueue_vcycle(Scene& s, bool base_red_done, int rz_mode, bool residual_exi
     if (!base_red_done) launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 0, 1);
     if (residual_exit && base_red_done)
         launch(pdl, k_smooth_exit, grid(0) + 1, kSegBlock, 0, st, L[0], s.ctl,
-               static_cast<const float4*>(part_res(s)), grid(0), rz_mode, s.props.solve_error);
+               static_cast<const float4*>(part_res(s)), grid(0), rz_mode, s.props.solve_error, s.pcg_h, s.pcg_cap,
+               s.pcg_dyn_cap, s.pcg_set_cond ? 1 : 0);
     else
         launch(pdl, k_smooth, grid(0), kSegBlock, 0, st, L[0], 0, s.ctl, 1, 1);
     if (last < 1) {

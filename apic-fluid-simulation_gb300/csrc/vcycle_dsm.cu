@@ -10,7 +10,7 @@
 // memory (distributed shared memory, a few hundred cycles instead of an L2
 // round trip); phases are separated by cluster barriers, whose release /
 // acquire order makes every CTA's writes visible to the others.  CTA 0 then
-// runs the coarse tail (levels of fewer than 32 rows) exactly as
+// runs the coarse tail (levels of fewer than 64 rows) exactly as
 // k_vcycle_tail does, through global memory.
 //
 // A phase over a level costs a few hundred cycles of shared-memory latency
@@ -30,6 +30,7 @@ namespace {
 namespace cg = cooperative_groups;
 
 constexpr uint32_t kDsmCtas = 16;
+constexpr uint32_t kDsmTailRows = 64;
 constexpr int kDsmMaxLevels = 6;
 constexpr size_t kDsmSmemBudget = 220 * 1024;
 
@@ -395,15 +396,18 @@ cudaLaunchConfig_t dsm_config(size_t smem, cudaStream_t st, cudaLaunchAttribute*
 }  // namespace
 
 // Pick the distributed levels: the tail starts at the first level with fewer
-// than 32 rows; going up from there, levels join while their height divides
-// by 16, their width is even and everything fits in 220 KB per CTA.
+// than kDsmTailRows rows (one CTA runs a level of 32 x 32 cells with
+// __syncthreads between phases faster than the cluster does with cluster
+// barriers); going up from there, levels join while their height divides by
+// 16 into an even band height, their width is a multiple of 32 and everything
+// fits in 220 KB per CTA.
 void plan_vcycle_dsm(Scene& s) {
     s.dsm_first = s.dsm_tail = s.nlevels;
     s.dsm_smem = 0;
     s.dsm_off = 0;
     if (s.nlevels < 3) return;
     int d = 1;
-    while (d < s.nlevels && s.lv[d].h >= 2 * kDsmCtas) ++d;
+    while (d < s.nlevels && s.lv[d].h >= kDsmTailRows) ++d;
     if (d >= s.nlevels || d < 2) return;
     uint32_t tail_words = 0;
     make_tail_params(s, d, &tail_words);

@@ -517,7 +517,7 @@ def roofline(iters, solve_ms, steps, counts, peak, peak_kind):
     traffic = solve_traffic()
     return {"bound": "hbm", "kernel": "pressure solve: MG-preconditioned CG (per iteration k_spmv_dot, "
                                       "k_pcg_update, k_smooth_exit, the V-cycle's sweep and transfer kernels, "
-                                      "k_vcycle_dsm, k_prolong_red_rz, k_pcg_cond)",
+                                      "k_vcycle_dsm, k_prolong_red_rz)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
             "traffic": traffic, "traffic_unit": "DRAM bytes per PCG iteration" if traffic else None,
             "algorithmic_bytes_per_iteration": per_iter, "iterations": iters,

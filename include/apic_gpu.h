@@ -221,7 +221,7 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
  * for its results); 0: plain stream order.  Same results bit for bit. */
 #define APIC_OPT_PDL 4
 /* 1 (default where the level sizes allow): the multigrid levels from the
- * largest that fits down to 32 rows live in the distributed shared memory of
+ * largest that fits down to 64 rows live in the distributed shared memory of
  * one 16-CTA thread-block cluster (each CTA owns a band of rows) and the
  * coarser ones in its first CTA.  0: every level above the shared-memory
  * tail runs as separate sweep and transfer kernels.
