@@ -132,6 +132,24 @@ __device__ __forceinline__ void v_stencil(float gx, float gy, int W, int H, floa
 __device__ __forceinline__ uint32_t bit_at(const uint32_t* m, uint32_t i) { return (m[i >> 5] >> (i & 31)) & 1u; }
 // Raw-index fluid test with the reference's index arithmetic; indices outside
 // [0, cells) read as non-fluid (the padding rows of the padded layout are zero).
+// (x, y) of raw index r on a grid w cells wide; shift = log2 w, or -1 when w
+// is not a power of two (then a division).
+__device__ __forceinline__ void raw_xy(uint32_t r, uint32_t w, int shift, uint32_t& x, uint32_t& y) {
+    if (shift >= 0) {
+        y = r >> shift;
+        x = r & (w - 1u);
+    } else {
+        y = r / w;
+        x = r - y * w;
+    }
+}
+// Red cell of the checkerboard ((x + y) even, src/apic.rs list build).
+__device__ __forceinline__ bool red_at(uint32_t r, uint32_t w, int shift) {
+    uint32_t x, y;
+    raw_xy(r, w, shift, x, y);
+    return ((x + y) & 1u) == 0u;
+}
+
 __device__ __forceinline__ uint32_t fluid_raw(const uint32_t* m, long long i, uint32_t cells) {
     if (i < 0 || i >= (long long)cells) return 0;
     return bit_at(m, uint32_t(i));

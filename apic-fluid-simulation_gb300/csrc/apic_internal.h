@@ -96,6 +96,7 @@ enum : uint32_t {
 
 struct Level {
     uint32_t w = 0, h = 0, cells = 0;
+    int wshift = -1;        // log2 w, or -1 when w is not a power of two
     uint32_t words = 0;     // u32 mask words (even)
     uint32_t padded = 0;    // cells + 2w rounded up to 8
     uint32_t* fluid = nullptr;

@@ -175,7 +175,7 @@ __device__ __forceinline__ void ph_update_search(const Level& B, uint32_t nseg, 
         s[c] = sc;
         x[xi] = nx;
         B.res[c] = nr;
-        if ((((raw_ % B.w) + (raw_ / B.w)) & 1u) == 0u)
+        if (red_at(raw_, B.w, B.wshift))
             B.err[c] = inv != 0.0f ? 0.0f + (kOmegaSor * (nr * inv - 0.0f)) : 0.0f;
         mx = fmaxf(mx, fabsf(nr));
         acc = f2_add(acc, f2_square(nr));

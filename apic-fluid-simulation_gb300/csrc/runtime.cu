@@ -662,6 +662,9 @@ int apic::create_scene(uint32_t width, uint32_t height, float cell_size, const a
     for (int l = 0; l < s.nlevels; ++l) {
         Level& L = s.lv[l];
         L.cells = L.w * L.h;
+        L.wshift = -1;
+        for (int k = 0; k < 31; ++k)
+            if ((1u << k) == L.w) L.wshift = k;
         L.words = even_words(L.cells);
         L.padded = uint32_t((size_t(L.cells) + 2 * size_t(L.w) + 7) / 8 * 8);
         max_words = std::max(max_words, L.words);

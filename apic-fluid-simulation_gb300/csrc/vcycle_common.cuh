@@ -136,7 +136,6 @@ __device__ __forceinline__ float restrict_cell_all(const uint32_t* fb, uint32_t 
     return sum;
 }
 
-__device__ __forceinline__ bool is_red(uint32_t raw, uint32_t w) { return (((raw % w) + (raw / w)) & 1u) == 0u; }
 
 // e + ec, plus ec again `reps` times (the padded base list, :611-615).
 __device__ __forceinline__ float prolonged(float e, float ec, uint32_t reps) {
@@ -345,7 +344,8 @@ static __device__ __noinline__ void warp_coarse_cg(const uint32_t* bits, uint32_
 
 // ---- the coarse tail in shared memory ----------------------------------------
 struct TailLevel {
-    uint32_t w, cells, words, padded;
+    uint32_t w, h, cells, words, padded;
+    int wshift;   // log2 w, or -1 when w is not a power of two
     const uint32_t* fluid;
     const float *diag, *inv, *px, *py;
     float* res;   // global residual (read for the first tail level)
@@ -360,26 +360,36 @@ struct TailParams {
 };
 
 struct SmemLevel {
-    uint32_t w, cells;
+    uint32_t w, h, cells;
+    int wshift;
     uint32_t* bits;
     float *diag, *inv, *px, *py, *res, *err;
 };
 
 __device__ __forceinline__ SmemLevel smem_level(uint32_t* sm, const TailLevel& t) {
     float* f = reinterpret_cast<float*>(sm);
-    return SmemLevel{t.w, t.cells, sm + t.o_bits, f + t.o_diag, f + t.o_inv, f + t.o_px, f + t.o_py, f + t.o_res,
-                     f + t.o_err};
+    return SmemLevel{t.w,          t.h,          t.cells,      t.wshift,     sm + t.o_bits, f + t.o_diag,
+                     f + t.o_inv,  f + t.o_px,   f + t.o_py,   f + t.o_res,  f + t.o_err};
 }
 
+// One colour sweep of a shared-memory level (w even: every level that is
+// swept has a coarser one).  Thread t visits the colour's cells k = t,
+// t + blockDim.x, ... directly, row by row, and skips the cells outside the
+// fluid mask (their result is never stored).
 __device__ __forceinline__ void cta_sweep(const SmemLevel& L, int color, int init) {
     const float* e = L.err;
-    for (uint32_t r = threadIdx.x; r < L.cells; r += blockDim.x) {
-        if (int(!is_red(r, L.w)) != color) continue;
+    const uint32_t half = L.w >> 1;
+    const int hs = L.wshift > 0 ? L.wshift - 1 : -1;
+    const uint32_t n = L.h * half;
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+        uint32_t kk, row;
+        raw_xy(k, half, hs, kk, row);
+        const uint32_t r = row * L.w + 2u * kk + ((row + uint32_t(color)) & 1u);
+        if (!bit_at(L.bits, r)) continue;
         const uint32_t c = r + L.w;
         const float old = init ? 0.0f : e[c];
-        const float v = sor_cell_all(L.bits, L.w, L.cells, L.inv, L.px, L.py, L.res, r, c, old,
-                                     !(init && color == 0), [e](uint32_t p, long long) { return e[p]; });
-        if (bit_at(L.bits, r)) L.err[c] = v;
+        L.err[c] = sor_cell_all(L.bits, L.w, L.cells, L.inv, L.px, L.py, L.res, r, c, old, !(init && color == 0),
+                                [e](uint32_t p, long long) { return e[p]; });
     }
     __syncthreads();
 }
@@ -403,7 +413,7 @@ __device__ __forceinline__ void ph_smooth(const Level& L, uint32_t nseg, uint32_
         const uint32_t word = nxt;
         nxt = seg_next(L.seg, nseg, s + nwarps);
         const uint32_t raw = word * 32 + lane;
-        if (raw >= L.cells || int(!is_red(raw, L.w)) != color) continue;
+        if (raw >= L.cells || int(!red_at(raw, L.w, L.wshift)) != color) continue;
         const bool fluid = (L.fluid[word] >> lane) & 1u;
         const uint32_t c = raw + L.w;
         const float old = init ? 0.0f : e[c];
@@ -424,12 +434,13 @@ __device__ __forceinline__ void ph_restrict(const Level& f, const Level& c, uint
         if (rc >= c.cells) continue;
         const bool fluid = (c.fluid[word] >> lane) & 1u;
         const uint32_t cp = rc + c.w;
-        const float r = restrict_cell_all(f.fluid, f.w, f.cells, f.diag, f.px, f.py, f.res, f.err, rc % c.w,
-                                          rc / c.w);
+        uint32_t cx, cy;
+        raw_xy(rc, c.w, c.wshift, cx, cy);
+        const float r = restrict_cell_all(f.fluid, f.w, f.cells, f.diag, f.px, f.py, f.res, f.err, cx, cy);
         const float inv = c.inv_diag[cp];
         if (!fluid) continue;
         c.res[cp] = r;
-        if (with_red && is_red(rc, c.w)) c.err[cp] = inv != 0.0f ? 0.0f + (kOmega * (r * inv - 0.0f)) : 0.0f;
+        if (with_red && ((cx + cy) & 1u) == 0u) c.err[cp] = inv != 0.0f ? 0.0f + (kOmega * (r * inv - 0.0f)) : 0.0f;
     }
 }
 
@@ -444,17 +455,20 @@ __device__ __forceinline__ void ph_prolong(const Level& c, const Level& f, uint3
     const float* ce = c.err;
     const uint32_t fw = f.w, cw = c.w;
     const long long fcells = f.cells;
+    const int fs = f.wshift;
     // coarse error under fine raw index rf; rf outside the grid (a neighbour
     // whose value a select drops) is clamped so the load stays in bounds
     auto coarse_e = [=](long long rf) {
         const uint32_t r = uint32_t(rf < 0 ? 0 : (rf >= fcells ? fcells - 1 : rf));
-        return ce[((r / fw) / 2) * cw + (r % fw) / 2 + cw];
+        uint32_t x, y;
+        raw_xy(r, fw, fs, x, y);
+        return ce[(y >> 1) * cw + (x >> 1) + cw];
     };
     for (uint32_t s = warp, nxt = seg_first(f.seg, nseg_f, warp, w0); s < nseg_f; s += nwarps) {
         const uint32_t word = nxt;
         nxt = seg_next(f.seg, nseg_f, s + nwarps);
         const uint32_t raw = word * 32 + lane;
-        if (raw >= f.cells || int(!is_red(raw, fw)) != color) continue;
+        if (raw >= f.cells || int(!red_at(raw, fw, fs)) != color) continue;
         const bool fluid = (f.fluid[word] >> lane) & 1u;
         const uint32_t p = raw + fw;
         const float old = prolonged(fe[p], coarse_e(raw), p == last ? extra : 0u);
@@ -490,8 +504,10 @@ __device__ __forceinline__ F2 ph_prolong_red_rz(const Level& c, const Level& f, 
         const bool fluid = (f.fluid[word] >> lane) & 1u;
         const uint32_t p = raw + fw;
         float z;
-        if (is_red(raw, fw)) {
-            const float ec = ce[((raw / fw) / 2) * cw + (raw % fw) / 2 + cw];
+        uint32_t x, y;
+        raw_xy(raw, fw, f.wshift, x, y);
+        if (((x + y) & 1u) == 0u) {
+            const float ec = ce[(y >> 1) * cw + (x >> 1) + cw];
             const float old = prolonged(fe[p], ec, p == last ? extra : 0u);
             z = sor_cell_all(f.fluid, fw, f.cells, f.inv_diag, f.px, f.py, f.res, raw, p, old, true,
                              [fe](uint32_t q, long long) { return fe[q]; });
@@ -576,9 +592,10 @@ __device__ __forceinline__ void cta_tail(const TailParams& tp, uint32_t* sm, boo
         cta_sweep(f, 0, 1);
         cta_sweep(f, 1, 1);
         for (uint32_t rc = threadIdx.x; rc < c.cells; rc += blockDim.x) {
-            const float r = restrict_cell_all(f.bits, f.w, f.cells, f.diag, f.px, f.py, f.res, f.err, rc % c.w,
-                                              rc / c.w);
-            if (bit_at(c.bits, rc)) c.res[rc + c.w] = r;
+            if (!bit_at(c.bits, rc)) continue;
+            uint32_t cx, cy;
+            raw_xy(rc, c.w, c.wshift, cx, cy);
+            c.res[rc + c.w] = restrict_cell_all(f.bits, f.w, f.cells, f.diag, f.px, f.py, f.res, f.err, cx, cy);
         }
         __syncthreads();
     }
@@ -597,8 +614,9 @@ __device__ __forceinline__ void cta_tail(const TailParams& tp, uint32_t* sm, boo
         SmemLevel c = smem_level(sm, tp.lv[l + 1]);
         for (uint32_t r = threadIdx.x; r < f.cells; r += blockDim.x)
             if (bit_at(f.bits, r)) {
-                uint32_t cx = (r % f.w) / 2, cy = (r / f.w) / 2;
-                f.err[r + f.w] = f.err[r + f.w] + c.err[cy * c.w + cx + c.w];
+                uint32_t x, y;
+                raw_xy(r, f.w, f.wshift, x, y);
+                f.err[r + f.w] = f.err[r + f.w] + c.err[(y >> 1) * c.w + (x >> 1) + c.w];
             }
         __syncthreads();
         cta_sweep(f, 1, 0);
@@ -623,7 +641,10 @@ inline TailParams make_tail_params(const Scene& s, int first, uint32_t* words_ou
     for (int k = 0; k < tp.n; ++k) {
         const Level& v = s.lv[first + k];
         TailLevel& t = tp.lv[k];
-        t.w = v.w; t.cells = v.cells; t.words = v.words; t.padded = v.padded;
+        t.w = v.w; t.h = v.h; t.cells = v.cells; t.words = v.words; t.padded = v.padded;
+        t.wshift = -1;
+        for (int k = 0; k < 31; ++k)
+            if ((1u << k) == v.w) t.wshift = k;
         t.fluid = v.fluid; t.diag = v.diag; t.inv = v.inv_diag; t.px = v.px; t.py = v.py;
         t.res = v.res; t.err = v.err;
         t.o_bits = off; off += v.words;

@@ -157,10 +157,9 @@ __device__ __forceinline__ void dsm_sweep(const View& v, const cg::cluster_group
         const int y = v.y0 + row;
         const int x = 2 * k + ((y + color) & 1);
         const int o = row * v.w + x;
+        if (!flb(v, o + v.w)) continue;  // only fluid cells store
         const float old = init ? 0.0f : v.err[o];
-        const float z = sor_dsm(v, x, y, old, !(init && color == 0),
-                                [&](int r, int, int) { return err_raw(v, cl, r); });
-        if (flb(v, o + v.w)) v.err[o] = z;
+        v.err[o] = sor_dsm(v, x, y, old, !(init && color == 0), [&](int r, int, int) { return err_raw(v, cl, r); });
     }
 }
 
@@ -180,6 +179,9 @@ __device__ __forceinline__ void dsm_restrict(const View& f, const cg::cluster_gr
         int row, cx;
         split(i, wc, f.half_shift, row, cx);
         const int cy = yc0 + row;
+        const int craw = cy * wc + cx;
+        // only fluid coarse cells store
+        if (c ? !flb(*c, craw - c->lo + wc) : !bit_at(p.tfluid, uint32_t(craw))) continue;
         float sum = 0.0f;
 #pragma unroll
         for (int dy = 0; dy < 2; ++dy)
@@ -202,16 +204,14 @@ __device__ __forceinline__ void dsm_restrict(const View& f, const cg::cluster_gr
                 t = sum + (b - ax);
                 sum = f0 ? t : sum;
             }
-        const int craw = cy * wc + cx;
         if (c) {
             const int co = craw - c->lo;
-            if (!flb(*c, co + wc)) continue;
             c->res[co] = sum;
             if (with_red && ((cx + cy) & 1) == 0) {
                 const float inv = c->inv[co + wc];
                 c->err[co] = inv != 0.0f ? 0.0f + (kOmega * (sum * inv - 0.0f)) : 0.0f;
             }
-        } else if (bit_at(p.tfluid, uint32_t(craw))) {
+        } else {
             tail_res[craw + wc] = sum;  // CTA 0's shared memory
         }
     }
@@ -239,6 +239,7 @@ __device__ __forceinline__ void dsm_prolong(const View& f, const cg::cluster_gro
         const int y = f.y0 + row;
         const int x = 2 * k + ((y + color) & 1);
         const int o = row * f.w + x;
+        if (!flb(f, o + f.w)) continue;  // only fluid cells store
         const float old = prolonged(f.err[o], coarse_e(x, y), 0u);
         float z;
         if (color == 1)
@@ -247,7 +248,7 @@ __device__ __forceinline__ void dsm_prolong(const View& f, const cg::cluster_gro
             });
         else
             z = sor_dsm(f, x, y, old, true, [&](int r, int, int) { return err_raw(f, cl, r); });
-        if (flb(f, o + f.w)) f.err[o] = z;
+        f.err[o] = z;
     }
 }
 
