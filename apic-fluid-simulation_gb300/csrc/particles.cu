@@ -44,10 +44,11 @@ namespace {
 //   k_p2g_bounds    each cell's run [lo, hi) in the sorted pairs
 //   k_p2g_gather    per 32 x 8 tile of cells: stage the particles of the
 //                   tile's cells and a two-cell halo below and to the left in
-//                   shared memory, compute their stencil contributions once
-//                   per grid, then let each face merge the runs of the (up to
-//                   six) cells whose particles can reach it by slot and fold
-//                   the contributions in (chunk, corner, lane) order.
+//                   shared memory (in bands of rows when they do not fit),
+//                   compute their stencil contributions once per grid, then
+//                   let each face merge the runs of the (up to six) cells
+//                   whose particles can reach it by slot and fold the
+//                   contributions in (chunk, corner, lane) order.
 //
 // Which cells can reach a face follows from the clamped index arithmetic
 // (u_index / v_index, :1029-1041): the u stencil's rows equal the density
@@ -220,18 +221,22 @@ __device__ __forceinline__ bool p2g_record(const PartPtrs* __restrict__ pp, uint
 }
 
 // Records staged in shared memory (fast path) or computed from global memory
-// when they are needed (tiles with more than kGatherCap particles).
+// when they are needed (regions with more particles than the stage holds).
+// A staged slot carries kLastInRun in bit 31 when it is the last particle of
+// its cell's run (slots are below 2^31).
+constexpr uint32_t kLastInRun = 0x80000000u;
 struct StagedRecs {
+    static constexpr bool kStaged = true;
     const uint32_t* slot;
     const uint32_t* code;
     const float* val;  // [4][kGatherCap]
     const float* w;    // [4][kGatherCap]
-    __device__ __forceinline__ uint32_t slot_at(int p) const { return slot[p]; }
     __device__ __forceinline__ uint32_t code_at(int p) const { return code[p]; }
     __device__ __forceinline__ float val_at(int k, int p) const { return val[k * kGatherCap + p]; }
     __device__ __forceinline__ float w_at(int k, int p) const { return w[k * kGatherCap + p]; }
 };
 struct GlobalRecs {
+    static constexpr bool kStaged = false;
     const uint32_t* vals;  // sorted slots
     const PartPtrs* pp;
     int grid, W, H;
@@ -249,49 +254,19 @@ struct GlobalRecs {
     __device__ __forceinline__ float w_at(int k, int p) const { return rec(p).w[k]; }
 };
 
-// Fold of one face: merge NR slot-ordered runs [b, e) by slot; run r's records
-// reach this face through the corners in bits sh[r] .. sh[r] + 3 of their
-// code.  Consecutive records of one chunk form the chunk's groups: per corner
-// k, the lanes' contributions summed in lane order; at the end of the chunk
-// the groups are added to the face in corner order.
-template <int NR, bool kVal, class Recs>
-__device__ __forceinline__ void fold_face(const Recs& R, int (&b)[NR], const int (&e)[NR], const int (&sh)[NR],
-                                          float& out_v, float& out_w) {
-    uint32_t hs[NR];
-#pragma unroll
-    for (int r = 0; r < NR; ++r) hs[r] = b[r] < e[r] ? R.slot_at(b[r]) : 0xFFFFFFFFu;
+// The fold of one face over its contributions in slot order.  Consecutive
+// contributions of one chunk form the chunk's groups: per corner k, the
+// lanes' contributions summed in lane order; at the end of the chunk the
+// groups are added to the face in corner order.
+struct FaceFold {
     float acc_v = 0.0f, acc_w = 0.0f;
     float gv[4] = {0.0f, 0.0f, 0.0f, 0.0f}, gw[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     uint32_t gm = 0, chunk = 0xFFFFFFFFu;
-    for (;;) {
-        uint32_t best = hs[0];
-        int m = 0;
-#pragma unroll
-        for (int r = 1; r < NR; ++r)
-            if (hs[r] < best) { best = hs[r]; m = r; }
-        if (best == 0xFFFFFFFFu) break;
-        int p = 0, s = 0;
-#pragma unroll
-        for (int r = 0; r < NR; ++r)
-            if (r == m) {
-                p = b[r];
-                s = sh[r];
-                b[r] = p + 1;
-                hs[r] = b[r] < e[r] ? R.slot_at(b[r]) : 0xFFFFFFFFu;
-            }
-        const uint32_t hit = (R.code_at(p) >> s) & 0xFu;
-        if (!hit) continue;
-        if ((best >> 3) != chunk) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (gm & (1u << k)) {
-                    if (kVal) acc_v = acc_v + gv[k];
-                    acc_w = acc_w + gw[k];
-                }
-#pragma unroll
-            for (int k = 0; k < 4; ++k) { gv[k] = 0.0f; gw[k] = 0.0f; }
-            gm = 0;
-            chunk = best >> 3;
+    template <bool kVal, class Recs>
+    __device__ __forceinline__ void add(const Recs& R, uint32_t slot, int p, uint32_t hit) {
+        if ((slot >> 3) != chunk) {
+            flush<kVal>();
+            chunk = slot >> 3;
         }
         // only the corners that land here are read (usually one)
 #pragma unroll
@@ -302,14 +277,79 @@ __device__ __forceinline__ void fold_face(const Recs& R, int (&b)[NR], const int
             }
         gm |= hit;
     }
+    template <bool kVal>
+    __device__ __forceinline__ void flush() {
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-        if (gm & (1u << k)) {
-            if (kVal) acc_v = acc_v + gv[k];
-            acc_w = acc_w + gw[k];
+        for (int k = 0; k < 4; ++k)
+            if (gm & (1u << k)) {
+                if (kVal) acc_v = acc_v + gv[k];
+                acc_w = acc_w + gw[k];
+            }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { gv[k] = 0.0f; gw[k] = 0.0f; }
+        gm = 0;
+    }
+};
+
+// Fold of one face: merge NR slot-ordered runs [b, e) by slot; run r's
+// records reach this face through the corners in bits 4r .. 4r + 3 of their
+// code.
+//
+// Staged form: each run's head is one 64-bit key (slot << 32 | position << 5
+// | last-in-run << 4 | run), so the merge step is a minimum over NR keys and
+// the head's successor is the next staged position unless the head ends its
+// run.  Global form: positions and ends in registers.
+template <int NR, bool kVal, class Recs>
+__device__ __forceinline__ void fold_face(const Recs& R, int (&b)[NR], const int (&e)[NR], float& out_v,
+                                          float& out_w) {
+    FaceFold f;
+    if constexpr (Recs::kStaged) {
+        auto key_at = [&](uint32_t p, uint32_t r) {
+            const uint32_t sw = R.slot[p];
+            return (uint64_t(sw & ~kLastInRun) << 32) | (uint64_t(p) << 5) | (uint64_t(sw >> 31) << 4) | uint64_t(r);
+        };
+        uint64_t key[NR];
+#pragma unroll
+        for (int r = 0; r < NR; ++r) key[r] = b[r] < e[r] ? key_at(uint32_t(b[r]), uint32_t(r)) : ~0ull;
+        for (;;) {
+            uint64_t best = key[0];
+#pragma unroll
+            for (int r = 1; r < NR; ++r) best = key[r] < best ? key[r] : best;
+            if (best == ~0ull) break;
+            const uint32_t m = uint32_t(best) & 0xFu;
+            const uint32_t p = uint32_t(best >> 5) & 0x07FFFFFFu;
+            const uint64_t nk = ((best >> 4) & 1u) ? ~0ull : key_at(p + 1u, m);
+#pragma unroll
+            for (int r = 0; r < NR; ++r) key[r] = uint32_t(r) == m ? nk : key[r];
+            const uint32_t hit = (R.code_at(int(p)) >> (4u * m)) & 0xFu;
+            if (hit) f.template add<kVal>(R, uint32_t(best >> 32), int(p), hit);
         }
-    out_v = acc_v;
-    out_w = acc_w;
+    } else {
+        uint32_t hs[NR];
+#pragma unroll
+        for (int r = 0; r < NR; ++r) hs[r] = b[r] < e[r] ? R.slot_at(b[r]) : 0xFFFFFFFFu;
+        for (;;) {
+            uint32_t best = hs[0];
+            int m = 0;
+#pragma unroll
+            for (int r = 1; r < NR; ++r)
+                if (hs[r] < best) { best = hs[r]; m = r; }
+            if (best == 0xFFFFFFFFu) break;
+            int p = 0;
+#pragma unroll
+            for (int r = 0; r < NR; ++r)
+                if (r == m) {
+                    p = b[r];
+                    b[r] = p + 1;
+                    hs[r] = b[r] < e[r] ? R.slot_at(b[r]) : 0xFFFFFFFFu;
+                }
+            const uint32_t hit = (R.code_at(p) >> (4 * m)) & 0xFu;
+            if (hit) f.template add<kVal>(R, best, p, hit);
+        }
+    }
+    f.template flush<kVal>();
+    out_v = f.acc_v;
+    out_w = f.acc_w;
 }
 
 struct GatherOut {
@@ -317,7 +357,8 @@ struct GatherOut {
 };
 
 // The faces and cells of this thread's cell (i, j) for one grid; bin(x, y)
-// gives a cell's run (empty outside the grid).
+// gives a cell's run (empty outside the grid).  Run r of a face is the cell
+// at offset (rx, ry) with r = ry * nx + rx, the index p2g_record codes.
 template <class Recs, class Bin>
 __device__ __forceinline__ void fold_cell(const Recs& R, const Bin& bin, int grid, int i, int j, int W, int H,
                                           const GatherOut& o) {
@@ -328,48 +369,42 @@ __device__ __forceinline__ void fold_cell(const Recs& R, const Bin& bin, int gri
     if (grid == kGridU) {
         // u face (fi, j), and (W, j) from the last column's thread
         for (int fi = i; fi <= (i == W - 1 ? W : i); ++fi) {
-            int b[6], e[6], sh[6];
+            int b[6], e[6];
 #pragma unroll
-            for (int r = 0; r < 6; ++r) {
-                const int rx = r % 3, ry = r / 3;  // face offset from the cell
-                run(fi - rx, j - ry, b[r], e[r]);
-                sh[r] = 4 * (ry * 3 + rx);
-            }
+            for (int r = 0; r < 6; ++r) run(fi - r % 3, j - r / 3, b[r], e[r]);
             float v, w;
-            fold_face<6, true>(R, b, e, sh, v, w);
+            fold_face<6, true>(R, b, e, v, w);
             const uint32_t f = uint32_t(j) * uint32_t(W + 1) + uint32_t(fi);
             o.acc_u[f] = v;
             o.acc_uw[f] = w;
         }
     } else if (grid == kGridV) {
         for (int fj = j; fj <= (j == H - 1 ? H : j); ++fj) {
-            int b[6], e[6], sh[6];
+            int b[6], e[6];
 #pragma unroll
-            for (int r = 0; r < 6; ++r) {
-                const int rx = r % 2, ry = r / 2;
-                run(i - rx, fj - ry, b[r], e[r]);
-                sh[r] = 4 * (ry * 2 + rx);
-            }
+            for (int r = 0; r < 6; ++r) run(i - r % 2, fj - r / 2, b[r], e[r]);
             float v, w;
-            fold_face<6, true>(R, b, e, sh, v, w);
+            fold_face<6, true>(R, b, e, v, w);
             const uint32_t f = uint32_t(fj) * uint32_t(W) + uint32_t(i);
             o.acc_v[f] = v;
             o.acc_vw[f] = w;
         }
     } else {
-        int b[4], e[4], sh[4];
+        int b[4], e[4];
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int rx = r % 2, ry = r / 2;
-            run(i - rx, j - ry, b[r], e[r]);
-            sh[r] = 4 * (ry * 2 + rx);
-        }
+        for (int r = 0; r < 4; ++r) run(i - r % 2, j - r / 2, b[r], e[r]);
         float v, w;
-        fold_face<4, false>(R, b, e, sh, v, w);
+        fold_face<4, false>(R, b, e, v, w);
         o.dens[uint32_t(j) * uint32_t(W) + uint32_t(i)] = w;
     }
 }
 
+// One CTA per 32 x 8 tile.  The region's cell counts are scanned once; when
+// the region holds more particles than the stage (dense scenes: the
+// reference's default block has 9 per cell), the tile is processed as 2, 4
+// or 8 bands of rows, each staging only its own region (band rows plus the
+// two-row halo); a single row whose region still overflows reads its records
+// from global memory.
 __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs* __restrict__ pp,
                                                                   const uint32_t* __restrict__ vals,
                                                                   const uint32_t* __restrict__ lo,
@@ -385,7 +420,7 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
     float* s_wt = s_gy + kGatherCap;
     uint32_t* s_off = reinterpret_cast<uint32_t*>(s_wt + kGatherCap);  // kRegionBins + 1
     uint32_t* s_glo = s_off + kRegionBins + 1;                            // kRegionBins
-    __shared__ uint32_t s_total;
+    __shared__ uint32_t s_total, s_band;
     __shared__ uint32_t s_rowg[kRegionH];
 
     const int x0 = blockIdx.x * kGatherTW, y0 = blockIdx.y * kGatherTH;
@@ -425,12 +460,23 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
         const int rb = 2 * threadIdx.x + h;
         if (rb < kRegionBins && cnt[h] > 0) atomicMin(&s_rowg[rb / kRegionW], s_glo[rb]);
     }
+    if (threadIdx.x == 0) {
+        // the tallest band whose every region fits the stage (0: none)
+        uint32_t band = 0;
+        for (uint32_t th = kGatherTH; th >= 1 && !band; th >>= 1) {
+            bool fits = true;
+            for (uint32_t r0 = 0; r0 < uint32_t(kGatherTH); r0 += th)
+                fits = fits && s_off[(r0 + th + 2) * kRegionW] - s_off[r0 * kRegionW] <= uint32_t(kGatherCap);
+            if (fits) band = th;
+        }
+        s_band = band;
+    }
     __syncthreads();
-    const uint32_t P = s_total;
+    const uint32_t band = s_band;
 
-    if (P > uint32_t(kGatherCap)) {
-        // more particles than the stage holds: every face reads its runs from
-        // global memory and computes the records it needs on the fly
+    if (band == 0) {
+        // more particles than the stage holds even for one row: every face
+        // reads its runs from global memory and computes the records it needs
         for (int g = 0; g < 3; ++g) {
             GlobalRecs R{vals, pp, g, W, H, dx, prev_dt, &ctl->status};
             auto bin = [&](int x, int y, int& b, int& e) {
@@ -442,42 +488,52 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
         }
         return;
     }
-    // stage the slots: each region row is one contiguous range of the sorted pairs
-    for (int r = 0; r < kRegionH; ++r) {
-        const uint32_t s0 = s_off[r * kRegionW], s1 = s_off[(r + 1) * kRegionW];
-        const uint32_t g0 = s_rowg[r];
-        for (uint32_t q = threadIdx.x; q < s1 - s0; q += kGatherThreads) s_slot[s0 + q] = vals[g0 + q];
-    }
-    __syncthreads();
-    for (uint32_t p = threadIdx.x; p < P; p += kGatherThreads) {
-        const P2gBase bs = p2g_base(pp, s_slot[p], dx, prev_dt);
-        s_gx[p] = bs.gx;
-        s_gy[p] = bs.gy;
-        s_wt[p] = bs.wt;
-    }
     const StagedRecs R{s_slot, s_code, s_val, s_w};
-    auto bin = [&](int x, int y, int& b, int& e) {
-        const int rb = (y - ry0) * kRegionW + (x - rx0);
-        b = int(s_off[rb]);
-        e = int(s_off[rb + 1]);
-    };
-    for (int g = 0; g < 3; ++g) {
-        bool bad = false;
-        for (uint32_t p = threadIdx.x; p < P; p += kGatherThreads) {
-            P2gRec rec;
-            const P2gBase bs{s_gx[p], s_gy[p], s_wt[p]};
-            if (!p2g_record(pp, s_slot[p], bs, g, W, H, dx, rec)) bad = true;
-            s_code[p] = rec.code;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (g != kGridD) s_val[k * kGatherCap + p] = rec.val[k];
-                s_w[k * kGatherCap + p] = rec.w[k];
-            }
+    for (uint32_t r0 = 0; r0 < uint32_t(kGatherTH); r0 += band) {
+        const uint32_t r1 = r0 + band + 2;  // region rows [r0, r1)
+        const uint32_t base = s_off[r0 * kRegionW];
+        const uint32_t P = s_off[r1 * kRegionW] - base;
+        // stage the slots: each region row is one contiguous range of the sorted pairs
+        for (uint32_t r = r0; r < r1; ++r) {
+            const uint32_t s0 = s_off[r * kRegionW] - base, s1 = s_off[(r + 1) * kRegionW] - base;
+            const uint32_t g0 = s_rowg[r];
+            for (uint32_t q = threadIdx.x; q < s1 - s0; q += kGatherThreads) s_slot[s0 + q] = vals[g0 + q];
         }
-        if (bad) atomicOr(&ctl->status, kStatusP2gLayout);
         __syncthreads();
-        if (cell) fold_cell(R, bin, g, i, j, W, H, o);
+        // mark each run's last particle (a select in the merge reads it)
+        for (uint32_t rb = r0 * kRegionW + threadIdx.x; rb < r1 * kRegionW; rb += kGatherThreads)
+            if (s_off[rb + 1] > s_off[rb]) s_slot[s_off[rb + 1] - 1u - base] |= kLastInRun;
         __syncthreads();
+        for (uint32_t p = threadIdx.x; p < P; p += kGatherThreads) {
+            const P2gBase bs = p2g_base(pp, s_slot[p] & ~kLastInRun, dx, prev_dt);
+            s_gx[p] = bs.gx;
+            s_gy[p] = bs.gy;
+            s_wt[p] = bs.wt;
+        }
+        auto bin = [&](int x, int y, int& b, int& e) {
+            const int rb = (y - ry0) * kRegionW + (x - rx0);
+            b = int(s_off[rb] - base);
+            e = int(s_off[rb + 1] - base);
+        };
+        const bool mine = cell && uint32_t(ty) >= r0 && uint32_t(ty) < r0 + band;
+        for (int g = 0; g < 3; ++g) {
+            bool bad = false;
+            for (uint32_t p = threadIdx.x; p < P; p += kGatherThreads) {
+                P2gRec rec;
+                const P2gBase bs{s_gx[p], s_gy[p], s_wt[p]};
+                if (!p2g_record(pp, s_slot[p] & ~kLastInRun, bs, g, W, H, dx, rec)) bad = true;
+                s_code[p] = rec.code;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (g != kGridD) s_val[k * kGatherCap + p] = rec.val[k];
+                    s_w[k * kGatherCap + p] = rec.w[k];
+                }
+            }
+            if (bad) atomicOr(&ctl->status, kStatusP2gLayout);
+            __syncthreads();
+            if (mine) fold_cell(R, bin, g, i, j, W, H, o);
+            __syncthreads();
+        }
     }
 }
 
