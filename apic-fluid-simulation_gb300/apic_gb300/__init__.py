@@ -30,6 +30,7 @@ OPT_PDL = 4
 OPT_DSM_VCYCLE = 5
 OPT_WARM_START = 7
 OPT_STREAM_PRIORITY = 8
+OPT_P2G_ORDER = 9  # 0 follow the solver mode, 1 the reference's order, 2 cell order
 
 FIELDS = {
     "pos_x": 0, "pos_y": 1, "vel_x": 2, "vel_y": 3, "cu_x": 4, "cu_y": 5, "cv_x": 6, "cv_y": 7, "tres": 8,

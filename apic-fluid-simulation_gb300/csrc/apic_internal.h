@@ -177,6 +177,7 @@ struct Scene {
     double* b64 = nullptr;                    // FP64 right-hand side (padded)
     bool p64_valid = false;                   // p64 holds the refined pressure (mixed mode)
     bool warm_start = true;                   // mixed mode: start from the previous solve's FP64 pressure
+    int p2g_order = 0;                        // APIC_OPT_P2G_ORDER (0: follow the solver mode)
 
     int nlevels = 0;                          // including the base (levels[0])
     int tail_first = 0;                       // first level of the shared-memory tail (nlevels: none)
@@ -246,6 +247,10 @@ inline float2* part_rz(const Scene& s) { return reinterpret_cast<float2*>(s.part
 // The mixed-precision solve starts from the FP64 pressure that the previous
 // solve left in p64 (zeroed whenever the particle set is replaced).
 inline int warm_start(const Scene& s) { return s.warm_start && s.solver_mode == APIC_SOLVER_REL_MIXED ? 1 : 0; }
+// P2G adds each face's contributions in the reference's order (else in cell order).
+inline bool p2g_reference_order(const Scene& s) {
+    return s.p2g_order == 1 || (s.p2g_order == 0 && s.solver_mode == APIC_SOLVER_REFERENCE);
+}
 // The reference solver mode reproduces the reference's FP32 reduction orders
 // (dot_product's eight lane sums, apply_matrix_and_dot's 8192-cell chunks,
 // the coarsest CG's serial sums), so its pressure is bit-identical to the

@@ -299,9 +299,39 @@ struct FaceFold {
 // | last-in-run << 4 | run), so the merge step is a minimum over NR keys and
 // the head's successor is the next staged position unless the head ends its
 // run.  Global form: positions and ends in registers.
-template <int NR, bool kVal, class Recs>
+template <int NR, bool kVal, bool kRef, class Recs>
 __device__ __forceinline__ void fold_face(const Recs& R, int (&b)[NR], const int (&e)[NR], float& out_v,
                                           float& out_w) {
+    if constexpr (!kRef) {
+        // cell order: the runs one after another, slots ascending in each,
+        // the corners that land here in corner order
+        float av = 0.0f, aw = 0.0f;
+#pragma unroll
+        for (int r = 0; r < NR; ++r)
+            for (int p = b[r]; p < e[r]; ++p) {
+                if constexpr (Recs::kStaged) {
+                    const uint32_t hit = (R.code_at(p) >> (4 * r)) & 0xFu;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (hit & (1u << k)) {
+                            if (kVal) av = av + R.val_at(k, p);
+                            aw = aw + R.w_at(k, p);
+                        }
+                } else {
+                    const P2gRec rr = R.rec(p);
+                    const uint32_t hit = (rr.code >> (4 * r)) & 0xFu;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (hit & (1u << k)) {
+                            if (kVal) av = av + rr.val[k];
+                            aw = aw + rr.w[k];
+                        }
+                }
+            }
+        out_v = av;
+        out_w = aw;
+        return;
+    }
     FaceFold f;
     if constexpr (Recs::kStaged) {
         auto key_at = [&](uint32_t p, uint32_t r) {
@@ -359,7 +389,7 @@ struct GatherOut {
 // The faces and cells of this thread's cell (i, j) for one grid; bin(x, y)
 // gives a cell's run (empty outside the grid).  Run r of a face is the cell
 // at offset (rx, ry) with r = ry * nx + rx, the index p2g_record codes.
-template <class Recs, class Bin>
+template <bool kRef, class Recs, class Bin>
 __device__ __forceinline__ void fold_cell(const Recs& R, const Bin& bin, int grid, int i, int j, int W, int H,
                                           const GatherOut& o) {
     auto run = [&](int x, int y, int& b, int& e) {
@@ -373,7 +403,7 @@ __device__ __forceinline__ void fold_cell(const Recs& R, const Bin& bin, int gri
 #pragma unroll
             for (int r = 0; r < 6; ++r) run(fi - r % 3, j - r / 3, b[r], e[r]);
             float v, w;
-            fold_face<6, true>(R, b, e, v, w);
+            fold_face<6, true, kRef>(R, b, e, v, w);
             const uint32_t f = uint32_t(j) * uint32_t(W + 1) + uint32_t(fi);
             o.acc_u[f] = v;
             o.acc_uw[f] = w;
@@ -384,7 +414,7 @@ __device__ __forceinline__ void fold_cell(const Recs& R, const Bin& bin, int gri
 #pragma unroll
             for (int r = 0; r < 6; ++r) run(i - r % 2, fj - r / 2, b[r], e[r]);
             float v, w;
-            fold_face<6, true>(R, b, e, v, w);
+            fold_face<6, true, kRef>(R, b, e, v, w);
             const uint32_t f = uint32_t(fj) * uint32_t(W) + uint32_t(i);
             o.acc_v[f] = v;
             o.acc_vw[f] = w;
@@ -394,7 +424,7 @@ __device__ __forceinline__ void fold_cell(const Recs& R, const Bin& bin, int gri
 #pragma unroll
         for (int r = 0; r < 4; ++r) run(i - r % 2, j - r / 2, b[r], e[r]);
         float v, w;
-        fold_face<4, false>(R, b, e, v, w);
+        fold_face<4, false, kRef>(R, b, e, v, w);
         o.dens[uint32_t(j) * uint32_t(W) + uint32_t(i)] = w;
     }
 }
@@ -404,7 +434,9 @@ __device__ __forceinline__ void fold_cell(const Recs& R, const Bin& bin, int gri
 // reference's default block has 9 per cell), the tile is processed as 2, 4
 // or 8 bands of rows, each staging only its own region (band rows plus the
 // two-row halo); a single row whose region still overflows reads its records
-// from global memory.
+// from global memory.  kRef: the reference's order, else cell order
+// (APIC_OPT_P2G_ORDER).
+template <bool kRef>
 __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs* __restrict__ pp,
                                                                   const uint32_t* __restrict__ vals,
                                                                   const uint32_t* __restrict__ lo,
@@ -484,7 +516,7 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
                 b = int(lo[c]);
                 e = int(hi[c]);
             };
-            if (cell) fold_cell(R, bin, g, i, j, W, H, o);
+            if (cell) fold_cell<kRef>(R, bin, g, i, j, W, H, o);
         }
         return;
     }
@@ -500,10 +532,12 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
             for (uint32_t q = threadIdx.x; q < s1 - s0; q += kGatherThreads) s_slot[s0 + q] = vals[g0 + q];
         }
         __syncthreads();
-        // mark each run's last particle (a select in the merge reads it)
-        for (uint32_t rb = r0 * kRegionW + threadIdx.x; rb < r1 * kRegionW; rb += kGatherThreads)
-            if (s_off[rb + 1] > s_off[rb]) s_slot[s_off[rb + 1] - 1u - base] |= kLastInRun;
-        __syncthreads();
+        if constexpr (kRef) {
+            // mark each run's last particle (the merge reads it)
+            for (uint32_t rb = r0 * kRegionW + threadIdx.x; rb < r1 * kRegionW; rb += kGatherThreads)
+                if (s_off[rb + 1] > s_off[rb]) s_slot[s_off[rb + 1] - 1u - base] |= kLastInRun;
+            __syncthreads();
+        }
         for (uint32_t p = threadIdx.x; p < P; p += kGatherThreads) {
             const P2gBase bs = p2g_base(pp, s_slot[p] & ~kLastInRun, dx, prev_dt);
             s_gx[p] = bs.gx;
@@ -531,7 +565,7 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
             }
             if (bad) atomicOr(&ctl->status, kStatusP2gLayout);
             __syncthreads();
-            if (mine) fold_cell(R, bin, g, i, j, W, H, o);
+            if (mine) fold_cell<kRef>(R, bin, g, i, j, W, H, o);
             __syncthreads();
         }
     }
@@ -721,7 +755,9 @@ static int bin_key_bits(const Scene& s) {
 // P2G stage; bin_lo / bin_hi and the base fluid mask must be zero (the
 // caller clears them), every accumulator entry is written.
 cudaError_t launch_p2g(Scene& s) {
-    cudaError_t e = cudaFuncSetAttribute(k_p2g_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGatherSmem));
+    const bool ref = p2g_reference_order(s);
+    auto gather = ref ? k_p2g_gather<true> : k_p2g_gather<false>;
+    cudaError_t e = cudaFuncSetAttribute(gather, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGatherSmem));
     if (e != cudaSuccess) return e;
     const uint32_t* svals = s.bin_vals;
     if (s.n > 0) {
@@ -737,7 +773,7 @@ cudaError_t launch_p2g(Scene& s) {
     }
     GatherOut o{s.acc_u, s.acc_uw, s.acc_v, s.acc_vw, s.density};
     dim3 grid(div_up(s.W, kGatherTW), div_up(s.H, kGatherTH));
-    launch(s.use_pdl && s.n > 0, k_p2g_gather, grid, kGatherThreads, kGatherSmem, s.stream,
+    launch(s.use_pdl && s.n > 0, gather, grid, kGatherThreads, kGatherSmem, s.stream,
            static_cast<const PartPtrs*>(s.pp), svals, static_cast<const uint32_t*>(s.bin_lo),
            static_cast<const uint32_t*>(s.bin_hi), int(s.W), int(s.H), s.dx, s.ctl, o);
     return cudaGetLastError();

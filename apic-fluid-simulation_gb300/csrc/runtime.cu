@@ -1337,6 +1337,11 @@ int apic_set_option(apic_handle* h, int option, int value) {
             s.warm_start = value != 0;
             invalidate_graphs(s);
             return APIC_OK;
+        case APIC_OPT_P2G_ORDER:
+            if (value < 0 || value > 2) return fail(APIC_ERR_INVALID_ARG, "P2G order must be 0, 1 or 2");
+            s.p2g_order = value;
+            invalidate_graphs(s);
+            return APIC_OK;
         case APIC_OPT_STREAM_PRIORITY: {
             if (value < 0) return fail(APIC_ERR_INVALID_ARG, "stream priority must be >= 0");
             // the scene's stream is idle (synchronised above): replace it by
@@ -1364,6 +1369,7 @@ int apic_get_option(apic_handle* h, int option, int* value) {
             return APIC_OK;
         case APIC_OPT_WARM_START: *value = h->s.warm_start ? 1 : 0; return APIC_OK;
         case APIC_OPT_STREAM_PRIORITY: *value = h->s.priority; return APIC_OK;
+        case APIC_OPT_P2G_ORDER: *value = p2g_reference_order(h->s) ? 1 : 2; return APIC_OK;
         default: return fail(APIC_ERR_INVALID_ARG, "unknown option");
     }
 }

@@ -506,7 +506,7 @@ int apic_server_set_mode(apic_server* sv, int mode, uint32_t prepare_threads) {
 int apic_server_scene_option(apic_server* sv, int option, int value, uint64_t min_cells, uint64_t max_cells) {
     if (!sv || min_cells > max_cells) return bad(APIC_ERR_INVALID_ARG, "apic_server_scene_option: bad argument");
     if (option != APIC_OPT_PDL && option != APIC_OPT_DSM_VCYCLE && option != APIC_OPT_WARM_START &&
-        option != APIC_OPT_STREAM_PRIORITY)
+        option != APIC_OPT_STREAM_PRIORITY && option != APIC_OPT_P2G_ORDER)
         return bad(APIC_ERR_INVALID_ARG, "apic_server_scene_option: unknown option");
     if (!sv->active.empty() || sv->pending > 0)
         return bad(APIC_ERR_INVALID_ARG, "apic_server_scene_option: scenes are running");

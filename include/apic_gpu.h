@@ -241,6 +241,20 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
  * GPU, the block scheduler starts the kernels of higher-priority streams
  * first.  Results do not change. */
 #define APIC_OPT_STREAM_PRIORITY 8
+/* Order in which P2G adds each face's contributions.  Every order is
+ * deterministic (two runs give the same bits).
+ *   1: the reference's single-thread order (transfer_particles_to_grid,
+ *      src/apic.rs:1218-1426, with add_to_mac's in-chunk merging): per chunk
+ *      of 8 slots and per corner the lanes' group sum, groups added in
+ *      (chunk, corner) order; bit-identical to the oracle.
+ *   2: cell order: the face's contributions by the cell of the particle's
+ *      density-stencil base (a fixed list of up to six cells per face), and
+ *      by slot within a cell; the same terms as order 1 in another order, so
+ *      the sums differ only in rounding.  About twice as fast.
+ *   0 (default): order 1 in APIC_SOLVER_REFERENCE, order 2 in the relative
+ *      solver modes (which have no counterpart in the reference).
+ * apic_get_option reports the order in use (1 or 2). */
+#define APIC_OPT_P2G_ORDER 9
 int apic_set_option(apic_handle* h, int option, int value);
 int apic_get_option(apic_handle* h, int option, int* value);
 

@@ -49,6 +49,8 @@ def test_lockstep_dam_break_with_forces(oracle_mod, mode):
     o, g = make_pair(oracle_mod, side, cs, props, scene)
     for sim in (o, g):
         sim.set_solver(mode, 1e-6, 500)
+    # the stage-by-stage comparison wants the oracle's P2G order in both modes
+    g.set_option(A.OPT_P2G_ORDER, 1)
     forces = {2: [(0.2, 0.3, 0.05, 150.0)], 3: [(0.25, 0.2, 0.06, -150.0)]}
     run_lockstep(o, g, 5, 1 / 240, props, cs, forces, exact=mode == A.SOLVER_REFERENCE)
 
@@ -275,3 +277,46 @@ def test_warm_start_option(oracle_mod):
         o.update(A.DebugOptions(), 1 / 240)
         its += o.stats().pcg_iterations_total
     assert iterations_close(its, totals[1]), (its, totals[1])
+
+
+P2G_CELL_ORDER_RTOL = 4e-6  # the same <= 24 terms per face in another order, relative to the field maximum
+
+
+def test_p2g_cell_order(oracle_mod):
+    """APIC_OPT_P2G_ORDER 2 (the relative solver modes' default) adds each
+    face's terms by cell, then by slot, instead of the reference's (chunk,
+    corner) order: fluid bits, lists and valid flags equal the oracle's, the
+    sums agree within a few float roundings, and the result is the same on
+    every run."""
+    props = A.WorldProperties(-9.81, 0.1, 5.0, 1e-5)
+    side = 128
+    cs = 1 / side
+    scene = A.scene_params(A.SCENE_DAM_BREAK, side, cell_size=cs, sub=2, seed=0, fluid_x=0.4, fluid_y=0.6)
+    o, g = make_pair(oracle_mod, side, cs, props, scene)
+    assert g.get_option(A.OPT_P2G_ORDER) == 1  # reference solver mode: the reference's order
+    run_lockstep(o, g, 3, 1 / 240, props, cs)
+    g.set_option(A.OPT_P2G_ORDER, 2)
+    assert g.get_option(A.OPT_P2G_ORDER) == 2
+    o.run_stage("p2g", 1 / 240)
+    g.run_stage("p2g", 1 / 240)
+    for f in ("fluid_bits", "fluid_list", "valid_u", "valid_v"):
+        eq(g.read_field(f), o.read_field(f), "cell-order p2g " + f)
+    first = {}
+    for f in ("u", "v", "density"):
+        a, b = g.read_field(f).astype(np.float64), o.read_field(f).astype(np.float64)
+        scale = float(np.max(np.abs(b)))
+        assert scale > 0
+        err = float(np.max(np.abs(a - b))) / scale
+        assert err <= P2G_CELL_ORDER_RTOL, (f, err)
+        first[f] = g.read_field(f).copy()
+    g.run_stage("p2g", 1 / 240)
+    for f in ("u", "v", "density"):
+        eq(g.read_field(f), first[f], "cell-order p2g, second run " + f)
+    # the relative modes default to cell order, the reference mode to the reference's
+    g.set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+    g.set_option(A.OPT_P2G_ORDER, 0)
+    assert g.get_option(A.OPT_P2G_ORDER) == 2
+    g.set_solver(A.SOLVER_REFERENCE, 1e-6, 500)
+    assert g.get_option(A.OPT_P2G_ORDER) == 1
+    with pytest.raises(A.ApicError):
+        g.set_option(A.OPT_P2G_ORDER, 3)
