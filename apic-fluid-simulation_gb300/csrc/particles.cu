@@ -571,6 +571,129 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
     }
 }
 
+// Cell order (APIC_OPT_P2G_ORDER 2), one CTA per 32 x 8 tile.  Each cell of
+// the tile's region (the tile plus two halo columns on the left and two halo
+// rows below) is summed by one thread: its particles in slot order, each
+// particle's corners in corner order, into one partial sum per relative face
+// position (6 u, 6 v, 4 density positions; the code bits of p2g_record).
+// Each face then adds the partial sums of the cells that reach it in run
+// order (the reference-order gather's cell offsets); empty cells are
+// skipped.  The terms are those of the reference's order; only the
+// association differs.  No particle is staged, so dense cells need no
+// fallback.
+constexpr int kCellRegion = kRegionW * kRegionH;  // 340
+struct CellPartials {
+    float uv[6][kCellRegion], uw[6][kCellRegion];
+    float vv[6][kCellRegion], vw[6][kCellRegion];
+    float dw[4][kCellRegion];
+    uint8_t has[kCellRegion];
+};
+
+template <int NQ, bool kVal>
+__device__ __forceinline__ void add_partials(const P2gRec& rec, float (&pv)[NQ], float (&pw)[NQ]) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        const uint32_t hit = (rec.code >> (4 * q)) & 0xFu;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (hit & (1u << k)) {
+                if (kVal) pv[q] = pv[q] + rec.val[k];
+                pw[q] = pw[q] + rec.w[k];
+            }
+    }
+}
+
+__global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_cells(const PartPtrs* __restrict__ pp,
+                                                                 const uint32_t* __restrict__ vals,
+                                                                 const uint32_t* __restrict__ lo,
+                                                                 const uint32_t* __restrict__ hi, int W, int H,
+                                                                 float dx, Ctl* __restrict__ ctl, GatherOut o) {
+    __shared__ CellPartials sp;
+    const int x0 = blockIdx.x * kGatherTW, y0 = blockIdx.y * kGatherTH;
+    const int rx0 = x0 - 2, ry0 = y0 - 2;
+    pdl_wait();
+    const float prev_dt = ctl->prev_dt;
+    bool bad = false;
+    for (int rc = threadIdx.x; rc < kCellRegion; rc += kGatherThreads) {
+        const int x = rx0 + rc % kRegionW, y = ry0 + rc / kRegionW;
+        uint32_t b = 0, e = 0;
+        if (x >= 0 && x < W && y >= 0 && y < H) {
+            const uint32_t c = uint32_t(y) * uint32_t(W) + uint32_t(x);
+            b = lo[c];
+            e = hi[c];
+        }
+        float uv[6] = {}, uw[6] = {}, vv[6] = {}, vw[6] = {}, dv[4] = {}, dw[4] = {};
+        for (uint32_t p = b; p < e; ++p) {
+            const uint32_t slot = vals[p];
+            const P2gBase bs = p2g_base(pp, slot, dx, prev_dt);
+            P2gRec rec;
+            if (!p2g_record(pp, slot, bs, kGridU, W, H, dx, rec)) bad = true;
+            add_partials<6, true>(rec, uv, uw);
+            if (!p2g_record(pp, slot, bs, kGridV, W, H, dx, rec)) bad = true;
+            add_partials<6, true>(rec, vv, vw);
+            if (!p2g_record(pp, slot, bs, kGridD, W, H, dx, rec)) bad = true;
+            add_partials<4, false>(rec, dv, dw);
+        }
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            sp.uv[q][rc] = uv[q];
+            sp.uw[q][rc] = uw[q];
+            sp.vv[q][rc] = vv[q];
+            sp.vw[q][rc] = vw[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) sp.dw[q][rc] = dw[q];
+        sp.has[rc] = e > b;
+    }
+    if (bad) atomicOr(&ctl->status, kStatusP2gLayout);
+    __syncthreads();
+    const int tx = threadIdx.x % kGatherTW, ty = threadIdx.x / kGatherTW;
+    const int i = x0 + tx, j = y0 + ty;
+    if (i >= W || j >= H) return;
+    // region index of cell (x, y), or -1 when it holds no particle (or lies
+    // outside the grid)
+    auto cell = [&](int x, int y) -> int {
+        if (x < 0 || y < 0 || x >= W || y >= H) return -1;
+        const int rc = (y - ry0) * kRegionW + (x - rx0);
+        return sp.has[rc] ? rc : -1;
+    };
+    for (int fi = i; fi <= (i == W - 1 ? W : i); ++fi) {
+        float av = 0.0f, aw = 0.0f;
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            const int rc = cell(fi - r % 3, j - r / 3);
+            if (rc >= 0) {
+                av = av + sp.uv[r][rc];
+                aw = aw + sp.uw[r][rc];
+            }
+        }
+        const uint32_t f = uint32_t(j) * uint32_t(W + 1) + uint32_t(fi);
+        o.acc_u[f] = av;
+        o.acc_uw[f] = aw;
+    }
+    for (int fj = j; fj <= (j == H - 1 ? H : j); ++fj) {
+        float av = 0.0f, aw = 0.0f;
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            const int rc = cell(i - r % 2, fj - r / 2);
+            if (rc >= 0) {
+                av = av + sp.vv[r][rc];
+                aw = aw + sp.vw[r][rc];
+            }
+        }
+        const uint32_t f = uint32_t(fj) * uint32_t(W) + uint32_t(i);
+        o.acc_v[f] = av;
+        o.acc_vw[f] = aw;
+    }
+    float aw = 0.0f;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int rc = cell(i - r % 2, j - r / 2);
+        if (rc >= 0) aw = aw + sp.dw[r][rc];
+    }
+    o.dens[uint32_t(j) * uint32_t(W) + uint32_t(i)] = aw;
+}
+
 // bilinear_interpolate, src/apic.rs:138-172.
 __device__ __forceinline__ float bilinear(const float w[4], const float v[4]) {
     float ws = w[0] + w[1] + w[2] + w[3];
@@ -756,8 +879,8 @@ static int bin_key_bits(const Scene& s) {
 // caller clears them), every accumulator entry is written.
 cudaError_t launch_p2g(Scene& s) {
     const bool ref = p2g_reference_order(s);
-    auto gather = ref ? k_p2g_gather<true> : k_p2g_gather<false>;
-    cudaError_t e = cudaFuncSetAttribute(gather, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGatherSmem));
+    cudaError_t e = cudaFuncSetAttribute(k_p2g_gather<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(kGatherSmem));
     if (e != cudaSuccess) return e;
     const uint32_t* svals = s.bin_vals;
     if (s.n > 0) {
@@ -773,9 +896,14 @@ cudaError_t launch_p2g(Scene& s) {
     }
     GatherOut o{s.acc_u, s.acc_uw, s.acc_v, s.acc_vw, s.density};
     dim3 grid(div_up(s.W, kGatherTW), div_up(s.H, kGatherTH));
-    launch(s.use_pdl && s.n > 0, gather, grid, kGatherThreads, kGatherSmem, s.stream,
-           static_cast<const PartPtrs*>(s.pp), svals, static_cast<const uint32_t*>(s.bin_lo),
-           static_cast<const uint32_t*>(s.bin_hi), int(s.W), int(s.H), s.dx, s.ctl, o);
+    if (ref)
+        launch(s.use_pdl && s.n > 0, k_p2g_gather<true>, grid, kGatherThreads, kGatherSmem, s.stream,
+               static_cast<const PartPtrs*>(s.pp), svals, static_cast<const uint32_t*>(s.bin_lo),
+               static_cast<const uint32_t*>(s.bin_hi), int(s.W), int(s.H), s.dx, s.ctl, o);
+    else
+        launch(s.use_pdl && s.n > 0, k_p2g_cells, grid, kGatherThreads, 0, s.stream,
+               static_cast<const PartPtrs*>(s.pp), svals, static_cast<const uint32_t*>(s.bin_lo),
+               static_cast<const uint32_t*>(s.bin_hi), int(s.W), int(s.H), s.dx, s.ctl, o);
     return cudaGetLastError();
 }
 
