@@ -603,7 +603,8 @@ __device__ __forceinline__ void add_partials(const P2gRec& rec, float (&pv)[NQ],
     }
 }
 
-__global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_cells(const PartPtrs* __restrict__ pp,
+// three CTAs per SM (80 registers): the per-cell loops are load-latency bound
+__global__ void __launch_bounds__(kGatherThreads, 3) k_p2g_cells(const PartPtrs* __restrict__ pp,
                                                                  const uint32_t* __restrict__ vals,
                                                                  const uint32_t* __restrict__ lo,
                                                                  const uint32_t* __restrict__ hi, int W, int H,
