@@ -603,8 +603,10 @@ __device__ __forceinline__ void add_partials(const P2gRec& rec, float (&pv)[NQ],
     }
 }
 
-// three CTAs per SM (80 registers): the per-cell loops are load-latency bound
-__global__ void __launch_bounds__(kGatherThreads, 3) k_p2g_cells(const PartPtrs* __restrict__ pp,
+// One thread per region cell (352 threads for 340 cells, then the tile's 256
+// cells' faces), two CTAs per SM: the per-cell loops are load-latency bound.
+constexpr int kCellThreads = 352;
+__global__ void __launch_bounds__(kCellThreads, 2) k_p2g_cells(const PartPtrs* __restrict__ pp,
                                                                  const uint32_t* __restrict__ vals,
                                                                  const uint32_t* __restrict__ lo,
                                                                  const uint32_t* __restrict__ hi, int W, int H,
@@ -615,7 +617,7 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_p2g_cells(const PartPtrs*
     pdl_wait();
     const float prev_dt = ctl->prev_dt;
     bool bad = false;
-    for (int rc = threadIdx.x; rc < kCellRegion; rc += kGatherThreads) {
+    for (int rc = threadIdx.x; rc < kCellRegion; rc += kCellThreads) {
         const int x = rx0 + rc % kRegionW, y = ry0 + rc / kRegionW;
         uint32_t b = 0, e = 0;
         if (x >= 0 && x < W && y >= 0 && y < H) {
@@ -624,8 +626,11 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_p2g_cells(const PartPtrs*
             e = hi[c];
         }
         float uv[6] = {}, uw[6] = {}, vv[6] = {}, vw[6] = {}, dv[4] = {}, dw[4] = {};
+        // the next particle's slot is loaded while this one's fields are
+        uint32_t next = b < e ? vals[b] : 0u;
         for (uint32_t p = b; p < e; ++p) {
-            const uint32_t slot = vals[p];
+            const uint32_t slot = next;
+            if (p + 1 < e) next = vals[p + 1];
             const P2gBase bs = p2g_base(pp, slot, dx, prev_dt);
             P2gRec rec;
             if (!p2g_record(pp, slot, bs, kGridU, W, H, dx, rec)) bad = true;
@@ -648,6 +653,7 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_p2g_cells(const PartPtrs*
     }
     if (bad) atomicOr(&ctl->status, kStatusP2gLayout);
     __syncthreads();
+    if (threadIdx.x >= kGatherThreads) return;
     const int tx = threadIdx.x % kGatherTW, ty = threadIdx.x / kGatherTW;
     const int i = x0 + tx, j = y0 + ty;
     if (i >= W || j >= H) return;
@@ -902,7 +908,7 @@ cudaError_t launch_p2g(Scene& s) {
                static_cast<const PartPtrs*>(s.pp), svals, static_cast<const uint32_t*>(s.bin_lo),
                static_cast<const uint32_t*>(s.bin_hi), int(s.W), int(s.H), s.dx, s.ctl, o);
     else
-        launch(s.use_pdl && s.n > 0, k_p2g_cells, grid, kGatherThreads, 0, s.stream,
+        launch(s.use_pdl && s.n > 0, k_p2g_cells, grid, kCellThreads, 0, s.stream,
                static_cast<const PartPtrs*>(s.pp), svals, static_cast<const uint32_t*>(s.bin_lo),
                static_cast<const uint32_t*>(s.bin_hi), int(s.W), int(s.H), s.dx, s.ctl, o);
     return cudaGetLastError();
