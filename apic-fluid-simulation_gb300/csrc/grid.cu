@@ -518,6 +518,9 @@ __global__ void __launch_bounds__(256) k_smoothed_view(uint32_t cells, const flo
 
 uint32_t seg_grid(uint32_t words) {
     uint32_t b = div_up(words, kSegWarps);
+#ifdef APIC_X_SEG_BPS
+    if (b > 152u * APIC_X_SEG_BPS) b = 152u * APIC_X_SEG_BPS;
+#endif
     if (b > uint32_t(kMaxRedBlocks)) b = kMaxRedBlocks;
     return b ? b : 1;
 }
