@@ -160,6 +160,11 @@ SIGNATURES = {
     "apic_read_field": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_uint64]),
     "apic_write_field": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_uint64]),
     "apic_read_vec2x8": (ctypes.c_int, [_VP, ctypes.c_int, _FP, ctypes.c_uint64]),
+    "apic_update_async": (ctypes.c_int, [_VP, ctypes.c_uint32, ctypes.c_float]),
+    "apic_update_wait": (ctypes.c_int, [_VP]),
+    "apic_stage_field": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_uint64]),
+    "apic_read_vec2x8_async": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_uint64]),
+    "apic_read_wait": (ctypes.c_int, [_VP]),
     "apic_set_particles": (ctypes.c_int, [_VP, ctypes.c_uint32, _FP, _FP, _FP, _FP]),
     "apic_set_solver": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_float, ctypes.c_uint32]),
     "apic_set_profiling": (ctypes.c_int, [_VP, ctypes.c_int]),
@@ -316,6 +321,26 @@ class Apic:
     def update(self, debug_options: DebugOptions, frame_deltatime: float) -> None:
         flags = UPDATE_DISABLE_SORT if debug_options.disable_particle_sort else 0
         _check(self._lib.apic_update(self._h, flags, frame_deltatime), "apic_update")
+
+    # pipelined host I/O (stream-ordered; host buffers given by address and
+    # size, pinned for the copies to overlap)
+    def update_async(self, debug_options: DebugOptions, frame_deltatime: float) -> None:
+        flags = UPDATE_DISABLE_SORT if debug_options.disable_particle_sort else 0
+        _check(self._lib.apic_update_async(self._h, flags, frame_deltatime), "apic_update_async")
+
+    def update_wait(self) -> None:
+        _check(self._lib.apic_update_wait(self._h), "apic_update_wait")
+
+    def stage_field(self, field, host_ptr: int, nbytes: int) -> None:
+        fid = FIELDS[field] if isinstance(field, str) else int(field)
+        _check(self._lib.apic_stage_field(self._h, fid, ctypes.c_void_p(host_ptr), nbytes), "apic_stage_field")
+
+    def read_vec2x8_async(self, which: int, host_ptr: int, nfloats: int) -> None:
+        _check(self._lib.apic_read_vec2x8_async(self._h, which, ctypes.c_void_p(host_ptr), nfloats),
+               "apic_read_vec2x8_async")
+
+    def read_wait(self) -> None:
+        _check(self._lib.apic_read_wait(self._h), "apic_read_wait")
 
     def add_radial_force(self, world_x: float, world_y: float, radius: float, strength: float) -> None:
         _check(self._lib.apic_add_radial_force(self._h, world_x, world_y, radius, strength), "apic_add_radial_force")

@@ -150,6 +150,19 @@ struct Scene {
     PartPtrs* pp = nullptr;                // device table: which allocation is current
     float* vec_stage = nullptr;            // Vec2x8 staging for host reads (allocated on first use)
     uint32_t vec_stage_floats = 0;
+    // pipelined host I/O (apic_stage_field / apic_read_vec2x8_async): an
+    // upload and a download stream; two device buffers per staged force
+    // field (ext u, ext v, post u, post v) and per Vec2x8 field pair, each
+    // with an event when filled and one when its contents were used
+    cudaStream_t up_stream = nullptr, down_stream = nullptr;
+    float* stage_buf[4][2] = {};
+    cudaEvent_t stage_ready[4][2] = {}, stage_used[4][2] = {};
+    int stage_next[4] = {};
+    int stage_pending[4] = {-1, -1, -1, -1};
+    float* read_buf[4][2] = {};
+    uint64_t read_floats[4][2] = {};
+    cudaEvent_t read_packed[4][2] = {}, read_done[4][2] = {};
+    int read_next[4] = {};
     uint32_t* keys = nullptr;
     uint32_t* vals = nullptr;
     uint32_t* keys_alt = nullptr;

@@ -261,6 +261,55 @@ void free_particles(Scene& s) {
     s.part_cap = 0;
 }
 
+// Pipelined host I/O: buffers, events and the two copy streams.
+void free_pipeline(Scene& s) {
+    if (s.up_stream) cudaStreamSynchronize(s.up_stream);
+    if (s.down_stream) cudaStreamSynchronize(s.down_stream);
+    for (int i = 0; i < 4; ++i)
+        for (int b = 0; b < 2; ++b) {
+            dfree(s.stage_buf[i][b], s.stream);
+            dfree(s.read_buf[i][b], s.stream);
+            s.read_floats[i][b] = 0;
+            for (cudaEvent_t* e : {&s.stage_ready[i][b], &s.stage_used[i][b], &s.read_packed[i][b], &s.read_done[i][b]})
+                if (*e) { cudaEventDestroy(*e); *e = nullptr; }
+        }
+    for (int i = 0; i < 4; ++i) { s.stage_next[i] = 0; s.stage_pending[i] = -1; s.read_next[i] = 0; }
+    if (s.up_stream) cudaStreamDestroy(s.up_stream);
+    if (s.down_stream) cudaStreamDestroy(s.down_stream);
+    s.up_stream = s.down_stream = nullptr;
+}
+
+cudaError_t ensure_pipeline(Scene& s) {
+    if (s.up_stream) return cudaSuccess;
+    cudaError_t e = cudaStreamCreateWithFlags(&s.up_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s.down_stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+        for (int b = 0; b < 2 && e == cudaSuccess; ++b)
+            for (cudaEvent_t* ev : {&s.stage_ready[i][b], &s.stage_used[i][b], &s.read_packed[i][b], &s.read_done[i][b]})
+                if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    return e;
+}
+
+// Force fields staged by apic_stage_field: each pending one is copied into
+// its field on the scene's stream once its upload finished, before the
+// update that follows reads it.
+cudaError_t apply_staged(Scene& s) {
+    for (int i = 0; i < 4; ++i) {
+        const int b = s.stage_pending[i];
+        if (b < 0) continue;
+        float* dst = i == 0 ? s.ext_u : i == 1 ? s.ext_v : i == 2 ? s.post_u : s.post_v;
+        const size_t n = (i % 2 == 0) ? s.uf : s.vf;
+        cudaError_t e = cudaStreamWaitEvent(s.stream, s.stage_ready[i][b], 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dst, s.stage_buf[i][b], n * sizeof(float), cudaMemcpyDeviceToDevice, s.stream);
+        if (e == cudaSuccess) e = cudaEventRecord(s.stage_used[i][b], s.stream);
+        if (e != cudaSuccess) return e;
+        if (i < 2) s.has_ext = true;
+        else s.has_post = true;
+        s.stage_pending[i] = -1;
+    }
+    return cudaSuccess;
+}
+
 void free_scene(Scene& s) {
     const cudaStream_t st = s.stream;
     free_particles(s);
@@ -282,6 +331,7 @@ void free_scene(Scene& s) {
     dfree(s.vec_stage, st);
     s.vec_stage = nullptr;
     s.vec_stage_floats = 0;
+    free_pipeline(s);
     dfree(s.ctl, st);
     ctl_mirror_put(s.ctl_host);
     s.ctl_host = nullptr;
@@ -760,6 +810,7 @@ int update_launch(apic_handle* h, uint32_t flags, float frame_dt) {
     if (!std::isfinite(frame_dt)) return fail(APIC_ERR_INVALID_ARG, "frame_deltatime must be finite");
     cudaStream_t st = s.stream;
     s.stats = apic_step_stats{};
+    CK(apply_staged(s));
     k_begin_update<<<1, 1, 0, st>>>(s.ctl, frame_dt, flags, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
     if (!s.vmax_valid) { CK(launch_vmax(s)); s.vmax_valid = true; }
     if (s.profiling) {
@@ -1101,6 +1152,80 @@ int apic_read_vec2x8(apic_handle* h, int which, float* dst, uint64_t floats) {
     CK(launch_pack_vec2x8(s, which, s.vec_stage));
     CK(cudaMemcpyAsync(dst, s.vec_stage, floats * sizeof(float), cudaMemcpyDeviceToHost, s.stream));
     CK(cudaStreamSynchronize(s.stream));
+    return APIC_OK;
+}
+
+// ---- pipelined host I/O -------------------------------------------------------
+// The stream-ordered forms of apic_update, apic_write_field (force fields)
+// and apic_read_vec2x8: the copies run on the handle's upload and download
+// streams, so a caller can upload the next update's forces and read back the
+// last update's particles while an update runs.
+
+int apic_update_async(apic_handle* h, uint32_t flags, float frame_dt) { return update_launch(h, flags, frame_dt); }
+
+int apic_update_wait(apic_handle* h) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    return update_finish(h);
+}
+
+int apic_stage_field(apic_handle* h, int field, const void* src, uint64_t bytes) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    Scene& s = h->s;
+    const int i = field == APIC_F_EXT_FORCE_U ? 0 : field == APIC_F_EXT_FORCE_V ? 1 : field == APIC_F_POST_FORCE_U ? 2
+                : field == APIC_F_POST_FORCE_V ? 3 : -1;
+    if (i < 0) return fail(APIC_ERR_INVALID_ARG, "only the external and post force fields can be staged");
+    const uint64_t n = (i % 2 == 0) ? s.uf : s.vf;
+    if (bytes != n * sizeof(float)) return fail(APIC_ERR_INVALID_ARG, "size mismatch");
+    if (!src) return fail(APIC_ERR_INVALID_ARG, "null source");
+    CK(ensure_pipeline(s));
+    const int b = s.stage_next[i];
+    if (!s.stage_buf[i][b]) {
+        if (dalloc(&s.stage_buf[i][b], n, s.stream) != cudaSuccess)
+            return fail(APIC_ERR_OOM, "out of device memory (force staging)");
+        CK(cudaStreamSynchronize(s.stream));  // the pool allocation is ordered on the scene's stream
+    }
+    // the buffer may still be read by the copy of an update staged two calls ago
+    CK(cudaStreamWaitEvent(s.up_stream, s.stage_used[i][b], 0));
+    CK(cudaMemcpyAsync(s.stage_buf[i][b], src, bytes, cudaMemcpyHostToDevice, s.up_stream));
+    CK(cudaEventRecord(s.stage_ready[i][b], s.up_stream));
+    s.stage_pending[i] = b;
+    s.stage_next[i] = b ^ 1;
+    return APIC_OK;
+}
+
+int apic_read_vec2x8_async(apic_handle* h, int which, float* dst, uint64_t floats) {
+    if (valid_handle(h) || which < 0 || which > 3) return fail(APIC_ERR_INVALID_ARG, "bad argument");
+    Scene& s = h->s;
+    if (floats != uint64_t(s.nchunks) * 16) return fail(APIC_ERR_INVALID_ARG, "size mismatch");
+    if (floats == 0) return APIC_OK;
+    if (!dst) return fail(APIC_ERR_INVALID_ARG, "null destination");
+    CK(ensure_pipeline(s));
+    const int b = s.read_next[which];
+    if (s.read_floats[which][b] < floats) {
+        CK(cudaStreamSynchronize(s.down_stream));
+        CK(cudaStreamSynchronize(s.stream));
+        dfree(s.read_buf[which][b], s.stream);
+        s.read_buf[which][b] = nullptr;
+        s.read_floats[which][b] = 0;
+        if (dalloc(&s.read_buf[which][b], floats, s.stream) != cudaSuccess)
+            return fail(APIC_ERR_OOM, "out of device memory (Vec2x8 staging)");
+        s.read_floats[which][b] = floats;
+    }
+    // pack after the work already on the scene's stream, once the copy out of
+    // this buffer two calls ago finished; copy out on the download stream
+    CK(cudaStreamWaitEvent(s.stream, s.read_done[which][b], 0));
+    CK(launch_pack_vec2x8(s, which, s.read_buf[which][b]));
+    CK(cudaEventRecord(s.read_packed[which][b], s.stream));
+    CK(cudaStreamWaitEvent(s.down_stream, s.read_packed[which][b], 0));
+    CK(cudaMemcpyAsync(dst, s.read_buf[which][b], floats * sizeof(float), cudaMemcpyDeviceToHost, s.down_stream));
+    CK(cudaEventRecord(s.read_done[which][b], s.down_stream));
+    s.read_next[which] = b ^ 1;
+    return APIC_OK;
+}
+
+int apic_read_wait(apic_handle* h) {
+    if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
+    if (h->s.down_stream) CK(cudaStreamSynchronize(h->s.down_stream));
     return APIC_OK;
 }
 

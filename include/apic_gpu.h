@@ -202,6 +202,35 @@ int apic_write_field(apic_handle* h, int field, const void* src, uint64_t bytes)
  * 8 x-lanes then 8 y-lanes (num_chunks*16 floats).  which: 0 positions,
  * 1 velocities, 2 c_u, 3 c_v.  Fills `Vec<Vec2x8>` mirrors directly. */
 int apic_read_vec2x8(apic_handle* h, int which, float* dst, uint64_t floats);
+
+/* ---- pipelined host I/O (no counterpart in the reference) -------------------
+ * Stream-ordered forms of apic_update, apic_write_field (force fields) and
+ * apic_read_vec2x8 for callers that overlap their host <-> device copies with
+ * the next update, e.g. a GUI or server that uploads each frame's forces and
+ * reads each frame's particles.  Host buffers should be pinned
+ * (cudaHostAlloc / cudaHostRegister) for the copies to be asynchronous.
+ * Results are those of the synchronous calls, bit for bit.
+ *
+ * apic_update_async enqueues Apic::update (src/apic.rs:2429) and returns;
+ * apic_update_wait waits for it and publishes its statistics (apic_get_stats)
+ * and status.  apic_update = apic_update_async + apic_update_wait. */
+int apic_update_async(apic_handle* h, uint32_t flags, float frame_deltatime);
+int apic_update_wait(apic_handle* h);
+/* Starts copying one external or post force field (APIC_F_EXT_FORCE_U/V,
+ * APIC_F_POST_FORCE_U/V; u: (W+1)*H floats, v: W*(H+1)) from host memory
+ * into a device staging buffer on the handle's upload stream and returns.
+ * The next update applies it to the field before it starts, as if
+ * apic_write_field had been called just before (after any apic_write_field
+ * of the same field); a field staged twice before an update applies the
+ * second.  Staged, not yet applied fields are not part of a snapshot. */
+int apic_stage_field(apic_handle* h, int field, const void* src, uint64_t bytes);
+/* Enqueues the Vec2x8 packing of `which` (as apic_read_vec2x8) after the
+ * work already enqueued on the handle (so after an apic_update_async) and its
+ * copy into dst on the handle's download stream; returns at once.  dst holds
+ * the values after apic_read_wait.  Two reads of the same pair may be in
+ * flight; the caller keeps their destinations apart. */
+int apic_read_vec2x8_async(apic_handle* h, int which, float* dst, uint64_t floats);
+int apic_read_wait(apic_handle* h);
 /* Replace the particle set (scene injection): n particles, C = 0, time
  * residual = 0; the last AoSoA chunk is padded with the last position and
  * zero velocity as in src/apic.rs:887-898. */
