@@ -307,26 +307,24 @@ __global__ void __launch_bounds__(kSegBlock) k_laplacian(const uint32_t* __restr
     }
 }
 
-// One coarse level from its finer level: thread per coarse cell, one warp per
-// coarse mask word.
-__global__ void __launch_bounds__(256) k_coarsen(Level f, Level c) {
-    pdl_wait();
-    uint32_t raw = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t word = raw >> 5;
-    if (word >= c.words) return;  // whole warps exit together
+// One coarse mask word of level c from its finer level f (src/apic.rs:
+// 1499-1602), by one warp: lane = the word's cell; the word itself (an OR of
+// each cell's 2 x 2 children) and, for the fluid cells, the coarse
+// coefficients.
+__device__ __forceinline__ void coarsen_word(const Level& f, const Level& c, uint32_t word, uint32_t lane) {
+    const uint32_t raw = word * 32u + lane;
     bool on = false;
     uint32_t cx = 0, cy = 0;
     if (raw < c.cells) {
-        cx = raw % c.w;
-        cy = raw / c.w;
+        raw_xy(raw, c.w, c.wshift, cx, cy);
         for (uint32_t dy = 0; dy < 2; ++dy)
             for (uint32_t dx = 0; dx < 2; ++dx) {
                 uint32_t fx = cx * 2 + dx, fy = cy * 2 + dy;
                 if (fx < f.w && fy < f.h && bit_at(f.fluid, fy * f.w + fx)) on = true;
             }
     }
-    uint32_t ballot = __ballot_sync(0xffffffffu, on);
-    if ((threadIdx.x & 31) == 0) c.fluid[word] = ballot;
+    const uint32_t ballot = __ballot_sync(0xffffffffu, on);
+    if (lane == 0) c.fluid[word] = ballot;
     if (!on) return;
     float diag = 0.0f, px = 0.0f, py = 0.0f;
     for (uint32_t dy = 0; dy < 2; ++dy)
@@ -348,6 +346,59 @@ __global__ void __launch_bounds__(256) k_coarsen(Level f, Level c) {
     c.inv_diag[cp] = fd > 1e-6f ? 1.0f / fd : 0.0f;
     c.px[cp] = px * 0.5f;
     c.py[cp] = py * 0.5f;
+}
+
+// One coarse level from its finer level: one warp per coarse mask word.
+__global__ void __launch_bounds__(256) k_coarsen(Level f, Level c) {
+    pdl_wait();
+    const uint32_t word = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (word >= c.words) return;  // whole warps exit together
+    coarsen_word(f, c, word, threadIdx.x & 31u);
+}
+
+// Segment list of one coarse level by one CTA of kOneThreads threads (levels
+// of at most kOneWords mask words): thread t takes the consecutive words
+// [t k, t k + k), so a block scan of the per-thread counts gives every
+// non-zero word its place in ascending order.
+constexpr uint32_t kOneThreads = 1024;
+constexpr uint32_t kOneWords = 8192;
+__device__ __forceinline__ void compact_one(const uint32_t* __restrict__ fluid, uint32_t words, uint32_t* __restrict__ seg,
+                                            int level, Ctl* __restrict__ ctl) {
+    const uint32_t per = (words + kOneThreads - 1) / kOneThreads;
+    const uint32_t w0 = threadIdx.x * per;
+    uint32_t nz = 0;
+    for (uint32_t k = 0; k < per; ++k)
+        if (w0 + k < words && fluid[w0 + k]) ++nz;
+    uint32_t tot;
+    uint32_t off = scan_1024(nz, &tot);
+    for (uint32_t k = 0; k < per; ++k)
+        if (w0 + k < words && fluid[w0 + k]) seg[off++] = w0 + k;
+    if (threadIdx.x == 0) ctl->seg_count[level] = tot;
+}
+
+__global__ void __launch_bounds__(kOneThreads) k_compact_one(const uint32_t* __restrict__ fluid, uint32_t words,
+                                                              uint32_t* __restrict__ seg, int level, Ctl* __restrict__ ctl) {
+    pdl_wait();
+    compact_one(fluid, words, seg, level, ctl);
+}
+
+// The smallest levels, [first, n), by one CTA: each level's coarsening (a
+// warp per mask word), then its segment list, with CTA barriers between.
+struct TailLevels {
+    int first, n;
+    Level lv[kMaxLevels];
+};
+__global__ void __launch_bounds__(kOneThreads) k_coarsen_tail(TailLevels t, Ctl* __restrict__ ctl) {
+    pdl_wait();
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    for (int l = t.first; l < t.n; ++l) {
+        const Level& f = t.lv[l - 1];
+        const Level& c = t.lv[l];
+        for (uint32_t w = warp; w < c.words; w += kOneThreads / 32u) coarsen_word(f, c, w, lane);
+        __syncthreads();
+        compact_one(c.fluid, c.words, c.seg, l, ctl);
+        __syncthreads();
+    }
 }
 
 __global__ void __launch_bounds__(256) k_gradient(uint32_t uf, uint32_t vf, int W, int H, float inv_dx,
@@ -546,6 +597,11 @@ cudaError_t launch_external_forces(Scene& s) {
 
 static cudaError_t compact_level(Scene& s, int level, const uint32_t* obstacle) {
     Level& L = s.lv[level];
+    if (level > 0 && L.words <= kOneWords) {
+        launch(s.use_pdl, k_compact_one, 1, kOneThreads, 0, s.stream, static_cast<const uint32_t*>(L.fluid), L.words,
+               L.seg, level, s.ctl);
+        return cudaGetLastError();
+    }
     uint32_t nb = div_up(L.words, kCompactWords);
     if (nb == 0) nb = 1;  // the last block records the (empty) level's totals
     launch(s.use_pdl, k_compact_count, nb, 256, 0, s.stream, L.fluid, obstacle, L.words, s.scan_tmp);
@@ -568,12 +624,24 @@ cudaError_t launch_build_pressure(Scene& s) {
     return cudaGetLastError();
 }
 
+// Levels of at most kTailWords mask words (4096 cells: 64^2 and below) are
+// built together by one CTA; each larger level by a coarsening launch and
+// its segment list.
+constexpr uint32_t kTailWords = 128;
 cudaError_t launch_multilevel(Scene& s) {
-    for (int l = 1; l < s.nlevels; ++l) {
+    int l = 1;
+    for (; l < s.nlevels && s.lv[l].words > kTailWords; ++l) {
         Level& c = s.lv[l];
         launch(s.use_pdl, k_coarsen, div_up(uint64_t(c.words) * 32, 256), 256, 0, s.stream, s.lv[l - 1], c);
         cudaError_t e = compact_level(s, l, nullptr);
         if (e != cudaSuccess) return e;
+    }
+    if (l < s.nlevels) {
+        TailLevels t;
+        t.first = l;
+        t.n = s.nlevels;
+        for (int k = 0; k < s.nlevels; ++k) t.lv[k] = s.lv[k];
+        launch(s.use_pdl, k_coarsen_tail, 1, kOneThreads, 0, s.stream, t, s.ctl);
     }
     return cudaGetLastError();
 }

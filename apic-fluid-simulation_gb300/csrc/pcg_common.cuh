@@ -266,9 +266,10 @@ __device__ __forceinline__ void ph_search(const Level& B, uint32_t nseg, uint32_
 __device__ __forceinline__ double ph_mixed_init(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
                                                 double* b64, double* p64, int warm) {
     double bb = 0;
-    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
-        uint32_t c = word_ * 32 + lane_ + B.w;
-        double b = double(B.res[c]);
+    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+        const uint32_t c = raw_ + B.w;
+        const double b = double(B.res[c]);
+        if (!fluid_) continue;
         b64[c] = b;
         if (!warm) p64[c] = 0.0;
         bb += b * b;
@@ -281,16 +282,28 @@ __device__ __forceinline__ double ph_mixed_init(const Level& B, uint32_t nseg, u
 __device__ __forceinline__ double ph_true_residual(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
                                                    const double* b64, const double* p64, float* x, int flags) {
     double rr = 0;
-    const long long W = B.w;
-    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
-        long long raw = (long long)word_ * 32 + lane_;
-        uint32_t c = uint32_t(raw) + B.w;
-        double v = double(B.diag[c]) * p64[c];
-        if (fluid_raw(B.fluid, raw + 1, B.cells)) v += double(B.px[c]) * p64[c + 1];
-        if (fluid_raw(B.fluid, raw - 1, B.cells)) v += double(B.px[c - 1]) * p64[c - 1];
-        if (fluid_raw(B.fluid, raw + W, B.cells)) v += double(B.py[c]) * p64[c + W];
-        if (fluid_raw(B.fluid, raw - W, B.cells)) v += double(B.py[c - W]) * p64[c - W];
-        double r = b64[c] - v;
+    const uint32_t W = B.w;
+    // every load is issued before the fluid tests (all neighbours of a cell
+    // inside the grid lie inside the padded arrays); non-fluid neighbours
+    // are dropped by selects, which adds exactly what skipping them adds
+    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+        const uint32_t c = raw_ + W;
+        const long long raw = raw_;
+        const float dg = B.diag[c], pxc = B.px[c], pxl = B.px[c - 1], pyc = B.py[c], pyd = B.py[c - W];
+        const double pc = p64[c], pr = p64[c + 1], pl = p64[c - 1], pu = p64[c + W], pd = p64[c - W], bc = b64[c];
+        const bool fr = fluid_raw(B.fluid, raw + 1, B.cells), fl = fluid_raw(B.fluid, raw - 1, B.cells);
+        const bool fu = fluid_raw(B.fluid, raw + W, B.cells), fd = fluid_raw(B.fluid, raw - (long long)W, B.cells);
+        double v = double(dg) * pc;
+        double t = v + double(pxc) * pr;
+        v = fr ? t : v;
+        t = v + double(pxl) * pl;
+        v = fl ? t : v;
+        t = v + double(pyc) * pu;
+        v = fu ? t : v;
+        t = v + double(pyd) * pd;
+        v = fd ? t : v;
+        if (!fluid_) continue;
+        const double r = bc - v;
         rr += r * r;
         if (flags & 1) B.res[c] = float(r);
         if (flags & 2) x[c] = 0.0f;
@@ -301,11 +314,13 @@ __device__ __forceinline__ double ph_true_residual(const Level& B, uint32_t nseg
 // p64 += x, or (finalize) pressure = float(p64).
 __device__ __forceinline__ void ph_accumulate(const Level& B, uint32_t nseg, uint32_t warp, uint32_t nwarps,
                                               double* p64, const float* x, float* pressure, int finalize) {
-    APIC_BASE_LOOP(B, nseg, warp, nwarps) {
-        uint32_t raw = word_ * 32 + lane_;
-        uint32_t c = raw + B.w;
-        if (!finalize) p64[c] += double(x[c]);
-        else pressure[raw] = float(p64[c]);
+    APIC_BASE_ALL(B, nseg, warp, nwarps) {
+        const uint32_t c = raw_ + B.w;
+        const double p = p64[c];
+        const float xv = finalize ? 0.0f : x[c];
+        if (!fluid_) continue;
+        if (!finalize) p64[c] = p + double(xv);
+        else pressure[raw_] = float(p);
     }
 }
 
