@@ -214,3 +214,22 @@ def test_p2g_unusual_particles(oracle_mod):
         g.run_stage("p2g", 1.0 / 240)
         for f in ("u", "v", "density", "valid_u", "valid_v", "fluid_bits"):
             eq(g.read_field(f), o.read_field(f), f"p2g {f} (sorted {sort})")
+
+
+def test_config3_lockstep_4096(oracle_mod):
+    """The stress scene at its full size (4096^2, value-noise mask > 0.5 with
+    lattice period 1/64, seed 2, 33.2 M particles, v ~ N(0, 0.5^2)): one
+    substep stage by stage in the reference solver mode, every stage
+    bit-identical to the oracle (serial, the reference's single-thread
+    order), including the Morton sort of 33 M particles and every multigrid
+    level."""
+    side = 4096
+    cs = 1.0 / side
+    scene = A.scene_params(A.SCENE_NOISE, side, cell_size=cs, sub=2, seed=2, noise_period=1.0 / 64,
+                           noise_threshold=0.5, vel_sigma=0.5)
+    o, g = make_pair(oracle_mod, side, cs, PROPS, scene)
+    assert g.num_particles == o.info().num_particles > 30_000_000
+    stats = run_lockstep(o, g, 1, 1.0 / 8000, PROPS, cs)
+    # the reference's exits stop this solve after a few iterations (gamma
+    # falls below SAFTY at dx = 1/4096); the iterations run are the oracle's
+    assert stats["pcg_iters"][0][0] == stats["pcg_iters"][0][1] > 0
