@@ -52,9 +52,20 @@ def _stale(target: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) -> str:
-    """Build libapic_gpu.so if any source changed; return its path."""
-    os.makedirs(BUILD_DIR, exist_ok=True)
+CHECKED_BUILD_DIR = os.path.join(PKG_ROOT, "_build_checked")
+CHECKED_LIB_PATH = os.path.join(LIB_DIR, "libapic_gpu_checked.so")
+
+
+def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False, checked: bool = False) -> str:
+    """Build libapic_gpu.so if any source changed; return its path.
+
+    checked: build libapic_gpu_checked.so instead, with -DAPIC_BOUNDS_CHECK
+    (data-dependent indices tested before use; an update that met one
+    outside its buffer fails with APIC_ERR_CUDA)."""
+    build_dir = CHECKED_BUILD_DIR if checked else BUILD_DIR
+    lib_path = CHECKED_LIB_PATH if checked else LIB_PATH
+    extra = ["-DAPIC_BOUNDS_CHECK"] if checked else []
+    os.makedirs(build_dir, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
     nvcc = _nvcc()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
@@ -63,11 +74,11 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     objs = []
     for src in CUDA_SOURCES + CXX_SOURCES:
         path = os.path.join(CSRC, src)
-        obj = os.path.join(BUILD_DIR, src + ".o")
+        obj = os.path.join(build_dir, src + ".o")
         objs.append(obj)
         if force or _stale(obj, [path] + headers):
             if src.endswith(".cu"):
-                cmd = [nvcc] + NVCC_FLAGS + (["-Xptxas", "-v"] if ptxas_info else []) + ["-c", path, "-o", obj]
+                cmd = [nvcc] + NVCC_FLAGS + extra + (["-Xptxas", "-v"] if ptxas_info else []) + ["-c", path, "-o", obj]
             else:
                 cmd = ["g++"] + CXX_FLAGS + ["-c", path, "-o", obj]
             jobs.append(cmd)
@@ -79,10 +90,11 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         for o in outs:
             if o.strip():
                 sys.stderr.write(o)
-    if force or jobs or _stale(LIB_PATH, objs):
-        _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", LIB_PATH] + objs + ["-lpthread", "-ldl", "-lrt"])
-    return LIB_PATH
+    if force or jobs or _stale(lib_path, objs):
+        _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", lib_path] + objs + ["-lpthread", "-ldl", "-lrt"])
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(verbose=True, force="--force" in sys.argv, ptxas_info="--ptxas" in sys.argv))
+    print(build(verbose=True, force="--force" in sys.argv, ptxas_info="--ptxas" in sys.argv,
+                checked="--checked" in sys.argv))

@@ -150,6 +150,23 @@ __device__ __forceinline__ bool red_at(uint32_t r, uint32_t w, int shift) {
     return ((x + y) & 1u) == 0u;
 }
 
+// Checked build (-DAPIC_BOUNDS_CHECK): data-dependent indices (particle
+// slots, cells, faces, sort destinations) are tested against their buffer
+// before use; an index outside it sets kStatusBounds in *status (when
+// given) and the access is skipped.  In the default build the test is
+// `true` and compiles away: the index arithmetic is bounded by construction
+// (clamped stencils, scans that sum to n).
+#ifdef APIC_BOUNDS_CHECK
+__device__ __forceinline__ bool in_bounds_checked(uint64_t i, uint64_t n, uint32_t* status) {
+    if (i < n) return true;
+    if (status) atomicOr(status, 16u);  // kStatusBounds
+    return false;
+}
+#define APIC_IN_BOUNDS(i, n, status) ::apic::in_bounds_checked(uint64_t(i), uint64_t(n), (status))
+#else
+#define APIC_IN_BOUNDS(i, n, status) true
+#endif
+
 __device__ __forceinline__ uint32_t fluid_raw(const uint32_t* m, long long i, uint32_t cells) {
     if (i < 0 || i >= (long long)cells) return 0;
     return bit_at(m, uint32_t(i));

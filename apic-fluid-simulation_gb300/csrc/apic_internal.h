@@ -92,6 +92,7 @@ enum : uint32_t {
     kStatusNonfinite = 1u,
     kStatusBadStep = 2u,
     kStatusP2gLayout = 8u,  // a particle's staggered stencil left the bins P2G searches (never expected)
+    kStatusBounds = 16u,    // checked build (APIC_BOUNDS_CHECK): an index left its buffer
 };
 
 struct Level {
@@ -278,9 +279,11 @@ cudaError_t radix_sort_pairs_in(uint32_t* keys, uint32_t* vals, uint32_t* keys_a
 // Stable LSD sort with digits of up to kMaxDigitBits bits; the sorted pairs
 // stay where the last pass wrote them (*keys_out / *vals_out: keys/vals or
 // keys_alt/vals_alt).  hist: sort_hist_words(n), scan_tmp: sort_scan_words(n).
+// status: where the checked build (APIC_BOUNDS_CHECK) records an index outside
+// its buffer (may be null).
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* hist,
                              uint32_t* scan_tmp, uint32_t n, int bits, cudaStream_t st, bool pdl,
-                             uint32_t** keys_out, uint32_t** vals_out);
+                             uint32_t** keys_out, uint32_t** vals_out, uint32_t* status = nullptr);
 bool radix_sort_in_alt(int bits);     // radix_sort_pairs over `bits` bits ends in the alt buffers
 uint32_t sort_hist_words(uint32_t n);
 uint32_t sort_scan_words(uint32_t n);

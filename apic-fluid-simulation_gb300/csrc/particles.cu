@@ -126,11 +126,13 @@ __global__ void __launch_bounds__(256) k_p2g_bin_keys(const PartPtrs* __restrict
 }
 
 __global__ void __launch_bounds__(256) k_p2g_bounds(const uint32_t* __restrict__ keys, uint32_t n,
-                                                    uint32_t* __restrict__ lo, uint32_t* __restrict__ hi) {
+                                                    uint32_t* __restrict__ lo, uint32_t* __restrict__ hi,
+                                                    uint32_t cells, uint32_t* __restrict__ status) {
     pdl_wait();
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const uint32_t k = keys[j];
+    if (!APIC_IN_BOUNDS(k, cells, status)) return;
     if (j == 0 || keys[j - 1] != k) lo[k] = j;
     if (j == n - 1 || keys[j + 1] != k) hi[k] = j + 1;
 }
@@ -242,10 +244,14 @@ struct GlobalRecs {
     int grid, W, H;
     float dx, prev_dt;
     uint32_t* status;
-    __device__ __forceinline__ uint32_t slot_at(int p) const { return vals[p]; }
+    uint32_t n, npad;  // sorted pairs, particle lanes (the checked build tests against them)
+    __device__ __forceinline__ uint32_t slot_at(int p) const {
+        const uint32_t sl = APIC_IN_BOUNDS(uint32_t(p), n, status) ? vals[p] : 0u;
+        return APIC_IN_BOUNDS(sl, npad, status) ? sl : 0u;
+    }
     __device__ __forceinline__ P2gRec rec(int p) const {
         P2gRec r;
-        const uint32_t sl = vals[p];
+        const uint32_t sl = slot_at(p);
         if (!p2g_record(pp, sl, p2g_base(pp, sl, dx, prev_dt), grid, W, H, dx, r)) atomicOr(status, kStatusP2gLayout);
         return r;
     }
@@ -441,7 +447,8 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
                                                                   const uint32_t* __restrict__ vals,
                                                                   const uint32_t* __restrict__ lo,
                                                                   const uint32_t* __restrict__ hi, int W, int H,
-                                                                  float dx, Ctl* __restrict__ ctl, GatherOut o) {
+                                                                  float dx, Ctl* __restrict__ ctl, GatherOut o,
+                                                                  uint32_t n, uint32_t npad) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t* s_slot = reinterpret_cast<uint32_t*>(smem);
     uint32_t* s_code = s_slot + kGatherCap;
@@ -510,7 +517,7 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
         // more particles than the stage holds even for one row: every face
         // reads its runs from global memory and computes the records it needs
         for (int g = 0; g < 3; ++g) {
-            GlobalRecs R{vals, pp, g, W, H, dx, prev_dt, &ctl->status};
+            GlobalRecs R{vals, pp, g, W, H, dx, prev_dt, &ctl->status, n, npad};
             auto bin = [&](int x, int y, int& b, int& e) {
                 const uint32_t c = uint32_t(y) * uint32_t(W) + uint32_t(x);
                 b = int(lo[c]);
@@ -529,7 +536,10 @@ __global__ void __launch_bounds__(kGatherThreads, 2) k_p2g_gather(const PartPtrs
         for (uint32_t r = r0; r < r1; ++r) {
             const uint32_t s0 = s_off[r * kRegionW] - base, s1 = s_off[(r + 1) * kRegionW] - base;
             const uint32_t g0 = s_rowg[r];
-            for (uint32_t q = threadIdx.x; q < s1 - s0; q += kGatherThreads) s_slot[s0 + q] = vals[g0 + q];
+            for (uint32_t q = threadIdx.x; q < s1 - s0; q += kGatherThreads) {
+                const uint32_t sl = APIC_IN_BOUNDS(g0 + q, n, &ctl->status) ? vals[g0 + q] : 0u;
+                s_slot[s0 + q] = APIC_IN_BOUNDS(sl, npad, &ctl->status) ? sl : 0u;
+            }
         }
         __syncthreads();
         if constexpr (kRef) {
@@ -610,7 +620,8 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_p2g_cells(const PartPtrs* _
                                                                  const uint32_t* __restrict__ vals,
                                                                  const uint32_t* __restrict__ lo,
                                                                  const uint32_t* __restrict__ hi, int W, int H,
-                                                                 float dx, Ctl* __restrict__ ctl, GatherOut o) {
+                                                                 float dx, Ctl* __restrict__ ctl, GatherOut o,
+                                                                 uint32_t n, uint32_t npad) {
     __shared__ CellPartials sp;
     const int x0 = blockIdx.x * kGatherTW, y0 = blockIdx.y * kGatherTH;
     const int rx0 = x0 - 2, ry0 = y0 - 2;
@@ -627,10 +638,12 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_p2g_cells(const PartPtrs* _
         }
         float uv[6] = {}, uw[6] = {}, vv[6] = {}, vw[6] = {}, dv[4] = {}, dw[4] = {};
         // the next particle's slot is loaded while this one's fields are
+        if (!APIC_IN_BOUNDS(e, uint64_t(n) + 1u, &ctl->status)) e = b;
         uint32_t next = b < e ? vals[b] : 0u;
         for (uint32_t p = b; p < e; ++p) {
             const uint32_t slot = next;
             if (p + 1 < e) next = vals[p + 1];
+            if (!APIC_IN_BOUNDS(slot, npad, &ctl->status)) continue;
             const P2gBase bs = p2g_base(pp, slot, dx, prev_dt);
             P2gRec rec;
             if (!p2g_record(pp, slot, bs, kGridU, W, H, dx, rec)) bad = true;
@@ -752,10 +765,12 @@ __global__ void __launch_bounds__(256) k_g2p(const PartPtrs* __restrict__ pp, ui
         float un[4], vn[4], uwm[4], vwm[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            un[k] = gu[su.idx[k]];
-            vn[k] = gv[sv.idx[k]];
-            uwm[k] = bit_at(u_open, su.idx[k]) ? su.w[k] : 0.0f;
-            vwm[k] = bit_at(v_open, sv.idx[k]) ? sv.w[k] : 0.0f;
+            const bool uin = APIC_IN_BOUNDS(su.idx[k], uint32_t(W + 1) * uint32_t(H), &ctl->status);
+            const bool vin = APIC_IN_BOUNDS(sv.idx[k], uint32_t(W) * uint32_t(H + 1), &ctl->status);
+            un[k] = uin ? gu[su.idx[k]] : 0.0f;
+            vn[k] = vin ? gv[sv.idx[k]] : 0.0f;
+            uwm[k] = uin && bit_at(u_open, su.idx[k]) ? su.w[k] : 0.0f;
+            vwm[k] = vin && bit_at(v_open, sv.idx[k]) ? sv.w[k] : 0.0f;
         }
         float nvx = bilinear(uwm, un), nvy = bilinear(vwm, vn);
         float res = pp->f[TR][i];
@@ -832,7 +847,7 @@ __global__ void k_zero_vmax(Ctl* ctl) {
 // Four consecutive slots per thread: 128-bit loads of the sorted slots and
 // 128-bit stores of each field (the gathered reads are one float each).
 __global__ void __launch_bounds__(256) k_permute(PartPtrs* __restrict__ pp, const uint32_t* __restrict__ vals,
-                                                 uint32_t n, uint32_t npad) {
+                                                 uint32_t n, uint32_t npad, uint32_t* __restrict__ status) {
     pdl_wait();
     const uint32_t i0 = 4u * (blockIdx.x * blockDim.x + threadIdx.x);
     if (i0 >= npad) return;  // npad is a multiple of 8
@@ -850,6 +865,8 @@ __global__ void __launch_bounds__(256) k_permute(PartPtrs* __restrict__ pp, cons
             src[k] = ok[k] ? vals[i0 + k] : 0u;
         }
     }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ok[k] = ok[k] && APIC_IN_BOUNDS(src[k], npad, status);
 #pragma unroll
     for (int f = 0; f < NPF; ++f) {
         const float* a = pp->f[f];
@@ -895,10 +912,10 @@ cudaError_t launch_p2g(Scene& s) {
                int(s.W), int(s.H), s.dx, s.bin_keys, s.bin_vals, s.lv[0].fluid);
         uint32_t *kres, *vres;
         e = radix_sort_pairs(s.bin_keys, s.bin_vals, s.bin_keys_alt, s.bin_vals_alt, s.sort_hist, s.sort_scan_tmp, s.n,
-                             bin_key_bits(s), s.stream, s.use_pdl, &kres, &vres);
+                             bin_key_bits(s), s.stream, s.use_pdl, &kres, &vres, &s.ctl->status);
         if (e != cudaSuccess) return e;
         launch(s.use_pdl, k_p2g_bounds, div_up(s.n, 256), 256, 0, s.stream, static_cast<const uint32_t*>(kres), s.n,
-               s.bin_lo, s.bin_hi);
+               s.bin_lo, s.bin_hi, s.cells, &s.ctl->status);
         svals = vres;
     }
     GatherOut o{s.acc_u, s.acc_uw, s.acc_v, s.acc_vw, s.density};
@@ -906,11 +923,11 @@ cudaError_t launch_p2g(Scene& s) {
     if (ref)
         launch(s.use_pdl && s.n > 0, k_p2g_gather<true>, grid, kGatherThreads, kGatherSmem, s.stream,
                static_cast<const PartPtrs*>(s.pp), svals, static_cast<const uint32_t*>(s.bin_lo),
-               static_cast<const uint32_t*>(s.bin_hi), int(s.W), int(s.H), s.dx, s.ctl, o);
+               static_cast<const uint32_t*>(s.bin_hi), int(s.W), int(s.H), s.dx, s.ctl, o, s.n, s.npad);
     else
         launch(s.use_pdl && s.n > 0, k_p2g_cells, grid, kCellThreads, 0, s.stream,
                static_cast<const PartPtrs*>(s.pp), svals, static_cast<const uint32_t*>(s.bin_lo),
-               static_cast<const uint32_t*>(s.bin_hi), int(s.W), int(s.H), s.dx, s.ctl, o);
+               static_cast<const uint32_t*>(s.bin_hi), int(s.W), int(s.H), s.dx, s.ctl, o, s.n, s.npad);
     return cudaGetLastError();
 }
 
@@ -947,7 +964,8 @@ cudaError_t launch_pack_vec2x8(Scene& s, int which, float* out) {
 
 cudaError_t launch_permute(Scene& s, const uint32_t* sorted_vals) {
     if (s.npad == 0) return cudaSuccess;
-    launch(s.use_pdl, k_permute, div_up(s.npad / 4, 256), 256, 0, s.stream, s.pp, sorted_vals, s.n, s.npad);
+    launch(s.use_pdl, k_permute, div_up(s.npad / 4, 256), 256, 0, s.stream, s.pp, sorted_vals, s.n, s.npad,
+           &s.ctl->status);
     launch(s.use_pdl, k_swap_tables, 1, 32, 0, s.stream, s.pp);
     return cudaGetLastError();
 }

@@ -856,6 +856,8 @@ int update_finish(apic_handle* h) {
     if (!s.profiling)
         s.stats.kernel_launches = uint64_t(s.kn_top) + (c.sorted ? s.kn_sort : 0u) + uint64_t(c.substeps) * s.kn_loop +
                                   uint64_t(c.pcg_iters_total) * s.kn_pcg + uint64_t(c.refinements_total) * s.kn_refine;
+    if (c.status & kStatusBounds)
+        return fail(APIC_ERR_CUDA, "bounds check: an index left its buffer (build with APIC_BOUNDS_CHECK)");
     if (c.status & kStatusP2gLayout)
         return fail(APIC_ERR_CUDA, "P2G: a particle's stencil left the cells its faces gather from (internal error)");
     if (c.status & kStatusBadStep) return fail(APIC_ERR_NONFINITE, "substep size is not positive (non-finite velocities)");

@@ -75,7 +75,8 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* _
                                                                 int shift, int dbits,
                                                                 const uint32_t* __restrict__ offs,
                                                                 uint32_t* __restrict__ okeys,
-                                                                uint32_t* __restrict__ ovals) {
+                                                                uint32_t* __restrict__ ovals,
+                                                                uint32_t* __restrict__ status) {
     pdl_wait();
     __shared__ uint16_t wh[kSortThreads / 32][kMaxBuckets];  // per-warp counts, then offsets
     __shared__ uint32_t boff[kMaxBuckets];                   // global start of this tile's digit d
@@ -143,6 +144,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* _
         uint32_t key = sk[q];
         uint32_t d = (key >> shift) & mask;
         uint32_t pos = boff[d] + (q - lstart[d]);
+        if (!APIC_IN_BOUNDS(pos, n, status)) continue;
         okeys[pos] = key;
         ovals[pos] = sv[q];
     }
@@ -262,7 +264,7 @@ static int digit_bits(int bits) {
 
 static cudaError_t lsd_passes(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt,
                               uint32_t* hist, uint32_t* scan_tmp, uint32_t n, int bits, int dbits, cudaStream_t st,
-                              bool pdl, uint32_t** keys_out, uint32_t** vals_out) {
+                              bool pdl, uint32_t** keys_out, uint32_t** vals_out, uint32_t* status) {
     uint32_t nb = div_up(n, kSortTile);
     uint32_t* k_in = keys;
     uint32_t* v_in = vals;
@@ -273,7 +275,8 @@ static cudaError_t lsd_passes(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt
         cudaError_t e = exclusive_scan_u32(hist, (1u << dbits) * nb, scan_tmp, st);
         if (e != cudaSuccess) return e;
         launch(pdl, k_sort_scatter, nb, kSortThreads, 0, st, static_cast<const uint32_t*>(k_in),
-               static_cast<const uint32_t*>(v_in), n, shift, dbits, static_cast<const uint32_t*>(hist), k_out, v_out);
+               static_cast<const uint32_t*>(v_in), n, shift, dbits, static_cast<const uint32_t*>(hist), k_out, v_out,
+               status);
         std::swap(k_in, k_out);
         std::swap(v_in, v_out);
     }
@@ -287,12 +290,12 @@ uint32_t sort_scan_words(uint32_t n) { return div_up(sort_hist_words(n), 1024) +
 
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* hist,
                              uint32_t* scan_tmp, uint32_t n, int bits, cudaStream_t st, bool pdl,
-                             uint32_t** keys_out, uint32_t** vals_out) {
+                             uint32_t** keys_out, uint32_t** vals_out, uint32_t* status) {
     *keys_out = keys;
     *vals_out = vals;
     if (n == 0) return cudaSuccess;
     return lsd_passes(keys, vals, keys_alt, vals_alt, hist, scan_tmp, n, bits, digit_bits(bits), st, pdl, keys_out,
-                      vals_out);
+                      vals_out, status);
 }
 
 bool radix_sort_in_alt(int bits) {
@@ -308,7 +311,7 @@ cudaError_t launch_sort(Scene& s) {
     // the sorted pairs stay where the last pass wrote them (no copy back)
     uint32_t *k_res, *v_res;
     cudaError_t e = radix_sort_pairs(s.keys, s.vals, s.keys_alt, s.vals_alt, s.sort_hist, s.sort_scan_tmp, s.n,
-                                     key_bits(s), s.stream, s.use_pdl, &k_res, &v_res);
+                                     key_bits(s), s.stream, s.use_pdl, &k_res, &v_res, &s.ctl->status);
     if (e != cudaSuccess) return e;
     return launch_permute(s, v_res);
 }
@@ -326,7 +329,7 @@ cudaError_t radix_sort_pairs_in(uint32_t* keys, uint32_t* vals, uint32_t* keys_a
     if (n == 0) return cudaSuccess;
     uint32_t *k_res, *v_res;
     cudaError_t e = lsd_passes(keys, vals, keys_alt, vals_alt, hist, scan_tmp, n, bits, bits > 0 ? 8 : 0, st,
-                               st != nullptr, &k_res, &v_res);
+                               st != nullptr, &k_res, &v_res, nullptr);
     if (e != cudaSuccess) return e;
     if (k_res != keys) {
         cudaMemcpyAsync(keys, k_res, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
