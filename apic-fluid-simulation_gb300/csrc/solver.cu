@@ -40,8 +40,8 @@ constexpr uint32_t kDeltaChunk = 8192;  // apply_matrix_and_dot's par_chunks(819
 __device__ __forceinline__ uint32_t gwarp() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
 __device__ __forceinline__ uint32_t gnwarps() { return (gridDim.x * blockDim.x) >> 5; }
 
-__global__ void k_pcg_begin(Ctl* ctl, int stamp) {
-    if (stamp) ctl->solve_t0 = global_ns();
+// A PCG solve's starting state.
+__device__ __forceinline__ void pcg_reset(Ctl* ctl) {
     ctl->pcg_done = 0;
     ctl->pcg_iters = 0;
     ctl->gamma = 0.0f;
@@ -50,6 +50,11 @@ __global__ void k_pcg_begin(Ctl* ctl, int stamp) {
     ctl->beta_valid = 0;
     ctl->delta_stop = 0;
     ctl->rnorm2 = 0.0;
+}
+
+__global__ void k_pcg_begin(Ctl* ctl, int stamp) {
+    if (stamp) ctl->solve_t0 = global_ns();
+    pcg_reset(ctl);
 }
 
 // ---- PCG kernels on the base level (phases in pcg_common.cuh) --------------
@@ -184,44 +189,58 @@ __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, float2*
 // zero outside the fluid cells (apply_preconditioner zeroes it, :1790-1792,
 // and only fluid cells are smoothed or prolonged), and adding a zero product
 // leaves a lane sum unchanged (the sums start at +0 and never become -0), so
-// only the fluid cells' products count.  One block: all threads stage the
+// only the fluid cells' products count.  One block: warps 1..31 stage the
 // products of a batch of segments (32 raw cells each, zero where not fluid)
-// in shared memory, then threads 0..7 add their lane's products in order;
-// only those eight add chains are serial.
+// in shared memory while threads 0..7 add the previous batch's products of
+// their lane in order (two stage buffers); only those eight add chains are
+// serial.
 // start: the solve's first gamma (sets gamma and the SAFTY exit,
 // :1887-1892), else the iteration's new gamma.
 constexpr int kGammaThreads = 1024;
 constexpr uint32_t kGammaBatch = 512;  // segments staged per round (64 KB)
-constexpr size_t kGammaSmem = size_t(kGammaBatch) * 32 * sizeof(float);
+constexpr size_t kGammaSmem = 2 * size_t(kGammaBatch) * 32 * sizeof(float);
 // The iteration's form (start 0) also finishes the iteration (beta, or the
 // SAFTY exit) and, when set_cond, sets the loop condition.
 __global__ void __launch_bounds__(kGammaThreads) k_gamma_exact(Level B, Ctl* ctl, int start,
                                                                cudaGraphConditionalHandle h, uint32_t cap,
                                                                int dyn_cap, int set_cond) {
-    extern __shared__ float stage[];
+    extern __shared__ float stage[];  // two buffers of kGammaBatch segments
     pdl_wait();
     if (ctl->pcg_done) return;
     const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const uint32_t nseg = ctl->seg_count[0];
     const uint32_t full = (B.cells / 8u) * 8u;
-    float acc = 0.0f;
-    for (uint32_t k0 = 0; k0 < nseg; k0 += kGammaBatch) {
-        const uint32_t nb = min(kGammaBatch, nseg - k0);
-        for (uint32_t q = warp; q < nb; q += kGammaThreads / 32) {
+    const uint32_t nbatch = (nseg + kGammaBatch - 1) / kGammaBatch;
+    // warps 1..31 stage batch b into buffer b % 2
+    auto fill = [&](uint32_t b) {
+        float* buf = stage + (b & 1u) * kGammaBatch * 32u;
+        const uint32_t k0 = b * kGammaBatch, nb = min(kGammaBatch, nseg - k0);
+        for (uint32_t q = warp - 1; q < nb; q += kGammaThreads / 32 - 1) {
             const uint32_t w = B.seg[k0 + q];
             const uint32_t raw = w * 32u + lane;
             const bool on = ((B.fluid[w] >> lane) & 1u) && raw < full;
-            stage[q * 32u + lane] = on ? B.res[raw + B.w] * B.err[raw + B.w] : 0.0f;
+            buf[q * 32u + lane] = on ? B.res[raw + B.w] * B.err[raw + B.w] : 0.0f;
         }
-        __syncthreads();
-        if (t < 8)
-            for (uint32_t q = 0; q < nb; ++q) {
-                const float* p = stage + q * 32u + t;
-                acc = acc + p[0];
-                acc = acc + p[8];
-                acc = acc + p[16];
-                acc = acc + p[24];
+    };
+    float acc = 0.0f;
+    if (warp != 0 && nbatch > 0) fill(0);
+    __syncthreads();
+    for (uint32_t b = 0; b < nbatch; ++b) {
+        if (warp == 0) {
+            if (t < 8) {
+                const float* buf = stage + (b & 1u) * kGammaBatch * 32u;
+                const uint32_t nb = min(kGammaBatch, nseg - b * kGammaBatch);
+                for (uint32_t q = 0; q < nb; ++q) {
+                    const float* p = buf + q * 32u + t;
+                    acc = acc + p[0];
+                    acc = acc + p[8];
+                    acc = acc + p[16];
+                    acc = acc + p[24];
+                }
             }
+        } else if (b + 1 < nbatch) {
+            fill(b + 1);
+        }
         __syncthreads();
     }
     __shared__ float lanes[8];
@@ -359,9 +378,12 @@ __global__ void __launch_bounds__(kSegBlock) k_true_residual(Level B, const doub
         ctl->true_rel = ctl->bnorm2 > 0.0 ? sqrt(tot / ctl->bnorm2) : 0.0;
 }
 
+// p64 += x (finalize 0; the refinement also counts the inner solve's
+// iterations), or pressure = float(p64) (finalize 1).
 __global__ void __launch_bounds__(kSegBlock) k_mixed_accumulate(Level B, double* p64, const float* x, float* pressure,
-                                                                const Ctl* ctl, int finalize) {
+                                                                Ctl* ctl, int finalize) {
     pcg::ph_accumulate(B, ctl->seg_count[0], gwarp(), gnwarps(), p64, x, pressure, finalize);
+    if (!finalize && blockIdx.x == 0 && threadIdx.x == 0) ctl->used_iters += ctl->pcg_iters;
 }
 
 __global__ void __launch_bounds__(kSegBlock) k_pressure_to64(Level B, const float* pressure, double* p64,
@@ -410,12 +432,11 @@ __global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol
         ctl->inner_cap = cap - ctl->used_iters;
         double t = kInnerReduction * ctl->true_rel;  // target relative to ||b||
         ctl->target_rel = t > 0.5 * tol ? t : 0.5 * tol;
+        pcg_reset(ctl);  // the inner solve that follows starts here
     }
     ctl->cond = cont ? 1u : 0u;
     if (graph) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
-
-__global__ void k_refine_post(Ctl* ctl) { ctl->used_iters += ctl->pcg_iters; }
 
 __global__ void k_refine_end(Ctl* ctl, double tol) {
     ctl->solve_ns += global_ns() - ctl->solve_t0;
@@ -461,8 +482,10 @@ static void pcg_iteration(Scene& s, int mode, float* x, int p_padded) {
 
 // PCG setup (src/apic.rs:1885-1892) followed by a device-controlled WHILE
 // loop over iterations.
+// begin: reset the PCG state first (the refinement loop's k_refine_cond has
+// already done so for its inner solves).
 static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p_padded, uint32_t cap, int dyn_cap,
-                             bool clear_pressure) {
+                             bool clear_pressure, bool begin = true) {
     const Level& B = s.lv[0];
     uint32_t g = seg_grid(B.words);
     cudaGraphConditionalHandle h;
@@ -471,7 +494,7 @@ static cudaError_t build_pcg(Scene& s, GraphCursor& c, int mode, float* x, int p
     e = capture_into(s, c, [&]() {
         cudaStream_t st = s.stream;
         // only the reference-mode solve clears the pressure, and it starts here
-        k_pcg_begin<<<1, 1, 0, st>>>(s.ctl, clear_pressure ? 1 : 0);
+        if (begin) k_pcg_begin<<<1, 1, 0, st>>>(s.ctl, clear_pressure ? 1 : 0);
         if (clear_pressure) k_clear_pressure<<<g, kSegBlock, 0, st>>>(B, s.pressure, s.ctl);
         if (mode == APIC_SOLVER_REFERENCE) k_seg_prefix<<<1, 1024, 0, st>>>(B, s.ctl, s.seg_pre);
         enqueue_vcycle(s);
@@ -552,12 +575,11 @@ cudaError_t build_solve(Scene& s, GraphCursor& c) {
     GraphCursor body;
     e = add_conditional_with(c, cudaGraphCondTypeWhile, hr, &body);
     if (e != cudaSuccess) return e;
-    e = build_pcg(s, body, APIC_SOLVER_REL_FP32, s.corr, 1, s.max_iter, 1, false);
+    e = build_pcg(s, body, APIC_SOLVER_REL_FP32, s.corr, 1, s.max_iter, 1, false, false);
     if (e != cudaSuccess) return e;
     e = capture_into(s, body, [&]() {
         cudaStream_t st = s.stream;
         k_mixed_accumulate<<<g, kSegBlock, 0, st>>>(B, s.p64, s.corr, s.pressure, s.ctl, 0);
-        k_refine_post<<<1, 1, 0, st>>>(s.ctl);
         k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 3);
         k_refine_cond<<<1, 1, 0, st>>>(s.ctl, hr, tol, s.max_iter, 1);
         return cudaGetLastError();
@@ -637,7 +659,6 @@ cudaError_t run_solve_eager(Scene& s) {
         if (!s.ctl_host->cond) break;
         if ((e = eager_pcg(s, APIC_SOLVER_REL_FP32, s.corr, 1, s.ctl_host->inner_cap, false)) != cudaSuccess) return e;
         k_mixed_accumulate<<<g, kSegBlock, 0, st>>>(B, s.p64, s.corr, s.pressure, s.ctl, 0);
-        k_refine_post<<<1, 1, 0, st>>>(s.ctl);
         k_true_residual<<<g, kSegBlock, 0, st>>>(B, s.b64, s.p64, s.corr, s.ctl, s.partials, 3);
         k_refine_cond<<<1, 1, 0, st>>>(s.ctl, 0, tol, s.max_iter, 0);
     }
