@@ -81,7 +81,12 @@ __global__ void __launch_bounds__(kSegBlock) k_smooth(Level L, int li, const Ctl
 }
 
 // Restriction only (into the first tail level or the coarsest level).
-__global__ void __launch_bounds__(kSegBlock) k_restrict(Level f, Level c, int lc, const Ctl* ctl) {
+// The transfer kernels come in two register budgets: kMinB 8 (32 registers,
+// eight CTAs per SM, a few spilled values) for levels of more than 2 M cells,
+// whose launches are bandwidth and occupancy bound (4096^2: 895 vs 983 us per
+// PCG iteration), and the unbounded form for the smaller, latency-bound ones.
+template <int kMinB>
+__global__ void __launch_bounds__(kSegBlock, kMinB) k_restrict(Level f, Level c, int lc, const Ctl* ctl) {
     const uint32_t nseg = ctl->seg_count[lc];
     const uint32_t w0 = early_word(c.seg, nseg);
     pdl_wait();
@@ -90,7 +95,8 @@ __global__ void __launch_bounds__(kSegBlock) k_restrict(Level f, Level c, int lc
 }
 
 // Restriction fused with the coarse level's first (red) sweep.
-__global__ void __launch_bounds__(kSegBlock) k_restrict_red(Level f, Level c, int lc, const Ctl* ctl) {
+template <int kMinB>
+__global__ void __launch_bounds__(kSegBlock, kMinB) k_restrict_red(Level f, Level c, int lc, const Ctl* ctl) {
     const uint32_t nseg = ctl->seg_count[lc];
     const uint32_t w0 = early_word(c.seg, nseg);
     pdl_wait();
@@ -99,7 +105,8 @@ __global__ void __launch_bounds__(kSegBlock) k_restrict_red(Level f, Level c, in
 }
 
 // Prolongation fused with the black sweep.
-__global__ void __launch_bounds__(kSegBlock) k_prolong_black(Level c, Level f, int lf, const Ctl* ctl, int base) {
+template <int kMinB>
+__global__ void __launch_bounds__(kSegBlock, kMinB) k_prolong_black(Level c, Level f, int lf, const Ctl* ctl, int base) {
     const uint32_t nseg = ctl->seg_count[lf];
     const uint32_t w0 = early_word(f.seg, nseg);
     const uint32_t last = base ? ctl->last_fluid : 0xFFFFFFFFu, extra = base ? ctl->pad_count : 0u;
@@ -174,6 +181,7 @@ void plan_vcycle(Scene& s) {
 // per transfer on the levels above the distributed-shared-memory cluster or
 // the tail (the reference's sequence launch by launch).  Returns false when
 // the caller must reduce r.z itself (a grid without multigrid levels).
+constexpr uint32_t kBigLevelWords = 65536;  // 2 M cells
 bool enqueue_vcycle(Scene& s, bool base_red_done, int rz_mode, bool residual_exit) {
     cudaStream_t st = s.stream;
     Level* L = s.lv;
@@ -194,34 +202,46 @@ bool enqueue_vcycle(Scene& s, bool base_red_done, int rz_mode, bool residual_exi
     }
     const bool dsm = s.use_dsm && s.dsm_first < s.dsm_tail && s.dsm_tail < s.nlevels;
     int deepest_mid = 0;  // deepest level smoothed by the global kernels
+    auto big = [&](int l) { return L[l].words > kBigLevelWords; };
+    auto restrict_red = [&](int l) {
+        launch(pdl, big(l) ? k_restrict_red<8> : k_restrict_red<1>, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l,
+               s.ctl);
+    };
+    auto restrict_plain = [&](int l) {
+        launch(pdl, big(l) ? k_restrict<8> : k_restrict<1>, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
+    };
+    auto prolong_black = [&](int l, int base) {
+        launch(pdl, big(l) ? k_prolong_black<8> : k_prolong_black<1>, grid(l), kSegBlock, 0, st, L[l + 1], L[l], l,
+               s.ctl, base);
+    };
     for (int l = 1; l <= last; ++l) {
         if (dsm && l == s.dsm_first) {
-            launch(pdl, k_restrict_red, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
+            restrict_red(l);
             launch_vcycle_dsm(s, st);
             break;
         }
         if (l == s.tail_first) {
-            launch(pdl, k_restrict, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
+            restrict_plain(l);
             uint32_t off = 0;
             TailParams tp = make_tail_params(s, l, &off);
             launch(pdl, k_vcycle_tail, 1, kTailThreads, size_t(off) * 4, st, tp, s.ctl);
             break;
         }
         if (l == last) {
-            launch(pdl, k_restrict, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
+            restrict_plain(l);
             launch(pdl, k_coarse_solve, 1, kTailThreads, 0, st, L[l], s.cg_s, s.cg_ap, s.cg_r, s.ctl,
                    coarse_cg_exact(s) ? 1 : 0);
             break;
         }
-        launch(pdl, k_restrict_red, grid(l), kSegBlock, 0, st, L[l - 1], L[l], l, s.ctl);
+        restrict_red(l);
         launch(pdl, k_smooth, grid(l), kSegBlock, 0, st, L[l], l, s.ctl, 1, 1);
         deepest_mid = l;
     }
     for (int l = deepest_mid; l >= 1; --l) {
-        launch(pdl, k_prolong_black, grid(l), kSegBlock, 0, st, L[l + 1], L[l], l, s.ctl, 0);
+        prolong_black(l, 0);
         launch(pdl, k_prolong_red, grid(l), kSegBlock, 0, st, L[l + 1], L[l], l, s.ctl, 0);
     }
-    launch(pdl, k_prolong_black, grid(0), kSegBlock, 0, st, L[1], L[0], 0, s.ctl, 1);
+    prolong_black(0, 1);
     if (rz_mode >= 0)
         launch(pdl, k_prolong_red_rz, grid(0), kSegBlock, 0, st, L[1], L[0], static_cast<const Ctl*>(s.ctl),
                part_rz(s));
