@@ -98,31 +98,42 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_u32(uint32_t v, uint32_
     return pre + x - v;
 }
 
+// Four particles per thread with 16-byte loads and stores (the arrays hold
+// npad, a multiple of 8, lanes; keys of lanes n .. npad-1 are never read).
 __global__ void __launch_bounds__(256) k_p2g_bin_keys(const PartPtrs* __restrict__ pp, uint32_t n, int W, int H,
                                                       float dx, uint32_t* __restrict__ keys,
                                                       uint32_t* __restrict__ vals, uint32_t* __restrict__ fluid) {
     pdl_wait();
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = i < n;
-    uint32_t word = 0xFFFFFFFFu, bit = 0;
-    if (live) {
-        const float gx = pp->f[PX][i] / dx, gy = pp->f[PY][i] / dx;
+    const uint32_t i0 = 4u * (blockIdx.x * blockDim.x + threadIdx.x);
+    const bool any = i0 < n;
+    float4 px = make_float4(0.0f, 0.0f, 0.0f, 0.0f), py = px;
+    if (any) {
+        px = *reinterpret_cast<const float4*>(pp->f[PX] + i0);
+        py = *reinterpret_cast<const float4*>(pp->f[PY] + i0);
+    }
+    const float xs[4] = {px.x, px.y, px.z, px.w}, ys[4] = {py.x, py.y, py.z, py.w};
+    uint32_t k[4];
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const bool live = i0 + uint32_t(q) < n;
+        const float gx = xs[q] / dx, gy = ys[q] / dx;
         const int cx0 = max(min(trunc_x86(floorf(gx - 0.5f)), W - 1), 0);
         const int cy0 = max(min(trunc_x86(floorf(gy - 0.5f)), H - 1), 0);
-        keys[i] = uint32_t(cy0) * uint32_t(W) + uint32_t(cx0);
-        vals[i] = i;
-        // the particle's own cell (:1358-1360)
+        k[q] = uint32_t(cy0) * uint32_t(W) + uint32_t(cx0);
+        // the particle's own cell (:1358-1360); one OR per mask word the warp touches
         const int fx = trunc_x86(fmax_x86(fmin_x86(gx, float(W) - 1.0f), 0.0f));
         const int fy = trunc_x86(fmax_x86(fmin_x86(gy, float(H) - 1.0f), 0.0f));
         const uint32_t fi = uint32_t(fy * W + fx);
-        word = fi >> 5;
-        bit = 1u << (fi & 31u);
+        const uint32_t word = live ? fi >> 5 : 0xFFFFFFFFu, bit = live ? 1u << (fi & 31u) : 0u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, word);
+        const uint32_t m = __reduce_or_sync(peers, bit);
+        if (live && (peers & ((1u << lane) - 1u)) == 0) atomicOr(fluid + word, m);
     }
-    // one OR per mask word that the warp touches
-    const uint32_t peers = __match_any_sync(0xffffffffu, word);
-    const uint32_t m = __reduce_or_sync(peers, bit);
-    const int lane = threadIdx.x & 31;
-    if (live && (peers & ((1u << lane) - 1u)) == 0) atomicOr(fluid + word, m);
+    if (any) {
+        *reinterpret_cast<uint4*>(keys + i0) = make_uint4(k[0], k[1], k[2], k[3]);
+        *reinterpret_cast<uint4*>(vals + i0) = make_uint4(i0, i0 + 1, i0 + 2, i0 + 3);
+    }
 }
 
 __global__ void __launch_bounds__(256) k_p2g_bounds(const uint32_t* __restrict__ keys, uint32_t n,
@@ -835,14 +846,21 @@ __global__ void __launch_bounds__(256, 4) k_g2p(const PartPtrs* __restrict__ pp,
     block_max_count(speed_out, bad, ctl);
 }
 
+// Max |v| over all npad lanes (a multiple of 8): a grid of one wave, four
+// lanes per step with 16-byte loads, one atomic per block.
 __global__ void __launch_bounds__(256) k_vmax(const PartPtrs* __restrict__ pp, uint32_t npad, Ctl* __restrict__ ctl) {
     pdl_wait();
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float m = 0.0f;
-    if (i < npad) {
-        float vx = pp->f[VX][i], vy = pp->f[VY][i];
-        float mg = sqrtf(vx * vx + vy * vy);
-        m = (mg == mg) ? mg : 0.0f;
+    const float* vx = pp->f[VX];
+    const float* vy = pp->f[VY];
+    for (uint32_t i0 = 4u * (blockIdx.x * blockDim.x + threadIdx.x); i0 < npad; i0 += 4u * gridDim.x * blockDim.x) {
+        const float4 x = *reinterpret_cast<const float4*>(vx + i0), y = *reinterpret_cast<const float4*>(vy + i0);
+        const float xs[4] = {x.x, x.y, x.z, x.w}, ys[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float mg = sqrtf(xs[q] * xs[q] + ys[q] * ys[q]);
+            m = fmaxf(m, (mg == mg) ? mg : 0.0f);
+        }
     }
     block_max_count(m, 0u, ctl);
 }
@@ -914,7 +932,7 @@ cudaError_t launch_p2g(Scene& s) {
     if (e != cudaSuccess) return e;
     const uint32_t* svals = s.bin_vals;
     if (s.n > 0) {
-        launch(s.use_pdl, k_p2g_bin_keys, div_up(s.n, 256), 256, 0, s.stream, static_cast<const PartPtrs*>(s.pp), s.n,
+        launch(s.use_pdl, k_p2g_bin_keys, div_up(s.n, 1024), 256, 0, s.stream, static_cast<const PartPtrs*>(s.pp), s.n,
                int(s.W), int(s.H), s.dx, s.bin_keys, s.bin_vals, s.lv[0].fluid);
         uint32_t *kres, *vres;
         e = radix_sort_pairs(s.bin_keys, s.bin_vals, s.bin_keys_alt, s.bin_vals_alt, s.sort_hist, s.sort_scan_tmp, s.n,
@@ -948,24 +966,30 @@ cudaError_t launch_g2p(Scene& s) {
 // Zero the running maximum, then reduce over the current velocities.
 cudaError_t launch_vmax(Scene& s) {
     launch(s.use_pdl, k_zero_vmax, 1, 1, 0, s.stream, s.ctl);
-    if (s.npad) launch(s.use_pdl, k_vmax, div_up(s.npad, 256), 256, 0, s.stream, s.pp, s.npad, s.ctl);
+    if (s.npad) {
+        const uint32_t g = std::min(div_up(s.npad, 1024), uint32_t(kMaxRedBlocks));
+        launch(s.use_pdl, k_vmax, g, 256, 0, s.stream, s.pp, s.npad, s.ctl);
+    }
     return cudaGetLastError();
 }
 
 // Interleave two SoA particle fields into the reference's Vec2x8 layout
 // (per chunk: 8 x lanes then 8 y lanes), for one contiguous copy to the host.
+// Thread t writes 16 bytes of the packed output: chunk t / 4, quarter t % 4
+// (quarters 0-1: x lanes 0-3, 4-7; quarters 2-3: y lanes).
 __global__ void __launch_bounds__(256) k_pack_vec2x8(const PartPtrs* __restrict__ pp, int fx, int fy, uint32_t nchunks,
                                                      float* __restrict__ out) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nchunks * 16u) return;
-    const uint32_t c = i >> 4, j = i & 15u;
-    out[i] = j < 8u ? pp->f[fx][c * 8u + j] : pp->f[fy][c * 8u + (j - 8u)];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nchunks * 4u) return;
+    const uint32_t c = t >> 2, q = t & 3u;
+    const float* src = (q < 2u ? pp->f[fx] : pp->f[fy]) + c * 8u + (q & 1u) * 4u;
+    *reinterpret_cast<float4*>(out + size_t(t) * 4u) = *reinterpret_cast<const float4*>(src);
 }
 
 cudaError_t launch_pack_vec2x8(Scene& s, int which, float* out) {
     if (s.nchunks == 0) return cudaSuccess;
-    k_pack_vec2x8<<<div_up(uint64_t(s.nchunks) * 16, 256), 256, 0, s.stream>>>(s.pp, 2 * which, 2 * which + 1,
-                                                                             s.nchunks, out);
+    k_pack_vec2x8<<<div_up(uint64_t(s.nchunks) * 4, 256), 256, 0, s.stream>>>(s.pp, 2 * which, 2 * which + 1,
+                                                                            s.nchunks, out);
     return cudaGetLastError();
 }
 

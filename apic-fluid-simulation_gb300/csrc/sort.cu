@@ -30,16 +30,28 @@ constexpr int kItems = kSortTile / kSortThreads;  // 8 keys per thread
 constexpr uint32_t kMaxBuckets = 1u << kMaxDigitBits;
 constexpr int kScanBlock = 1024;                  // elements per scan block
 
-__global__ void k_morton_keys(const PartPtrs* __restrict__ pp, uint32_t n, float dx, float max_x, float max_y,
-                              uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+// Four particles per thread with 16-byte loads and stores: the particle
+// arrays and the pair buffers hold npad (a multiple of 8) lanes, so lanes
+// n .. npad-1 get keys too, which the sort of n pairs never reads.
+__global__ void __launch_bounds__(256) k_morton_keys(const PartPtrs* __restrict__ pp, uint32_t n, float dx, float max_x,
+                                                     float max_y, uint32_t* __restrict__ keys,
+                                                     uint32_t* __restrict__ vals) {
     pdl_wait();
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float gx = pp->f[PX][i] / dx, gy = pp->f[PY][i] / dx;  // Vec2x8 / f32x8: per-component division
-    uint32_t cx = uint32_t(trunc_x86(fmin_x86(fmax_x86(gx, 0.0f), max_x)));
-    uint32_t cy = uint32_t(trunc_x86(fmin_x86(fmax_x86(gy, 0.0f), max_y)));
-    keys[i] = morton(cx, cy);
-    vals[i] = i;
+    const uint32_t i0 = 4u * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (i0 >= n) return;
+    const float4 px = *reinterpret_cast<const float4*>(pp->f[PX] + i0);
+    const float4 py = *reinterpret_cast<const float4*>(pp->f[PY] + i0);
+    const float xs[4] = {px.x, px.y, px.z, px.w}, ys[4] = {py.x, py.y, py.z, py.w};
+    uint32_t k[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float gx = xs[q] / dx, gy = ys[q] / dx;  // Vec2x8 / f32x8: per-component division
+        const uint32_t cx = uint32_t(trunc_x86(fmin_x86(fmax_x86(gx, 0.0f), max_x)));
+        const uint32_t cy = uint32_t(trunc_x86(fmin_x86(fmax_x86(gy, 0.0f), max_y)));
+        k[q] = morton(cx, cy);
+    }
+    *reinterpret_cast<uint4*>(keys + i0) = make_uint4(k[0], k[1], k[2], k[3]);
+    *reinterpret_cast<uint4*>(vals + i0) = make_uint4(i0, i0 + 1, i0 + 2, i0 + 3);
 }
 
 // Per-tile digit histogram of a `dbits`-bit digit (dbits <= kMaxDigitBits),
@@ -307,7 +319,8 @@ bool radix_sort_in_alt(int bits) {
 cudaError_t launch_sort(Scene& s) {
     if (s.n == 0) return cudaSuccess;
     float max_x = float(s.W > 0 ? s.W - 1 : 0), max_y = float(s.H > 0 ? s.H - 1 : 0);
-    launch(s.use_pdl, k_morton_keys, div_up(s.n, 256), 256, 0, s.stream, s.pp, s.n, s.dx, max_x, max_y, s.keys, s.vals);
+    launch(s.use_pdl, k_morton_keys, div_up(s.n, 1024), 256, 0, s.stream, s.pp, s.n, s.dx, max_x, max_y, s.keys,
+           s.vals);
     // the sorted pairs stay where the last pass wrote them (no copy back)
     uint32_t *k_res, *v_res;
     cudaError_t e = radix_sort_pairs(s.keys, s.vals, s.keys_alt, s.vals_alt, s.sort_hist, s.sort_scan_tmp, s.n,
