@@ -23,6 +23,8 @@ LIB_PATH = os.path.join(_PKG_ROOT, "lib", "libapic_gpu.so")
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_NONFINITE, ERR_NOT_CONVERGED, ERR_NO_DEVICE = range(8)
 ERR_UNSUPPORTED = 8
 UPDATE_DISABLE_SORT = 0x1
+UPDATE_BATCH_STREAMS = 0x2  # apic_update_batch: each scene on its own stream
+UPDATE_BATCH_JOINT = 0x4    # apic_update_batch: the joint form whenever it applies
 SOLVER_REFERENCE, SOLVER_REL_FP32, SOLVER_REL_MIXED = 0, 1, 2
 SERVER_ROUNDS, SERVER_CONTINUOUS = 0, 1
 SCENE_REFERENCE_DEFAULT, SCENE_DAM_BREAK, SCENE_DAM_BREAK_DISK, SCENE_NOISE = 0, 1, 2, 3
@@ -95,6 +97,13 @@ class RequestInfoC(ctypes.Structure):
                 ("max_true_residual", ctypes.c_double), ("submit_ms", ctypes.c_double),
                 ("admit_ms", ctypes.c_double), ("done_ms", ctypes.c_double), ("bytes", ctypes.c_uint64),
                 ("result_floats", ctypes.c_uint64)]
+
+
+class BatchInfoC(ctypes.Structure):
+    _fields_ = [("scenes", ctypes.c_uint32), ("joint", ctypes.c_uint32), ("batch_kernel_launches", ctypes.c_uint64),
+                ("substep_rounds", ctypes.c_uint32), ("refine_rounds", ctypes.c_uint32),
+                ("pcg_rounds", ctypes.c_uint32), ("tuned", ctypes.c_uint32), ("chunk_segs", ctypes.c_uint32),
+                ("block_group", ctypes.c_uint32)]
 
 
 class ServerStatsC(ctypes.Structure):
@@ -181,6 +190,7 @@ SIGNATURES = {
     "apic_debug_finish_substep": (ctypes.c_int, [_VP, ctypes.c_float]),
     "apic_update_batch": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
                                          ctypes.POINTER(ctypes.c_int)]),
+    "apic_batch_last_info": (ctypes.c_int, [ctypes.POINTER(BatchInfoC)]),
     "apic_place_scenes": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                                          ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
                                          ctypes.POINTER(ctypes.c_int32)]),
@@ -532,14 +542,30 @@ class Apic:
 
 # ---- batched and served scenes (no counterpart in the reference) -------------
 
-def update_batch(sims, debug_options: DebugOptions | None = None, frame_deltatime: float = 1 / 60) -> list[int]:
-    """One update of every scene in `sims`, enqueued side by side (apic_update_batch)."""
+def update_batch(sims, debug_options: DebugOptions | None = None, frame_deltatime: float = 1 / 60,
+                 streams: bool = False, joint: bool = False) -> list[int]:
+    """One update of every scene in `sims` (apic_update_batch), in the form
+    the library's batch tuner chose for this makeup of scenes: the pressure
+    solves as one launch per phase over all scenes, or every scene's update
+    on its own stream.  streams=True / joint=True force one of the two."""
     lib = load_library()
     flags = UPDATE_DISABLE_SORT if (debug_options is not None and debug_options.disable_particle_sort) else 0
+    if streams:
+        flags |= UPDATE_BATCH_STREAMS
+    if joint:
+        flags |= UPDATE_BATCH_JOINT
     arr = (_VP * len(sims))(*[s._h for s in sims])
     status = (ctypes.c_int * len(sims))()
     _check(lib.apic_update_batch(arr, len(sims), flags, frame_deltatime, status), "apic_update_batch")
     return list(status)
+
+
+def batch_last_info() -> dict:
+    """The last update_batch call: scenes, joint (1: solves as one launch per
+    phase), the batch's own kernel launches and its loop rounds."""
+    out = BatchInfoC()
+    _check(load_library().apic_batch_last_info(ctypes.byref(out)), "apic_batch_last_info")
+    return {f: getattr(out, f) for f, _ in BatchInfoC._fields_}
 
 
 def scene_bytes(width: int, height: int, particles: int) -> int:

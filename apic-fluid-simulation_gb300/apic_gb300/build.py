@@ -19,7 +19,7 @@ BUILD_DIR = os.path.join(PKG_ROOT, "_build")
 LIB_DIR = os.path.join(PKG_ROOT, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libapic_gpu.so")
 
-CUDA_SOURCES = ["sort.cu", "particles.cu", "grid.cu", "vcycle.cu", "vcycle_dsm.cu", "solver.cu",
+CUDA_SOURCES = ["sort.cu", "particles.cu", "grid.cu", "vcycle.cu", "vcycle_dsm.cu", "solver.cu", "batch.cu",
                 "runtime.cu", "noalloc.cu", "serve.cu", "render.cu"]
 CXX_SOURCES = ["scene.cpp"]
 

@@ -202,6 +202,19 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
+// ---- block coordinates ----
+// A block's index within its scene's grid and that grid's size in blocks.  A
+// launch for one scene uses the hardware's values; a launch over many scenes
+// (one grid whose blocks map to (scene, block) pairs through a table) gives
+// each scene's blocks the indices that a launch of that scene alone would
+// give them, so block partials and their sums come out the same bit for bit.
+struct Blk {
+    uint32_t id, n;
+};
+__device__ __forceinline__ Blk hw_blk() { return Blk{blockIdx.x, gridDim.x}; }
+__device__ __forceinline__ uint32_t blk_warp(Blk b) { return (b.id * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ uint32_t blk_nwarps(Blk b) { return (b.n * blockDim.x) >> 5; }
+
 // ---- reductions ----
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -214,12 +227,12 @@ __device__ __forceinline__ float warp_maxf(float v) {
     return v;
 }
 
-// Deterministic block sum into partials[blockIdx.x]; returns true in the last
+// Deterministic block sum into partials[bk.id]; returns true in the last
 // block to finish, whose thread 0 receives the total of all partials (summed
 // by a fixed strided pattern and tree, so the result does not depend on
 // scheduling; no block waits on another).
 template <int kThreads>
-__device__ __forceinline__ bool block_sum_last(double v, double* partials, uint32_t* counter, double* total) {
+__device__ __forceinline__ bool block_sum_last(Blk bk, double v, double* partials, uint32_t* counter, double* total) {
     __shared__ double s_w[kThreads / 32];
     __shared__ bool s_last;
     v = warp_sum(v);
@@ -229,17 +242,17 @@ __device__ __forceinline__ bool block_sum_last(double v, double* partials, uint3
     if (threadIdx.x == 0) {
         double b = 0;
         for (int w = 0; w < kThreads / 32; ++w) b += s_w[w];
-        partials[blockIdx.x] = b;
+        partials[bk.id] = b;
         __threadfence();
         uint32_t prev = atomicAdd(counter, 1u);
-        s_last = (prev == gridDim.x - 1);
+        s_last = (prev == bk.n - 1);
     }
     __syncthreads();
     if (!s_last) return false;
     __threadfence();
     const volatile double* vp = partials;
     double t = 0;
-    for (uint32_t b = threadIdx.x; b < gridDim.x; b += kThreads) t += vp[b];
+    for (uint32_t b = threadIdx.x; b < bk.n; b += kThreads) t += vp[b];
     t = warp_sum(t);
     __syncthreads();
     if (lane == 0) s_w[warp] = t;
@@ -293,7 +306,7 @@ __device__ __forceinline__ F2 warp_sum(F2 v) {
 // block_sum_last for double-float sums; partials holds one F2 per block in
 // the 8 bytes of a double.
 template <int kThreads>
-__device__ __forceinline__ bool block_sum_last(F2 v, double* partials, uint32_t* counter, double* total) {
+__device__ __forceinline__ bool block_sum_last(Blk bk, F2 v, double* partials, uint32_t* counter, double* total) {
     __shared__ F2 s_f[kThreads / 32];
     __shared__ bool s_last_f;
     float2* part = reinterpret_cast<float2*>(partials);
@@ -304,16 +317,16 @@ __device__ __forceinline__ bool block_sum_last(F2 v, double* partials, uint32_t*
     if (threadIdx.x == 0) {
         F2 b{0.0f, 0.0f};
         for (int w = 0; w < kThreads / 32; ++w) b = f2_add(b, s_f[w]);
-        part[blockIdx.x] = make_float2(b.hi, b.lo);
+        part[bk.id] = make_float2(b.hi, b.lo);
         __threadfence();
         uint32_t prev = atomicAdd(counter, 1u);
-        s_last_f = (prev == gridDim.x - 1);
+        s_last_f = (prev == bk.n - 1);
     }
     __syncthreads();
     if (!s_last_f) return false;
     __threadfence();
     F2 t{0.0f, 0.0f};
-    for (uint32_t b = threadIdx.x; b < gridDim.x; b += kThreads) {
+    for (uint32_t b = threadIdx.x; b < bk.n; b += kThreads) {
         float2 q = __ldcg(part + b);  // from L2: written by other blocks
         t = f2_add(t, F2{q.x, q.y});
     }
@@ -357,9 +370,9 @@ __device__ __forceinline__ uint32_t seg_step(const uint32_t* seg, uint32_t nseg,
 // in the order of block_sum_last's last block, so both forms give the same
 // total.
 
-// This block's F2 sum (and, with mx, its maximum) into slot blockIdx.x.
+// This block's F2 sum (and, with mx, its maximum) into slot bk.id.
 template <int kThreads>
-__device__ __forceinline__ void block_store(F2 v, float2* part) {
+__device__ __forceinline__ void block_store(Blk bk, F2 v, float2* part) {
     __shared__ F2 s_bs[kThreads / 32];
     v = warp_sum(v);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -368,12 +381,12 @@ __device__ __forceinline__ void block_store(F2 v, float2* part) {
     if (threadIdx.x == 0) {
         F2 b{0.0f, 0.0f};
         for (int w = 0; w < kThreads / 32; ++w) b = f2_add(b, s_bs[w]);
-        part[blockIdx.x] = make_float2(b.hi, b.lo);
+        part[bk.id] = make_float2(b.hi, b.lo);
     }
 }
 
 template <int kThreads>
-__device__ __forceinline__ void block_store(F2 v, float mx, float4* part) {
+__device__ __forceinline__ void block_store(Blk bk, F2 v, float mx, float4* part) {
     __shared__ F2 s_bs[kThreads / 32];
     __shared__ float s_bm[kThreads / 32];
     v = warp_sum(v);
@@ -391,7 +404,7 @@ __device__ __forceinline__ void block_store(F2 v, float mx, float4* part) {
             b = f2_add(b, s_bs[w]);
             m = fmaxf(m, s_bm[w]);
         }
-        part[blockIdx.x] = make_float4(b.hi, b.lo, m, 0.0f);
+        part[bk.id] = make_float4(b.hi, b.lo, m, 0.0f);
     }
 }
 

@@ -23,28 +23,35 @@ struct GraphCursor {
     std::vector<cudaGraphNode_t> tail;
 };
 
-// Record the launches that `f` enqueues on s.stream as nodes of c.g after c.tail.
-template <class F> cudaError_t capture_into(Scene& s, GraphCursor& c, F&& f) {
-    cudaError_t e = cudaStreamBeginCaptureToGraph(s.cap_stream, c.g, c.tail.empty() ? nullptr : c.tail.data(), nullptr,
+// Record the launches that `f` enqueues on the capture stream `cap` as nodes
+// of c.g after c.tail.
+template <class F> cudaError_t capture_on(cudaStream_t cap, GraphCursor& c, F&& f) {
+    cudaError_t e = cudaStreamBeginCaptureToGraph(cap, c.g, c.tail.empty() ? nullptr : c.tail.data(), nullptr,
                                                   c.tail.size(), cudaStreamCaptureModeRelaxed);
     if (e != cudaSuccess) return e;
-    cudaStream_t saved = s.stream;
-    s.stream = s.cap_stream;
     cudaError_t fe = f();
-    s.stream = saved;
     cudaStreamCaptureStatus st;
     const cudaGraphNode_t* deps = nullptr;
     size_t nd = 0;
-    cudaError_t ge = cudaStreamGetCaptureInfo(s.cap_stream, &st, nullptr, nullptr, &deps, nullptr, &nd);
+    cudaError_t ge = cudaStreamGetCaptureInfo(cap, &st, nullptr, nullptr, &deps, nullptr, &nd);
     std::vector<cudaGraphNode_t> nt;
     if (ge == cudaSuccess && deps) nt.assign(deps, deps + nd);
     cudaGraph_t out = nullptr;
-    cudaError_t ee = cudaStreamEndCapture(s.cap_stream, &out);
+    cudaError_t ee = cudaStreamEndCapture(cap, &out);
     if (fe != cudaSuccess) return fe;
     if (ge != cudaSuccess) return ge;
     if (ee != cudaSuccess) return ee;
     if (!nt.empty()) c.tail = nt;
     return cudaSuccess;
+}
+
+// Record the launches that `f` enqueues on s.stream as nodes of c.g after c.tail.
+template <class F> cudaError_t capture_into(Scene& s, GraphCursor& c, F&& f) {
+    cudaStream_t saved = s.stream;
+    s.stream = s.cap_stream;
+    cudaError_t e = capture_on(s.cap_stream, c, [&]() { return f(); });
+    s.stream = saved;
+    return e;
 }
 
 // Append a conditional node (IF or WHILE) after c.tail for handle h (created

@@ -86,6 +86,9 @@ struct Ctl {
     uint32_t last_fluid;    // padded index of the last base fluid cell
     uint32_t pad_count;     // duplicates padding the base list to a multiple of 8
     uint32_t red_counter;   // last-block-done counter of the reductions
+    uint32_t pcg_on;        // the PCG loop goes on (a batched solve gates its phases on it)
+    float b_rz;             // batched solve: the iteration's r.z sum (from the last V-cycle's parts)
+    float b_sap;            // batched solve: the iteration's s.Ap sum
 };
 
 enum : uint32_t {
@@ -211,6 +214,9 @@ struct Scene {
     int priority = 0;                         // stream priority: levels above the lowest
     cudaStream_t cap_stream = nullptr;        // stream used to record graphs
     cudaGraphExec_t update_exec = nullptr;    // whole Apic::update as one graph
+    uint64_t graph_version = 0;               // bumped whenever recorded graphs go stale
+    bool batched = false;                     // the last update ran inside a joint batch
+    uint32_t kn_bsort = 0, kn_bstep = 0;      // ... its own kernels there: sort, one substep
     bool use_pdl = true;                      // programmatic dependent launch inside the PCG loop
     // levels [dsm_first, dsm_tail) of the V-cycle held in a cluster's
     // distributed shared memory, dsm_tail.. in CTA 0 (dsm_first == nlevels: none)
@@ -336,6 +342,18 @@ cudaError_t launch_advance(Scene& s);
 // runtime.cu: Apic::update split in two, so several scenes can be enqueued
 // before any is waited on (apic_update_batch, the request server)
 int update_launch(apic_handle* h, uint32_t flags, float frame_dt);
+int update_begin(apic_handle* h, uint32_t flags, float frame_dt);  // update_launch before the substep loop
+int update_end(apic_handle* h);                                    // ... and after it
+Scene& scene_of(apic_handle* h);
+cudaError_t scene_pre_solve(Scene& s);   // the substep's stages before the pressure solve
+cudaError_t scene_post_solve(Scene& s);  // ... and after it
+// batch.cu: apic_update_batch with the solves as one launch per phase
+bool batch_eligible(apic_handle* const* handles, uint32_t count);
+int update_batch_joint(apic_handle* const* handles, uint32_t count, uint32_t flags, float frame_dt, int* rc);
+void batch_note_streams(uint32_t count);
+int batch_choose(apic_handle* const* handles, uint32_t count, bool force_joint);  // 1 joint, 0 streams
+void batch_record(double wall_ms, uint64_t iterations);
+void batch_release_scene(const Scene* s);
 int create_scene(uint32_t width, uint32_t height, float cell_size, const apic_world_props* props,
                  bool default_particles, apic_handle** out);
 int update_finish(apic_handle* h);

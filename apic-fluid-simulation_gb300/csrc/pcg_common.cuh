@@ -204,12 +204,17 @@ __device__ __forceinline__ void finish_rz_reference(Ctl* ctl, float ng) {
 // refinement).  In the relative modes a continuing loop's next iteration
 // forms beta from the r.z parts that this iteration's V-cycle stores
 // (beta_valid); the reference mode's k_gamma_exact does that itself.  Run by
-// thread 0 of one block; sets the graph's loop condition when set_cond.
-__device__ __forceinline__ void loop_decision(Ctl* ctl, int mode, cudaGraphConditionalHandle h, uint32_t cap,
-                                              int dyn_cap, int set_cond) {
+// thread 0 of one block; loop_decision sets the graph's loop condition when
+// set_cond.
+__device__ __forceinline__ bool loop_continue(Ctl* ctl, int mode, uint32_t cap, int dyn_cap) {
     const uint32_t c = dyn_cap ? ctl->inner_cap : cap;
     const bool cont = !ctl->pcg_done && ctl->pcg_iters < c;
     if (cont && mode != APIC_SOLVER_REFERENCE) ctl->beta_valid = 1;
+    return cont;
+}
+__device__ __forceinline__ void loop_decision(Ctl* ctl, int mode, cudaGraphConditionalHandle h, uint32_t cap,
+                                              int dyn_cap, int set_cond) {
+    const bool cont = loop_continue(ctl, mode, cap, dyn_cap);
     if (set_cond) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 

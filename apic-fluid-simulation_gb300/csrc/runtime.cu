@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -21,6 +22,7 @@
 #include "apic_device.cuh"
 #include "apic_graph.h"
 #include "apic_internal.h"
+#include "substep.cuh"
 
 using namespace apic;
 
@@ -62,36 +64,7 @@ __global__ void k_begin_update(Ctl* ctl, float frame_dt, uint32_t flags, uint32_
     ctl->solve_ns = 0;
 }
 
-// Substep size (src/apic.rs:2433-2441) and the loop condition (:2432).
-__device__ void plan(Ctl* ctl) {
-    float t = ctl->t, frame = ctl->frame_dt;
-    if (!(t < frame)) { ctl->go = 0; return; }
-    float vmax = __uint_as_float(ctl->vmax_bits);
-    float safe = vmax > 1e-5f ? ctl->cfl_cs / vmax : frame;
-    float step = fminf(safe, frame - t);
-    if (!(step > 0.0f) || ctl->substeps >= 100000u) {  // the reference would loop forever
-        ctl->status |= kStatusBadStep;
-        ctl->go = 0;
-        return;
-    }
-    ctl->dt = step;
-    ctl->go = 1;
-    ctl->sort_now = (!(ctl->flags & APIC_UPDATE_DISABLE_SORT) && t == 0.0f) ? 1u : 0u;
-    if (ctl->sort_now) ctl->sorted = 1;
-    ctl->vmax_bits = 0;    // the coming G2P reduces the next maximum
-    ctl->nonfinite = 0;
-}
-
 __global__ void k_plan_first(Ctl* ctl) { plan(ctl); }
-
-// End of a substep (src/apic.rs:2463-2467), then plan the next one.
-__device__ void advance(Ctl* ctl) {
-    ctl->t = ctl->t + ctl->dt;
-    ctl->prev_dt = ctl->dt;
-    ctl->timestamp += 1;
-    ctl->substeps += 1;
-    plan(ctl);
-}
 __global__ void k_advance(Ctl* ctl) { advance(ctl); }
 
 // Graph forms: the same planning, then the loop / sort conditions.
@@ -350,6 +323,7 @@ void free_scene(Scene& s) {
 void invalidate_graphs(Scene& s) {
     if (s.update_exec) cudaGraphExecDestroy(s.update_exec);
     s.update_exec = nullptr;
+    s.graph_version++;  // batched updates that recorded this scene's kernels rebuild too
 }
 
 // Open-face masks from the obstacle mask (update_world, src/apic.rs:918-944).
@@ -570,6 +544,11 @@ int valid_handle(apic_handle* h) {
 
 }  // namespace
 
+// The stages either side of the pressure solve, for batched updates (batch.cu).
+cudaError_t apic::scene_pre_solve(Scene& s) { return enqueue_pre_solve(s); }
+cudaError_t apic::scene_post_solve(Scene& s) { return enqueue_post_solve(s); }
+Scene& apic::scene_of(apic_handle* h) { return h->s; }
+
 // ---- scene generators live in scene.cpp ----------------------------------
 
 void apic::set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
@@ -766,6 +745,7 @@ extern "C" {
 int apic_destroy(apic_handle* h) {
     if (!h) return APIC_OK;
     if (h->s.stream) cudaStreamSynchronize(h->s.stream);
+    batch_release_scene(&h->s);
     free_scene(h->s);
     delete h;
     return APIC_OK;
@@ -801,18 +781,42 @@ int apic_set_solver(apic_handle* h, int mode, float rel_tol, uint32_t max_iterat
 
 namespace apic {
 
-// First half of Apic::update: everything up to the copy of the control block
-// back to the host is enqueued on the scene's stream; nothing waits (except
-// in profiling mode, whose host-driven loop reads the device state).
-int update_launch(apic_handle* h, uint32_t flags, float frame_dt) {
+// What an update enqueues on the scene's stream before its substep loop:
+// staged uploads, the control block's reset for the new update, and the max
+// speed when no G2P has reduced it yet.
+int update_begin(apic_handle* h, uint32_t flags, float frame_dt) {
     if (valid_handle(h)) return APIC_ERR_INVALID_ARG;
     Scene& s = h->s;
     if (!std::isfinite(frame_dt)) return fail(APIC_ERR_INVALID_ARG, "frame_deltatime must be finite");
     cudaStream_t st = s.stream;
     s.stats = apic_step_stats{};
+    s.batched = false;
     CK(apply_staged(s));
     k_begin_update<<<1, 1, 0, st>>>(s.ctl, frame_dt, flags, s.has_ext ? 1u : 0u, s.has_post ? 1u : 0u);
     if (!s.vmax_valid) { CK(launch_vmax(s)); s.vmax_valid = true; }
+    return APIC_OK;
+}
+
+// ... and after it: the force fields of this update are used up, and the
+// control block is copied back for update_finish.
+int update_end(apic_handle* h) {
+    Scene& s = h->s;
+    cudaStream_t st = s.stream;
+    if (s.has_ext) { CK(cudaMemsetAsync(s.ext_u, 0, sizeof(float) * s.uf, st)); CK(cudaMemsetAsync(s.ext_v, 0, sizeof(float) * s.vf, st)); }
+    if (s.has_post) { CK(cudaMemsetAsync(s.post_u, 0, sizeof(float) * s.uf, st)); CK(cudaMemsetAsync(s.post_v, 0, sizeof(float) * s.vf, st)); }
+    s.has_ext = s.has_post = false;
+    CK(cudaMemcpyAsync(s.ctl_host, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    return APIC_OK;
+}
+
+// First half of Apic::update: everything up to the copy of the control block
+// back to the host is enqueued on the scene's stream; nothing waits (except
+// in profiling mode, whose host-driven loop reads the device state).
+int update_launch(apic_handle* h, uint32_t flags, float frame_dt) {
+    int rc0 = update_begin(h, flags, frame_dt);
+    if (rc0 != APIC_OK) return rc0;
+    Scene& s = h->s;
+    cudaStream_t st = s.stream;
     if (s.profiling) {
         // stage-by-stage with host control of the substep loop
         k_plan_first<<<1, 1, 0, st>>>(s.ctl);
@@ -831,11 +835,7 @@ int update_launch(apic_handle* h, uint32_t flags, float frame_dt) {
         if (rc != APIC_OK) return rc;
         CK(cudaGraphLaunch(s.update_exec, st));
     }
-    if (s.has_ext) { CK(cudaMemsetAsync(s.ext_u, 0, sizeof(float) * s.uf, st)); CK(cudaMemsetAsync(s.ext_v, 0, sizeof(float) * s.vf, st)); }
-    if (s.has_post) { CK(cudaMemsetAsync(s.post_u, 0, sizeof(float) * s.uf, st)); CK(cudaMemsetAsync(s.post_v, 0, sizeof(float) * s.vf, st)); }
-    s.has_ext = s.has_post = false;
-    CK(cudaMemcpyAsync(s.ctl_host, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-    return APIC_OK;
+    return update_end(h);
 }
 
 // Second half: wait for the scene's stream and publish the step statistics.
@@ -853,7 +853,9 @@ int update_finish(apic_handle* h) {
     s.stats.not_converged = c.not_converged;
     s.stats.nonfinite_lanes = c.nonfinite;
     s.stats.solve_ms = double(c.solve_ns) * 1e-6;
-    if (!s.profiling)
+    if (s.batched)  // the scene's own kernels; the batch's solve kernels are counted by the batch
+        s.stats.kernel_launches = (c.sorted ? s.kn_bsort : 0u) + uint64_t(c.substeps) * s.kn_bstep;
+    else if (!s.profiling)
         s.stats.kernel_launches = uint64_t(s.kn_top) + (c.sorted ? s.kn_sort : 0u) + uint64_t(c.substeps) * s.kn_loop +
                                   uint64_t(c.pcg_iters_total) * s.kn_pcg + uint64_t(c.refinements_total) * s.kn_refine;
     if (c.status & kStatusBounds)
@@ -889,12 +891,28 @@ int apic_update_batch(apic_handle* const* handles, uint32_t count, uint32_t flag
     if (count && !handles) return fail(APIC_ERR_INVALID_ARG, "null handle array");
     for (uint32_t i = 0; i < count; ++i)
         if (valid_handle(handles[i])) return fail(APIC_ERR_INVALID_ARG, "invalid handle in batch");
-    // every scene's update is enqueued on its own stream before any is waited
-    // on, so the GPU runs the scenes' kernels side by side
+    for (uint32_t i = 0; i < count; ++i)
+        for (uint32_t j = 0; j < i; ++j)
+            if (handles[i] == handles[j]) return fail(APIC_ERR_INVALID_ARG, "a scene appears twice in the batch");
     std::vector<int> rc(count, APIC_OK);
-    for (uint32_t i = 0; i < count; ++i) rc[i] = update_launch(handles[i], flags, frame_dt);
+    const uint32_t uflags = flags & ~uint32_t(APIC_UPDATE_BATCH_STREAMS | APIC_UPDATE_BATCH_JOINT);
+    // the tuner picks the form (and the joint form's shape) unless told
+    const bool tuned = !(flags & APIC_UPDATE_BATCH_STREAMS) && batch_eligible(handles, count);
+    const auto t0 = std::chrono::steady_clock::now();
+    const bool joint = tuned && batch_choose(handles, count, (flags & APIC_UPDATE_BATCH_JOINT) != 0) != 0;
+    if (joint) {
+        // one graph: every scene's own stages, the pressure solves of all
+        // scenes as one launch per phase (batch.cu)
+        update_batch_joint(handles, count, uflags, frame_dt, rc.data());
+    } else {
+        batch_note_streams(count);
+        // every scene's update is enqueued on its own stream before any is
+        // waited on, so the GPU runs the scenes' kernels side by side
+        for (uint32_t i = 0; i < count; ++i) rc[i] = update_launch(handles[i], uflags, frame_dt);
+    }
     int first = APIC_OK;
     std::string first_msg;
+    uint64_t iterations = 0;
     for (uint32_t i = 0; i < count; ++i) {
         if (rc[i] == APIC_OK) rc[i] = update_finish(handles[i]);
         if (status) status[i] = rc[i];
@@ -902,7 +920,11 @@ int apic_update_batch(apic_handle* const* handles, uint32_t count, uint32_t flag
             first = rc[i];
             first_msg = apic_last_error();
         }
+        iterations += handles[i]->s.stats.pcg_iterations_total;
     }
+    if (tuned && first == APIC_OK)
+        batch_record(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(),
+                     iterations);
     if (first != APIC_OK) return fail(first, "apic_update_batch: " + first_msg);
     return APIC_OK;
 }

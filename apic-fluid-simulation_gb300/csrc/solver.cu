@@ -29,6 +29,7 @@
 #include "apic_device.cuh"
 #include "apic_graph.h"
 #include "apic_internal.h"
+#include "batch.h"
 #include "pcg_common.cuh"
 
 namespace apic {
@@ -59,23 +60,30 @@ __global__ void k_pcg_begin(Ctl* ctl, int stamp) {
 
 // ---- PCG kernels on the base level (phases in pcg_common.cuh) --------------
 
+// Each kernel's work is a body taking the block's coordinates in its scene's
+// grid (bk), run by the single-scene kernel with the hardware's and by the
+// batch kernel (one launch over many scenes, batch.h) with the scene's.
+
 __global__ void __launch_bounds__(kSegBlock) k_clear_pressure(Level B, float* p, const Ctl* ctl) {
     pcg::ph_clear_pressure(B, ctl->seg_count[0], gwarp(), gnwarps(), p);
 }
 
 // s = z and gamma = r.z (src/apic.rs:1887-1892).
 // In the reference mode k_gamma_exact forms gamma and the exit instead.
-__global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl* ctl, double* partials, int mode) {
-    pdl_wait();
-    F2 acc = pcg::ph_start(B, ctl->seg_count[0], gwarp(), gnwarps(), s);
+__device__ __forceinline__ void kb_pcg_start(Blk bk, const Level& B, float* s, Ctl* ctl, double* partials, int mode) {
+    F2 acc = pcg::ph_start(B, ctl->seg_count[0], blk_warp(bk), blk_nwarps(bk), s);
     if (mode == APIC_SOLVER_REFERENCE) return;
     double tot;
-    if (block_sum_last<kSegBlock>(acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
+    if (block_sum_last<kSegBlock>(bk, acc, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) {
         float gamma = float(tot);
         ctl->gamma = gamma;
         ctl->dgamma = tot;
         if (mode == APIC_SOLVER_REFERENCE ? (gamma < kSafety) : !(gamma != 0.0f)) ctl->pcg_done = 1;
     }
+}
+__global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl* ctl, double* partials, int mode) {
+    pdl_wait();
+    kb_pcg_start(hw_blk(), B, s, ctl, partials, mode);
 }
 
 // s' = z + beta s, Ap = A s' and this block's part of delta = s'.Ap
@@ -85,6 +93,23 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_start(Level B, float* s, Ctl*
 // its V-cycle stored (rz): every block sums them into gamma' and forms
 // beta = gamma' / gamma (:1934-1943); a zero r.z ends the solve (k_pcg_update
 // records it).  Block 0 keeps beta for k_pcg_update.
+// (after the dependency wait; w0: this warp's first segment word)
+// rz_sum: the parts' sum formed once beforehand (batched solves), else null.
+__device__ __forceinline__ void kb_spmv_dot(Blk bk, const Level& B, uint32_t nseg, uint32_t w0, const float* s,
+                                            float* ap, Ctl* ctl, float2* part, int mode, const float2* rz,
+                                            uint32_t nrz, const float* rz_sum = nullptr) {
+    if (ctl->pcg_done) return;
+    float beta = ctl->beta;
+    const bool bv = ctl->beta_valid != 0;
+    if (mode != APIC_SOLVER_REFERENCE && bv) {
+        const float ng = rz_sum ? *rz_sum : float(sum_partials<kSegBlock>(rz, nrz));
+        if (!(ng != 0.0f)) return;
+        beta = ng / ctl->gamma;
+        if (bk.id == 0 && threadIdx.x == 0) ctl->beta = beta;
+    }
+    F2 acc = pcg::ph_spmv_search(B, nseg, blk_warp(bk), blk_nwarps(bk), s, beta, bv, ap, w0);
+    block_store<kSegBlock>(bk, acc, part);
+}
 __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s, float* ap, Ctl* ctl, float2* part,
                                                         int mode, const float2* rz, uint32_t nrz) {
     // the base segment list is written by the substep's setup: load this
@@ -92,17 +117,7 @@ __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s,
     const uint32_t nseg = ctl->seg_count[0];
     const uint32_t w0 = gwarp() < nseg ? B.seg[gwarp()] : 0xFFFFFFFFu;
     pdl_wait();
-    if (ctl->pcg_done) return;
-    float beta = ctl->beta;
-    const bool bv = ctl->beta_valid != 0;
-    if (mode != APIC_SOLVER_REFERENCE && bv) {
-        const float ng = float(sum_partials<kSegBlock>(rz, nrz));
-        if (!(ng != 0.0f)) return;
-        beta = ng / ctl->gamma;
-        if (blockIdx.x == 0 && threadIdx.x == 0) ctl->beta = beta;
-    }
-    F2 acc = pcg::ph_spmv_search(B, nseg, gwarp(), gnwarps(), s, beta, bv, ap, w0);
-    block_store<kSegBlock>(acc, part);
+    kb_spmv_dot(hw_blk(), B, nseg, w0, s, ap, ctl, part, mode, rz, nrz);
 }
 
 // delta (the sum of k_spmv_dot's parts, formed by every block) gives alpha or
@@ -111,22 +126,20 @@ __global__ void __launch_bounds__(kSegBlock) k_spmv_dot(Level B, const float* s,
 // (:1907-1932), s = s', the V-cycle's first red sweep on the base level, and
 // this block's part of ||r||^2 and max|r|, whose exit test runs in the next
 // kernel (k_smooth_conv).
-__global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int p_padded, float* s,
-                                                          const float* ap, Ctl* ctl, const float2* sap,
-                                                          uint32_t nsap, float4* part, int mode,
-                                                          const float* exact_parts, const uint32_t* seg_pre,
-                                                          const float2* rz, uint32_t nrz) {
-    const uint32_t nseg = ctl->seg_count[0];
-    const uint32_t w0 = gwarp() < nseg ? B.seg[gwarp()] : 0xFFFFFFFFu;
-    pdl_wait();
+// rz_sum, sap_sum: the parts' sums formed once beforehand (batched solves).
+__device__ __forceinline__ void kb_pcg_update(Blk bk, const Level& B, uint32_t nseg, uint32_t w0, float* p,
+                                              int p_padded, float* s, const float* ap, Ctl* ctl, const float2* sap,
+                                              uint32_t nsap, float4* part, int mode, const float* exact_parts,
+                                              const uint32_t* seg_pre, const float2* rz, uint32_t nrz,
+                                              const float* rz_sum = nullptr, const float* sap_sum = nullptr) {
     if (ctl->pcg_done) return;
     // this iteration's gamma: from the solve's start, or (relative modes) the
     // previous iteration's r.z parts, which k_spmv_dot summed the same way
     float gamma = ctl->gamma;
     if (mode != APIC_SOLVER_REFERENCE && ctl->beta_valid) {
-        gamma = float(sum_partials<kSegBlock>(rz, nrz));
+        gamma = rz_sum ? *rz_sum : float(sum_partials<kSegBlock>(rz, nrz));
         if (!(gamma != 0.0f)) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pcg_done = 1;
+            if (bk.id == 0 && threadIdx.x == 0) ctl->pcg_done = 1;
             return;
         }
     }
@@ -137,13 +150,13 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int
         delta = 0.0f;
         for (uint32_t c = 0; c < nchunks; ++c) delta = delta + exact_parts[c];
     } else {
-        delta = float(sum_partials<kSegBlock>(sap, nsap));
+        delta = sap_sum ? *sap_sum : float(sum_partials<kSegBlock>(sap, nsap));
     }
     const bool stop = mode == APIC_SOLVER_REFERENCE ? fabsf(delta) < kSafety : (!(delta != 0.0f) || !isfinite(delta));
     const float alpha = gamma / delta;
     // every block reads pcg_done on entry, so the stop is recorded aside and
     // the next kernel turns it into pcg_done
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (bk.id == 0 && threadIdx.x == 0) {
         ctl->gamma = gamma;
         ctl->pcg_iters++;
         ctl->delta_stop = stop ? 1u : 0u;
@@ -152,9 +165,20 @@ __global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int
     if (stop) return;
     float mx;
     F2 acc;
-    pcg::ph_update_search(B, nseg, gwarp(), gnwarps(), alpha, ctl->beta, ctl->beta_valid != 0, p, p_padded, s, ap,
-                          &mx, &acc, w0);
-    block_store<kSegBlock>(acc, mx, part);
+    pcg::ph_update_search(B, nseg, blk_warp(bk), blk_nwarps(bk), alpha, ctl->beta, ctl->beta_valid != 0, p, p_padded,
+                          s, ap, &mx, &acc, w0);
+    block_store<kSegBlock>(bk, acc, mx, part);
+}
+__global__ void __launch_bounds__(kSegBlock) k_pcg_update(Level B, float* p, int p_padded, float* s,
+                                                          const float* ap, Ctl* ctl, const float2* sap,
+                                                          uint32_t nsap, float4* part, int mode,
+                                                          const float* exact_parts, const uint32_t* seg_pre,
+                                                          const float2* rz, uint32_t nrz) {
+    const uint32_t nseg = ctl->seg_count[0];
+    const uint32_t w0 = gwarp() < nseg ? B.seg[gwarp()] : 0xFFFFFFFFu;
+    pdl_wait();
+    kb_pcg_update(hw_blk(), B, nseg, w0, p, p_padded, s, ap, ctl, sap, nsap, part, mode, exact_parts, seg_pre, rz,
+                  nrz);
 }
 
 // Stand-alone exit test (paths whose V-cycle does not start with the base
@@ -173,7 +197,7 @@ __global__ void __launch_bounds__(kSegBlock) k_dot_rz(Level B, Ctl* ctl, float2*
     pdl_wait();
     if (ctl->pcg_done) return;
     F2 acc = pcg::ph_rz(B, ctl->seg_count[0], gwarp(), gnwarps());
-    block_store<kSegBlock>(acc, part);
+    block_store<kSegBlock>(hw_blk(), acc, part);
 }
 
 // ---- the reference's FP32 reduction orders (APIC_SOLVER_REFERENCE) --------
@@ -361,29 +385,41 @@ __global__ void __launch_bounds__(kDeltaThreads) k_delta_exact(Level B, const fl
 // ---- FP64 refinement helpers (APIC_SOLVER_REL_MIXED) ----------------------
 
 // b64 = res, p64 = 0 (unless warm) and ||b||^2.
+__device__ __forceinline__ void kb_mixed_init(Blk bk, const Level& B, double* b64, double* p64, Ctl* ctl,
+                                              double* partials, int warm) {
+    if (bk.id == 0 && threadIdx.x == 0) ctl->solve_t0 = global_ns();  // the relative-mode solve starts here
+    double bb = pcg::ph_mixed_init(B, ctl->seg_count[0], blk_warp(bk), blk_nwarps(bk), b64, p64, warm);
+    double tot;
+    if (block_sum_last<kSegBlock>(bk, bb, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) ctl->bnorm2 = tot;
+}
 __global__ void __launch_bounds__(kSegBlock) k_mixed_init(Level B, double* b64, double* p64, Ctl* ctl,
                                                           double* partials, int warm) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->solve_t0 = global_ns();  // the relative-mode solve starts here
-    double bb = pcg::ph_mixed_init(B, ctl->seg_count[0], gwarp(), gnwarps(), b64, p64, warm);
-    double tot;
-    if (block_sum_last<kSegBlock>(bb, partials, &ctl->red_counter, &tot) && threadIdx.x == 0) ctl->bnorm2 = tot;
+    kb_mixed_init(hw_blk(), B, b64, p64, ctl, partials, warm);
 }
 
 // True relative residual of p64 (flags: see pcg::ph_true_residual).
+__device__ __forceinline__ void kb_true_residual(Blk bk, const Level& B, const double* b64, const double* p64,
+                                                 float* x, Ctl* ctl, double* partials, int flags) {
+    double rr = pcg::ph_true_residual(B, ctl->seg_count[0], blk_warp(bk), blk_nwarps(bk), b64, p64, x, flags);
+    double tot;
+    if (block_sum_last<kSegBlock>(bk, rr, partials, &ctl->red_counter, &tot) && threadIdx.x == 0)
+        ctl->true_rel = ctl->bnorm2 > 0.0 ? sqrt(tot / ctl->bnorm2) : 0.0;
+}
 __global__ void __launch_bounds__(kSegBlock) k_true_residual(Level B, const double* b64, const double* p64, float* x,
                                                              Ctl* ctl, double* partials, int flags) {
-    double rr = pcg::ph_true_residual(B, ctl->seg_count[0], gwarp(), gnwarps(), b64, p64, x, flags);
-    double tot;
-    if (block_sum_last<kSegBlock>(rr, partials, &ctl->red_counter, &tot) && threadIdx.x == 0)
-        ctl->true_rel = ctl->bnorm2 > 0.0 ? sqrt(tot / ctl->bnorm2) : 0.0;
+    kb_true_residual(hw_blk(), B, b64, p64, x, ctl, partials, flags);
 }
 
 // p64 += x (finalize 0; the refinement also counts the inner solve's
 // iterations), or pressure = float(p64) (finalize 1).
+__device__ __forceinline__ void kb_mixed_accumulate(Blk bk, const Level& B, double* p64, const float* x,
+                                                    float* pressure, Ctl* ctl, int finalize) {
+    pcg::ph_accumulate(B, ctl->seg_count[0], blk_warp(bk), blk_nwarps(bk), p64, x, pressure, finalize);
+    if (!finalize && bk.id == 0 && threadIdx.x == 0) ctl->used_iters += ctl->pcg_iters;
+}
 __global__ void __launch_bounds__(kSegBlock) k_mixed_accumulate(Level B, double* p64, const float* x, float* pressure,
                                                                 Ctl* ctl, int finalize) {
-    pcg::ph_accumulate(B, ctl->seg_count[0], gwarp(), gnwarps(), p64, x, pressure, finalize);
-    if (!finalize && blockIdx.x == 0 && threadIdx.x == 0) ctl->used_iters += ctl->pcg_iters;
+    kb_mixed_accumulate(hw_blk(), B, p64, x, pressure, ctl, finalize);
 }
 
 __global__ void __launch_bounds__(kSegBlock) k_pressure_to64(Level B, const float* pressure, double* p64,
@@ -398,31 +434,36 @@ __global__ void __launch_bounds__(kSegBlock) k_pressure_to64(Level B, const floa
 // refinement.  Inside the loop the same decision is taken by the kernel that
 // runs the residual's exit test (pcg::loop_decision) or, in the reference
 // mode, by k_gamma_exact.
+__device__ __forceinline__ bool pcg_entry(const Ctl* ctl, uint32_t cap, int dyn_cap) {
+    const uint32_t c = dyn_cap ? ctl->inner_cap : cap;
+    return !ctl->pcg_done && ctl->pcg_iters < c;
+}
 __global__ void k_pcg_cond(const Ctl* __restrict__ ctl, cudaGraphConditionalHandle h, uint32_t cap, int dyn_cap) {
     pdl_wait();
-    const uint32_t c = dyn_cap ? ctl->inner_cap : cap;
-    cudaGraphSetConditional(h, (!ctl->pcg_done && ctl->pcg_iters < c) ? 1u : 0u);
+    cudaGraphSetConditional(h, pcg_entry(ctl, cap, dyn_cap) ? 1u : 0u);
 }
 
-__global__ void k_finish_solve(Ctl* ctl, uint32_t cap) {
+__device__ __forceinline__ void finish_solve(Ctl* ctl, uint32_t cap) {
     ctl->solve_ns += global_ns() - ctl->solve_t0;
     ctl->pcg_iters_total += ctl->pcg_iters;
     if (ctl->pcg_iters >= cap && !ctl->pcg_done) ctl->not_converged++;
 }
+__global__ void k_finish_solve(Ctl* ctl, uint32_t cap) { finish_solve(ctl, cap); }
 
-__global__ void k_rel_begin(Ctl* ctl, double tol, uint32_t cap) {
+__device__ __forceinline__ void rel_begin(Ctl* ctl, double tol, uint32_t cap) {
     ctl->target_rel = tol;
     ctl->inner_cap = cap;
     ctl->refinements = 0;
     ctl->used_iters = 0;
 }
+__global__ void k_rel_begin(Ctl* ctl, double tol, uint32_t cap) { rel_begin(ctl, tol, cap); }
 
 // Refinement loop: go on while the FP64 true residual is above tol and
 // iterations remain.  Each inner FP32 solve reduces its own right-hand side
 // (the current true residual) by kInnerReduction, or down to tol / 2 of ||b||
 // when that is reached first; FP32 cannot usefully reduce it further.
 constexpr double kInnerReduction = 1e-4;
-__global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol, uint32_t cap, int graph) {
+__device__ __forceinline__ bool refine_cond(Ctl* ctl, double tol, uint32_t cap) {
     bool cont = ctl->true_rel > tol && ctl->used_iters < cap && ctl->refinements < 32u;
     // an inner solve that could not take a single step (r.z underflows or is
     // zero) will not make progress on the next round either
@@ -435,19 +476,295 @@ __global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol
         pcg_reset(ctl);  // the inner solve that follows starts here
     }
     ctl->cond = cont ? 1u : 0u;
+    return cont;
+}
+__global__ void k_refine_cond(Ctl* ctl, cudaGraphConditionalHandle h, double tol, uint32_t cap, int graph) {
+    const bool cont = refine_cond(ctl, tol, cap);
     if (graph) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 
-__global__ void k_refine_end(Ctl* ctl, double tol) {
+__device__ __forceinline__ void refine_end(Ctl* ctl, double tol) {
     ctl->solve_ns += global_ns() - ctl->solve_t0;
     ctl->refinements_total += ctl->refinements;
     ctl->pcg_iters = ctl->used_iters;
     ctl->pcg_iters_total += ctl->used_iters;
     if (ctl->true_rel > tol) ctl->not_converged++;
 }
+__global__ void k_refine_end(Ctl* ctl, double tol) { refine_end(ctl, tol); }
 
+// ---- the same phases over a batch of scenes (batch.h) ----------------------
+// Segment phases: persistent CTAs walk the listed items of their gate (each a
+// block of a scene's own launch, with that launch's coordinates) and run the
+// single-scene body.  Control phases: one CTA, a thread per scene; they list
+// the scenes for the phases that follow, and the OR of the scenes' loop
+// decisions is the batch loop's condition.  The PCG runs in a relative mode
+// (APIC_SOLVER_REL_FP32 arithmetic, as the inner solves of both relative
+// modes do).
+constexpr int kBatCtlThreads = 1024;
+constexpr int kRel = APIC_SOLVER_REL_FP32;
+
+// Start of the batch's solves: list the scenes with a substep due (their
+// segment lists are those of this substep's multigrid setup).
+__global__ void __launch_bounds__(kBatCtlThreads) k_bat_solve_begin(const BScene* __restrict__ tab, uint32_t n,
+                                                                   const BCtl* bc, BListRef l1) {
+    bat_build_list(tab, n, kGateSolve, l1, bc);
+}
+
+__global__ void __launch_bounds__(kBatCtlThreads) k_bat_rel_begin(const BScene* __restrict__ tab, uint32_t n,
+                                                                 int mixed, const BCtl* bc, BListRef l2) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        Ctl* ctl = tab[i].ctl;
+        if (!bat_gate(ctl, kGateSolve)) continue;
+        rel_begin(ctl, tab[i].tol, tab[i].max_iter);
+        if (!mixed) ctl->cond = 1u;  // no refinement loop: its gate stays open
+    }
+    if (mixed) return;
+    __syncthreads();
+    bat_build_list(tab, n, kGateRefine, l2, bc);
+}
+
+// gate kGateSolve: the loop's entry (every scene with a substep due decides);
+// kGateRefine: the end of a refinement (the scenes still refining decide).
+__global__ void __launch_bounds__(kBatCtlThreads) k_bat_refine_cond(const BScene* __restrict__ tab, uint32_t n,
+                                                                   BCtl* bc, cudaGraphConditionalHandle h, int gate,
+                                                                   BListRef l2) {
+    bool any = false;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        Ctl* ctl = tab[i].ctl;
+        if (bat_gate(ctl, gate) && refine_cond(ctl, tab[i].tol, tab[i].max_iter)) any = true;
+    }
+    any = __syncthreads_or(any) != 0;
+    if (threadIdx.x == 0) {
+        cudaGraphSetConditional(h, any ? 1u : 0u);
+        if (any) bc->refine_iters++;
+    }
+    if (any) bat_build_list(tab, n, kGateRefine, l2, bc);
+}
+
+__global__ void __launch_bounds__(kBatCtlThreads) k_bat_refine_end(const BScene* __restrict__ tab, uint32_t n) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        if (bat_gate(tab[i].ctl, kGateSolve)) refine_end(tab[i].ctl, tab[i].tol);
+}
+
+__global__ void __launch_bounds__(kBatCtlThreads) k_bat_finish_solve(const BScene* __restrict__ tab, uint32_t n) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        if (bat_gate(tab[i].ctl, kGateSolve)) finish_solve(tab[i].ctl, tab[i].max_iter);
+}
+
+__global__ void __launch_bounds__(kBatCtlThreads) k_bat_pcg_begin(const BScene* __restrict__ tab, uint32_t n,
+                                                                 int gate) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        if (bat_gate(tab[i].ctl, gate)) pcg_reset(tab[i].ctl);
+}
+
+// Entry of the PCG loops (k_pcg_cond with the refinement's dynamic cap).
+__global__ void __launch_bounds__(kBatCtlThreads) k_bat_pcg_cond(const BScene* __restrict__ tab, uint32_t n,
+                                                                const BCtl* bc, cudaGraphConditionalHandle h,
+                                                                int gate, BListRef l3) {
+    pdl_wait();
+    bool any = false;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        Ctl* ctl = tab[i].ctl;
+        if (!bat_gate(ctl, gate)) continue;
+        const bool cont = pcg_entry(ctl, 0u, 1);
+        ctl->pcg_on = cont ? 1u : 0u;
+        any = any || cont;
+    }
+    any = __syncthreads_or(any) != 0;
+    if (threadIdx.x == 0) cudaGraphSetConditional(h, any ? 1u : 0u);
+    if (any) bat_build_list(tab, n, kGatePcg, l3, bc);
+}
+
+// End of a batch PCG iteration: the exit items have taken every listed
+// scene's decision.  CTA 0 lists the scenes that go on and sets the loop
+// condition; CTA 1 + i sums scene i's r.z parts (stored by the V-cycle's
+// last kernel) for the next iteration, once instead of in every block of
+// k_spmv_dot and k_pcg_update (the same function of the same parts).
+__global__ void __launch_bounds__(kSegBlock) k_bat_round_end(const BScene* __restrict__ tab, uint32_t n, BCtl* bc,
+                                                            cudaGraphConditionalHandle h, BListRef l3) {
+    pdl_wait();
+    if (blockIdx.x == 0) {
+        bat_build_list(tab, n, kGatePcg, l3, bc);
+        if (threadIdx.x == 0) {
+            cudaGraphSetConditional(h, l3.p[0] ? 1u : 0u);
+            bc->pcg_iters++;
+        }
+        return;
+    }
+    const BScene& S = tab[blockIdx.x - 1];
+    Ctl* ctl = S.ctl;
+    if (!bat_gate(ctl, kGatePcg) || ctl->pcg_done) return;
+    const float rz = float(sum_partials<kSegBlock>(bs_part_rz(S), busy_blocks(S)));
+    if (threadIdx.x == 0) ctl->b_rz = rz;
+}
+
+// s.Ap of every listed scene (after k_bat_spmv_dot), once per scene.
+__global__ void __launch_bounds__(kSegBlock) k_bat_sap(const BScene* __restrict__ tab, uint32_t n) {
+    pdl_wait();
+    const BScene& S = tab[blockIdx.x];
+    Ctl* ctl = S.ctl;
+    if (!bat_gate(ctl, kGatePcg) || ctl->pcg_done) return;
+    const float sap = float(sum_partials<kSegBlock>(bs_part_sap(S), busy_blocks(S)));
+    if (threadIdx.x == 0) ctl->b_sap = sap;
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_bat_mixed_init(const BScene* __restrict__ tab, BListRef L, int gate) {
+    pdl_wait();
+    bat_for_items(L, kKindBase, [&](uint32_t sc, uint32_t lb, Shape sh) {
+        const BScene& S = tab[sc];
+        if (!bat_gate(S.ctl, gate)) return;
+        kb_mixed_init(Blk{lb, S.grid[0]}, S.lv[0], S.b64, S.p64, S.ctl, S.partials, S.warm);
+    });
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_bat_clear_pressure(const BScene* __restrict__ tab, BListRef L,
+                                                                  int gate) {
+    pdl_wait();
+    bat_for_items(L, kind_chunk(0), [&](uint32_t sc, uint32_t lb, Shape sh) {
+        const BScene& S = tab[sc];
+        if (!bat_gate(S.ctl, gate)) return;
+        const Chunk ch = chunk_of(lb, S.ctl->seg_count[0], sh);
+        pcg::ph_clear_pressure(S.lv[0], ch.end, ch.warp, ch.nwarps, S.pressure);
+    });
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_bat_true_residual(const BScene* __restrict__ tab, BListRef L, int gate,
+                                                                 int flags) {
+    pdl_wait();
+    bat_for_items(L, kKindBase, [&](uint32_t sc, uint32_t lb, Shape sh) {
+        const BScene& S = tab[sc];
+        if (!bat_gate(S.ctl, gate)) return;
+        kb_true_residual(Blk{lb, S.grid[0]}, S.lv[0], S.b64, S.p64, S.corr, S.ctl, S.partials, flags);
+    });
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_bat_pcg_start(const BScene* __restrict__ tab, BListRef L, int gate) {
+    pdl_wait();
+    bat_for_items(L, kKindBase, [&](uint32_t sc, uint32_t lb, Shape sh) {
+        const BScene& S = tab[sc];
+        if (!bat_gate(S.ctl, gate)) return;
+        kb_pcg_start(Blk{lb, S.grid[0]}, S.lv[0], S.search, S.ctl, S.partials, kRel);
+    });
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_bat_spmv_dot(const BScene* __restrict__ tab, BListRef L) {
+    pdl_wait();
+    bat_for_items(L, kKindBlocks, [&](uint32_t sc, uint32_t item, Shape sh) {
+        const BScene& S = tab[sc];
+        Ctl* ctl = S.ctl;
+        if (!bat_gate(ctl, kGatePcg)) return;
+        const uint32_t nseg = ctl->seg_count[0], end = group_end(S, item, sh);
+        for (uint32_t b = item * sh.block_group; b < end; ++b) {
+            kb_spmv_dot(Blk{b, S.grid[0]}, S.lv[0], nseg, 0xFFFFFFFFu, S.search, S.ap, ctl, bs_part_sap(S), kRel,
+                        bs_part_rz(S), S.grid[0], &ctl->b_rz);
+            __syncthreads();  // block_store's shared slots are reused by the next block
+        }
+    });
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_bat_pcg_update(const BScene* __restrict__ tab, BListRef L,
+                                                              int into_corr) {
+    pdl_wait();
+    bat_for_items(L, kKindBlocks, [&](uint32_t sc, uint32_t item, Shape sh) {
+        const BScene& S = tab[sc];
+        Ctl* ctl = S.ctl;
+        if (!bat_gate(ctl, kGatePcg)) return;
+        const uint32_t nseg = ctl->seg_count[0], end = group_end(S, item, sh);
+        for (uint32_t b = item * sh.block_group; b < end; ++b) {
+            kb_pcg_update(Blk{b, S.grid[0]}, S.lv[0], nseg, 0xFFFFFFFFu, into_corr ? S.corr : S.pressure, into_corr,
+                          S.search, S.ap, ctl, bs_part_sap(S), S.grid[0], bs_part_res(S), kRel, nullptr, nullptr,
+                          bs_part_rz(S), S.grid[0], &ctl->b_rz, &ctl->b_sap);
+            __syncthreads();
+        }
+    });
+}
+
+// (k_mixed_accumulate: chunk 0 also counts the inner solve's iterations)
+__global__ void __launch_bounds__(kSegBlock) k_bat_mixed_accumulate(const BScene* __restrict__ tab, BListRef L,
+                                                                    int gate, int finalize) {
+    pdl_wait();
+    bat_for_items(L, kind_chunk(0), [&](uint32_t sc, uint32_t lb, Shape sh) {
+        const BScene& S = tab[sc];
+        Ctl* ctl = S.ctl;
+        if (!bat_gate(ctl, gate)) return;
+        const Chunk ch = chunk_of(lb, ctl->seg_count[0], sh);
+        pcg::ph_accumulate(S.lv[0], ch.end, ch.warp, ch.nwarps, S.p64, S.corr, S.pressure, finalize);
+        if (!finalize && lb == 0 && threadIdx.x == 0) ctl->used_iters += ctl->pcg_iters;
+    });
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_bat_pressure_to64(const BScene* __restrict__ tab, BListRef L,
+                                                                 int gate) {
+    pdl_wait();
+    bat_for_items(L, kind_chunk(0), [&](uint32_t sc, uint32_t lb, Shape sh) {
+        const BScene& S = tab[sc];
+        if (!bat_gate(S.ctl, gate)) return;
+        const Chunk ch = chunk_of(lb, S.ctl->seg_count[0], sh);
+        pcg::ph_pressure_to64(S.lv[0], ch.end, ch.warp, ch.nwarps, S.pressure, S.p64);
+    });
+}
 
 }  // namespace
+
+// ---- batch phase launchers (batch.h); launch kinds as in the single-scene
+// graph: programmatic dependent launch where the predecessor is a kernel of
+// the PCG setup or loop, plain launches elsewhere ----
+#define APIC_PGRID(kern) static const uint32_t g = persistent_grid(kern, kSegBlock, 0)
+void bat_solve_begin(const BatchRun& r) {
+    k_bat_solve_begin<<<1, kBatCtlThreads, 0, r.st>>>(r.tab, r.nscenes, r.bc, r.list[kGateSolve]);
+}
+void bat_mixed_init(const BatchRun& r, int gate) {
+    APIC_PGRID(k_bat_mixed_init);
+    launch(false, k_bat_mixed_init, g, kSegBlock, 0, r.st, r.tab, r.list[gate], gate);
+}
+void bat_clear_pressure(const BatchRun& r, int gate) {
+    APIC_PGRID(k_bat_clear_pressure);
+    launch(false, k_bat_clear_pressure, g, kSegBlock, 0, r.st, r.tab, r.list[gate], gate);
+}
+void bat_rel_begin(const BatchRun& r, int mixed) {
+    k_bat_rel_begin<<<1, kBatCtlThreads, 0, r.st>>>(r.tab, r.nscenes, mixed, r.bc, r.list[kGateRefine]);
+}
+void bat_true_residual(const BatchRun& r, int gate, int flags) {
+    APIC_PGRID(k_bat_true_residual);
+    launch(false, k_bat_true_residual, g, kSegBlock, 0, r.st, r.tab, r.list[gate], gate, flags);
+}
+void bat_refine_cond(const BatchRun& r, cudaGraphConditionalHandle h, int gate) {
+    k_bat_refine_cond<<<1, kBatCtlThreads, 0, r.st>>>(r.tab, r.nscenes, r.bc, h, gate, r.list[kGateRefine]);
+}
+void bat_pcg_begin(const BatchRun& r, int gate) {
+    k_bat_pcg_begin<<<1, kBatCtlThreads, 0, r.st>>>(r.tab, r.nscenes, gate);
+}
+void bat_pcg_start(const BatchRun& r, int gate) {
+    APIC_PGRID(k_bat_pcg_start);
+    launch(r.pdl, k_bat_pcg_start, g, kSegBlock, 0, r.st, r.tab, r.list[gate], gate);
+}
+void bat_pcg_cond(const BatchRun& r, cudaGraphConditionalHandle h, int gate) {
+    launch(r.pdl, k_bat_pcg_cond, 1, kBatCtlThreads, 0, r.st, r.tab, r.nscenes, static_cast<const BCtl*>(r.bc), h,
+           gate, r.list[kGatePcg]);
+}
+void bat_round_end(const BatchRun& r, cudaGraphConditionalHandle h) {
+    launch(r.pdl, k_bat_round_end, r.nscenes + 1, kSegBlock, 0, r.st, r.tab, r.nscenes, r.bc, h, r.list[kGatePcg]);
+}
+void bat_sap(const BatchRun& r) { launch(r.pdl, k_bat_sap, r.nscenes, kSegBlock, 0, r.st, r.tab, r.nscenes); }
+void bat_spmv_dot(const BatchRun& r) {
+    APIC_PGRID(k_bat_spmv_dot);
+    k_bat_spmv_dot<<<g, kSegBlock, 0, r.st>>>(r.tab, r.list[kGatePcg]);
+}
+void bat_pcg_update(const BatchRun& r, int into_corr) {
+    APIC_PGRID(k_bat_pcg_update);
+    launch(r.pdl, k_bat_pcg_update, g, kSegBlock, 0, r.st, r.tab, r.list[kGatePcg], into_corr);
+}
+void bat_mixed_accumulate(const BatchRun& r, int gate, int finalize) {
+    APIC_PGRID(k_bat_mixed_accumulate);
+    launch(false, k_bat_mixed_accumulate, g, kSegBlock, 0, r.st, r.tab, r.list[gate], gate, finalize);
+}
+void bat_refine_end(const BatchRun& r) { k_bat_refine_end<<<1, kBatCtlThreads, 0, r.st>>>(r.tab, r.nscenes); }
+void bat_finish_solve(const BatchRun& r) { k_bat_finish_solve<<<1, kBatCtlThreads, 0, r.st>>>(r.tab, r.nscenes); }
+void bat_pressure_to64(const BatchRun& r, int gate) {
+    APIC_PGRID(k_bat_pressure_to64);
+    launch(false, k_bat_pressure_to64, g, kSegBlock, 0, r.st, r.tab, r.list[gate], gate);
+}
+#undef APIC_PGRID
 
 // One PCG iteration (src/apic.rs:1899-1955); x receives alpha * s.  The
 // search update that ends the reference's iteration happens at the start of

@@ -33,6 +33,7 @@
 
 #include "apic_device.cuh"
 #include "apic_internal.h"
+#include "batch.h"
 #include "pcg_common.cuh"
 #include "vcycle_common.cuh"
 
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(kSegBlock) k_prolong_red_rz(Level c, Level B, 
     pdl_wait();
     if (ctl->pcg_done) return;
     const F2 acc = ph_prolong_red_rz(c, B, nseg, gwarp(), gnwarps(), last, extra, w0);
-    block_store<kSegBlock>(acc, part);
+    block_store<kSegBlock>(hw_blk(), acc, part);
 }
 
 // Prolongation fused with the final red sweep (black neighbours are final).
@@ -155,7 +156,143 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(TailParams tp, con
 
 size_t tail_level_bytes(const Level& L) { return 4ull * (L.words + 6ull * L.padded); }
 
+// ---- the V-cycle's phases over a batch of scenes (batch.h) ------------------
+// Persistent CTAs walk the listed items of their gate; each runs the
+// single-scene kernel's work for one block of its scene's own launch.
+
+// k_smooth_exit: item 0 of each scene takes the scene's exit test and loop
+// decision (k_bat_pcg_next then lists the scenes that go on); the others
+// are chunks of the base level's black sweep.
+__global__ void __launch_bounds__(kSegBlock) k_bat_smooth_exit(const BScene* __restrict__ tab, BListRef L) {
+    pdl_wait();
+    bat_for_items(L, kKindExit, [&](uint32_t sc, uint32_t lb, Shape sh) {
+        const BScene& S = tab[sc];
+        Ctl* ctl = S.ctl;
+        if (!bat_gate(ctl, kGatePcg)) return;
+        if (lb == 0) {  // the residual's parts: those of the blocks k_bat_pcg_update ran
+            if (!ctl->pcg_done) pcg::residual_exit(ctl, bs_part_res(S), busy_blocks(S), APIC_SOLVER_REL_FP32, 0.0f);
+            if (threadIdx.x == 0) ctl->pcg_on = pcg::loop_continue(ctl, APIC_SOLVER_REL_FP32, 0u, 1) ? 1u : 0u;
+            return;
+        }
+        if (ctl->pcg_done) return;
+        const Chunk ch = chunk_of(lb - 1, ctl->seg_count[0], sh);
+        ph_smooth(S.lv[0], ch.end, ch.warp, ch.nwarps, 1, 1, kNoWord);
+    });
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_bat_smooth(const BScene* __restrict__ tab, BListRef L, int li,
+                                                          int gate, int color, int init) {
+    pdl_wait();
+    bat_for_items(L, kind_chunk(li), [&](uint32_t sc, uint32_t lb, Shape sh) {
+        const BScene& S = tab[sc];
+        const Ctl* ctl = S.ctl;
+        if (!bat_gate(ctl, gate) || ctl->pcg_done) return;
+        const Chunk ch = chunk_of(lb, ctl->seg_count[li], sh);
+        ph_smooth(S.lv[li], ch.end, ch.warp, ch.nwarps, color, init, kNoWord);
+    });
+}
+
+// Restriction into level lc: fused with the level's first red sweep when the
+// level is smoothed by the segment kernels, plain into the first tail level.
+__global__ void __launch_bounds__(kSegBlock) k_bat_restrict(const BScene* __restrict__ tab, BListRef L, int lc,
+                                                            int gate) {
+    pdl_wait();
+    bat_for_items(L, kind_rchunk(lc), [&](uint32_t sc, uint32_t lb, Shape sh) {
+        const BScene& S = tab[sc];
+        const Ctl* ctl = S.ctl;
+        if (!bat_gate(ctl, gate) || ctl->pcg_done) return;
+        const Chunk ch = chunk_of(lb, ctl->seg_count[lc], sh);
+        ph_restrict(S.lv[lc - 1], S.lv[lc], ch.end, ch.warp, ch.nwarps, uint32_t(lc) < S.tail_first, kNoWord);
+    });
+}
+
+// Prolongation from level lf + 1 fused with level lf's black (color 1) or
+// red (color 0) sweep; base: lf is the base level.
+__global__ void __launch_bounds__(kSegBlock) k_bat_prolong(const BScene* __restrict__ tab, BListRef L, int lf,
+                                                           int gate, int color, int base) {
+    pdl_wait();
+    bat_for_items(L, kind_chunk(lf), [&](uint32_t sc, uint32_t lb, Shape sh) {
+        const BScene& S = tab[sc];
+        const Ctl* ctl = S.ctl;
+        if (!bat_gate(ctl, gate) || ctl->pcg_done) return;
+        const uint32_t last = base ? ctl->last_fluid : 0xFFFFFFFFu, extra = base ? ctl->pad_count : 0u;
+        const Chunk ch = chunk_of(lb, ctl->seg_count[lf], sh);
+        ph_prolong(S.lv[lf + 1], S.lv[lf], ch.end, ch.warp, ch.nwarps, color, last, extra, kNoWord);
+    });
+}
+
+// The iteration's last V-cycle kernel (k_prolong_red_rz).
+__global__ void __launch_bounds__(kSegBlock) k_bat_prolong_red_rz(const BScene* __restrict__ tab, BListRef L) {
+    pdl_wait();
+    bat_for_items(L, kKindBlocks, [&](uint32_t sc, uint32_t item, Shape sh) {
+        const BScene& S = tab[sc];
+        const Ctl* ctl = S.ctl;
+        if (!bat_gate(ctl, kGatePcg) || ctl->pcg_done) return;
+        const uint32_t nseg = ctl->seg_count[0], end = group_end(S, item, sh);
+        const uint32_t last = ctl->last_fluid, extra = ctl->pad_count;
+        for (uint32_t b = item * sh.block_group; b < end; ++b) {
+            const Blk bk{b, S.grid[0]};
+            const F2 acc = ph_prolong_red_rz(S.lv[1], S.lv[0], nseg, blk_warp(bk), blk_nwarps(bk), last, extra,
+                                             kNoWord);
+            block_store<kSegBlock>(bk, acc, bs_part_rz(S));
+            __syncthreads();  // block_store's shared slots are reused by the next block
+        }
+    });
+}
+
+// The coarse tail (k_vcycle_tail): persistent CTAs take the listed scenes one
+// at a time; the scene's tail parameters are copied into shared memory beside
+// the levels.
+__global__ void __launch_bounds__(kTailThreads) k_bat_tail(const BScene* __restrict__ tab, BListRef L, int gate) {
+    __shared__ TailParams s_tp;
+    extern __shared__ uint32_t sm[];
+    pdl_wait();
+    const uint32_t nact = L.p[0];
+    for (uint32_t j = blockIdx.x; j < nact; j += gridDim.x) {
+        const BScene& S = tab[L.scenes()[j]];
+        if (!bat_gate(S.ctl, gate) || S.ctl->pcg_done) continue;
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(&S.tp);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&s_tp);
+        for (uint32_t i = threadIdx.x; i < sizeof(TailParams) / 4; i += blockDim.x) dst[i] = src[i];
+        __syncthreads();
+        cta_tail(s_tp, sm, true);
+        __syncthreads();
+    }
+}
+
 }  // namespace
+
+void bat_smooth_exit(const BatchRun& r) {
+    static const uint32_t g = persistent_grid(k_bat_smooth_exit, kSegBlock, 0);
+    launch(r.pdl, k_bat_smooth_exit, g, kSegBlock, 0, r.st, r.tab, r.list[kGatePcg]);
+}
+void bat_smooth(const BatchRun& r, int l, int gate, int color, int init) {
+    static const uint32_t g = persistent_grid(k_bat_smooth, kSegBlock, 0);
+    launch(r.pdl, k_bat_smooth, g, kSegBlock, 0, r.st, r.tab, r.list[gate], l, gate, color, init);
+}
+void bat_restrict(const BatchRun& r, int l, int gate) {
+    static const uint32_t g = persistent_grid(k_bat_restrict, kSegBlock, 0);
+    launch(r.pdl, k_bat_restrict, g, kSegBlock, 0, r.st, r.tab, r.list[gate], l, gate);
+}
+void bat_prolong_black(const BatchRun& r, int l, int gate, int base) {
+    static const uint32_t g = persistent_grid(k_bat_prolong, kSegBlock, 0);
+    launch(r.pdl, k_bat_prolong, g, kSegBlock, 0, r.st, r.tab, r.list[gate], l, gate, 1, base);
+}
+void bat_prolong_red(const BatchRun& r, int l, int gate, int base) {
+    static const uint32_t g = persistent_grid(k_bat_prolong, kSegBlock, 0);
+    launch(r.pdl, k_bat_prolong, g, kSegBlock, 0, r.st, r.tab, r.list[gate], l, gate, 0, base);
+}
+void bat_prolong_red_rz(const BatchRun& r) {
+    static const uint32_t g = persistent_grid(k_bat_prolong_red_rz, kSegBlock, 0);
+    launch(r.pdl, k_bat_prolong_red_rz, g, kSegBlock, 0, r.st, r.tab, r.list[kGatePcg]);
+}
+void bat_tail(const BatchRun& r, int gate) {
+    const uint32_t g = r.nscenes < 152u ? r.nscenes : 152u;  // one CTA per SM holds the largest tail
+    launch(r.pdl, k_bat_tail, g, kTailThreads, r.tail_smem, r.st, r.tab, r.list[gate], gate);
+}
+void bat_prepare_tail() {
+    cudaFuncSetAttribute(k_bat_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTailSmemBudget));
+}
 
 // Choose the coarse levels that run in one CTA (all of them fit in shared memory).
 void plan_vcycle(Scene& s) {

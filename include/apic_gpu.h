@@ -40,6 +40,12 @@ extern "C" {
 
 /* ---- update flags (DebugOptions, src/apic.rs:397-400) ------------------ */
 #define APIC_UPDATE_DISABLE_SORT  0x1u  /* DebugOptions::disable_particle_sort */
+/* apic_update_batch only: run each scene's whole update on its own stream
+ * even where the pressure solves could run as one launch per phase ... */
+#define APIC_UPDATE_BATCH_STREAMS 0x2u
+/* ... or run the joint form whenever it applies, whatever the batch tuner
+ * has found (see apic_batch_info). */
+#define APIC_UPDATE_BATCH_JOINT   0x4u
 
 /* ---- pressure-solver modes --------------------------------------------- */
 /* Reference semantics (src/apic.rs:1865-1956): absolute max-norm exit at
@@ -321,16 +327,51 @@ int apic_morton_sort_noalloc(const float* pos_x, const float* pos_y, uint32_t n,
 
 /* ---- batched and served scenes ------------------------------------------ */
 /* No counterpart in the reference, which simulates one scene per process.
- * One Apic::update of each of `count` scenes: every update is enqueued on its
- * scene's own stream before any is waited on, so the GPU runs the scenes'
- * kernels side by side (a small scene alone leaves most SMs idle).  Each
- * scene computes exactly what apic_update computes for it.  status (may be
+ * One Apic::update of each of `count` distinct scenes; each scene computes
+ * exactly what apic_update computes for it, bit for bit.  When every scene
+ * uses a relative solver mode (all the same one), has a multigrid level and
+ * a shared-memory coarse tail, and no scene is in profiling mode, the whole
+ * batch runs as one CUDA graph: each scene's stages before and after the
+ * pressure solve are its own kernels (side by side, each under a
+ * device-side condition for its substeps), and the pressure solves of all
+ * scenes run as ONE launch per solve phase over a table of scenes.  The
+ * graph is built on the first call for a given list of scenes and reused
+ * while the list and the scenes' settings stay the same.  Otherwise, or with
+ * APIC_UPDATE_BATCH_STREAMS in flags, every scene's update is enqueued on its
+ * own stream before any is waited on, so the GPU runs the scenes' kernels
+ * side by side.  Calls are serialised inside the library.  status (may be
  * NULL): per-scene result; the return value is the first failure. */
 int apic_update_batch(apic_handle* const* handles, uint32_t count, uint32_t flags, float frame_deltatime,
                       int* status);
 
 /* Estimated device bytes of a scene (upper bound used for admission). */
 int apic_scene_bytes(uint32_t width, uint32_t height, uint64_t particles, uint64_t* bytes_out);
+
+/* The last apic_update_batch call in this process: scenes, whether the
+ * solves ran as one launch per phase (joint 1) or on the scenes' streams
+ * (joint 0), and, for a joint batch, the kernels the batch itself launched
+ * (the solve phases and the substep control: every scene's own kernels are
+ * in its apic_step_stats.kernel_launches) and how many times the batch's
+ * substep, refinement and PCG loop bodies ran.  The library tunes how it
+ * runs a batch of a given makeup (every scene's sides and solver mode, in
+ * order) over the first calls for that makeup, trying the stream-per-scene
+ * form and the joint form with several work shapes on the caller's own
+ * updates (the results are the same bits whichever runs); tuned is 1 once
+ * the choice is made, and chunk_segs / block_group give the joint shape
+ * used (segments per item of the sweeps and transfers, blocks per item of
+ * the PCG iteration's reductions). */
+typedef struct apic_batch_info {
+    uint32_t scenes;
+    uint32_t joint;
+    uint64_t batch_kernel_launches;
+    uint32_t substep_rounds;
+    uint32_t refine_rounds;
+    uint32_t pcg_rounds;
+    uint32_t tuned;
+    uint32_t chunk_segs;
+    uint32_t block_group;
+} apic_batch_info;
+int apic_batch_last_info(apic_batch_info* out);
 
 /* Placement of independent scenes on several GPUs (no counterpart in the
  * reference, which runs one scene in one process).  Scenes share nothing, so

@@ -64,6 +64,120 @@ def test_update_batch_matches_alone(gpu_lib):
         assert np.array_equal(g.read_vec2x8(0), ref.read_vec2x8(0)), sc.width
 
 
+FIELDS = tuple(A.PARTICLE_FIELDS)
+
+
+def fast_disk(side, seed, vy):
+    return A.scene_params(A.SCENE_DAM_BREAK_DISK, side, cell_size=1.0 / side, sub=2, seed=seed, fluid_x=0.25,
+                          fluid_y=0.25, disk=(0.6, 0.6, 0.12), disk_v=(0.0, vy))
+
+
+def make(scene, mode):
+    g = A.Apic(scene.width, scene.height, scene.cell_size, PROPS)
+    px, py, vx, vy = A.generate_scene(scene)
+    g.set_particles(px, py, vx, vy)
+    g.set_solver(mode, 1e-6, 500)
+    return g
+
+
+def assert_same(a, b, what):
+    for f in FIELDS + ("pressure", "u", "v"):
+        x, y = a.read_field(f), b.read_field(f)
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (what, f)
+
+
+@pytest.mark.parametrize("mode", [A.SOLVER_REL_MIXED, A.SOLVER_REL_FP32], ids=["mixed", "fp32"])
+def test_joint_batch_bit_exact(gpu_lib, mode):
+    """The joint batch (the solves of all scenes as one launch per phase):
+    uneven sides (powers of two and not, one without segment-kernel levels
+    above its coarse tail), scenes with different substep counts in the same
+    update, and a graph reused across updates; every scene equals itself run
+    alone bit for bit, and the stream-per-scene batch too."""
+    scenes = [dam_break(64, 31, 0.3), dam_break(88, 32, 0.5), fast_disk(120, 33, -25.0), dam_break(176, 34, 0.4),
+              disk_drop(200, 35), fast_disk(256, 36, -6.0), dam_break(344, 37, 0.25), dam_break(512, 38, 0.2)]
+    steps, dt = 4, 1 / 120
+    joint = [make(sc, mode) for sc in scenes]
+    streams = [make(sc, mode) for sc in scenes]
+    subs = []
+    for _ in range(steps):
+        assert A.update_batch(joint, A.DebugOptions(), dt, joint=True) == [A.OK] * len(scenes)
+        info = A.batch_last_info()
+        assert info["joint"] == 1 and info["scenes"] == len(scenes), info
+        assert info["batch_kernel_launches"] > 0 and info["pcg_rounds"] > 0, info
+        subs.append([g.stats().substeps for g in joint])
+        assert A.update_batch(streams, A.DebugOptions(), dt, streams=True) == [A.OK] * len(scenes)
+        assert A.batch_last_info()["joint"] == 0
+        for g, h in zip(joint, streams):
+            assert g.stats().substeps == h.stats().substeps
+            assert g.stats().pcg_iterations_total == h.stats().pcg_iterations_total
+            assert g.stats().refinement_steps == h.stats().refinement_steps
+    assert any(len(set(row)) > 1 for row in subs), subs  # the scenes' substep counts differed
+    for sc, g, h in zip(scenes, joint, streams):
+        ref = make(sc, mode)
+        for _ in range(steps):
+            ref.update(A.DebugOptions(), dt)
+        assert_same(g, ref, ("joint", sc.width))
+        assert_same(h, ref, ("streams", sc.width))
+        assert g.stats().pcg_iterations_total == ref.stats().pcg_iterations_total
+        if mode == A.SOLVER_REL_MIXED:
+            assert float(g.stats().true_residual_rel) <= 1e-6
+
+
+def test_joint_batch_rebuilds(gpu_lib):
+    """The batch graph follows its scenes: a changed setting, a scene list in
+    another order and a destroyed scene all rebuild it; the reference solver
+    mode falls back to the stream-per-scene batch."""
+    scenes = [dam_break(96, 41, 0.4), disk_drop(128, 42), dam_break(160, 43, 0.3)]
+    dt = 1 / 240
+    sims = [make(sc, A.SOLVER_REL_MIXED) for sc in scenes]
+    refs = [make(sc, A.SOLVER_REL_MIXED) for sc in scenes]
+    A.update_batch(sims, A.DebugOptions(), dt, joint=True)
+    for r in refs:
+        r.update(A.DebugOptions(), dt)
+    sims[1].set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)  # invalidates its graphs
+    refs[1].set_solver(A.SOLVER_REL_MIXED, 1e-6, 500)
+    A.update_batch(sims[::-1], A.DebugOptions(), dt, joint=True)
+    assert A.batch_last_info()["joint"] == 1
+    for r in refs:
+        r.update(A.DebugOptions(), dt)
+    for g, r, sc in zip(sims, refs, scenes):
+        assert_same(g, r, ("rebuilt", sc.width))
+    sims[0].close()
+    A.update_batch(sims[1:], A.DebugOptions(), dt, joint=True)
+    assert A.batch_last_info()["joint"] == 1
+    for r in refs[1:]:
+        r.update(A.DebugOptions(), dt)
+    for g, r, sc in zip(sims[1:], refs[1:], scenes[1:]):
+        assert_same(g, r, ("after destroy", sc.width))
+    ref_mode = [make(sc, A.SOLVER_REFERENCE) for sc in scenes[:2]]
+    A.update_batch(ref_mode, A.DebugOptions(), dt)
+    assert A.batch_last_info()["joint"] == 0
+
+
+def test_batch_tuner(gpu_lib):
+    """The tuner tries the stream-per-scene form and the joint form's shapes
+    on the caller's updates, then keeps one; every form gives the bits the
+    scenes give alone."""
+    scenes = [dam_break(72, 51, 0.4), disk_drop(104, 52), dam_break(136, 53, 0.3), fast_disk(64, 54, -8.0)]
+    dt = 1 / 240
+    sims = [make(sc, A.SOLVER_REL_MIXED) for sc in scenes]
+    seen, tuned_at = set(), None
+    for k in range(20):
+        assert A.update_batch(sims, A.DebugOptions(), dt) == [A.OK] * len(scenes)
+        info = A.batch_last_info()
+        seen.add((info["joint"], info["chunk_segs"], info["block_group"]))
+        if info["tuned"] and tuned_at is None:
+            tuned_at = k
+    assert tuned_at is not None, "the tuner never settled"
+    assert len(seen) >= 4, seen  # both forms and several shapes ran
+    assert info["chunk_segs"] % 8 == 0 and info["block_group"] >= 1
+    for sc, g in zip(scenes, sims):
+        ref = make(sc, A.SOLVER_REL_MIXED)
+        for _ in range(20):
+            ref.update(A.DebugOptions(), dt)
+        assert_same(g, ref, ("tuned", sc.width))
+
+
 def test_update_batch_rejects_bad_input(gpu_lib):
     with pytest.raises(A.ApicError) as ei:
         A.update_batch([A.Apic(64, 64, 1 / 64, PROPS), type("X", (), {"_h": None})()], None, 1 / 240)
