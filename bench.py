@@ -16,7 +16,9 @@ pinned memory and the particle state read back every step (pipelined: the
 copies of neighbouring steps overlap the updates); ``roofline`` for
 the pressure solve (the dominant part of a step, timed inside the update
 graph by the device's global timer), ``cpu_baseline`` = the C++ restatement
-of the reference step (OpenMP, all host cores) over the same updates.
+of the reference step (OpenMP, all host cores) over the same updates;
+``batched_config4`` = a brief run of 256 uneven scenes through
+apic_update_batch (``--workload batched`` in a child process).
 
 ``--impl reference`` times that CPU restatement alone as the reference arm.
 Under torchrun (N > 1) each rank runs an independent replica on its own GPU
@@ -368,6 +370,9 @@ def run_gpu_arm(args, world, rank, local):
     compare = None
     if args.solver == "mixed" and not args.no_solver_compare and not args.eager:
         compare = solver_compare(A, torch, args, px, py, vx, vy, mode)
+    batched = None
+    if rank == 0 and world == 1 and not args.eager and not args.no_batched_summary:
+        batched = batched_summary()
 
     result = None
     if rank == 0:
@@ -410,6 +415,7 @@ def run_gpu_arm(args, world, rank, local):
             "gpu_launches": launches if not args.eager else None,
             "roofline": roof,
             "solver_compare": compare,
+            "batched_config4": batched,
             "stage_ms_profiling": {
                 "note": "profiling mode, not additive to ms_per_step: each stage of each substep launched on "
                         "its own between CUDA events and the solve's loops driven from the host (every PCG "
@@ -421,6 +427,28 @@ def run_gpu_arm(args, world, rank, local):
         print(json.dumps(result), flush=True)
     sim.close()
     return result
+
+
+def batched_summary() -> dict:
+    """Config 4 in brief, beside the single-scene line: 256 uneven scenes
+    through apic_update_batch as tuned, against the same updates one scene at
+    a time and with every scene on its own stream (bench.py --workload
+    batched in a child process, so that CUDA_DEVICE_MAX_CONNECTIONS=32 holds
+    for it from CUDA's start)."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--workload", "batched", "--steps", "5", "--compare-steps", "3"]
+    env = dict(os.environ, CUDA_DEVICE_MAX_CONNECTIONS="32")
+    try:
+        out = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=600)
+        line = json.loads(out.stdout.strip().splitlines()[-1])
+    except Exception as e:  # the summary is evidence beside the headline, never a reason to lose it
+        return {"error": f"{type(e).__name__}: {str(e)[:300]}"}
+    keep = ("value", "unit", "batched_vs_plain", "round_ms_p50", "round_ms_p99", "gpu_launches", "clocks",
+            "true_residual_rel_max")
+    res = {k: line.get(k) for k in keep}
+    res["config"] = {k: line["config"].get(k) for k in ("workload", "particles", "sides_min_median_max", "batching",
+                                                        "tuner", "cuda_device_max_connections")}
+    res["command"] = " ".join(["python", "bench.py"] + cmd[2:])
+    return res
 
 
 def ctypes_stream(sim) -> int:
@@ -972,6 +1000,8 @@ def main():
     ap.add_argument("--solver", default="mixed", choices=["mixed", "fp32", "reference"])
     ap.add_argument("--side", type=int, default=SIDE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched-summary", action="store_true",
+                    help="single: skip the brief config-4 batched run reported beside the headline")
     ap.add_argument("--no-solver-compare", action="store_true",
                     help="skip the plain-FP32-vs-mixed solve comparison of the default workload")
     ap.add_argument("--eager", action="store_true",
