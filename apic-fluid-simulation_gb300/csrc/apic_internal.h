@@ -348,11 +348,22 @@ Scene& scene_of(apic_handle* h);
 cudaError_t scene_pre_solve(Scene& s);   // the substep's stages before the pressure solve
 cudaError_t scene_post_solve(Scene& s);  // ... and after it
 // batch.cu: apic_update_batch with the solves as one launch per phase
+struct BatchShape {
+    uint32_t chunk_segs, block_group;
+};
+// The form of one apic_update_batch call, as the batch tuner planned it.
+struct BatchTicket {
+    uint64_t key = 0;   // makeup of the batch
+    int step = -1;      // the tuner's step this call measures (-1: none)
+    int joint = 0;      // 1: joint form with `shape`; 0: a stream per scene
+    BatchShape shape{64, 4};
+};
 bool batch_eligible(apic_handle* const* handles, uint32_t count);
-int update_batch_joint(apic_handle* const* handles, uint32_t count, uint32_t flags, float frame_dt, int* rc);
+int update_batch_joint(apic_handle* const* handles, uint32_t count, uint32_t flags, float frame_dt, BatchShape shape,
+                       int* rc);
 void batch_note_streams(uint32_t count);
-int batch_choose(apic_handle* const* handles, uint32_t count, bool force_joint);  // 1 joint, 0 streams
-void batch_record(double wall_ms, uint64_t iterations);
+void batch_choose(apic_handle* const* handles, uint32_t count, bool force_joint, BatchTicket* tk);
+void batch_record(const BatchTicket& tk, double wall_ms, uint64_t iterations);
 void batch_release_scene(const Scene* s);
 int create_scene(uint32_t width, uint32_t height, float cell_size, const apic_world_props* props,
                  bool default_particles, apic_handle** out);

@@ -151,9 +151,7 @@ struct Tuner {
     int best = -1;             // the chosen step once all have run
 };
 std::map<uint64_t, Tuner> g_tuners;
-uint64_t g_tuning_key = 0;     // makeup of the batch that the running call measures
-int g_tuning_step = -1;        // ... and the step it runs (-1: none)
-Shape g_shape{64, 4};          // the shape the next joint call runs with
+constexpr size_t kMaxTuners = 256;  // makeups remembered (all are forgotten beyond this)
 
 const std::vector<TuneStep>& tune_steps() {
     static const std::vector<TuneStep> steps = [] {
@@ -466,29 +464,32 @@ void batch_note_streams(uint32_t count) {
     g_last_info.scenes = count;
 }
 
-// The way to run this call (1: joint, with g_shape set; 0: streams).
+// The way to run this call: t->joint (with t->shape) or streams.
 // force_joint: joint whatever the tuner's state (its best shape when tuned).
-int batch_choose(apic_handle* const* handles, uint32_t count, bool force_joint) {
+void batch_choose(apic_handle* const* handles, uint32_t count, bool force_joint, BatchTicket* tk) {
     std::lock_guard<std::mutex> lk(g_batch_mu);
-    g_tuning_step = -1;
+    const uint64_t key = makeup_key(handles, count);
+    tk->key = key;
+    tk->step = -1;
     if (force_joint) {
-        auto it = g_tuners.find(makeup_key(handles, count));
+        auto it = g_tuners.find(key);
         const bool tuned_joint = it != g_tuners.end() && it->second.best >= 0 &&
                                  it->second.steps[size_t(it->second.best)].joint;
-        g_shape = tuned_joint ? it->second.steps[size_t(it->second.best)].shape : Shape{64, 4};
-        return 1;
+        tk->shape = tuned_joint ? it->second.steps[size_t(it->second.best)].shape : Shape{64, 4};
+        tk->joint = 1;
+        return;
     }
-    const uint64_t key = makeup_key(handles, count);
+    if (g_tuners.size() >= kMaxTuners && g_tuners.find(key) == g_tuners.end()) g_tuners.clear();
     Tuner& t = g_tuners[key];
     if (t.steps.empty()) {
         t.steps = tune_steps();
         t.cost.assign(t.steps.size(), -1.0);
     }
     if (t.best < 0 && t.next < t.steps.size()) {
-        g_tuning_key = key;
-        g_tuning_step = int(t.next++);
-        g_shape = t.steps[size_t(g_tuning_step)].shape;
-        return t.steps[size_t(g_tuning_step)].joint;
+        tk->step = int(t.next++);
+        tk->shape = t.steps[size_t(tk->step)].shape;
+        tk->joint = t.steps[size_t(tk->step)].joint;
+        return;
     }
     if (t.best < 0) {  // every step ran: keep the cheapest measured
         double c = 0.0;
@@ -499,26 +500,25 @@ int batch_choose(apic_handle* const* handles, uint32_t count, bool force_joint) 
             }
         if (t.best < 0) t.best = 0;
     }
-    g_shape = t.steps[size_t(t.best)].shape;
-    return t.steps[size_t(t.best)].joint;
+    tk->shape = t.steps[size_t(t.best)].shape;
+    tk->joint = t.steps[size_t(t.best)].joint;
 }
 
 // Cost of the call that batch_choose planned (wall time, PCG iterations over
 // all scenes).
-void batch_record(double wall_ms, uint64_t iterations) {
+void batch_record(const BatchTicket& tk, double wall_ms, uint64_t iterations) {
     std::lock_guard<std::mutex> lk(g_batch_mu);
-    g_last_info.chunk_segs = g_shape.chunk_segs;
-    g_last_info.block_group = g_shape.block_group;
-    auto it = g_tuners.find(g_tuning_key);
-    if (g_tuning_step < 0 || it == g_tuners.end()) {
+    g_last_info.chunk_segs = tk.shape.chunk_segs;
+    g_last_info.block_group = tk.shape.block_group;
+    auto it = g_tuners.find(tk.key);
+    if (tk.step < 0 || it == g_tuners.end() || size_t(tk.step) >= it->second.steps.size()) {
         g_last_info.tuned = 1;
         return;
     }
     Tuner& t = it->second;
-    const size_t i = size_t(g_tuning_step);
+    const size_t i = size_t(tk.step);
     if (t.steps[i].measure) t.cost[i] = wall_ms / double(iterations + 1);
     g_last_info.tuned = 0;
-    g_tuning_step = -1;
 }
 
 void batch_release_scene(const Scene* s) {
@@ -529,7 +529,8 @@ void batch_release_scene(const Scene* s) {
 // Begin every scene's update on its stream, run the batch graph on the
 // batch's stream after all of them, end every update on its stream after it.
 // rc[i]: per-scene result (apic_update_batch then waits for each scene).
-int update_batch_joint(apic_handle* const* handles, uint32_t count, uint32_t flags, float frame_dt, int* rc) {
+int update_batch_joint(apic_handle* const* handles, uint32_t count, uint32_t flags, float frame_dt, Shape shape,
+                       int* rc) {
     std::lock_guard<std::mutex> lk(g_batch_mu);
     auto fail_all = [&](int code, const std::string& msg) {
         set_last_error(("apic_update_batch: " + msg).c_str());
@@ -558,8 +559,8 @@ int update_batch_joint(apic_handle* const* handles, uint32_t count, uint32_t fla
     }
     if (e == cudaSuccess) {
         *b.h_bc = BCtl{};
-        b.h_bc->chunk_segs = g_shape.chunk_segs;
-        b.h_bc->block_group = g_shape.block_group;
+        b.h_bc->chunk_segs = shape.chunk_segs;
+        b.h_bc->block_group = shape.block_group;
         e = cudaMemcpyAsync(b.d_bc, b.h_bc, sizeof(BCtl), cudaMemcpyHostToDevice, b.stream);
     }
     if (e == cudaSuccess) e = cudaGraphLaunch(b.exec, b.stream);

@@ -83,9 +83,7 @@ inline __host__ __device__ float2* bs_part_rz(const BScene& s) {
 // kKindExit: the base level's chunks after one item for the exit test.  The
 // chunk counts follow the segment lists of the substep (ctl->seg_count).
 // chunk_segs and block_group are the batch's shape (chosen by its tuner).
-struct Shape {
-    uint32_t chunk_segs, block_group;
-};
+using Shape = BatchShape;
 enum : int { kKindBase = 0, kKindExit = 1, kKindBlocks = 2 };
 inline __host__ __device__ int kind_chunk(int l) { return 3 + 2 * l; }
 inline __host__ __device__ int kind_rchunk(int l) { return 4 + 2 * l; }

@@ -899,11 +899,12 @@ int apic_update_batch(apic_handle* const* handles, uint32_t count, uint32_t flag
     // the tuner picks the form (and the joint form's shape) unless told
     const bool tuned = !(flags & APIC_UPDATE_BATCH_STREAMS) && batch_eligible(handles, count);
     const auto t0 = std::chrono::steady_clock::now();
-    const bool joint = tuned && batch_choose(handles, count, (flags & APIC_UPDATE_BATCH_JOINT) != 0) != 0;
-    if (joint) {
+    BatchTicket tk;
+    if (tuned) batch_choose(handles, count, (flags & APIC_UPDATE_BATCH_JOINT) != 0, &tk);
+    if (tuned && tk.joint) {
         // one graph: every scene's own stages, the pressure solves of all
         // scenes as one launch per phase (batch.cu)
-        update_batch_joint(handles, count, uflags, frame_dt, rc.data());
+        update_batch_joint(handles, count, uflags, frame_dt, tk.shape, rc.data());
     } else {
         batch_note_streams(count);
         // every scene's update is enqueued on its own stream before any is
@@ -923,7 +924,7 @@ int apic_update_batch(apic_handle* const* handles, uint32_t count, uint32_t flag
         iterations += handles[i]->s.stats.pcg_iterations_total;
     }
     if (tuned && first == APIC_OK)
-        batch_record(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(),
+        batch_record(tk, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(),
                      iterations);
     if (first != APIC_OK) return fail(first, "apic_update_batch: " + first_msg);
     return APIC_OK;
