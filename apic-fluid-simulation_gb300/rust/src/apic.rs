@@ -58,6 +58,7 @@ unsafe extern "C" {
     fn apic_read_vec2x8(h: *mut ApicHandle, which: i32, dst: *mut f32, floats: u64) -> i32;
     fn apic_read_field(h: *mut ApicHandle, field: i32, dst: *mut c_void, bytes: u64) -> i32;
     fn apic_last_error() -> *const c_char;
+    fn apic_update_batch(h: *const *mut ApicHandle, count: u32, flags: u32, frame_dt: f32, status: *mut i32) -> i32;
 }
 
 fn ck(rc: i32) {
@@ -203,6 +204,25 @@ impl Apic {
         let mut bits: Vec<u64> = Vec::new();
         self.read_field(APIC_F_FLUID_BITS, &mut bits, cells.div_ceil(64));
         self.type_fluid = bits;
+    }
+}
+
+/// One `update` of every scene in `scenes` through `apic_update_batch` (no
+/// counterpart in the reference): each scene's result is the one its own
+/// `update` gives, bit for bit; the library runs the pressure solves of all
+/// scenes as one launch per solve phase where they qualify (its batch tuner
+/// chooses), else each scene on its own stream.  Mirrors are refreshed for the
+/// scenes that keep `mirror` set.
+pub fn update_batch(scenes: &mut [&mut Apic], debug_options: &DebugOptions, frame_deltatime: f32) {
+    let hs: Vec<*mut ApicHandle> = scenes.iter().map(|a| a.handle).collect();
+    ck(unsafe {
+        apic_update_batch(hs.as_ptr(), hs.len() as u32, debug_options.disable_particle_sort as u32, frame_deltatime,
+                          std::ptr::null_mut())
+    });
+    for a in scenes.iter_mut() {
+        if a.mirror {
+            a.sync_to_host();
+        }
     }
 }
 
