@@ -134,10 +134,11 @@ apic_batch_info g_last_info{};
 // The first calls for a batch of a given makeup (sides, coarse-tail depth and
 // solver mode of every scene, in order) try each way of running it: every
 // scene on its own stream, and the joint graph with each shape (segments per
-// chunk item, blocks per reduction item).  A call's cost is its wall time per
-// PCG iteration summed over the scenes; the first call of each mode (which
-// builds graphs) is not measured.  Every way computes the same bits, so the
-// tuning runs on the caller's own updates.  Then the cheapest is kept for
+// chunk item, blocks per reduction item), each twice in two interleaved
+// sweeps.  A call's cost is its wall time per PCG iteration summed over the
+// scenes; the first call of each form (which builds graphs) is not
+// measured.  Every way computes the same bits, so the tuning runs on the
+// caller's own updates.  Then the way with the lowest mean cost is kept for
 // every later batch of that makeup.
 struct TuneStep {
     int joint;       // 0: each scene on its own stream
@@ -157,10 +158,15 @@ const std::vector<TuneStep>& tune_steps() {
     static const std::vector<TuneStep> steps = [] {
         std::vector<TuneStep> v;
         v.push_back({0, {64, 4}, false});
-        v.push_back({0, {64, 4}, true});
         v.push_back({1, {64, 4}, false});
+        // every measured form twice, interleaved: a scene's cost drifts from
+        // update to update as its flow evolves
+        const size_t first = v.size();
+        v.push_back({0, {64, 4}, true});
         for (uint32_t cs : {16u, 32u, 64u})
             for (uint32_t bg : {4u, 8u, 16u, 32u}) v.push_back({1, {cs, bg}, true});
+        const size_t last = v.size();
+        for (size_t i = first; i < last; ++i) v.push_back(v[i]);
         return v;
     }();
     return steps;
@@ -491,13 +497,24 @@ void batch_choose(apic_handle* const* handles, uint32_t count, bool force_joint,
         tk->joint = t.steps[size_t(tk->step)].joint;
         return;
     }
-    if (t.best < 0) {  // every step ran: keep the cheapest measured
+    if (t.best < 0) {  // every step ran: keep the form with the lowest mean cost
         double c = 0.0;
-        for (size_t i = 0; i < t.steps.size(); ++i)
-            if (t.steps[i].measure && t.cost[i] >= 0.0 && (t.best < 0 || t.cost[i] < c)) {
+        for (size_t i = 0; i < t.steps.size(); ++i) {
+            if (!t.steps[i].measure || t.cost[i] < 0.0) continue;
+            double sum = 0.0;
+            int k = 0;
+            for (size_t j = 0; j < t.steps.size(); ++j)
+                if (t.steps[j].measure && t.cost[j] >= 0.0 && t.steps[j].joint == t.steps[i].joint &&
+                    t.steps[j].shape.chunk_segs == t.steps[i].shape.chunk_segs &&
+                    t.steps[j].shape.block_group == t.steps[i].shape.block_group) {
+                    sum += t.cost[j];
+                    ++k;
+                }
+            if (t.best < 0 || sum / k < c) {
                 t.best = int(i);
-                c = t.cost[i];
+                c = sum / k;
             }
+        }
         if (t.best < 0) t.best = 0;
     }
     tk->shape = t.steps[size_t(t.best)].shape;

@@ -647,7 +647,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_pcg_start(const BScene* __res
     });
 }
 
-__global__ void __launch_bounds__(kSegBlock) k_bat_spmv_dot(const BScene* __restrict__ tab, BListRef L) {
+__global__ void __launch_bounds__(kSegBlock, 8) k_bat_spmv_dot(const BScene* __restrict__ tab, BListRef L) {
     pdl_wait();
     bat_for_items(L, kKindBlocks, [&](uint32_t sc, uint32_t item, Shape sh) {
         const BScene& S = tab[sc];
@@ -662,7 +662,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_spmv_dot(const BScene* __rest
     });
 }
 
-__global__ void __launch_bounds__(kSegBlock) k_bat_pcg_update(const BScene* __restrict__ tab, BListRef L,
+__global__ void __launch_bounds__(kSegBlock, 8) k_bat_pcg_update(const BScene* __restrict__ tab, BListRef L,
                                                               int into_corr) {
     pdl_wait();
     bat_for_items(L, kKindBlocks, [&](uint32_t sc, uint32_t item, Shape sh) {

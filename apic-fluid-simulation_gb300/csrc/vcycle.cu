@@ -158,7 +158,11 @@ size_t tail_level_bytes(const Level& L) { return 4ull * (L.words + 6ull * L.padd
 
 // ---- the V-cycle's phases over a batch of scenes (batch.h) ------------------
 // Persistent CTAs walk the listed items of their gate; each runs the
-// single-scene kernel's work for one block of its scene's own launch.
+// single-scene kernel's work for one block of its scene's own launch.  The
+// prolongations run at eight CTAs per SM (32 registers, a few spilled): an
+// item is a chain of dependent loads, and more of them in flight beat the
+// spills (config 4: 17% per batched update with the reductions of
+// solver.cu bounded alike).
 
 // k_smooth_exit: item 0 of each scene takes the scene's exit test and loop
 // decision (k_bat_pcg_next then lists the scenes that go on); the others
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_restrict(const BScene* __rest
 
 // Prolongation from level lf + 1 fused with level lf's black (color 1) or
 // red (color 0) sweep; base: lf is the base level.
-__global__ void __launch_bounds__(kSegBlock) k_bat_prolong(const BScene* __restrict__ tab, BListRef L, int lf,
+__global__ void __launch_bounds__(kSegBlock, 8) k_bat_prolong(const BScene* __restrict__ tab, BListRef L, int lf,
                                                            int gate, int color, int base) {
     pdl_wait();
     bat_for_items(L, kind_chunk(lf), [&](uint32_t sc, uint32_t lb, Shape sh) {
@@ -222,7 +226,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_prolong(const BScene* __restr
 }
 
 // The iteration's last V-cycle kernel (k_prolong_red_rz).
-__global__ void __launch_bounds__(kSegBlock) k_bat_prolong_red_rz(const BScene* __restrict__ tab, BListRef L) {
+__global__ void __launch_bounds__(kSegBlock, 8) k_bat_prolong_red_rz(const BScene* __restrict__ tab, BListRef L) {
     pdl_wait();
     bat_for_items(L, kKindBlocks, [&](uint32_t sc, uint32_t item, Shape sh) {
         const BScene& S = tab[sc];

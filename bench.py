@@ -704,8 +704,8 @@ def run_batched(args, world=1, rank=0, local=0):
                    "tuner": {"calls": tune_calls, "joint": int(chosen["joint"]), "chunk_segs": chosen["chunk_segs"],
                              "block_group": chosen["block_group"],
                              "how": "the library's batch tuner: the first calls for this makeup of scenes try the "
-                                    "stream-per-scene form and the joint form with 12 shapes, cost = wall time "
-                                    "per PCG iteration over all scenes; the cheapest is kept"},
+                                    "stream-per-scene form and the joint form with 12 shapes, each twice, cost = "
+                                    "wall time per PCG iteration over all scenes; the lowest mean cost is kept"},
                    "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8 (default)"),
                    "dsm_vcycle": not args.no_dsm},
         "batched_vs_plain": {"updates_compared": cmp_steps, "batched": sub_cmp / cmp_s, "plain": sub_plain / plain_s,

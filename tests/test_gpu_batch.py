@@ -162,7 +162,8 @@ def test_batch_tuner(gpu_lib):
     dt = 1 / 240
     sims = [make(sc, A.SOLVER_REL_MIXED) for sc in scenes]
     seen, tuned_at = set(), None
-    for k in range(20):
+    steps = 32
+    for k in range(steps):
         assert A.update_batch(sims, A.DebugOptions(), dt) == [A.OK] * len(scenes)
         info = A.batch_last_info()
         seen.add((info["joint"], info["chunk_segs"], info["block_group"]))
@@ -173,7 +174,7 @@ def test_batch_tuner(gpu_lib):
     assert info["chunk_segs"] % 8 == 0 and info["block_group"] >= 1
     for sc, g in zip(scenes, sims):
         ref = make(sc, A.SOLVER_REL_MIXED)
-        for _ in range(20):
+        for _ in range(steps):
             ref.update(A.DebugOptions(), dt)
         assert_same(g, ref, ("tuned", sc.width))
 
