@@ -103,3 +103,44 @@ def test_server_host_logic_without_device(gpu_lib, has_gpu):
             info = sv.request(rid)
             assert info.finished and info.status == A.ERR_NO_DEVICE
         sv.close()
+
+
+STRUCTS = {  # C struct of include/apic_gpu.h -> its ctypes mirror in apic_gb300
+    "apic_world_props": "WorldPropsC", "apic_info": "InfoC", "apic_step_stats": "StatsC",
+    "apic_scene_params": "SceneParamsC", "apic_server_round": "ServerRoundC", "apic_request_info": "RequestInfoC",
+    "apic_batch_info": "BatchInfoC", "apic_server_stats": "ServerStatsC", "apic_render_params": "RenderParamsC",
+    "apic_render_stats": "RenderStatsC",
+}
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every struct the C-ABI passes has the same size and field offsets in the
+    header (compiled here with the host C compiler) as in the ctypes mirror."""
+    import shutil
+    import subprocess
+    import apic_gb300 as A
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    text = open(os.path.join(ROOT, "include", "apic_gpu.h")).read()
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "apic_gpu.h"', "int main(void) {"]
+    for c_name, py_name in STRUCTS.items():
+        body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (c_name, c_name), text, re.S)
+        assert body, c_name
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (c_name, c_name))
+        for f, _ in getattr(A, py_name)._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (c_name, f, c_name, f))
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        c_name, f, v = line.split()
+        got[(c_name, f)] = int(v)
+    for c_name, py_name in STRUCTS.items():
+        cls = getattr(A, py_name)
+        assert got[(c_name, "size")] == A.ctypes.sizeof(cls), c_name
+        for f, _ in cls._fields_:
+            assert got[(c_name, f)] == getattr(cls, f).offset, (c_name, f)
