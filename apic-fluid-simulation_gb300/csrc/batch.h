@@ -213,38 +213,66 @@ __device__ __forceinline__ void bat_build_list(const BScene* __restrict__ tab, u
 }
 
 // Walk the listed items of one kind, grid-stride: f(scene, item, shape) with
-// the whole CTA, all three uniform across the CTA.
-// Warp 0 finds an item's scene with a 32-way search of the prefix (two
-// rounds for up to 1024 scenes).
+// the whole CTA, all three uniform across the CTA; the walk waits on the
+// previous kernel (pdl_wait) itself.  Warp 0 finds an item's scene with a
+// 32-way search of the prefix (two rounds for up to 1024 scenes).  early:
+// the list was written two or more launches before this kernel (every phase
+// of a PCG iteration after the first), so the header and the first item's
+// scene are read while the previous kernel drains, from L2 (a grid that has
+// completed has its writes there).
+template <bool kL2>
+__device__ __forceinline__ uint32_t list_word(const uint32_t* p) {
+    return kL2 ? __ldcg(p) : *p;
+}
+template <bool kL2>
+__device__ __forceinline__ void bat_find(const BListRef& L, const uint32_t* pre, uint32_t t, uint32_t nact,
+                                         uint32_t* s_sc, uint32_t* s_lb) {
+    if (threadIdx.x >= 32) return;
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t lo = 0, hi = nact;  // the last listed scene with pre <= t lies in [lo, hi)
+    while (hi - lo > 1) {
+        const uint32_t step = (hi - lo + 31) >> 5;
+        const uint32_t j = lo + lane * step;
+        const uint32_t ok = __ballot_sync(0xffffffffu, j < hi && list_word<kL2>(pre + j) <= t);
+        lo += (31u - uint32_t(__clz(ok))) * step;  // lane 0 always holds (pre[lo] <= t)
+        hi = min(hi, lo + step);
+    }
+    if (lane == 0) {
+        *s_sc = list_word<kL2>(L.scenes() + lo);
+        *s_lb = t - list_word<kL2>(pre + lo);
+    }
+}
 template <class F>
-__device__ __forceinline__ void bat_for_items(const BListRef L, int kind, F&& f) {
+__device__ __forceinline__ void bat_for_items(const BListRef L, int kind, bool early, F&& f) {
     __shared__ uint32_t s_sc, s_lb, s_tot, s_nact, s_shape;
     const uint32_t* pre = L.prefix(uint32_t(kind));
-    if (threadIdx.x == 0) {
-        s_tot = L.p[2 + kind];
-        s_nact = L.p[0];
-        s_shape = L.p[1];
+    if (early) {
+        if (threadIdx.x == 0) {
+            s_tot = __ldcg(L.p + 2 + kind);
+            s_nact = __ldcg(L.p);
+            s_shape = __ldcg(L.p + 1);
+        }
+        __syncthreads();
+        if (blockIdx.x < s_tot) bat_find<true>(L, pre, blockIdx.x, s_nact, &s_sc, &s_lb);
+        pdl_wait();
+    } else {
+        pdl_wait();
+        if (threadIdx.x == 0) {
+            s_tot = L.p[2 + kind];
+            s_nact = L.p[0];
+            s_shape = L.p[1];
+        }
+        __syncthreads();
+        if (blockIdx.x < s_tot) bat_find<false>(L, pre, blockIdx.x, s_nact, &s_sc, &s_lb);
     }
     __syncthreads();
     const uint32_t tot = s_tot, nact = s_nact;
     const Shape sh{s_shape & 0xFFFFu, s_shape >> 16};
-    const uint32_t lane = threadIdx.x & 31;
     for (uint32_t t = blockIdx.x; t < tot; t += gridDim.x) {
-        if (threadIdx.x < 32) {
-            uint32_t lo = 0, hi = nact;  // the last listed scene with pre <= t lies in [lo, hi)
-            while (hi - lo > 1) {
-                const uint32_t step = (hi - lo + 31) >> 5;
-                const uint32_t j = lo + lane * step;
-                const uint32_t ok = __ballot_sync(0xffffffffu, j < hi && pre[j] <= t);
-                lo += (31u - uint32_t(__clz(ok))) * step;  // lane 0 always holds (pre[lo] <= t)
-                hi = min(hi, lo + step);
-            }
-            if (lane == 0) {
-                s_sc = L.scenes()[lo];
-                s_lb = t - pre[lo];
-            }
+        if (t != blockIdx.x) {
+            bat_find<false>(L, pre, t, nact, &s_sc, &s_lb);
+            __syncthreads();
         }
-        __syncthreads();
         f(s_sc, s_lb, sh);
         __syncthreads();
     }

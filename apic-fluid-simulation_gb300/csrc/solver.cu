@@ -609,8 +609,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_sap(const BScene* __restrict_
 }
 
 __global__ void __launch_bounds__(kSegBlock) k_bat_mixed_init(const BScene* __restrict__ tab, BListRef L, int gate) {
-    pdl_wait();
-    bat_for_items(L, kKindBase, [&](uint32_t sc, uint32_t lb, Shape sh) {
+    bat_for_items(L, kKindBase, false, [&](uint32_t sc, uint32_t lb, Shape sh) {
         const BScene& S = tab[sc];
         if (!bat_gate(S.ctl, gate)) return;
         kb_mixed_init(Blk{lb, S.grid[0]}, S.lv[0], S.b64, S.p64, S.ctl, S.partials, S.warm);
@@ -619,8 +618,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_mixed_init(const BScene* __re
 
 __global__ void __launch_bounds__(kSegBlock) k_bat_clear_pressure(const BScene* __restrict__ tab, BListRef L,
                                                                   int gate) {
-    pdl_wait();
-    bat_for_items(L, kind_chunk(0), [&](uint32_t sc, uint32_t lb, Shape sh) {
+    bat_for_items(L, kind_chunk(0), false, [&](uint32_t sc, uint32_t lb, Shape sh) {
         const BScene& S = tab[sc];
         if (!bat_gate(S.ctl, gate)) return;
         const Chunk ch = chunk_of(lb, S.ctl->seg_count[0], sh);
@@ -630,8 +628,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_clear_pressure(const BScene* 
 
 __global__ void __launch_bounds__(kSegBlock) k_bat_true_residual(const BScene* __restrict__ tab, BListRef L, int gate,
                                                                  int flags) {
-    pdl_wait();
-    bat_for_items(L, kKindBase, [&](uint32_t sc, uint32_t lb, Shape sh) {
+    bat_for_items(L, kKindBase, false, [&](uint32_t sc, uint32_t lb, Shape sh) {
         const BScene& S = tab[sc];
         if (!bat_gate(S.ctl, gate)) return;
         kb_true_residual(Blk{lb, S.grid[0]}, S.lv[0], S.b64, S.p64, S.corr, S.ctl, S.partials, flags);
@@ -639,8 +636,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_true_residual(const BScene* _
 }
 
 __global__ void __launch_bounds__(kSegBlock) k_bat_pcg_start(const BScene* __restrict__ tab, BListRef L, int gate) {
-    pdl_wait();
-    bat_for_items(L, kKindBase, [&](uint32_t sc, uint32_t lb, Shape sh) {
+    bat_for_items(L, kKindBase, false, [&](uint32_t sc, uint32_t lb, Shape sh) {
         const BScene& S = tab[sc];
         if (!bat_gate(S.ctl, gate)) return;
         kb_pcg_start(Blk{lb, S.grid[0]}, S.lv[0], S.search, S.ctl, S.partials, kRel);
@@ -648,8 +644,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_pcg_start(const BScene* __res
 }
 
 __global__ void __launch_bounds__(kSegBlock, 8) k_bat_spmv_dot(const BScene* __restrict__ tab, BListRef L) {
-    pdl_wait();
-    bat_for_items(L, kKindBlocks, [&](uint32_t sc, uint32_t item, Shape sh) {
+    bat_for_items(L, kKindBlocks, false, [&](uint32_t sc, uint32_t item, Shape sh) {
         const BScene& S = tab[sc];
         Ctl* ctl = S.ctl;
         if (!bat_gate(ctl, kGatePcg)) return;
@@ -664,8 +659,7 @@ __global__ void __launch_bounds__(kSegBlock, 8) k_bat_spmv_dot(const BScene* __r
 
 __global__ void __launch_bounds__(kSegBlock, 8) k_bat_pcg_update(const BScene* __restrict__ tab, BListRef L,
                                                               int into_corr) {
-    pdl_wait();
-    bat_for_items(L, kKindBlocks, [&](uint32_t sc, uint32_t item, Shape sh) {
+    bat_for_items(L, kKindBlocks, true, [&](uint32_t sc, uint32_t item, Shape sh) {
         const BScene& S = tab[sc];
         Ctl* ctl = S.ctl;
         if (!bat_gate(ctl, kGatePcg)) return;
@@ -682,8 +676,7 @@ __global__ void __launch_bounds__(kSegBlock, 8) k_bat_pcg_update(const BScene* _
 // (k_mixed_accumulate: chunk 0 also counts the inner solve's iterations)
 __global__ void __launch_bounds__(kSegBlock) k_bat_mixed_accumulate(const BScene* __restrict__ tab, BListRef L,
                                                                     int gate, int finalize) {
-    pdl_wait();
-    bat_for_items(L, kind_chunk(0), [&](uint32_t sc, uint32_t lb, Shape sh) {
+    bat_for_items(L, kind_chunk(0), false, [&](uint32_t sc, uint32_t lb, Shape sh) {
         const BScene& S = tab[sc];
         Ctl* ctl = S.ctl;
         if (!bat_gate(ctl, gate)) return;
@@ -695,8 +688,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_mixed_accumulate(const BScene
 
 __global__ void __launch_bounds__(kSegBlock) k_bat_pressure_to64(const BScene* __restrict__ tab, BListRef L,
                                                                  int gate) {
-    pdl_wait();
-    bat_for_items(L, kind_chunk(0), [&](uint32_t sc, uint32_t lb, Shape sh) {
+    bat_for_items(L, kind_chunk(0), false, [&](uint32_t sc, uint32_t lb, Shape sh) {
         const BScene& S = tab[sc];
         if (!bat_gate(S.ctl, gate)) return;
         const Chunk ch = chunk_of(lb, S.ctl->seg_count[0], sh);

@@ -168,8 +168,7 @@ size_t tail_level_bytes(const Level& L) { return 4ull * (L.words + 6ull * L.padd
 // decision (k_bat_pcg_next then lists the scenes that go on); the others
 // are chunks of the base level's black sweep.
 __global__ void __launch_bounds__(kSegBlock) k_bat_smooth_exit(const BScene* __restrict__ tab, BListRef L) {
-    pdl_wait();
-    bat_for_items(L, kKindExit, [&](uint32_t sc, uint32_t lb, Shape sh) {
+    bat_for_items(L, kKindExit, true, [&](uint32_t sc, uint32_t lb, Shape sh) {
         const BScene& S = tab[sc];
         Ctl* ctl = S.ctl;
         if (!bat_gate(ctl, kGatePcg)) return;
@@ -186,8 +185,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_smooth_exit(const BScene* __r
 
 __global__ void __launch_bounds__(kSegBlock) k_bat_smooth(const BScene* __restrict__ tab, BListRef L, int li,
                                                           int gate, int color, int init) {
-    pdl_wait();
-    bat_for_items(L, kind_chunk(li), [&](uint32_t sc, uint32_t lb, Shape sh) {
+    bat_for_items(L, kind_chunk(li), gate == kGatePcg, [&](uint32_t sc, uint32_t lb, Shape sh) {
         const BScene& S = tab[sc];
         const Ctl* ctl = S.ctl;
         if (!bat_gate(ctl, gate) || ctl->pcg_done) return;
@@ -200,8 +198,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_smooth(const BScene* __restri
 // level is smoothed by the segment kernels, plain into the first tail level.
 __global__ void __launch_bounds__(kSegBlock) k_bat_restrict(const BScene* __restrict__ tab, BListRef L, int lc,
                                                             int gate) {
-    pdl_wait();
-    bat_for_items(L, kind_rchunk(lc), [&](uint32_t sc, uint32_t lb, Shape sh) {
+    bat_for_items(L, kind_rchunk(lc), gate == kGatePcg, [&](uint32_t sc, uint32_t lb, Shape sh) {
         const BScene& S = tab[sc];
         const Ctl* ctl = S.ctl;
         if (!bat_gate(ctl, gate) || ctl->pcg_done) return;
@@ -214,8 +211,7 @@ __global__ void __launch_bounds__(kSegBlock) k_bat_restrict(const BScene* __rest
 // red (color 0) sweep; base: lf is the base level.
 __global__ void __launch_bounds__(kSegBlock, 8) k_bat_prolong(const BScene* __restrict__ tab, BListRef L, int lf,
                                                            int gate, int color, int base) {
-    pdl_wait();
-    bat_for_items(L, kind_chunk(lf), [&](uint32_t sc, uint32_t lb, Shape sh) {
+    bat_for_items(L, kind_chunk(lf), gate == kGatePcg, [&](uint32_t sc, uint32_t lb, Shape sh) {
         const BScene& S = tab[sc];
         const Ctl* ctl = S.ctl;
         if (!bat_gate(ctl, gate) || ctl->pcg_done) return;
@@ -227,8 +223,7 @@ __global__ void __launch_bounds__(kSegBlock, 8) k_bat_prolong(const BScene* __re
 
 // The iteration's last V-cycle kernel (k_prolong_red_rz).
 __global__ void __launch_bounds__(kSegBlock, 8) k_bat_prolong_red_rz(const BScene* __restrict__ tab, BListRef L) {
-    pdl_wait();
-    bat_for_items(L, kKindBlocks, [&](uint32_t sc, uint32_t item, Shape sh) {
+    bat_for_items(L, kKindBlocks, true, [&](uint32_t sc, uint32_t item, Shape sh) {
         const BScene& S = tab[sc];
         const Ctl* ctl = S.ctl;
         if (!bat_gate(ctl, kGatePcg) || ctl->pcg_done) return;
