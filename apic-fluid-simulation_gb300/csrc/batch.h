@@ -4,15 +4,17 @@
 // The stages before and after the pressure solve are each scene's own
 // kernels; the pressure solves of all scenes (solve_pcg :1865-1956 with the
 // V-cycle of apply_preconditioner :1788-1821) run as one launch per phase
-// over a table of scenes.  The work items of a phase are (scene, block)
-// pairs: block b of the launch the scene alone would make, with that launch's
-// grid size, so every item does exactly what that block does (block partials,
-// their sums and every cell's arithmetic are the same bit for bit).  Only the
-// scenes whose own solve runs the phase take part (a substep is due, their
-// refinement and PCG loops go on): the control kernel at each of those points
-// lists them, with a prefix of their item counts per kind of phase, and the
-// phase kernels are persistent, one wave of CTAs walking the listed items
-// (grid-stride), so scenes that have converged cost nothing.
+// over a table of scenes.  A phase with a block reduction runs, as its work
+// items, blocks of the launch the scene alone would make (one or a group of
+// consecutive ones per item), each with that launch's block index and grid
+// size, so the block partials and their sums are the same bit for bit; a
+// phase whose cells are independent of each other runs chunks of the level's
+// segments.  Only the scenes whose own solve runs the phase take part (a
+// substep is due, their refinement and PCG loops go on): the control kernel
+// at each of those points lists them, with a prefix of their item counts per
+// kind of phase, and the phase kernels are persistent, one wave of CTAs
+// walking the listed items (grid-stride), so scenes that have converged cost
+// nothing.
 #pragma once
 
 #include <cuda_runtime.h>
