@@ -215,6 +215,7 @@ struct Scene {
     cudaStream_t cap_stream = nullptr;        // stream used to record graphs
     cudaGraphExec_t update_exec = nullptr;    // whole Apic::update as one graph
     uint64_t graph_version = 0;               // bumped whenever recorded graphs go stale
+    int device = 0;                           // the CUDA device the scene lives on
     bool batched = false;                     // the last update ran inside a joint batch
     uint32_t kn_bsort = 0, kn_bstep = 0;      // ... its own kernels there: sort, one substep
     bool use_pdl = true;                      // programmatic dependent launch inside the PCG loop

@@ -449,15 +449,19 @@ std::string build_batch(Batch& b, apic_handle* const* handles, uint32_t count) {
 }  // namespace
 
 // The joint form applies when every scene solves in the same relative mode,
-// has a multigrid level and a shared-memory coarse tail, and is not in
-// profiling mode (whose host-driven loops read each scene's state).
+// has a multigrid level and a shared-memory coarse tail, lives on the
+// current device, and is not in profiling mode (whose host-driven loops read
+// each scene's state).
 bool batch_eligible(apic_handle* const* handles, uint32_t count) {
     if (count < 2 || count > 0xFFFFu) return false;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
     const int mode = scene_of(handles[0]).solver_mode;
     if (mode != APIC_SOLVER_REL_FP32 && mode != APIC_SOLVER_REL_MIXED) return false;
     for (uint32_t i = 0; i < count; ++i) {
         const Scene& s = scene_of(handles[i]);
         if (s.profiling || s.solver_mode != mode || s.nlevels < 2) return false;
+        if (s.device != dev) return false;  // one graph runs on one device
         if (s.tail_first < 1 || s.tail_first >= s.nlevels) return false;
         if (s.n == 0) return false;
     }

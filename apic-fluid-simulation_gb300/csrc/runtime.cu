@@ -645,6 +645,7 @@ int apic::create_scene(uint32_t width, uint32_t height, float cell_size, const a
     apic_handle* h = new (std::nothrow) apic_handle();
     if (!h) return fail(APIC_ERR_OOM, "host allocation failed");
     Scene& s = h->s;
+    if (cudaGetDevice(&s.device) != cudaSuccess) s.device = 0;
     s.W = width; s.H = height; s.cells = width * height; s.dx = cell_size; s.props = *props;
     s.uf = (width + 1) * height;
     s.vf = width * (height + 1);

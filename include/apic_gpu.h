@@ -330,7 +330,8 @@ int apic_morton_sort_noalloc(const float* pos_x, const float* pos_y, uint32_t n,
  * One Apic::update of each of `count` distinct scenes; each scene computes
  * exactly what apic_update computes for it, bit for bit.  When every scene
  * uses a relative solver mode (all the same one), has a multigrid level and
- * a shared-memory coarse tail, and no scene is in profiling mode, the whole
+ * a shared-memory coarse tail, lives on the calling thread's current device,
+ * and no scene is in profiling mode, the whole
  * batch runs as one CUDA graph: each scene's stages before and after the
  * pressure solve are its own kernels (side by side, each under a
  * device-side condition for its substeps), and the pressure solves of all
